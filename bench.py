@@ -1,0 +1,358 @@
+"""Benchmark: agent-steps/s of the plain per-frame pipeline (sort -> cell ranges -> physics).
+
+Default workload (one GPU): 1,048,576 spheres, N = 1024 cells per side, uniform
+positions, N(0, 1) m/s velocities, rigid response, dt = 1/60 (runs as 0.016).
+A "step" is one frame of the pipeline over the whole scene.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload P-1M|P-small|P-4M] [--cpu-seconds S]
+
+Timing: W untimed frames, then K frames, each bracketed by CUDA events on the
+world's stream; L2 is flushed (a 256 MB write) before every timed frame, outside
+the events.  Per-stage times come from the library's own event nodes inside the
+frame graph.  ``e2e`` goes through the public API with host buffers: upload the
+scene from pinned memory, run INIT + F frames, download the state.
+
+Under torchrun (N > 1) every rank runs its own independent scene (weak scaling,
+no collective on the data path); only the barrier and the max over ranks of the
+elapsed time use torch.distributed.
+
+``--impl reference`` times the CPU restatement of the reference pipeline (the
+oracle; the reference itself is Rust + wgpu and cannot run here) on the host
+cores, same workload, same metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+# Algorithmic bytes per agent and frame (each array touched once; neighbour and
+# cell-table gathers counted as cache hits):
+#   physics: read own state 32 + perm 4, write state 32 + key 4      = 72 B/agent
+#   sort:    3 x (8 read + 8 write) + histogram read 4                = 52 B/agent
+#   cells:   read sorted keys 4 + write start/close 8                 = 12 B/agent, + 4 B/cell
+PHYSICS_BYTES_PER_AGENT = 72
+FRAME_BYTES_PER_AGENT = 136
+FRAME_BYTES_PER_CELL = 4
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch from a committed ncu summary, or None."""
+    f = ROOT / "profiles" / f"{kernel}_{workload}.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_oracle_run(scene, frames_budget_s: float, max_frames: int | None = None):
+    """Time the oracle (CPU restatement) on the scene: INIT untimed, then LOOP frames
+    until the time budget is spent.  Returns (agent-steps/s, frames, seconds, threads)."""
+    import oracle
+
+    threads = oracle.hardware_threads()
+    ow = oracle.OracleWorld(scene.plugin.to_c(), threads=threads)
+    ow.set_state(scene.pos_scale, scene.vfme)
+    ow.step(1)  # INIT frame
+    frames, t0 = 0, time.perf_counter()
+    while True:
+        ow.step(1)
+        frames += 1
+        el = time.perf_counter() - t0
+        if el >= frames_budget_s or (max_frames is not None and frames >= max_frames):
+            break
+    ow.close()
+    return scene.n * frames / el, frames, el, threads
+
+
+def workload_desc(name, sc):
+    p = sc.plugin
+    return (f"{name}: {sc.n:,} spheres, N={p.number_of_grids_one_dimension}, grid_size={p.grid_size}, "
+            f"H={p.half_map_height}, {'spring' if p.enable_spring else 'rigid'}, dt=1/60 (runs 0.016)")
+
+
+def run_reference(args, rank, world_size):
+    """CPU restatement of the reference pipeline on the host cores (the oracle port)."""
+    if rank != 0:
+        return 0
+    from bevy_millions_ball_gb300 import scenes
+
+    sc = scenes.workload(args.workload)
+    import oracle
+
+    threads = oracle.hardware_threads()
+    ow = oracle.OracleWorld(sc.plugin.to_c(), threads=threads)
+    ow.set_state(sc.pos_scale, sc.vfme)
+    ow.step(1)  # INIT
+    for _ in range(args.warmup):
+        ow.step(1)
+    budget = args.reference_seconds
+    times = []
+    t_all = time.perf_counter()
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        ow.step(1)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > budget:
+            break
+    total = sum(times)
+    v = sc.n * len(times) / total
+    sample = (f"{len(times)} of {args.steps} requested frames of the full scene (time budget {budget:.0f} s), "
+              f"{threads} threads")
+    line = {
+        "impl": "reference", "metric": "agent-steps/s", "value": v, "unit": "agent-steps/s",
+        "n_gpus": world_size, "steps": len(times), "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_desc(args.workload, sc), "n": sc.n, "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": "agent-steps/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "agent-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference is Rust + wgpu (no Rust toolchain or graphics stack here): timed its CPU restatement",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world_size, local_rank):
+    import numpy as np
+    import torch
+
+    from bevy_millions_ball_gb300 import World, scenes
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    sc = scenes.workload(args.workload, seed=rank)
+    n = sc.n
+    p = sc.plugin
+    cells = p.number_of_grids_one_dimension ** 2
+    stream = torch.cuda.current_stream()
+    w = World(p, stream=stream.cuda_stream)
+    w.set_profiling(True)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    w.set_state(sc.pos_scale, sc.vfme)
+    w.step(1)  # INIT frame
+    for _ in range(max(args.warmup, 3)):
+        w.step(1)
+    w.sync()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stage = np.zeros((args.steps, 3))
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    smi_index = int(vis.split(",")[local_rank]) if vis and vis.split(",")[0].isdigit() else local_rank
+    with ClockSampler(smi_index) as clocks:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            w.step(1)
+            ev[k][1].record(stream)
+            stage[k] = w.last_frame_times()  # waits for this frame; stage events are inside the graph
+        torch.cuda.synchronize()
+    w.sync()
+    if dist:
+        dist.barrier()
+    per = np.array([a.elapsed_time(b) for a, b in ev])  # ms
+    total_ms = float(per.sum())
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world_size * n * args.steps / (total_ms * 1e-3)
+    kernels = w.kernels_per_frame
+
+    # e2e through the public API with host buffers (pinned)
+    e2e = None
+    if rank == 0 or world_size > 1:
+        F = args.e2e_frames
+        pin_p = torch.from_numpy(sc.pos_scale).pin_memory()
+        pin_q = torch.from_numpy(sc.vfme.view(np.int32)).pin_memory()
+        out_p = torch.empty_like(pin_p).pin_memory()
+        out_q = torch.empty_like(pin_q).pin_memory()
+        lib = w._lib
+
+        def job():
+            w._check(lib.mb_set_state(w._h, pin_p.data_ptr(), pin_q.data_ptr(), 0))
+            w.step(1 + F)
+            w._check(lib.mb_get_state(w._h, out_p.data_ptr(), out_q.data_ptr(), 0))
+
+        w.set_profiling(False)
+        job()
+        reps = max(3, args.e2e_reps)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            job()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        e2e = {"value": world_size * n * F * reps / el, "unit": "agent-steps/s",
+               "h2d_bytes_per_step": int(pin_p.numel() * 4 + pin_q.numel() * 4),
+               "d2h_bytes_per_step": int(out_p.numel() * 4 + out_q.numel() * 4),
+               "frames_per_step": F,
+               "what": f"per step: upload {n:,} spheres from pinned host memory, INIT + {F} frames, download state"}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        w.close()
+        return 0
+
+    hbm, peak_kind = peaks()
+    phys_ms = float(stage[:, 2].mean())
+    phys_bytes = PHYSICS_BYTES_PER_AGENT * n
+    achieved = phys_bytes / (phys_ms * 1e-3) / 1e9
+    frame_bytes = FRAME_BYTES_PER_AGENT * n + FRAME_BYTES_PER_CELL * cells
+    roofline = {
+        "bound": "hbm", "kernel": "k_physics_loop", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+        "frac": achieved / hbm, "peak_kind": peak_kind,
+        "traffic": ncu_traffic("k_physics_loop", args.workload),
+        "algorithmic_bytes_per_launch": phys_bytes,
+        "frame": {"algorithmic_bytes": frame_bytes,
+                  "achieved_gbs": frame_bytes / (total_ms / args.steps * 1e-3) / 1e9,
+                  "frac": frame_bytes / (total_ms / args.steps * 1e-3) / 1e9 / hbm},
+    }
+    cpu = None
+    if world_size == 1 and not args.no_cpu_baseline:
+        v, frames, el, thr = cpu_oracle_run(sc, args.cpu_seconds)
+        cpu = {"value": v, "unit": "agent-steps/s", "cores": thr, "kind": "port",
+               "sample": f"{frames} LOOP frames of the same {n:,}-sphere scene ({el:.1f} s wall), oracle, {thr} threads"}
+    line = {
+        "metric": "agent-steps/s", "value": value, "unit": "agent-steps/s", "n_gpus": world_size,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": workload_desc(args.workload, sc), "n": n, "grids": p.number_of_grids_one_dimension,
+                   "cells": cells, "parallelism": f"replicas{world_size}" if world_size > 1 else "single",
+                   "l2": "flushed before every timed frame (256 MB write, outside the events)",
+                   "digit_bits_max": w.tuning.digit_bits_max, "collide_block": w.tuning.collide_block},
+        "stages_ms": {"sort": float(stage[:, 0].mean()), "cells": float(stage[:, 1].mean()),
+                      "physics": phys_ms},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(kernels * args.steps),
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    w.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="P-1M", choices=["P-small", "P-1M", "P-4M"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--reference-seconds", type=float, default=120.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-frames", type=int, default=100)
+    ap.add_argument("--e2e-reps", type=int, default=5)
+    args = ap.parse_args()
+    rank, world_size, local_rank = env_rank()
+    if args.impl == "reference":
+        return run_reference(args, rank, world_size)
+    from __graft_entry__ import build
+
+    build()
+    return run_ours(args, rank, world_size, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

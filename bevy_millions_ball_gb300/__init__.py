@@ -1,0 +1,302 @@
+"""GB300-native per-step sphere-collision pipeline (bevy_millions_ball's physics passes).
+
+Host-side mirror of the reference plugin interface:
+
+* :class:`PhysicsPlugin` / :class:`PhysicsSettings` — the reference's
+  ``PhysicsPlugin`` fields and defaults (src/physics/mod.rs:53-109) and the
+  runtime ``PhysicsSettings`` helpers (mod.rs:294-400).
+* :class:`World` — one scene resident on the GPU with a headless ``step()``; it
+  stands in for ``PhysicsNode::run`` (mod.rs:846-912), which the reference only
+  runs from its render graph.
+
+Everything computes in ``libmillionsball.so`` (hand-written sm_103a kernels behind
+the C ABI in ``include/millionsball.h``); this module only marshals arguments.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from ._abi import MB_DEVICE, MB_HOST, MbConsts, MbError, MbSettings, MbTuning
+
+__all__ = [
+    "PhysicsPlugin",
+    "PhysicsSettings",
+    "World",
+    "SortPlan",
+    "MbError",
+    "pack_vfme",
+    "unpack_vfme",
+    "quantize",
+    "library",
+]
+
+
+def library() -> C.CDLL:
+    return _abi.load()
+
+
+@dataclass
+class PhysicsPlugin:
+    """Fields and defaults of the reference ``PhysicsPlugin`` (src/physics/mod.rs:53-109)."""
+
+    enable_simulation: bool = True
+    enable_spring: bool = False
+    number_of_grids_one_dimension: int = 128
+    grid_size: int = 8
+    half_map_height: int = 16
+    gravity: tuple = (0.0, -9.8, 0.0)
+    e_envir: float = 0.90
+    e_agent: float = 0.95
+    k_agent: float = 25.0
+    c_agent: float = 0.1
+    r_agent: float = 0.9
+    max_number_of_agents: int = 16 * 1024
+    time_delta: float = 1.0 / 120.0
+    # not in the reference: use the f32 values as given instead of the x1000 quantisation
+    exact_constants: bool = False
+
+    def to_c(self) -> MbSettings:
+        s = MbSettings()
+        s.max_number_of_agents = int(self.max_number_of_agents)
+        s.number_of_grids_one_dimension = int(self.number_of_grids_one_dimension)
+        s.grid_size = int(self.grid_size)
+        s.half_map_height = int(self.half_map_height)
+        for i in range(3):
+            s.gravity[i] = float(self.gravity[i])
+        s.e_envir, s.e_agent = float(self.e_envir), float(self.e_agent)
+        s.k_agent, s.c_agent, s.r_agent = float(self.k_agent), float(self.c_agent), float(self.r_agent)
+        s.time_delta = float(self.time_delta)
+        s.enable_simulation = 1 if self.enable_simulation else 0
+        s.enable_spring = 1 if self.enable_spring else 0
+        s.exact_constants = 1 if self.exact_constants else 0
+        return s
+
+    @classmethod
+    def from_c(cls, s: MbSettings) -> "PhysicsPlugin":
+        return cls(
+            enable_simulation=bool(s.enable_simulation),
+            enable_spring=bool(s.enable_spring),
+            number_of_grids_one_dimension=s.number_of_grids_one_dimension,
+            grid_size=s.grid_size,
+            half_map_height=s.half_map_height,
+            gravity=tuple(s.gravity),
+            e_envir=s.e_envir,
+            e_agent=s.e_agent,
+            k_agent=s.k_agent,
+            c_agent=s.c_agent,
+            r_agent=s.r_agent,
+            max_number_of_agents=s.max_number_of_agents,
+            time_delta=s.time_delta,
+            exact_constants=bool(s.exact_constants),
+        )
+
+    def replace(self, **kw) -> "PhysicsPlugin":
+        return dataclasses.replace(self, **kw)
+
+
+class PhysicsSettings(PhysicsPlugin):
+    """Runtime settings with the reference's map helpers (src/physics/mod.rs:365-400)."""
+
+    def max_number_of_grids_on_dimension(self) -> int:
+        import math
+
+        return math.isqrt(self.max_number_of_agents)
+
+    def map_size_u(self) -> int:
+        return self.number_of_grids_one_dimension * self.grid_size
+
+    def half_map_size_u(self) -> int:
+        return self.map_size_u() // 2
+
+    def map_size(self) -> float:
+        return float(self.map_size_u())
+
+    def half_map_size(self) -> float:
+        return float(self.half_map_size_u())
+
+    def half_map_height_f(self) -> float:
+        return float(self.half_map_height)
+
+    def map_height(self) -> float:
+        return 2.0 * float(self.half_map_height)
+
+
+def quantize(plugin: PhysicsPlugin) -> MbConsts:
+    """Constants as the kernels use them (CompiledConsts, src/physics/mod.rs:459-485)."""
+    lib = library()
+    out = MbConsts()
+    _abi.check(lib, lib.mb_quantize_settings(C.byref(plugin.to_c()), C.byref(out)))
+    return out
+
+
+def pack_vfme(velocity, force, mass) -> np.ndarray:
+    """pack_vfme (src/physics/mod.rs:214-239): f16 (RNE) pairs (vx,vy) (vz,fx) (fy,fz) (m,0)."""
+    v = np.asarray(velocity, np.float32).reshape(-1, 3)
+    f = np.asarray(force, np.float32).reshape(-1, 3)
+    m = np.broadcast_to(np.asarray(mass, np.float32), (v.shape[0],))
+    h = np.zeros((v.shape[0], 8), np.float16)
+    h[:, 0:3] = v.astype(np.float16)
+    h[:, 3:6] = f.astype(np.float16)
+    h[:, 6] = m.astype(np.float16)
+    return np.ascontiguousarray(h).view(np.uint32).reshape(-1, 4).copy()
+
+
+def unpack_vfme(vfme: np.ndarray):
+    """Inverse of :func:`pack_vfme`: (velocity (n,3), force (n,3), mass (n,)) as float32."""
+    h = np.ascontiguousarray(vfme, np.uint32).view(np.float16).reshape(-1, 8).astype(np.float32)
+    return h[:, 0:3].copy(), h[:, 3:6].copy(), h[:, 6].copy()
+
+
+def _stream_handle(stream) -> int:
+    if stream is None:
+        return 0
+    if isinstance(stream, int):
+        return stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+class World:
+    """One scene resident on the GPU (the reference plugin's buffers + per-frame node)."""
+
+    def __init__(self, plugin: PhysicsPlugin, stream=None):
+        self._lib = library()
+        self.n = int(plugin.max_number_of_agents)
+        self._h = C.c_void_p()
+        _abi.check(self._lib, self._lib.mb_create(C.byref(plugin.to_c()), _stream_handle(stream), C.byref(self._h)))
+
+    # -- lifecycle
+    def close(self) -> None:
+        if self._h:
+            self._lib.mb_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int) -> None:
+        _abi.check(self._lib, st, self._h)
+
+    # -- settings
+    @property
+    def settings(self) -> PhysicsPlugin:
+        s = MbSettings()
+        self._check(self._lib.mb_get_settings(self._h, C.byref(s)))
+        return PhysicsPlugin.from_c(s)
+
+    def set_settings(self, plugin: PhysicsPlugin) -> None:
+        self._check(self._lib.mb_set_settings(self._h, C.byref(plugin.to_c())))
+
+    @property
+    def tuning(self) -> MbTuning:
+        t = MbTuning()
+        self._check(self._lib.mb_get_tuning(self._h, C.byref(t)))
+        return t
+
+    def set_tuning(self, digit_bits_max: int | None = None, collide_block: int | None = None) -> None:
+        t = self.tuning
+        if digit_bits_max is not None:
+            t.digit_bits_max = digit_bits_max
+        if collide_block is not None:
+            t.collide_block = collide_block
+        self._check(self._lib.mb_set_tuning(self._h, C.byref(t)))
+
+    # -- state
+    def set_state(self, pos_scale: np.ndarray, vfme: np.ndarray) -> None:
+        p = np.ascontiguousarray(pos_scale, np.float32)
+        q = np.ascontiguousarray(vfme, np.uint32)
+        if p.size != 4 * self.n or q.size != 4 * self.n:
+            raise ValueError(f"expected {self.n} x 4 arrays")
+        self._check(self._lib.mb_set_state(self._h, p.ctypes.data, q.ctypes.data, MB_HOST))
+
+    def set_state_device(self, pos_ptr: int, vfme_ptr: int) -> None:
+        self._check(self._lib.mb_set_state(self._h, pos_ptr, vfme_ptr, MB_DEVICE))
+
+    def get_state(self):
+        p = np.empty((self.n, 4), np.float32)
+        q = np.empty((self.n, 4), np.uint32)
+        self._check(self._lib.mb_get_state(self._h, p.ctypes.data, q.ctypes.data, MB_HOST))
+        return p, q
+
+    def get_state_device(self, pos_ptr: int, vfme_ptr: int) -> None:
+        self._check(self._lib.mb_get_state(self._h, pos_ptr, vfme_ptr, MB_DEVICE))
+
+    def device_buffers(self):
+        a, b = C.c_void_p(), C.c_void_p()
+        self._check(self._lib.mb_device_buffers(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    # -- stepping
+    def step(self, k: int = 1) -> None:
+        self._check(self._lib.mb_step(self._h, int(k)))
+
+    def sync(self) -> None:
+        self._check(self._lib.mb_sync(self._h))
+
+    @property
+    def time(self) -> int:
+        return int(self._lib.mb_time(self._h))
+
+    def set_profiling(self, on: bool = True) -> None:
+        self._check(self._lib.mb_set_profiling(self._h, 1 if on else 0))
+
+    def last_frame_times(self):
+        """(sort_ms, cells_ms, physics_ms) of the most recent frame (profiling on)."""
+        ms = (C.c_float * 3)()
+        self._check(self._lib.mb_last_frame_times(self._h, ms))
+        return tuple(ms)
+
+    @property
+    def kernels_per_frame(self) -> int:
+        return int(self._lib.mb_kernels_per_frame(self._h))
+
+    def debug(self, cells: int | None = None):
+        s = self.settings
+        cells = cells or s.number_of_grids_one_dimension ** 2
+        keys = np.empty(self.n, np.uint32)
+        perm = np.empty(self.n, np.uint32)
+        start = np.empty(cells, np.uint32)
+        close = np.empty(cells, np.uint32)
+        self._check(self._lib.mb_get_debug(self._h, keys.ctypes.data, perm.ctypes.data, start.ctypes.data,
+                                           close.ctypes.data, MB_HOST))
+        return {"keys": keys, "perm": perm, "start": start, "close": close}
+
+
+class SortPlan:
+    """Stage API: stable sort + cell-range build on device buffers (mb_sort_and_hash)."""
+
+    def __init__(self, max_keys: int, max_cells: int):
+        self._lib = library()
+        self._h = C.c_void_p()
+        _abi.check(self._lib, self._lib.mb_sort_plan_create(int(max_keys), int(max_cells), C.byref(self._h)))
+
+    def run(self, keys_ptr: int, vals_ptr: int | None, n: int, cells: int, sorted_keys_ptr: int,
+            sorted_vals_ptr: int, start_ptr: int | None, close_ptr: int | None, stream=None) -> None:
+        _abi.check(self._lib, self._lib.mb_sort_and_hash(self._h, keys_ptr, vals_ptr, int(n), int(cells),
+                                                         sorted_keys_ptr, sorted_vals_ptr, start_ptr,
+                                                         close_ptr, _stream_handle(stream)))
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.mb_sort_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

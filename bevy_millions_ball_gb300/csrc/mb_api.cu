@@ -1,0 +1,518 @@
+// mb_api.cu — the C ABI (include/millionsball.h): worlds, frames, graphs, stages.
+//
+// One frame = PhysicsNode::run (src/physics/mod.rs:846-912): sort the cell keys
+// emitted by the previous frame, build the cell offsets, run the physics pass
+// (INIT on frame 0 after an upload, LOOP afterwards, mod.rs:929-939).  The
+// reference's eve/odd bind groups (mod.rs:659-705) become two state buffers that
+// swap every frame; each LOOP frame parity is one captured CUDA graph.
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "mb_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+std::string cuda_msg(const char* what, cudaError_t e) {
+    return std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+}
+
+// (x * 1000.) as i32 / as u32: truncation toward zero, saturating, NaN -> 0
+// (src/physics/mod.rs:473-481).
+int32_t q_i32(float x) {
+    float v = x * 1000.0f;
+    if (std::isnan(v)) return 0;
+    if (v >= 2147483648.0f) return INT32_MAX;
+    if (v <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)v;
+}
+uint32_t q_u32(float x) {
+    float v = x * 1000.0f;
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)v;
+}
+
+}  // namespace
+
+struct mb_world {
+    mb_settings s{};
+    mb_consts c{};
+    mb::PhysParams P{};
+    uint32_t n = 0;
+    uint32_t cells = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;     // caller's stream: all work is ordered on it
+    cudaStream_t cap_stream = nullptr; // private stream used only to capture graphs
+    float4* pos[2] = {nullptr, nullptr};
+    uint4* vfme[2] = {nullptr, nullptr};
+    uint32_t* keys = nullptr;          // unsorted keys emitted by the last physics pass
+    uint32_t* sorted_keys = nullptr;
+    uint32_t* perm = nullptr;
+    mb::SortScratch scratch;
+    mb::SortSchedule sched;
+    mb_tuning tuning{};
+    int cur = 0;
+    int64_t time = -1;
+    bool has_state = false;
+    bool frame_done = false;           // a frame ran since the last upload
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool profiling = false;
+    cudaEvent_t prof_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::string err;
+};
+
+namespace {
+
+mb_status fail(mb_world* w, mb_status st, const std::string& msg) {
+    if (w) w->err = msg;
+    g_last_error = msg;
+    return st;
+}
+mb_status cuda_fail(mb_world* w, const char* what, cudaError_t e) {
+    return fail(w, e == cudaErrorMemoryAllocation ? MB_ERR_OOM : MB_ERR_CUDA, cuda_msg(what, e));
+}
+
+bool settings_valid(const mb_settings* s, std::string& why) {
+    if (!s) { why = "settings is NULL"; return false; }
+    if (s->max_number_of_agents == 0 || s->max_number_of_agents > mb::kMaxAgents) {
+        why = "max_number_of_agents must be in [1, 2^28-1]";
+        return false;
+    }
+    if (s->number_of_grids_one_dimension == 0 || s->grid_size == 0) {
+        why = "number_of_grids_one_dimension and grid_size must be >= 1";
+        return false;
+    }
+    uint64_t cells = (uint64_t)s->number_of_grids_one_dimension * s->number_of_grids_one_dimension;
+    if (cells > mb::kMaxCells) { why = "number_of_grids_one_dimension^2 must be <= 2^28"; return false; }
+    if ((uint64_t)s->number_of_grids_one_dimension * s->grid_size > 0xFFFFFFFFull) {
+        why = "number_of_grids_one_dimension * grid_size overflows u32";
+        return false;
+    }
+    mb_consts c;
+    mb_quantize_settings(s, &c);
+    if (!(c.time_delta > 0.0f)) { why = "time_delta quantises to 0 (needs >= 0.001)"; return false; }
+    return true;
+}
+
+void drop_graphs(mb_world* w) {
+    for (auto& g : w->graph) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
+}
+
+void apply_settings(mb_world* w, const mb_settings& s) {
+    w->s = s;
+    mb_quantize_settings(&s, &w->c);
+    w->P = mb::make_params(w->c);
+    w->cells = s.number_of_grids_one_dimension * s.number_of_grids_one_dimension;
+    w->sched = mb::make_schedule(w->n, w->cells, w->tuning.digit_bits_max);
+}
+
+// Record a profiling event; inside a stream capture it becomes an event-record
+// node that fires on every graph launch.
+cudaError_t mark(mb_world* w, int i, cudaStream_t st, bool capturing) {
+    if (!w->profiling) return cudaSuccess;
+    return capturing ? cudaEventRecordWithFlags(w->prof_ev[i], st, cudaEventRecordExternal)
+                     : cudaEventRecord(w->prof_ev[i], st);
+}
+
+// Enqueue one frame on `st`.
+cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool capturing = false) {
+    cudaError_t e;
+    if ((e = mark(w, 0, st, capturing))) return e;
+    if ((e = mb::sort_pairs(w->scratch, w->sched, w->keys, nullptr, w->sorted_keys, w->perm, st))) return e;
+    if ((e = mark(w, 1, st, capturing))) return e;
+    if ((e = mb::cell_offsets(w->scratch, w->sched, w->sorted_keys, st))) return e;
+    if ((e = mark(w, 2, st, capturing))) return e;
+    int nxt = cur ^ 1;
+    if (init)
+        e = mb::launch_physics_init(w->P, w->n, w->perm, w->pos[cur], w->vfme[cur], w->pos[nxt],
+                                    w->vfme[nxt], w->keys, st);
+    else
+        e = mb::launch_physics_loop(w->P, w->n, w->perm, w->scratch.offs, w->pos[cur], w->vfme[cur],
+                                    w->pos[nxt], w->vfme[nxt], w->keys, (int)w->tuning.collide_block, st);
+    if (e) return e;
+    return mark(w, 3, st, capturing);
+}
+
+cudaError_t build_graph(mb_world* w, int cur) {
+    cudaError_t e = cudaStreamBeginCapture(w->cap_stream, cudaStreamCaptureModeThreadLocal);
+    if (e) return e;
+    cudaError_t fe = enqueue_frame(w, w->cap_stream, cur, false, true);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(w->cap_stream, &g);
+    if (fe) {
+        if (g) cudaGraphDestroy(g);
+        return fe;
+    }
+    if (e) return e;
+    e = cudaGraphInstantiate(&w->graph[cur], g, 0);
+    cudaGraphDestroy(g);
+    return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mb_settings_default(mb_settings* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    // PhysicsPlugin::default (src/physics/mod.rs:87-109)
+    o->enable_simulation = 1;
+    o->enable_spring = 0;
+    o->number_of_grids_one_dimension = 128;
+    o->grid_size = 8;
+    o->half_map_height = 16;
+    o->gravity[0] = 0.0f;
+    o->gravity[1] = -9.8f;
+    o->gravity[2] = 0.0f;
+    o->e_envir = 0.90f;
+    o->e_agent = 0.95f;
+    o->k_agent = 25.0f;
+    o->c_agent = 0.1f;
+    o->r_agent = 0.9f;
+    o->max_number_of_agents = 16 * 1024;
+    o->time_delta = 1.0f / 120.0f;
+}
+
+mb_status mb_quantize_settings(const mb_settings* s, mb_consts* c) {
+    if (!s || !c) return MB_ERR_INVALID_ARG;
+    std::memset(c, 0, sizeof(*c));
+    c->number_of_grids_one_dimension = s->number_of_grids_one_dimension;
+    c->grid_size = s->grid_size;
+    c->half_map_height = (float)s->half_map_height;  // HALF_MAP_HEIGHT = f32(u32)
+    c->half_map_size = (float)((s->number_of_grids_one_dimension * s->grid_size) / 2u);
+    if (s->exact_constants) {
+        for (int i = 0; i < 3; ++i) c->gravity[i] = s->gravity[i];
+        c->e_envir = s->e_envir;
+        c->e_agent = s->e_agent;
+        c->k_agent = s->k_agent;
+        c->c_agent = s->c_agent;
+        c->r_agent = s->r_agent;
+        c->time_delta = s->time_delta;
+    } else {
+        // f32(#DEF) / 1000. (physics.wgsl:7-16)
+        for (int i = 0; i < 3; ++i) c->gravity[i] = (float)q_i32(s->gravity[i]) / 1000.0f;
+        c->e_envir = (float)q_u32(s->e_envir) / 1000.0f;
+        c->e_agent = (float)q_u32(s->e_agent) / 1000.0f;
+        c->k_agent = (float)q_u32(s->k_agent) / 1000.0f;
+        c->c_agent = (float)q_u32(s->c_agent) / 1000.0f;
+        c->r_agent = (float)q_u32(s->r_agent) / 1000.0f;
+        c->time_delta = (float)q_u32(s->time_delta) / 1000.0f;
+    }
+    c->enable_spring = s->enable_spring ? 1u : 0u;
+    return MB_OK;
+}
+
+mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out) {
+    if (!out) return fail(nullptr, MB_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    std::string why;
+    if (!settings_valid(s, why)) return fail(nullptr, MB_ERR_INVALID_ARG, why);
+    mb_world* w = new (std::nothrow) mb_world();
+    if (!w) return fail(nullptr, MB_ERR_OOM, "host allocation failed");
+    cudaGetDevice(&w->device);
+    w->stream = (cudaStream_t)cuda_stream;
+    w->n = s->max_number_of_agents;
+    w->tuning.digit_bits_max = 11;
+    w->tuning.collide_block = 128;
+    apply_settings(w, *s);
+    const size_t n = w->n;
+    auto alloc_all = [&]() -> cudaError_t {
+        cudaError_t e;
+        if ((e = cudaStreamCreateWithFlags(&w->cap_stream, cudaStreamNonBlocking))) return e;
+        for (int i = 0; i < 2; ++i) {
+            if ((e = cudaMalloc(&w->pos[i], sizeof(float4) * n))) return e;
+            if ((e = cudaMalloc(&w->vfme[i], sizeof(uint4) * n))) return e;
+        }
+        if ((e = cudaMalloc(&w->keys, sizeof(uint32_t) * n))) return e;
+        if ((e = cudaMalloc(&w->sorted_keys, sizeof(uint32_t) * n))) return e;
+        if ((e = cudaMalloc(&w->perm, sizeof(uint32_t) * n))) return e;
+        return mb::scratch_alloc(w->scratch, w->n, w->cells);
+    };
+    cudaError_t e = alloc_all();
+    if (e) {
+        mb_status st = cuda_fail(nullptr, "mb_create", e);
+        mb_destroy(w);
+        return st;
+    }
+    *out = w;
+    return MB_OK;
+}
+
+mb_status mb_destroy(mb_world* w) {
+    if (!w) return MB_OK;
+    if (w->stream || w->cap_stream) cudaStreamSynchronize(w->stream);
+    drop_graphs(w);
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(w->pos[i]);
+        cudaFree(w->vfme[i]);
+    }
+    cudaFree(w->keys);
+    cudaFree(w->sorted_keys);
+    cudaFree(w->perm);
+    mb::scratch_free(w->scratch);
+    if (w->cap_stream) cudaStreamDestroy(w->cap_stream);
+    for (auto& ev : w->prof_ev)
+        if (ev) cudaEventDestroy(ev);
+    delete w;
+    return MB_OK;
+}
+
+mb_status mb_set_settings(mb_world* w, const mb_settings* s) {
+    if (!w) return fail(nullptr, MB_ERR_INVALID_ARG, "world is NULL");
+    std::string why;
+    if (!settings_valid(s, why)) return fail(w, MB_ERR_INVALID_ARG, why);
+    if (s->max_number_of_agents != w->n)
+        return fail(w, MB_ERR_INVALID_ARG, "max_number_of_agents is fixed for a world");
+    bool grid_changed = s->number_of_grids_one_dimension != w->s.number_of_grids_one_dimension ||
+                        s->grid_size != w->s.grid_size;
+    uint32_t new_cells = s->number_of_grids_one_dimension * s->number_of_grids_one_dimension;
+    if (new_cells > w->scratch.max_cells) {
+        cudaError_t e = cudaStreamSynchronize(w->stream);
+        if (e) return cuda_fail(w, "mb_set_settings", e);
+        uint32_t* offs = nullptr;
+        if ((e = cudaMalloc(&offs, sizeof(uint32_t) * ((size_t)new_cells + 1u))))
+            return cuda_fail(w, "mb_set_settings", e);
+        cudaFree(w->scratch.offs);
+        w->scratch.offs = offs;
+        w->scratch.max_cells = new_cells;
+    }
+    drop_graphs(w);
+    apply_settings(w, *s);
+    // keys emitted under the old grid are re-derived under the new one
+    if (grid_changed && w->has_state && w->frame_done) {
+        cudaError_t e = mb::launch_rekey(w->P, w->n, w->pos[w->cur], w->keys, w->stream);
+        if (e) return cuda_fail(w, "mb_set_settings", e);
+    }
+    return MB_OK;
+}
+
+mb_status mb_get_settings(const mb_world* w, mb_settings* out) {
+    if (!w || !out) return MB_ERR_INVALID_ARG;
+    *out = w->s;
+    return MB_OK;
+}
+
+mb_status mb_set_state(mb_world* w, const float* pos_scale, const uint32_t* vfme, mb_memory where) {
+    if (!w || !pos_scale || !vfme) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
+    cudaMemcpyKind kind = where == MB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(w->pos[0], pos_scale, sizeof(float4) * w->n, kind, w->stream)))
+        return cuda_fail(w, "mb_set_state", e);
+    if ((e = cudaMemcpyAsync(w->vfme[0], vfme, sizeof(uint4) * w->n, kind, w->stream)))
+        return cuda_fail(w, "mb_set_state", e);
+    // fresh sort buffers hold zeros: frame 0 sorts all-zero keys (identity order)
+    if ((e = cudaMemsetAsync(w->keys, 0, sizeof(uint32_t) * w->n, w->stream)))
+        return cuda_fail(w, "mb_set_state", e);
+    if (where == MB_HOST && (e = cudaStreamSynchronize(w->stream)))
+        return cuda_fail(w, "mb_set_state", e);
+    w->cur = 0;
+    w->time = 0;
+    w->has_state = true;
+    w->frame_done = false;
+    return MB_OK;
+}
+
+mb_status mb_get_state(mb_world* w, float* pos_scale, uint32_t* vfme, mb_memory where) {
+    if (!w) return fail(nullptr, MB_ERR_INVALID_ARG, "world is NULL");
+    if (!w->has_state) return fail(w, MB_ERR_NOT_READY, "no state uploaded");
+    cudaMemcpyKind kind = where == MB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    cudaError_t e;
+    if (pos_scale && (e = cudaMemcpyAsync(pos_scale, w->pos[w->cur], sizeof(float4) * w->n, kind, w->stream)))
+        return cuda_fail(w, "mb_get_state", e);
+    if (vfme && (e = cudaMemcpyAsync(vfme, w->vfme[w->cur], sizeof(uint4) * w->n, kind, w->stream)))
+        return cuda_fail(w, "mb_get_state", e);
+    if (where == MB_HOST && (e = cudaStreamSynchronize(w->stream))) return cuda_fail(w, "mb_get_state", e);
+    return MB_OK;
+}
+
+mb_status mb_step(mb_world* w, uint32_t k) {
+    if (!w) return fail(nullptr, MB_ERR_INVALID_ARG, "world is NULL");
+    if (!w->has_state) return fail(w, MB_ERR_NOT_READY, "no state uploaded");
+    if (!w->s.enable_simulation) return MB_OK;
+    cudaError_t e;
+    for (uint32_t f = 0; f < k; ++f) {
+        if (w->time == 0) {
+            if ((e = enqueue_frame(w, w->stream, w->cur, true))) return cuda_fail(w, "mb_step(init)", e);
+        } else {
+            if (!w->graph[w->cur] && (e = build_graph(w, w->cur)))
+                return cuda_fail(w, "mb_step(capture)", e);
+            if ((e = cudaGraphLaunch(w->graph[w->cur], w->stream))) return cuda_fail(w, "mb_step", e);
+        }
+        w->cur ^= 1;
+        w->time += 1;
+        w->frame_done = true;
+    }
+    return MB_OK;
+}
+
+mb_status mb_sync(mb_world* w) {
+    if (!w) return fail(nullptr, MB_ERR_INVALID_ARG, "world is NULL");
+    cudaError_t e = cudaStreamSynchronize(w->stream);
+    if (e) return cuda_fail(w, "mb_sync", e);
+    uint32_t flag = 0;
+    if ((e = cudaMemcpy(&flag, w->scratch.ctl + mb::kCtlError, sizeof(uint32_t), cudaMemcpyDeviceToHost)))
+        return cuda_fail(w, "mb_sync", e);
+    if (flag) {
+        cudaMemset(w->scratch.ctl + mb::kCtlError, 0, sizeof(uint32_t));
+        w->scratch.last_tiles = 0;  // force a clean look-back table next sort
+        drop_graphs(w);
+        return fail(w, MB_ERR_TIMEOUT, "sort look-back wait gave up; results of that frame are invalid");
+    }
+    return MB_OK;
+}
+
+mb_status mb_get_debug(mb_world* w, uint32_t* keys, uint32_t* perm, uint32_t* start, uint32_t* close,
+                       mb_memory where) {
+    if (!w) return fail(nullptr, MB_ERR_INVALID_ARG, "world is NULL");
+    if (!w->frame_done) return fail(w, MB_ERR_NOT_READY, "no frame has run since the upload");
+    cudaError_t e;
+    cudaMemcpyKind kind = where == MB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (keys && (e = cudaMemcpyAsync(keys, w->keys, sizeof(uint32_t) * w->n, kind, w->stream)))
+        return cuda_fail(w, "mb_get_debug", e);
+    if (perm && (e = cudaMemcpyAsync(perm, w->perm, sizeof(uint32_t) * w->n, kind, w->stream)))
+        return cuda_fail(w, "mb_get_debug", e);
+    if (start || close) {
+        if (where == MB_DEVICE) {
+            if ((e = mb::offsets_to_start_close(w->scratch.offs, w->cells, start, close, w->stream)))
+                return cuda_fail(w, "mb_get_debug", e);
+        } else {
+            std::vector<uint32_t> offs((size_t)w->cells + 1u);
+            if ((e = cudaMemcpyAsync(offs.data(), w->scratch.offs, sizeof(uint32_t) * offs.size(),
+                                     cudaMemcpyDeviceToHost, w->stream)))
+                return cuda_fail(w, "mb_get_debug", e);
+            if ((e = cudaStreamSynchronize(w->stream))) return cuda_fail(w, "mb_get_debug", e);
+            for (uint32_t c = 0; c < w->cells; ++c) {
+                bool full = offs[c + 1] > offs[c];
+                if (start) start[c] = full ? offs[c] : mb::kInvalid;
+                if (close) close[c] = full ? offs[c + 1] - 1u : mb::kInvalid;
+            }
+        }
+    }
+    if (where == MB_HOST && (e = cudaStreamSynchronize(w->stream))) return cuda_fail(w, "mb_get_debug", e);
+    return MB_OK;
+}
+
+mb_status mb_device_buffers(mb_world* w, const float** pos_scale, const uint32_t** vfme) {
+    if (!w) return fail(nullptr, MB_ERR_INVALID_ARG, "world is NULL");
+    if (pos_scale) *pos_scale = reinterpret_cast<const float*>(w->pos[w->cur]);
+    if (vfme) *vfme = reinterpret_cast<const uint32_t*>(w->vfme[w->cur]);
+    return MB_OK;
+}
+
+int64_t mb_time(const mb_world* w) { return w ? w->time : -1; }
+
+const char* mb_last_error(const mb_world* w) { return w ? w->err.c_str() : g_last_error.c_str(); }
+
+mb_status mb_get_tuning(const mb_world* w, mb_tuning* out) {
+    if (!w || !out) return MB_ERR_INVALID_ARG;
+    *out = w->tuning;
+    return MB_OK;
+}
+
+mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
+    if (!w || !t) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
+    if (t->digit_bits_max < 4 || t->digit_bits_max > mb::kMaxDigitBits)
+        return fail(w, MB_ERR_INVALID_ARG, "digit_bits_max must be in [4, 11]");
+    if (t->collide_block < 32 || t->collide_block > 256 || (t->collide_block & 31u))
+        return fail(w, MB_ERR_INVALID_ARG, "collide_block must be a multiple of 32 in [32, 256]");
+    drop_graphs(w);
+    w->tuning = *t;
+    w->sched = mb::make_schedule(w->n, w->cells, w->tuning.digit_bits_max);
+    return MB_OK;
+}
+
+// ------------------------------------------------------------------ stages
+struct mb_sort_plan {
+    mb::SortScratch scratch;
+    uint32_t digit_bits_max = 11;
+};
+
+mb_status mb_sort_plan_create(uint32_t max_keys, uint32_t max_cells, mb_sort_plan** out) {
+    if (!out) return fail(nullptr, MB_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (max_keys > mb::kMaxAgents || max_cells == 0 || max_cells > mb::kMaxCells)
+        return fail(nullptr, MB_ERR_INVALID_ARG, "max_keys must be < 2^28 and max_cells in [1, 2^28]");
+    mb_sort_plan* p = new (std::nothrow) mb_sort_plan();
+    if (!p) return fail(nullptr, MB_ERR_OOM, "host allocation failed");
+    cudaError_t e = mb::scratch_alloc(p->scratch, max_keys, max_cells);
+    if (e) {
+        mb::scratch_free(p->scratch);
+        delete p;
+        return cuda_fail(nullptr, "mb_sort_plan_create", e);
+    }
+    *out = p;
+    return MB_OK;
+}
+
+mb_status mb_sort_plan_destroy(mb_sort_plan* p) {
+    if (!p) return MB_OK;
+    cudaDeviceSynchronize();
+    mb::scratch_free(p->scratch);
+    delete p;
+    return MB_OK;
+}
+
+mb_status mb_sort_and_hash(mb_sort_plan* p, const uint32_t* keys, const uint32_t* vals, uint32_t n,
+                           uint32_t number_of_cells, uint32_t* sorted_keys, uint32_t* sorted_vals,
+                           uint32_t* start, uint32_t* close, void* cuda_stream) {
+    if (!p) return fail(nullptr, MB_ERR_INVALID_ARG, "plan is NULL");
+    if (n > p->scratch.max_keys || number_of_cells == 0 || number_of_cells > p->scratch.max_cells)
+        return fail(nullptr, MB_ERR_INVALID_ARG, "n or number_of_cells exceeds the plan");
+    if (n && (!keys || !sorted_keys || !sorted_vals))
+        return fail(nullptr, MB_ERR_INVALID_ARG, "NULL key/value buffer");
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    mb::SortSchedule sch = mb::make_schedule(n, number_of_cells, p->digit_bits_max);
+    cudaError_t e = mb::sort_and_offsets(p->scratch, sch, keys, vals, sorted_keys, sorted_vals, st);
+    if (e) return cuda_fail(nullptr, "mb_sort_and_hash", e);
+    if ((start || close) && (e = mb::offsets_to_start_close(p->scratch.offs, number_of_cells, start, close, st)))
+        return cuda_fail(nullptr, "mb_sort_and_hash", e);
+    return MB_OK;
+}
+
+mb_status mb_set_profiling(mb_world* w, int enable) {
+    if (!w) return fail(nullptr, MB_ERR_INVALID_ARG, "world is NULL");
+    if (enable) {
+        for (auto& ev : w->prof_ev) {
+            if (ev) continue;
+            cudaError_t e = cudaEventCreate(&ev);
+            if (e) return cuda_fail(w, "mb_set_profiling", e);
+        }
+    }
+    drop_graphs(w);
+    w->profiling = enable != 0;
+    return MB_OK;
+}
+
+mb_status mb_last_frame_times(mb_world* w, float* ms) {
+    if (!w || !ms) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
+    if (!w->profiling || !w->frame_done) return fail(w, MB_ERR_NOT_READY, "profiling off or no frame yet");
+    cudaError_t e = cudaEventSynchronize(w->prof_ev[3]);
+    if (e) return cuda_fail(w, "mb_last_frame_times", e);
+    for (int i = 0; i < 3; ++i) {
+        if ((e = cudaEventElapsedTime(&ms[i], w->prof_ev[i], w->prof_ev[i + 1])))
+            return cuda_fail(w, "mb_last_frame_times", e);
+    }
+    return MB_OK;
+}
+
+uint32_t mb_kernels_per_frame(const mb_world* w) {
+    // histogram + one onesweep kernel per digit pass + cell offsets + physics
+    return w ? (uint32_t)w->sched.passes + 3u : 0u;
+}
+
+const char* mb_version(void) { return "millionsball-gb300 " __DATE__ " sm_103a"; }
+
+}  // extern "C"

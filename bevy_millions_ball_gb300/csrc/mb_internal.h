@@ -1,0 +1,109 @@
+// mb_internal.h — host-side interfaces between the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/millionsball.h"
+
+namespace mb {
+
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+constexpr int kMaxPasses = 4;
+constexpr uint32_t kMaxDigitBits = 11;
+constexpr uint32_t kMaxRadix = 1u << kMaxDigitBits;
+constexpr uint32_t kMaxAgents = (1u << 28) - 1u;   // look-back words keep 28 value bits
+constexpr uint32_t kMaxCells = 1u << 28;
+
+// Onesweep tile shape: 256 threads x 16 keys.
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr uint32_t kSortTile = kSortThreads * kSortItems;
+
+// Control words of a sort plan (device u32 array).
+enum : int {
+    kCtlTile0 = 0,                // [kMaxPasses] tile tickets
+    kCtlDone = kMaxPasses,        // histogram blocks finished
+    kCtlError = kMaxPasses + 1,   // nonzero: a bounded wait gave up
+    kCtlEpoch = kMaxPasses + 2,   // look-back epoch of the running sort (1..3)
+    kCtlWords = 8
+};
+
+// Digit schedule of one sort: LSD first; the last (most significant) digit is
+// also the chunking of the cell-offset build.
+struct SortSchedule {
+    uint32_t n = 0;
+    uint32_t cells = 0;
+    uint32_t total_bits = 0;
+    int passes = 0;
+    uint32_t shift[kMaxPasses] = {0, 0, 0, 0};
+    uint32_t bits[kMaxPasses] = {0, 0, 0, 0};
+    uint32_t tiles = 0;
+};
+
+SortSchedule make_schedule(uint32_t n, uint32_t cells, uint32_t digit_bits_max);
+
+// Device scratch of the sort + cell-offset build, sized for (max_keys, max_cells).
+struct SortScratch {
+    uint32_t max_keys = 0;
+    uint32_t max_cells = 0;
+    uint32_t* alt_keys = nullptr;   // [max_keys]
+    uint32_t* alt_vals = nullptr;   // [max_keys]
+    uint32_t* counts = nullptr;     // [kMaxPasses][kMaxRadix]   digit counts, zero between sorts
+    uint32_t* bases = nullptr;      // [kMaxPasses][kMaxRadix+1] exclusive digit bases
+    uint32_t* lookback = nullptr;   // [kMaxPasses][tiles_max * kMaxRadix]
+    uint32_t* ctl = nullptr;        // [kCtlWords]
+    uint32_t* offs = nullptr;       // [max_cells + 1] cell offsets (CSR)
+    size_t lookback_words_per_pass = 0;
+    uint32_t last_tiles = 0;        // tiles of the previous sort (look-back reuse check)
+    int last_passes = 0;
+};
+
+cudaError_t scratch_alloc(SortScratch& s, uint32_t max_keys, uint32_t max_cells);
+void scratch_free(SortScratch& s);
+
+// Stable sort of (keys, vals or iota) -> (sorted_keys, sorted_vals).
+cudaError_t sort_pairs(SortScratch& s, const SortSchedule& sch, const uint32_t* keys,
+                       const uint32_t* vals, uint32_t* sorted_keys, uint32_t* sorted_vals,
+                       cudaStream_t st);
+// Cell offsets offs[c] = number of keys < c for c in [0, cells], from the sorted
+// keys and the most significant digit's bases of the sort that produced them.
+cudaError_t cell_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t* sorted_keys,
+                         cudaStream_t st);
+// sort_pairs then cell_offsets.
+cudaError_t sort_and_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t* keys,
+                             const uint32_t* vals, uint32_t* sorted_keys, uint32_t* sorted_vals,
+                             cudaStream_t st);
+
+// start/close tables (spatial_hashing.wgsl semantics) from cell offsets.
+cudaError_t offsets_to_start_close(const uint32_t* offs, uint32_t cells, uint32_t* start,
+                                   uint32_t* close, cudaStream_t st);
+
+// Physics constants as kernel parameters.
+struct PhysParams {
+    uint32_t N;
+    uint32_t grid_size;
+    float half_map_size;
+    float half_map_height;
+    float gx, gy, gz;
+    float e_envir, e_agent, k_agent, c_agent, r_agent, dt;
+    float neg_c_over_dt;      // -C_AGENT / T_DELTA
+    float neg_1pe_over_dt;    // -(1 + E_ENVIR) / T_DELTA
+    uint32_t spring;
+};
+
+PhysParams make_params(const mb_consts& c);
+
+cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t* perm,
+                                const float4* pos_in, const uint4* vfme_in, float4* pos_out,
+                                uint4* vfme_out, uint32_t* keys_out, cudaStream_t st);
+cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* perm,
+                                const uint32_t* offs, const float4* pos_in, const uint4* vfme_in,
+                                float4* pos_out, uint4* vfme_out, uint32_t* keys_out, int block,
+                                cudaStream_t st);
+cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,
+                         cudaStream_t st);
+
+int device_sm_count();
+
+}  // namespace mb

@@ -1,0 +1,330 @@
+// mb_physics.cu — INIT / LOOP physics pass (fused Verlet + neighbour-stencil
+// contacts + jitter + wall constraint + f16 pack + next cell key).
+//
+// Restates src/physics/physics.wgsl:57-337 as CUDA for sm_103a.  This translation
+// unit is compiled with --fmad=false and IEEE division / square root so every
+// arithmetic step rounds exactly like the WGSL expression it follows; with that,
+// positions, packed velocities and keys are bit-identical to the CPU oracle.
+//
+// Neighbour ranges come from cell offsets (offs[c] = number of agents in cells
+// < c): the reference's three-cell merge with its INVALID-skipping logic
+// (physics.wgsl:122-147, 171-206) always yields [offs[first], offs[last + 1]),
+// because empty cells have zero width.
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "mb_internal.h"
+
+namespace mb {
+namespace {
+
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ V3 operator*(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ V3 operator/(V3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ V3 splat(float s) { return {s, s, s}; }
+__device__ __forceinline__ float dot3(V3 a, V3 b) {
+    float xx = a.x * b.x;
+    float yy = a.y * b.y;
+    float zz = a.z * b.z;
+    return (xx + yy) + zz;
+}
+__device__ __forceinline__ float len3(V3 a) { return sqrtf(dot3(a, a)); }
+__device__ __forceinline__ V3 normalize3(V3 a) { return a / len3(a); }
+
+// WGSL min/max: "e2 if e2 < e1 (resp. >), else e1; a NaN operand yields the other".
+__device__ __forceinline__ float wmin(float a, float b) {
+    if (isnan(a)) return b;
+    if (isnan(b)) return a;
+    return b < a ? b : a;
+}
+__device__ __forceinline__ float wmax(float a, float b) {
+    if (isnan(a)) return b;
+    if (isnan(b)) return a;
+    return b > a ? b : a;
+}
+__device__ __forceinline__ float wclamp(float e, float lo, float hi) { return wmin(wmax(e, lo), hi); }
+__device__ __forceinline__ float wsign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+
+struct Agent {  // physics.wgsl:208-215
+    V3 position;
+    float scale;
+    V3 velocity;
+    float massv;
+    V3 force;
+};
+
+__device__ __forceinline__ float h2f(uint32_t bits16) {
+    return __half2float(__ushort_as_half((unsigned short)bits16));
+}
+__device__ __forceinline__ uint32_t f2h(float f) { return (uint32_t)__half_as_ushort(__float2half_rn(f)); }
+
+// agent_new + unpack_vfme (physics.wgsl:217-233, 244-253)
+__device__ __forceinline__ Agent unpack(float4 p, uint4 q) {
+    Agent a;
+    a.position = {p.x, p.y, p.z};
+    a.scale = p.w;
+    a.velocity = {h2f(q.x & 0xFFFFu), h2f(q.x >> 16), h2f(q.y & 0xFFFFu)};
+    a.force = {h2f(q.y >> 16), h2f(q.z & 0xFFFFu), h2f(q.z >> 16)};
+    a.massv = h2f(q.w & 0xFFFFu);
+    return a;
+}
+
+// pack_vfme (physics.wgsl:235-242)
+__device__ __forceinline__ uint4 pack(const Agent& a) {
+    uint4 q;
+    q.x = f2h(a.velocity.x) | (f2h(a.velocity.y) << 16);
+    q.y = f2h(a.velocity.z) | (f2h(a.force.x) << 16);
+    q.z = f2h(a.force.y) | (f2h(a.force.z) << 16);
+    q.w = f2h(a.massv) | (f2h(0.0f) << 16);
+    return q;
+}
+
+// get_collision_grid_id (physics.wgsl:107-109): saturating f32->u32, integer
+// division by GRID_SIZE; clamped to the border cell for positions off the map.
+__device__ __forceinline__ void cell_of(const PhysParams& P, float x, float z, uint32_t& cx,
+                                        uint32_t& cz) {
+    cx = __float2uint_rz(x + P.half_map_size) / P.grid_size;
+    cz = __float2uint_rz(z + P.half_map_size) / P.grid_size;
+    cx = min(cx, P.N - 1u);
+    cz = min(cz, P.N - 1u);
+}
+
+// solve_sphere_constraint (physics.wgsl:300-331)
+__device__ __forceinline__ void sphere(const PhysParams& P, Agent& a, const Agent& b) {
+    float edge = b.scale + a.scale;
+    V3 tpos = a.position - b.position;
+    float dist = len3(tpos);
+    if (dist <= edge) {
+        V3 norm = normalize3(tpos);
+        if (!P.spring) {
+            float m1 = a.massv, m2 = b.massv;
+            V3 rvel = a.velocity - b.velocity;
+            float rspd = dot3(rvel, norm);
+            if (rspd < 0.0f) {
+                V3 rvel_n = rspd * norm;
+                float e_m2 = P.e_agent * m2;
+                float num = m1 - e_m2;
+                float den = m1 + m2;
+                V3 rvel_c = (num * rvel_n) / den;
+                a.velocity = (b.velocity + (rvel - rvel_n)) + rvel_c;
+            }
+            float h = 0.5f * (edge - dist);
+            a.position = a.position + h * norm;
+        } else {
+            float makeup = edge - dist;
+            V3 kforce = (P.k_agent * makeup) * norm;
+            V3 cforce = P.neg_c_over_dt * a.velocity;
+            a.force = a.force + (kforce + cforce);
+            float limit = makeup - P.r_agent * a.scale;
+            if (limit > 0.0f) a.position = a.position + limit * norm;
+        }
+    }
+}
+
+// solve_cube_constraint (physics.wgsl:269-298)
+__device__ __forceinline__ void cube(const PhysParams& P, Agent& a) {
+    V3 edge = V3{P.half_map_size, P.half_map_height, P.half_map_size} - splat(a.scale);
+    V3 cetr = {0.0f, P.half_map_height, 0.0f};
+    V3 tpos = a.position - cetr;
+    V3 makeup = {edge.x - fabsf(tpos.x), edge.y - fabsf(tpos.y), edge.z - fabsf(tpos.z)};
+    bool tx = makeup.x < 0.0f, ty = makeup.y < 0.0f, tz = makeup.z < 0.0f;
+    if (!(tx || ty || tz)) return;
+    if (!P.spring) {
+        a.position = V3{wclamp(tpos.x, -edge.x, edge.x), wclamp(tpos.y, -edge.y, edge.y),
+                        wclamp(tpos.z, -edge.z, edge.z)} + cetr;
+        float ne = -P.e_envir;
+        V3 f = {tx ? ne : 1.0f, ty ? ne : 1.0f, tz ? ne : 1.0f};
+        a.velocity = a.velocity * f;
+    } else {
+        float mm = -(a.scale * P.r_agent);
+        V3 sgn = {wsign(tpos.x), wsign(tpos.y), wsign(tpos.z)};
+        V3 kforce = (P.k_agent * sgn) *
+                    V3{wclamp(makeup.x, mm, 0.0f), wclamp(makeup.y, mm, 0.0f), wclamp(makeup.z, mm, 0.0f)};
+        V3 cforce = P.neg_c_over_dt * a.velocity;
+        a.force = a.force + (kforce + cforce);
+        bool ux = makeup.x < mm, uy = makeup.y < mm, uz = makeup.z < mm;
+        if (ux || uy || uz) {
+            V3 e2 = edge - splat(mm);
+            a.position = V3{wclamp(tpos.x, -e2.x, e2.x), wclamp(tpos.y, -e2.y, e2.y),
+                            wclamp(tpos.z, -e2.z, e2.z)} + cetr;
+            V3 sel = {ux ? a.velocity.x : 0.0f, uy ? a.velocity.y : 0.0f, uz ? a.velocity.z : 0.0f};
+            V3 dv = P.neg_1pe_over_dt * sel;
+            V3 acc = dv / P.dt;
+            a.force = a.force + a.massv * acc;
+        }
+    }
+}
+
+// Contacts against the candidate slots [lo, hi), skipping `skip`.
+__device__ __forceinline__ void contacts(const PhysParams& P, Agent& a, uint32_t lo, uint32_t hi,
+                                         uint32_t skip, const uint32_t* __restrict__ perm,
+                                         const float4* __restrict__ pos_in,
+                                         const uint4* __restrict__ vfme_in) {
+    if (lo >= hi) return;
+    uint32_t old = __ldg(perm + lo);
+    for (uint32_t j = lo; j < hi; ++j) {
+        uint32_t nxt = (j + 1u < hi) ? __ldg(perm + j + 1u) : 0u;
+        if (j != skip) {
+            float4 p = __ldg(pos_in + old);
+            uint4 q = __ldg(vfme_in + old);
+            sphere(P, a, unpack(p, q));
+        }
+        old = nxt;
+    }
+}
+
+// main, INIT pipeline (physics.wgsl:91-96): gather through perm, re-pack, emit key.
+__global__ void __launch_bounds__(256)
+    k_physics_init(PhysParams P, uint32_t n, const uint32_t* __restrict__ perm,
+                   const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in,
+                   float4* __restrict__ pos_out, uint4* __restrict__ vfme_out,
+                   uint32_t* __restrict__ keys_out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t old = perm[i];
+    float4 p = pos_in[old];
+    Agent a = unpack(p, vfme_in[old]);
+    uint32_t cx, cz;
+    cell_of(P, a.position.x, a.position.z, cx, cz);
+    pos_out[i] = make_float4(a.position.x, a.position.y, a.position.z, a.scale);
+    vfme_out[i] = pack(a);
+    keys_out[i] = cz * P.N + cx;
+}
+
+// main, LOOP pipeline (physics.wgsl:57-89), one thread per sorted slot.
+__global__ void __launch_bounds__(256)
+    k_physics_loop(PhysParams P, uint32_t n, const uint32_t* __restrict__ perm,
+                   const uint32_t* __restrict__ offs, const float4* __restrict__ pos_in,
+                   const uint4* __restrict__ vfme_in, float4* __restrict__ pos_out,
+                   uint4* __restrict__ vfme_out, uint32_t* __restrict__ keys_out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t old = __ldg(perm + i);
+    Agent a = unpack(__ldg(pos_in + old), __ldg(vfme_in + old));
+    uint32_t cx, cz;
+    cell_of(P, a.position.x, a.position.z, cx, cz);
+    const uint32_t N = P.N;
+    const uint32_t key = cz * N + cx;
+    const uint32_t l = cx > 0u ? 1u : 0u, r = cx < N - 1u ? 2u : 1u;
+
+    // neighbour ranges (independent loads, issued before the integration math)
+    uint32_t m_lo = __ldg(offs + key - l), m_hi = __ldg(offs + key + r);
+    uint32_t b_lo = 0, b_hi = 0, t_lo = 0, t_hi = 0;
+    if (cz > 0u) {
+        b_lo = __ldg(offs + key - N - l);
+        b_hi = __ldg(offs + key - N + r);
+    }
+    if (cz < N - 1u) {
+        t_lo = __ldg(offs + key + N - l);
+        t_hi = __ldg(offs + key + N + r);
+    }
+
+    // verlet_integration (physics.wgsl:262-266)
+    {
+        V3 acc = a.force / a.massv;
+        a.velocity = a.velocity + ((V3{P.gx, P.gy, P.gz} + acc) * P.dt) * P.dt;
+        a.position = a.position + a.velocity;
+    }
+    a.force = splat(0.0f);
+
+    // handle_collisions (physics.wgsl:119-169)
+    V3 old_pos = a.position;
+    contacts(P, a, m_lo, m_hi, i, perm, pos_in, vfme_in);
+    contacts(P, a, b_lo, b_hi, 0xFFFFFFFFu, perm, pos_in, vfme_in);
+    contacts(P, a, t_lo, t_hi, 0xFFFFFFFFu, perm, pos_in, vfme_in);
+    V3 diff = a.position - old_pos;
+    if (len3(diff) > a.scale) {
+        // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337)
+        uint32_t v = i * (i ^ (i >> 15));
+        const float d = 4294967296.0f;
+        V3 h = {__uint2float_rn(v * 0x1u) / d, __uint2float_rn(v * 0x1FFu) / d,
+                __uint2float_rn(v * 0x3FFFFu) / d};
+        V3 jitter = {h.x * 2.0f - 1.0f, h.y * 2.0f - 1.0f, h.z * 2.0f - 1.0f};
+        a.position = a.position + normalize3(jitter);
+    }
+
+    cube(P, a);
+
+    const float lim = 65504.0f;  // CLAMP_F16
+    a.velocity = {wclamp(a.velocity.x, -lim, lim), wclamp(a.velocity.y, -lim, lim),
+                  wclamp(a.velocity.z, -lim, lim)};
+    a.force = {wclamp(a.force.x, -lim, lim), wclamp(a.force.y, -lim, lim), wclamp(a.force.z, -lim, lim)};
+
+    pos_out[i] = make_float4(a.position.x, a.position.y, a.position.z, a.scale);
+    vfme_out[i] = pack(a);
+    uint32_t nx, nz;
+    cell_of(P, a.position.x, a.position.z, nx, nz);
+    keys_out[i] = nz * N + nx;
+}
+
+__global__ void k_rekey(PhysParams P, uint32_t n, const float4* __restrict__ pos,
+                        uint32_t* __restrict__ keys) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos[i];
+    uint32_t cx, cz;
+    cell_of(P, p.x, p.z, cx, cz);
+    keys[i] = cz * P.N + cx;
+}
+
+}  // namespace
+
+PhysParams make_params(const mb_consts& c) {
+    PhysParams p;
+    p.N = c.number_of_grids_one_dimension;
+    p.grid_size = c.grid_size;
+    p.half_map_size = c.half_map_size;
+    p.half_map_height = c.half_map_height;
+    p.gx = c.gravity[0];
+    p.gy = c.gravity[1];
+    p.gz = c.gravity[2];
+    p.e_envir = c.e_envir;
+    p.e_agent = c.e_agent;
+    p.k_agent = c.k_agent;
+    p.c_agent = c.c_agent;
+    p.r_agent = c.r_agent;
+    p.dt = c.time_delta;
+    // const-folded in the shader (physics.wgsl:285, 292): one f32 division each
+    volatile float nc = -c.c_agent;
+    volatile float n1pe = -(1.0f + c.e_envir);
+    p.neg_c_over_dt = nc / c.time_delta;
+    p.neg_1pe_over_dt = n1pe / c.time_delta;
+    p.spring = c.enable_spring;
+    return p;
+}
+
+cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t* perm,
+                                const float4* pos_in, const uint4* vfme_in, float4* pos_out,
+                                uint4* vfme_out, uint32_t* keys_out, cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    k_physics_init<<<(n + 255u) / 256u, 256, 0, st>>>(p, n, perm, pos_in, vfme_in, pos_out, vfme_out,
+                                                      keys_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* perm,
+                                const uint32_t* offs, const float4* pos_in, const uint4* vfme_in,
+                                float4* pos_out, uint4* vfme_out, uint32_t* keys_out, int block,
+                                cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    if (block <= 0 || block > 256 || (block & 31)) block = 128;
+    k_physics_loop<<<(n + (uint32_t)block - 1u) / (uint32_t)block, block, 0, st>>>(
+        p, n, perm, offs, pos_in, vfme_in, pos_out, vfme_out, keys_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,
+                         cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    k_rekey<<<(n + 255u) / 256u, 256, 0, st>>>(p, n, pos, keys);
+    return cudaGetLastError();
+}
+
+}  // namespace mb

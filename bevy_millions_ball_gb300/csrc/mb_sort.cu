@@ -1,0 +1,488 @@
+// mb_sort.cu — onesweep LSD radix sort of cell keys + cell-offset build.
+//
+// Replaces the external bevy_radix_sort crate (called at src/physics/mod.rs:880-890
+// with pass range 0..3, vals = iota) and the spatial-hashing passes
+// (src/physics/spatial_hashing.wgsl:29-70).
+//
+// Sort: one histogram kernel computes the digit counts of every pass in a single
+// read of the keys and the exclusive digit bases (last-block-done scan).  Each
+// pass is one onesweep kernel: a block takes the next tile (atomic ticket), ranks
+// its keys per warp with match.any (stable: warp-striped order, warps in order),
+// publishes per-digit tile counts into a look-back table, resolves its global
+// digit offsets by decoupled look-back over predecessor tiles, stages the tile in
+// shared memory in digit order and writes it out in contiguous runs.
+//
+// Cell offsets: offs[c] = number of keys < c, c in [0, cells].  One block per value
+// of the most significant digit: that digit's keys occupy the contiguous slot
+// range [base[d], base[d+1]) and cover a contiguous block of cells, so every
+// cell's offset is a lower_bound into at most one chunk, done in shared memory.
+// start[c] / close[c] of the reference are offs[c] / offs[c+1]-1 for non-empty
+// cells.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "mb_internal.h"
+
+namespace mb {
+namespace {
+
+constexpr uint32_t kFlagAggregate = 1u;
+constexpr uint32_t kFlagPrefix = 2u;
+constexpr uint32_t kValueMask = (1u << 28) - 1u;
+constexpr uint32_t kSpinLimit = 1u << 21;
+
+__device__ __forceinline__ uint32_t lb_pack(uint32_t flag, uint32_t epoch, uint32_t value) {
+    return (flag << 30) | ((epoch & 3u) << 28) | (value & kValueMask);
+}
+
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+struct HistParams {
+    int passes;
+    uint32_t shift[kMaxPasses];
+    uint32_t bits[kMaxPasses];
+    uint32_t hist_off[kMaxPasses];   // offset of each pass inside the shared histogram
+    uint32_t total_bins;
+};
+
+// ---------------------------------------------------------------- histogram
+// Digit counts of every pass in one read of the keys; the block that finishes
+// last turns the counts into exclusive bases and zeroes them for the next sort.
+__global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n,
+                                                   HistParams hp, uint32_t* counts,
+                                                   uint32_t* bases, uint32_t* ctl) {
+    extern __shared__ uint32_t s_hist[];
+    __shared__ uint32_t s_last;
+    __shared__ uint32_t s_warp[16];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    for (uint32_t b = tid; b < hp.total_bins; b += blockDim.x) s_hist[b] = 0;
+    if (blockIdx.x == 0 && tid < (uint32_t)kMaxPasses) ctl[kCtlTile0 + tid] = 0;
+    __syncthreads();
+
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        uint32_t i = i0 + tid;
+        bool valid = i < n;
+        uint32_t key = valid ? __ldg(keys + i) : 0u;
+        for (int p = 0; p < hp.passes; ++p) {
+            uint32_t d = valid ? ((key >> hp.shift[p]) & ((1u << hp.bits[p]) - 1u)) : 0xFFFFFFFFu;
+            uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+            if (valid && lane == (uint32_t)(__ffs(peers) - 1))
+                atomicAdd(&s_hist[hp.hist_off[p] + d], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+    for (int p = 0; p < hp.passes; ++p) {
+        uint32_t R = 1u << hp.bits[p];
+        for (uint32_t d = tid; d < R; d += blockDim.x) {
+            uint32_t c = s_hist[hp.hist_off[p] + d];
+            if (c) atomicAdd(&counts[p * kMaxRadix + d], c);
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = (atomicAdd(&ctl[kCtlDone], 1u) == gridDim.x - 1u) ? 1u : 0u;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+
+    // exclusive scan of each pass's counts (blockDim.x threads, consecutive bins)
+    const uint32_t nt = blockDim.x, warp = tid >> 5, nwarps = nt >> 5;
+    for (int p = 0; p < hp.passes; ++p) {
+        uint32_t R = 1u << hp.bits[p];
+        uint32_t per = (R + nt - 1u) / nt;
+        uint32_t beg = min(R, tid * per), end = min(R, beg + per);
+        uint32_t sum = 0;
+        for (uint32_t d = beg; d < end; ++d) sum += __ldcg(&counts[p * kMaxRadix + d]);
+        uint32_t incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        if (lane == 31u) s_warp[warp] = incl;
+        __syncthreads();
+        uint32_t wbase = 0;
+        for (uint32_t w = 0; w < warp; ++w) wbase += s_warp[w];
+        uint32_t run = wbase + incl - sum;
+        for (uint32_t d = beg; d < end; ++d) {
+            uint32_t c = __ldcg(&counts[p * kMaxRadix + d]);
+            bases[p * (kMaxRadix + 1) + d] = run;
+            run += c;
+            counts[p * kMaxRadix + d] = 0;
+        }
+        if (tid == 0) bases[p * (kMaxRadix + 1) + R] = n;
+        __syncthreads();
+        (void)nwarps;
+    }
+    if (tid == 0) {
+        ctl[kCtlDone] = 0;
+        ctl[kCtlEpoch] = ctl[kCtlEpoch] % 3u + 1u;  // new look-back epoch for this sort
+    }
+}
+
+// ---------------------------------------------------------------- onesweep pass
+template <int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS)
+    k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+               uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
+               uint32_t shift, uint32_t bits, const uint32_t* __restrict__ bases,
+               uint32_t* lookback, uint32_t* tile_ticket, uint32_t* err, const uint32_t* epoch_word) {
+    constexpr int WARPS = THREADS / 32;
+    constexpr uint32_t TILE = THREADS * ITEMS;
+    const uint32_t R = 1u << bits, mask = R - 1u;
+    extern __shared__ uint4 smem_raw[];
+    uint32_t* s_keys = reinterpret_cast<uint32_t*>(smem_raw);  // [TILE]
+    uint32_t* s_vals = s_keys + TILE;                            // [TILE]
+    uint32_t* s_cnt = s_vals + TILE;                             // [R] tile count -> local excl
+    uint32_t* s_goff = s_cnt + R;                                // [R] global base of the tile
+    uint16_t* s_whist = reinterpret_cast<uint16_t*>(s_goff + R); // [WARPS][R]
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_wsum[WARPS];
+
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    __shared__ uint32_t s_epoch;
+    if (tid == 0) {
+        s_tile = atomicAdd(tile_ticket, 1u);
+        s_epoch = __ldcg(epoch_word);
+    }
+    {
+        uint32_t* wz = reinterpret_cast<uint32_t*>(s_whist);
+        for (uint32_t i = tid; i < (uint32_t)WARPS * R / 2u; i += THREADS) wz[i] = 0u;
+    }
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t epoch = s_epoch;
+    const uint32_t wbase = tile * TILE + warp * 32u * ITEMS;
+
+    uint32_t k[ITEMS], v[ITEMS], rank[ITEMS];
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        uint32_t idx = wbase + (uint32_t)j * 32u + lane;
+        bool valid = idx < n;
+        k[j] = valid ? __ldg(keys_in + idx) : 0u;
+        v[j] = vals_in ? (valid ? __ldg(vals_in + idx) : 0u) : idx;
+    }
+
+    // per-warp stable ranking
+    uint16_t* wh = s_whist + warp * R;
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        uint32_t idx = wbase + (uint32_t)j * 32u + lane;
+        bool valid = idx < n;
+        uint32_t d = valid ? ((k[j] >> shift) & mask) : 0xFFFFFFFFu;
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        uint32_t b = valid ? (uint32_t)wh[d] : 0u;
+        rank[j] = b + (uint32_t)__popc(peers & lt);
+        __syncwarp();
+        if (valid && lane == (uint32_t)(__ffs(peers) - 1)) wh[d] = (uint16_t)(b + __popc(peers));
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // per digit: exclusive scan across warps, tile count, publish to look-back
+    uint32_t* lb_tile = lookback + (size_t)tile * R;
+    for (uint32_t d = tid; d < R; d += THREADS) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < WARPS; ++w) {
+            uint32_t c = s_whist[w * R + d];
+            s_whist[w * R + d] = (uint16_t)run;
+            run += c;
+        }
+        s_cnt[d] = run;
+        st_relaxed(lb_tile + d, lb_pack(tile == 0 ? kFlagPrefix : kFlagAggregate, epoch, run));
+    }
+    __syncthreads();
+
+    // decoupled look-back: exclusive prefix of this digit over all earlier tiles
+    bool gave_up = false;
+    for (uint32_t d = tid; d < R; d += THREADS) {
+        uint32_t cnt = s_cnt[d];
+        uint32_t excl = 0;
+        if (tile > 0) {
+            int32_t t = (int32_t)tile - 1;
+            uint32_t spins = 0;
+            while (t >= 0) {
+                uint32_t e = ld_relaxed(lookback + (size_t)t * R + d);
+                uint32_t f = e >> 30;
+                if (f == 0u || ((e >> 28) & 3u) != (epoch & 3u)) {
+                    if (gave_up || ++spins > kSpinLimit) {
+                        if (!gave_up) atomicOr(err, 1u);
+                        gave_up = true;
+                        break;
+                    }
+                    if (spins > 64u) __nanosleep(64);
+                    continue;
+                }
+                excl += e & kValueMask;
+                if (f == kFlagPrefix) break;
+                --t;
+            }
+            st_relaxed(lb_tile + d, lb_pack(kFlagPrefix, epoch, excl + cnt));
+        }
+        s_goff[d] = __ldg(bases + d) + excl;
+    }
+    __syncthreads();
+
+    // block-wide exclusive scan of the tile counts (consecutive digits per thread)
+    {
+        uint32_t per = (R + THREADS - 1u) / THREADS;
+        uint32_t beg = min(R, tid * per), end = min(R, beg + per);
+        uint32_t sum = 0;
+        for (uint32_t d = beg; d < end; ++d) sum += s_cnt[d];
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        if (lane == 31u) s_wsum[warp] = incl;
+        __syncthreads();
+        uint32_t run = incl - sum;
+        for (uint32_t w = 0; w < warp; ++w) run += s_wsum[w];
+        for (uint32_t d = beg; d < end; ++d) {
+            uint32_t c = s_cnt[d];
+            s_cnt[d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+
+    // stage in digit order
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        uint32_t idx = wbase + (uint32_t)j * 32u + lane;
+        if (idx < n) {
+            uint32_t d = (k[j] >> shift) & mask;
+            uint32_t lpos = s_cnt[d] + (uint32_t)s_whist[warp * R + d] + rank[j];
+            s_keys[lpos] = k[j];
+            s_vals[lpos] = v[j];
+        }
+    }
+    __syncthreads();
+
+    // contiguous runs out
+    const uint32_t tile_begin = tile * TILE;
+    const uint32_t tile_n = (tile_begin < n) ? min(TILE, n - tile_begin) : 0u;
+    for (uint32_t i = tid; i < tile_n; i += THREADS) {
+        uint32_t key = s_keys[i];
+        uint32_t d = (key >> shift) & mask;
+        uint32_t pos = s_goff[d] + (i - s_cnt[d]);
+        keys_out[pos] = key;
+        vals_out[pos] = s_vals[i];
+    }
+}
+
+// ---------------------------------------------------------------- cell offsets
+constexpr int kOffsThreads = 256;
+constexpr uint32_t kOffsBatch = 1024;
+
+__global__ void __launch_bounds__(kOffsThreads)
+    k_cell_offsets(const uint32_t* __restrict__ sorted_keys, uint32_t cells, uint32_t chunk_shift,
+                   uint32_t chunks, const uint32_t* __restrict__ top_bases, uint32_t* offs) {
+    __shared__ uint32_t s_k[kOffsBatch];
+    const uint32_t d = blockIdx.x;
+    const uint64_t cell_lo64 = (uint64_t)d << chunk_shift;
+    if (cell_lo64 > cells) return;
+    const uint32_t cell_lo = (uint32_t)cell_lo64;
+    uint64_t hi64 = (uint64_t)(d + 1u) << chunk_shift;
+    uint32_t cell_hi = (d == chunks - 1u || hi64 > (uint64_t)cells + 1u) ? cells + 1u : (uint32_t)hi64;
+    const uint32_t slot_lo = __ldg(top_bases + d), slot_hi = __ldg(top_bases + d + 1u);
+    uint32_t next_cell = cell_lo;
+    for (uint32_t p0 = slot_lo; p0 < slot_hi; p0 += kOffsBatch) {
+        uint32_t cnt = min(kOffsBatch, slot_hi - p0);
+        for (uint32_t i = threadIdx.x; i < cnt; i += kOffsThreads) s_k[i] = __ldg(sorted_keys + p0 + i);
+        __syncthreads();
+        uint32_t last = min(s_k[cnt - 1u], cells);  // keys >= cells are a caller error; stay in bounds
+        for (uint32_t c = next_cell + threadIdx.x; c <= last; c += kOffsThreads) {
+            uint32_t lo = 0, hi = cnt;  // first index with s_k[idx] >= c
+            while (lo < hi) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (s_k[mid] < c) lo = mid + 1u;
+                else hi = mid;
+            }
+            offs[c] = p0 + lo;
+        }
+        next_cell = last + 1u;
+        __syncthreads();
+    }
+    for (uint32_t c = next_cell + threadIdx.x; c < cell_hi; c += kOffsThreads) offs[c] = slot_hi;
+}
+
+__global__ void k_offs_to_start_close(const uint32_t* __restrict__ offs, uint32_t cells,
+                                      uint32_t* start, uint32_t* close) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cells) return;
+    uint32_t a = offs[c], b = offs[c + 1u];
+    bool full = b > a;
+    if (start) start[c] = full ? a : kInvalid;
+    if (close) close[c] = full ? b - 1u : kInvalid;
+}
+
+size_t onesweep_smem(uint32_t R) {
+    return sizeof(uint32_t) * (2u * kSortTile + 2u * R) + sizeof(uint16_t) * (kSortThreads / 32) * R;
+}
+
+}  // namespace
+
+int device_sm_count() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
+SortSchedule make_schedule(uint32_t n, uint32_t cells, uint32_t digit_bits_max) {
+    SortSchedule s;
+    s.n = n;
+    s.cells = cells;
+    uint32_t dmax = std::min<uint32_t>(std::max<uint32_t>(digit_bits_max, 4u), kMaxDigitBits);
+    uint32_t bits = 1;
+    while (bits < 32u && (1ull << bits) < (uint64_t)cells) ++bits;
+    s.total_bits = bits;
+    uint32_t last = std::min(bits, dmax);
+    uint32_t rest = bits - last;
+    int prest = (int)((rest + dmax - 1u) / dmax);
+    s.passes = prest + 1;
+    uint32_t shift = 0;
+    for (int p = 0; p < prest; ++p) {
+        uint32_t b = rest / (uint32_t)prest + ((uint32_t)p < rest % (uint32_t)prest ? 1u : 0u);
+        s.shift[p] = shift;
+        s.bits[p] = b;
+        shift += b;
+    }
+    s.shift[prest] = shift;
+    s.bits[prest] = last;
+    s.tiles = (n + kSortTile - 1u) / kSortTile;
+    return s;
+}
+
+cudaError_t scratch_alloc(SortScratch& s, uint32_t max_keys, uint32_t max_cells) {
+    s.max_keys = max_keys;
+    s.max_cells = max_cells;
+    size_t tiles = (max_keys + kSortTile - 1u) / kSortTile;
+    if (tiles == 0) tiles = 1;
+    s.lookback_words_per_pass = tiles * kMaxRadix;
+    cudaError_t e;
+    if ((e = cudaMalloc(&s.alt_keys, sizeof(uint32_t) * std::max<uint32_t>(max_keys, 1u)))) return e;
+    if ((e = cudaMalloc(&s.alt_vals, sizeof(uint32_t) * std::max<uint32_t>(max_keys, 1u)))) return e;
+    if ((e = cudaMalloc(&s.counts, sizeof(uint32_t) * kMaxPasses * kMaxRadix))) return e;
+    if ((e = cudaMalloc(&s.bases, sizeof(uint32_t) * kMaxPasses * (kMaxRadix + 1)))) return e;
+    if ((e = cudaMalloc(&s.lookback, sizeof(uint32_t) * kMaxPasses * s.lookback_words_per_pass))) return e;
+    if ((e = cudaMalloc(&s.ctl, sizeof(uint32_t) * kCtlWords))) return e;
+    if ((e = cudaMalloc(&s.offs, sizeof(uint32_t) * ((size_t)max_cells + 1u)))) return e;
+    if ((e = cudaMemset(s.counts, 0, sizeof(uint32_t) * kMaxPasses * kMaxRadix))) return e;
+    if ((e = cudaMemset(s.lookback, 0, sizeof(uint32_t) * kMaxPasses * s.lookback_words_per_pass))) return e;
+    if ((e = cudaMemset(s.ctl, 0, sizeof(uint32_t) * kCtlWords))) return e;
+    if ((e = cudaFuncSetAttribute(k_onesweep<kSortThreads, kSortItems>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)onesweep_smem(kMaxRadix))))
+        return e;
+    s.last_tiles = 0;
+    s.last_passes = 0;
+    return cudaSuccess;
+}
+
+void scratch_free(SortScratch& s) {
+    cudaFree(s.alt_keys);
+    cudaFree(s.alt_vals);
+    cudaFree(s.counts);
+    cudaFree(s.bases);
+    cudaFree(s.lookback);
+    cudaFree(s.ctl);
+    cudaFree(s.offs);
+    s = SortScratch();
+}
+
+cudaError_t sort_pairs(SortScratch& s, const SortSchedule& sch, const uint32_t* keys,
+                       const uint32_t* vals, uint32_t* sorted_keys, uint32_t* sorted_vals,
+                       cudaStream_t st) {
+    const uint32_t n = sch.n;
+    if (n == 0) return cudaSuccess;
+    // look-back words are reused across sorts with an epoch tag; a different
+    // tile count or pass count could leave same-epoch words from older sorts.
+    if (sch.tiles != s.last_tiles || sch.passes != s.last_passes) {
+        cudaError_t e = cudaMemsetAsync(s.lookback, 0,
+                                        sizeof(uint32_t) * kMaxPasses * s.lookback_words_per_pass, st);
+        if (e) return e;
+        if ((e = cudaMemsetAsync(s.ctl + kCtlEpoch, 0, sizeof(uint32_t), st))) return e;
+        s.last_tiles = sch.tiles;
+        s.last_passes = sch.passes;
+    }
+
+    HistParams hp;
+    hp.passes = sch.passes;
+    hp.total_bins = 0;
+    for (int p = 0; p < kMaxPasses; ++p) {
+        hp.shift[p] = sch.shift[p];
+        hp.bits[p] = sch.bits[p];
+        hp.hist_off[p] = hp.total_bins;
+        if (p < sch.passes) hp.total_bins += 1u << sch.bits[p];
+    }
+    int sms = device_sm_count();
+    uint32_t hist_blocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + 511u) / 512u, (uint32_t)sms * 2u));
+    k_sort_hist<<<hist_blocks, 512, sizeof(uint32_t) * hp.total_bins, st>>>(keys, n, hp, s.counts,
+                                                                             s.bases, s.ctl);
+    cudaError_t e = cudaGetLastError();
+    if (e) return e;
+
+    // ping-pong so that the last pass lands in the outputs
+    const uint32_t* kin = keys;
+    const uint32_t* vin = vals;
+    for (int p = 0; p < sch.passes; ++p) {
+        bool to_out = ((sch.passes - 1 - p) % 2) == 0;
+        uint32_t* kout = to_out ? sorted_keys : s.alt_keys;
+        uint32_t* vout = to_out ? sorted_vals : s.alt_vals;
+        uint32_t R = 1u << sch.bits[p];
+        k_onesweep<kSortThreads, kSortItems><<<sch.tiles, kSortThreads, onesweep_smem(R), st>>>(
+            kin, vin, kout, vout, n, sch.shift[p], sch.bits[p], s.bases + p * (kMaxRadix + 1),
+            s.lookback + (size_t)p * s.lookback_words_per_pass, s.ctl + kCtlTile0 + p,
+            s.ctl + kCtlError, s.ctl + kCtlEpoch);
+        if ((e = cudaGetLastError())) return e;
+        kin = kout;
+        vin = vout;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t cell_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t* sorted_keys,
+                         cudaStream_t st) {
+    if (sch.n == 0)  // every cell offset is 0
+        return cudaMemsetAsync(s.offs, 0, sizeof(uint32_t) * ((size_t)sch.cells + 1u), st);
+    const int last = sch.passes - 1;
+    uint32_t chunks = 1u << sch.bits[last];
+    k_cell_offsets<<<chunks, kOffsThreads, 0, st>>>(sorted_keys, sch.cells, sch.shift[last], chunks,
+                                                    s.bases + last * (kMaxRadix + 1), s.offs);
+    return cudaGetLastError();
+}
+
+cudaError_t sort_and_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t* keys,
+                             const uint32_t* vals, uint32_t* sorted_keys, uint32_t* sorted_vals,
+                             cudaStream_t st) {
+    cudaError_t e = sort_pairs(s, sch, keys, vals, sorted_keys, sorted_vals, st);
+    if (e) return e;
+    return cell_offsets(s, sch, sorted_keys, st);
+}
+
+cudaError_t offsets_to_start_close(const uint32_t* offs, uint32_t cells, uint32_t* start,
+                                   uint32_t* close, cudaStream_t st) {
+    if (cells == 0) return cudaSuccess;
+    k_offs_to_start_close<<<(cells + 255u) / 256u, 256, 0, st>>>(offs, cells, start, close);
+    return cudaGetLastError();
+}
+
+}  // namespace mb

@@ -1,0 +1,229 @@
+/*
+ * millionsball.h — C ABI of the GB300 (sm_103a) sphere-collision step library.
+ *
+ * This header is the drop-in boundary for the per-frame compute passes of
+ * bevy_millions_ball's physics plugin.  The reference drives those passes from a
+ * Bevy render-graph node once per rendered frame:
+ *
+ *     radix sort      bevy_radix_sort::run(.., n, 0..3, true, is_even)   src/physics/mod.rs:880-890
+ *     cell ranges     spatial_hashing::run(.., n, !is_even)              src/physics/mod.rs:892-900
+ *     physics         physics::run(..)   (INIT on frame 0, LOOP after)   src/physics/mod.rs:902-909, 915-956
+ *
+ * Here the same three stages are hand-written CUDA kernels behind a headless
+ * step() call.  All functions return an mb_status and never abort the process.
+ *
+ * Threading: one mb_world per host thread (a world is not internally locked).
+ * All device work of a world is issued on the CUDA stream given at creation;
+ * mb_step() is asynchronous with respect to the host.
+ */
+#ifndef MILLIONSBALL_H
+#define MILLIONSBALL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MB_ABI_VERSION 1u
+
+/* Status codes.  The reference panics / unwraps on every failure
+ * (src/physics/mod.rs:788-798, 930-937); this library reports instead. */
+typedef enum mb_status {
+    MB_OK = 0,
+    MB_ERR_INVALID_ARG = 1,     /* bad pointer, size or setting                         */
+    MB_ERR_OOM = 2,             /* device or host allocation failed                     */
+    MB_ERR_CUDA = 3,            /* a CUDA runtime call failed (see mb_last_error)       */
+    MB_ERR_TIMEOUT = 4,         /* a bounded device-side wait gave up (sort look-back)  */
+    MB_ERR_BUDGET_EXCEEDED = 5, /* the request does not fit the device-memory budget    */
+    MB_ERR_NOT_READY = 6        /* state was never uploaded / request still running     */
+} mb_status;
+
+/* Where a caller's buffer lives. */
+typedef enum mb_memory {
+    MB_HOST = 0,   /* host memory (pageable or pinned); copied synchronously on the world's stream */
+    MB_DEVICE = 1  /* device memory of the world's GPU; copied on the world's stream, asynchronously */
+} mb_memory;
+
+/*
+ * Physics settings.  Field-for-field the reference's PhysicsPlugin /
+ * PhysicsSettings (src/physics/mod.rs:53-85 and 294-363), with the same meaning:
+ *
+ *   max_number_of_agents            number of simulated spheres n (fixed per world,
+ *                                   like the private field at mod.rs:362)
+ *   number_of_grids_one_dimension   N; the grid has N*N square collision cells
+ *   grid_size                       integer edge length of one cell
+ *   half_map_height                 H; the box is y in [0, 2H]
+ *   gravity                         acceleration, m/s^2
+ *   e_envir / e_agent               restitution against the walls / other spheres
+ *   k_agent / c_agent / r_agent     spring stiffness, damping and rigid threshold
+ *   time_delta                      step length, seconds
+ *   enable_simulation               0 makes mb_step() a no-op (mod.rs:778, 854)
+ *   enable_spring                   spring response instead of rigid restitution
+ *
+ * The reference bakes every real-valued setting into its shaders as
+ * (value * 1000) truncated to an integer and divides by 1000 again on the GPU
+ * (mod.rs:460-484, physics.wgsl:7-16); so dt = 1/60 runs as 0.016.  This library
+ * applies exactly that quantisation unless `exact_constants` is set, in which
+ * case the f32 values are used as given (no counterpart in the reference).
+ */
+typedef struct mb_settings {
+    uint32_t max_number_of_agents;
+    uint32_t number_of_grids_one_dimension;
+    uint32_t grid_size;
+    uint32_t half_map_height;
+    float gravity[3];
+    float e_envir;
+    float e_agent;
+    float k_agent;
+    float c_agent;
+    float r_agent;
+    float time_delta;
+    uint8_t enable_simulation;
+    uint8_t enable_spring;
+    uint8_t exact_constants;
+    uint8_t reserved0;
+} mb_settings;
+
+/* PhysicsPlugin::default() (src/physics/mod.rs:87-109). */
+void mb_settings_default(mb_settings* out);
+
+/*
+ * Constants exactly as the kernels use them after quantisation
+ * (CompiledConsts::shader_defs, src/physics/mod.rs:459-485; physics.wgsl:2-16).
+ */
+typedef struct mb_consts {
+    uint32_t number_of_grids_one_dimension;
+    uint32_t grid_size;
+    float half_map_height;   /* HALF_MAP_HEIGHT */
+    float half_map_size;     /* HALF_MAP_SIZE = f32(N * grid_size / 2) */
+    float gravity[3];
+    float e_envir, e_agent, k_agent, c_agent, r_agent, time_delta;
+    uint32_t enable_spring;
+} mb_consts;
+
+mb_status mb_quantize_settings(const mb_settings* s, mb_consts* out);
+
+/* ------------------------------------------------------------------------- */
+/* World: one scene, resident in device memory.                               */
+/* ------------------------------------------------------------------------- */
+typedef struct mb_world mb_world;
+
+/*
+ * Create a world for s->max_number_of_agents spheres on the current CUDA device.
+ * `cuda_stream` is a cudaStream_t (NULL = the legacy default stream).  Replaces
+ * PhysicsPlugin::build + create_shader_storage_buffers + RadixSortPlugin buffer
+ * set-up (src/physics/mod.rs:111-125, 241-292).
+ */
+mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out);
+mb_status mb_destroy(mb_world* w);
+
+/*
+ * Replace the runtime settings (the egui path, src/main.rs:155-210 and the
+ * recompile at src/physics/mod.rs:808-837).  No recompilation: settings are
+ * kernel parameters.  max_number_of_agents cannot change (mod.rs:362).
+ */
+mb_status mb_set_settings(mb_world* w, const mb_settings* s);
+mb_status mb_get_settings(const mb_world* w, mb_settings* out);
+
+/*
+ * Upload n = max_number_of_agents agent states.
+ *   pos_scale : n x float4  (x, y, z, radius)            physics.wgsl:25 position_with_scale
+ *   vfme      : n x uint4   f16 pairs (vx,vy) (vz,fx)    physics.wgsl:26 packed_vfme,
+ *                           (fy,fz) (mass,0); velocity is the displacement per step
+ * The frame counter restarts: the next step is the INIT frame (mod.rs:929-933),
+ * which reorders nothing and only emits cell keys.
+ */
+mb_status mb_set_state(mb_world* w, const float* pos_scale, const uint32_t* vfme, mb_memory where);
+
+/* Download the current state, in the current slot (sorted-cell) order. */
+mb_status mb_get_state(mb_world* w, float* pos_scale, uint32_t* vfme, mb_memory where);
+
+/* Advance k frames (sort -> cell ranges -> physics per frame).  Asynchronous. */
+mb_status mb_step(mb_world* w, uint32_t k);
+
+/* Wait for the world's stream; reports a device-side timeout as MB_ERR_TIMEOUT. */
+mb_status mb_sync(mb_world* w);
+
+/*
+ * Debug view of the last frame, each array optional (NULL = skip):
+ *   keys  : n  u32  unsorted cell keys emitted by the last physics pass (the next sort's input)
+ *   perm  : n  u32  sorted permutation of the last frame (old slot of each sorted slot)
+ *   start : N*N u32 first sorted slot of each cell, 0xFFFFFFFF if the cell is empty
+ *   close : N*N u32 last sorted slot of each cell (inclusive); 0xFFFFFFFF if empty
+ * start/close follow spatial_hashing.wgsl:29-70 (ZEROING + HASHING).
+ */
+mb_status mb_get_debug(mb_world* w, uint32_t* keys, uint32_t* perm, uint32_t* start,
+                       uint32_t* close, mb_memory where);
+
+/*
+ * Device pointers of the current state (headless replacement of the buffer
+ * handles the renderer binds, src/physics/mod.rs:40-51 and
+ * src/custom_materials/physics_ball/mod.rs:709-740).  Valid until the next
+ * mb_step / mb_set_state / mb_destroy on this world.
+ */
+mb_status mb_device_buffers(mb_world* w, const float** pos_scale, const uint32_t** vfme);
+
+/* Frames run since the last mb_set_state (PhysicsBindGroup::time, mod.rs:711-743). */
+int64_t mb_time(const mb_world* w);
+
+/* Last error message of this world ("" if none).  Pass NULL for process-wide errors. */
+const char* mb_last_error(const mb_world* w);
+
+/* ------------------------------------------------------------------------- */
+/* Stage entry points (device pointers, caller's stream).                     */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * Stable key/index sort followed by the cell-range build: what one frame runs
+ * before physics (bevy_radix_sort::run, src/physics/mod.rs:880-890, then
+ * spatial_hashing::run, src/physics/spatial_hashing.rs:191-243).  The reference's
+ * own test drives exactly this pair (spatial_hashing.rs:408-600).
+ *
+ *   keys        : n u32, every key < number_of_cells
+ *   vals        : n u32 or NULL; NULL sorts the identity 0..n-1 (the `true`
+ *                 argument at mod.rs:888)
+ *   sorted_keys, sorted_vals : n u32 outputs
+ *   start, close: number_of_cells u32 outputs (as in mb_get_debug); either may be NULL
+ *
+ * Scratch comes from a plan sized by mb_sort_plan_create (max keys, max cells).
+ */
+typedef struct mb_sort_plan mb_sort_plan;
+mb_status mb_sort_plan_create(uint32_t max_keys, uint32_t max_cells, mb_sort_plan** out);
+mb_status mb_sort_plan_destroy(mb_sort_plan* p);
+mb_status mb_sort_and_hash(mb_sort_plan* p, const uint32_t* keys, const uint32_t* vals, uint32_t n,
+                           uint32_t number_of_cells, uint32_t* sorted_keys, uint32_t* sorted_vals,
+                           uint32_t* start, uint32_t* close, void* cuda_stream);
+
+/* Pick sort digit widths / block shapes for a scene size (the autotuner). */
+typedef struct mb_tuning {
+    uint32_t digit_bits_max;   /* widest radix digit, 4..11 */
+    uint32_t collide_block;    /* threads per block of the physics kernel */
+    uint32_t reserved[6];
+} mb_tuning;
+mb_status mb_get_tuning(const mb_world* w, mb_tuning* out);
+mb_status mb_set_tuning(mb_world* w, const mb_tuning* t);
+
+/*
+ * Per-stage device timing (no counterpart in the reference, which only labels
+ * its passes, src/physics/mod.rs:925).  With profiling on, every frame records
+ * CUDA events around its three stages; mb_last_frame_times waits for the most
+ * recent frame and reports milliseconds: [0] sort (histogram + digit passes),
+ * [1] cell-range build, [2] physics pass.  Enabling or disabling re-captures the
+ * frame graphs.
+ */
+mb_status mb_set_profiling(mb_world* w, int enable);
+mb_status mb_last_frame_times(mb_world* w, float* stage_ms3);
+
+/* Kernels one frame launches (graph nodes that are kernels). */
+uint32_t mb_kernels_per_frame(const mb_world* w);
+
+/* Library version string (build id). */
+const char* mb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MILLIONSBALL_H */

@@ -1,0 +1,236 @@
+"""GPU parity of whole frames (sort -> cell ranges -> physics) through the C ABI,
+against the oracle and the golden fixtures.
+
+Bar: keys, permutation and cell ranges bit-exact; positions and packed velocity /
+force bit-exact as well (the physics kernel rounds like the oracle).  The stated
+float tolerances (|dx| <= 1e-5 after 1 frame, <= 1e-3 after 10 frames) are also
+asserted explicitly, although bit-exactness implies them.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+from bevy_millions_ball_gb300 import MbError, PhysicsPlugin, World, pack_vfme, scenes
+from tests.conftest import GOLDEN
+from tests.test_oracle import settings_from_fixture
+
+pytestmark = pytest.mark.gpu
+INV = 0xFFFFFFFF
+TOL_1 = 1e-5   # position error after 1 frame
+TOL_10 = 1e-3  # position error after 10 frames
+
+
+def plugin_from_settings(s) -> PhysicsPlugin:
+    return PhysicsPlugin.from_c(s)
+
+
+def compare(world: World, ow: "oracle.OracleWorld", frame: int, tol: float | None = None):
+    p, q = world.get_state()
+    rp, rq = ow.get_state()
+    d, rd = world.debug(), ow.debug()
+    np.testing.assert_array_equal(d["keys"], rd["keys"], err_msg=f"keys, frame {frame}")
+    np.testing.assert_array_equal(d["perm"], rd["perm"], err_msg=f"perm, frame {frame}")
+    np.testing.assert_array_equal(d["start"], rd["start"], err_msg=f"start, frame {frame}")
+    full = rd["start"] != INV
+    np.testing.assert_array_equal(d["close"][full], rd["close"][full], err_msg=f"close, frame {frame}")
+    if tol is not None:
+        assert np.nanmax(np.abs(p[:, :3] - rp[:, :3])) <= tol
+    np.testing.assert_array_equal(p.view(np.uint32), rp.view(np.uint32), err_msg=f"pos, frame {frame}")
+    np.testing.assert_array_equal(q, rq, err_msg=f"vfme, frame {frame}")
+
+
+@pytest.mark.parametrize("name", ["rigid", "spring", "rigid_sparse"])
+def test_world_matches_golden_fixtures(built_lib, cuda, name):
+    d = np.load(GOLDEN / f"physics_{name}.npz")
+    with World(plugin_from_settings(settings_from_fixture(d))) as w:
+        w.set_state(d["pos0"], d["vfme0"])
+        for f in range(int(d["frames"])):
+            w.step(1)
+            p, q = w.get_state()
+            dbg = w.debug()
+            np.testing.assert_array_equal(p.view(np.uint32), d[f"f{f}_pos"].view(np.uint32), err_msg=f"frame {f}")
+            np.testing.assert_array_equal(q, d[f"f{f}_vfme"])
+            np.testing.assert_array_equal(dbg["keys"], d[f"f{f}_keys"])
+            np.testing.assert_array_equal(dbg["perm"], d[f"f{f}_perm"])
+            np.testing.assert_array_equal(dbg["start"], d[f"f{f}_start"])
+
+
+def run_pair(scene, frames, checkpoints, world_kw=None):
+    with World(scene.plugin, **(world_kw or {})) as w:
+        ow = oracle.OracleWorld(scene.plugin.to_c())
+        w.set_state(scene.pos_scale, scene.vfme)
+        ow.set_state(scene.pos_scale, scene.vfme)
+        done = 0
+        for cp in checkpoints:
+            w.step(cp - done)
+            ow.step(cp - done)
+            done = cp
+            w.sync()
+            tol = TOL_1 if cp == 2 else (TOL_10 if cp == 11 else None)
+            compare(w, ow, cp, tol)
+        assert w.time == ow.time == done
+
+
+def test_small_uniform_rigid(built_lib, cuda):
+    """65,536 spheres, N=256 (the small plain workload), 100 frames."""
+    sc = scenes.workload("P-small")
+    run_pair(sc, 101, [1, 2, 11, 50, 101])
+
+
+def test_uniform_spring(built_lib, cuda):
+    sc = scenes.plain_uniform(50_000, 256, seed=4, spring=True, k=400.0, c=4.0)
+    run_pair(sc, 60, [1, 2, 11, 60])
+
+
+def test_clustered_spring(built_lib, cuda):
+    """Uneven occupancy (~40 spheres per cell at cluster centres)."""
+    sc = scenes.plain_clustered(262_144, 512, clusters=4, sigma_xz=16.0, seed=9)
+    run_pair(sc, 40, [1, 2, 11, 40])
+
+
+def test_nonpow2_grid_and_grid_size(built_lib, cuda):
+    sc = scenes.plain_uniform(30_000, 300, grid_size=2, half_map_height=4, seed=12)
+    run_pair(sc, 30, [1, 2, 11, 30])
+
+
+def test_sparse_grid_more_cells_than_agents(built_lib, cuda):
+    """C = N*N > n: every cell cleared, not just n (the reference needs n >= N*N)."""
+    sc = scenes.plain_uniform(5_000, 512, seed=13)
+    run_pair(sc, 25, [1, 2, 11, 25])
+
+
+@pytest.mark.parametrize("digit_bits", [4, 6, 8, 11])
+def test_digit_widths_agree(built_lib, cuda, digit_bits):
+    sc = scenes.plain_uniform(70_000, 256, seed=21)
+    with World(sc.plugin) as w:
+        w.set_tuning(digit_bits_max=digit_bits, collide_block=64 if digit_bits == 4 else 128)
+        ow = oracle.OracleWorld(sc.plugin.to_c())
+        w.set_state(sc.pos_scale, sc.vfme)
+        ow.set_state(sc.pos_scale, sc.vfme)
+        w.step(12)
+        ow.step(12)
+        compare(w, ow, 12)
+
+
+def test_settings_change_midrun(built_lib, cuda):
+    """Runtime edits (the egui path) including a grid change that re-keys the agents."""
+    sc = scenes.plain_uniform(40_000, 256, seed=3)
+    with World(sc.plugin) as w:
+        ow = oracle.OracleWorld(sc.plugin.to_c())
+        w.set_state(sc.pos_scale, sc.vfme)
+        ow.set_state(sc.pos_scale, sc.vfme)
+        w.step(5)
+        ow.step(5)
+        for new in [sc.plugin.replace(e_agent=0.3, gravity=(0.5, -3.0, 0.0)),
+                    sc.plugin.replace(enable_spring=True, k_agent=300.0, c_agent=2.0),
+                    sc.plugin.replace(number_of_grids_one_dimension=128, grid_size=2),
+                    sc.plugin.replace(number_of_grids_one_dimension=512, grid_size=1)]:
+            w.set_settings(new)
+            ow.set_settings(new.to_c())
+            w.step(4)
+            ow.step(4)
+            compare(w, ow, ow.time)
+
+
+def test_full_size_1m_frames_bit_exact(built_lib, cuda):
+    """1,048,576 spheres, N=1024: the benchmark workload, 3 frames against the oracle."""
+    sc = scenes.workload("P-1M")
+    run_pair(sc, 3, [1, 2, 3])
+
+
+def test_full_size_1m_properties(built_lib, cuda):
+    """Size-independent properties after many frames at full size."""
+    sc = scenes.workload("P-1M")
+    with World(sc.plugin) as w:
+        w.set_state(sc.pos_scale, sc.vfme)
+        w.step(200)
+        w.sync()
+        p, q = w.get_state()
+        d = w.debug()
+        n = sc.n
+        assert np.array_equal(np.sort(d["perm"]), np.arange(n, dtype=np.uint32))  # a permutation
+        # every cell's range is consistent and the ranges tile [0, n)
+        full = d["start"] != INV
+        sizes = (d["close"][full].astype(np.int64) - d["start"][full] + 1)
+        assert sizes.sum() == n and np.all(sizes >= 1)
+        order = np.argsort(d["start"][full])
+        st = d["start"][full][order].astype(np.int64)
+        assert st[0] == 0 and np.all(st[1:] == (st[:-1] + sizes[order][:-1]))
+        hs = 512
+        assert np.all(np.abs(p[:, 0]) <= hs) and np.all(np.abs(p[:, 2]) <= hs)
+        assert np.all(p[:, 1] >= 0.5 - 1e-6) and np.all(p[:, 1] <= 15.5 + 1e-6)
+        assert not np.isnan(p).any()
+
+
+def test_disabled_simulation_is_noop(built_lib, cuda):
+    sc = scenes.plain_uniform(4096, 64, seed=1)
+    with World(sc.plugin.replace(enable_simulation=False)) as w:
+        w.set_state(sc.pos_scale, sc.vfme)
+        w.step(5)
+        p, q = w.get_state()
+        assert w.time == 0
+        np.testing.assert_array_equal(p, sc.pos_scale)
+
+
+def test_reupload_restarts_with_init(built_lib, cuda):
+    sc = scenes.plain_uniform(8192, 128, seed=2)
+    with World(sc.plugin) as w:
+        ow = oracle.OracleWorld(sc.plugin.to_c())
+        w.set_state(sc.pos_scale, sc.vfme)
+        w.step(7)
+        w.set_state(sc.pos_scale, sc.vfme)
+        ow.set_state(sc.pos_scale, sc.vfme)
+        assert w.time == 0
+        w.step(6)
+        ow.step(6)
+        compare(w, ow, 6)
+
+
+def test_device_pointer_state_roundtrip(built_lib, cuda):
+    torch = cuda
+    sc = scenes.plain_uniform(10_000, 128, seed=6)
+    dp = torch.from_numpy(sc.pos_scale.copy()).cuda()
+    dq = torch.from_numpy(sc.vfme.view(np.int32).copy()).cuda()
+    with World(sc.plugin, stream=torch.cuda.current_stream().cuda_stream) as w:
+        w.set_state_device(dp.data_ptr(), dq.data_ptr())
+        w.step(3)
+        out_p = torch.empty_like(dp)
+        out_q = torch.empty_like(dq)
+        w.get_state_device(out_p.data_ptr(), out_q.data_ptr())
+        torch.cuda.synchronize()
+        p, q = w.get_state()
+        np.testing.assert_array_equal(out_p.cpu().numpy(), p)
+        np.testing.assert_array_equal(out_q.cpu().numpy().view(np.uint32), q)
+        a, b = w.device_buffers()
+        assert a and b
+
+
+def test_errors_are_reported_not_fatal(built_lib, cuda):
+    with pytest.raises(MbError) as e:
+        World(PhysicsPlugin(number_of_grids_one_dimension=0))
+    assert e.value.status == 1
+    with pytest.raises(MbError):
+        World(PhysicsPlugin(time_delta=0.0001))  # quantises to 0
+    w = World(PhysicsPlugin(max_number_of_agents=1024, number_of_grids_one_dimension=32, grid_size=1))
+    with pytest.raises(MbError) as e:
+        w.step(1)  # no state yet
+    assert e.value.status == 6
+    with pytest.raises(MbError):
+        w.set_settings(PhysicsPlugin(max_number_of_agents=2048))
+    with pytest.raises(MbError):
+        w.set_tuning(digit_bits_max=12)
+    w.close()
+
+
+def test_single_agent_and_tiny_grid(built_lib, cuda):
+    p = PhysicsPlugin(max_number_of_agents=1, number_of_grids_one_dimension=1, grid_size=4, half_map_height=2)
+    pos = np.array([[0.3, 3.0, -0.2, 0.5]], np.float32)
+    q = pack_vfme(np.array([[0.01, 0.0, 0.02]], np.float32), np.zeros((1, 3), np.float32), 1.0)
+    with World(p) as w:
+        ow = oracle.OracleWorld(p.to_c())
+        w.set_state(pos, q)
+        ow.set_state(pos, q)
+        w.step(30)
+        ow.step(30)
+        compare(w, ow, 30)
