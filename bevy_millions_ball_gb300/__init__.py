@@ -207,12 +207,15 @@ class World:
         self._check(self._lib.mb_get_tuning(self._h, C.byref(t)))
         return t
 
-    def set_tuning(self, digit_bits_max: int | None = None, collide_block: int | None = None) -> None:
+    def set_tuning(self, digit_bits_max: int | None = None, collide_block: int | None = None,
+                   sort_algorithm: int | None = None) -> None:
         t = self.tuning
         if digit_bits_max is not None:
             t.digit_bits_max = digit_bits_max
         if collide_block is not None:
             t.collide_block = collide_block
+        if sort_algorithm is not None:
+            t.sort_algorithm = sort_algorithm
         self._check(self._lib.mb_set_tuning(self._h, C.byref(t)))
 
     # -- state

@@ -58,7 +58,11 @@ class MbConsts(C.Structure):
 
 
 class MbTuning(C.Structure):
-    _fields_ = [("digit_bits_max", u32), ("collide_block", u32), ("reserved", u32 * 6)]
+    _fields_ = [("digit_bits_max", u32), ("collide_block", u32), ("sort_algorithm", u32),
+                ("reserved", u32 * 5)]
+
+
+MB_SORT_COUNTING, MB_SORT_ONESWEEP = 0, 1
 
 
 MB_OK = 0

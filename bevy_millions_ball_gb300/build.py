@@ -30,6 +30,7 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-
 UNITS = {
     "mb_api.cu": [],
     "mb_sort.cu": [],
+    "mb_count.cu": [],
     "mb_physics.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
 }
 HEADERS = [CSRC / "mb_internal.h", ROOT / "include" / "millionsball.h"]

@@ -57,7 +57,8 @@ struct mb_world {
     uint32_t* keys = nullptr;          // unsorted keys emitted by the last physics pass
     uint32_t* sorted_keys = nullptr;
     uint32_t* perm = nullptr;
-    mb::SortScratch scratch;
+    mb::SortScratch scratch;      // onesweep sort scratch + the cell offsets (offs)
+    mb::CountScratch cnt;         // counting-sort scratch (per-cell counts, cursors)
     mb::SortSchedule sched;
     mb_tuning tuning{};
     int cur = 0;
@@ -126,23 +127,42 @@ cudaError_t mark(mb_world* w, int i, cudaStream_t st, bool capturing) {
                      : cudaEventRecord(w->prof_ev[i], st);
 }
 
-// Enqueue one frame on `st`.
+bool counting(const mb_world* w) { return w->tuning.sort_algorithm == MB_SORT_COUNTING; }
+
+// Enqueue one frame on `st`.  Profiling marks: [0] frame start, [1] after the
+// first ordering stage, [2] after the second, [3] after physics.
 cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool capturing = false) {
     cudaError_t e;
+    uint32_t* hist = nullptr;
     if ((e = mark(w, 0, st, capturing))) return e;
-    if ((e = mb::sort_pairs(w->scratch, w->sched, w->keys, nullptr, w->sorted_keys, w->perm, st))) return e;
-    if ((e = mark(w, 1, st, capturing))) return e;
-    if ((e = mb::cell_offsets(w->scratch, w->sched, w->sorted_keys, st))) return e;
+    if (counting(w)) {
+        // cell offsets first (scan of the counts), then the permutation
+        if ((e = mb::count_scan(w->cnt, w->scratch.ctl, w->cells, w->scratch.offs, st))) return e;
+        if ((e = mark(w, 1, st, capturing))) return e;
+        if ((e = mb::count_scatter(w->cnt, w->keys, w->n, w->cells, w->scratch.offs, w->perm, st))) return e;
+        hist = w->cnt.hist;
+    } else {
+        if ((e = mb::sort_pairs(w->scratch, w->sched, w->keys, nullptr, w->sorted_keys, w->perm, st))) return e;
+        if ((e = mark(w, 1, st, capturing))) return e;
+        if ((e = mb::cell_offsets(w->scratch, w->sched, w->sorted_keys, st))) return e;
+    }
     if ((e = mark(w, 2, st, capturing))) return e;
     int nxt = cur ^ 1;
     if (init)
         e = mb::launch_physics_init(w->P, w->n, w->perm, w->pos[cur], w->vfme[cur], w->pos[nxt],
-                                    w->vfme[nxt], w->keys, st);
+                                    w->vfme[nxt], w->keys, hist, st);
     else
         e = mb::launch_physics_loop(w->P, w->n, w->perm, w->scratch.offs, w->pos[cur], w->vfme[cur],
-                                    w->pos[nxt], w->vfme[nxt], w->keys, (int)w->tuning.collide_block, st);
+                                    w->pos[nxt], w->vfme[nxt], w->keys, hist, st);
     if (e) return e;
     return mark(w, 3, st, capturing);
+}
+
+// Rebuild the per-cell counts of the current keys (counting mode only).
+cudaError_t recount(mb_world* w) {
+    if (!counting(w)) return cudaSuccess;
+    if (!w->frame_done) return mb::count_reset_zero_keys(w->cnt, w->n, w->cells, w->stream);
+    return mb::count_keys(w->cnt, w->keys, w->n, w->cells, w->stream);
 }
 
 cudaError_t build_graph(mb_world* w, int cur) {
@@ -227,6 +247,7 @@ mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out) {
     w->n = s->max_number_of_agents;
     w->tuning.digit_bits_max = 11;
     w->tuning.collide_block = 128;
+    w->tuning.sort_algorithm = MB_SORT_COUNTING;
     apply_settings(w, *s);
     const size_t n = w->n;
     auto alloc_all = [&]() -> cudaError_t {
@@ -239,7 +260,8 @@ mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out) {
         if ((e = cudaMalloc(&w->keys, sizeof(uint32_t) * n))) return e;
         if ((e = cudaMalloc(&w->sorted_keys, sizeof(uint32_t) * n))) return e;
         if ((e = cudaMalloc(&w->perm, sizeof(uint32_t) * n))) return e;
-        return mb::scratch_alloc(w->scratch, w->n, w->cells);
+        if ((e = mb::scratch_alloc(w->scratch, w->n, w->cells))) return e;
+        return mb::count_scratch_alloc(w->cnt, w->cells);
     };
     cudaError_t e = alloc_all();
     if (e) {
@@ -263,6 +285,7 @@ mb_status mb_destroy(mb_world* w) {
     cudaFree(w->sorted_keys);
     cudaFree(w->perm);
     mb::scratch_free(w->scratch);
+    mb::count_scratch_free(w->cnt);
     if (w->cap_stream) cudaStreamDestroy(w->cap_stream);
     for (auto& ev : w->prof_ev)
         if (ev) cudaEventDestroy(ev);
@@ -285,15 +308,30 @@ mb_status mb_set_settings(mb_world* w, const mb_settings* s) {
         uint32_t* offs = nullptr;
         if ((e = cudaMalloc(&offs, sizeof(uint32_t) * ((size_t)new_cells + 1u))))
             return cuda_fail(w, "mb_set_settings", e);
+        mb::CountScratch cnt;
+        if ((e = mb::count_scratch_alloc(cnt, new_cells))) {
+            cudaFree(offs);
+            mb::count_scratch_free(cnt);
+            return cuda_fail(w, "mb_set_settings", e);
+        }
         cudaFree(w->scratch.offs);
         w->scratch.offs = offs;
         w->scratch.max_cells = new_cells;
+        mb::count_scratch_free(w->cnt);
+        w->cnt = cnt;
     }
     drop_graphs(w);
     apply_settings(w, *s);
     // keys emitted under the old grid are re-derived under the new one
-    if (grid_changed && w->has_state && w->frame_done) {
-        cudaError_t e = mb::launch_rekey(w->P, w->n, w->pos[w->cur], w->keys, w->stream);
+    if (grid_changed && w->has_state) {
+        cudaError_t e = cudaSuccess;
+        if (!w->frame_done) {
+            e = recount(w);  // still the all-zero keys of the upload
+        } else {
+            uint32_t* hist = counting(w) ? w->cnt.hist : nullptr;
+            if (hist) e = cudaMemsetAsync(hist, 0, sizeof(uint32_t) * w->cells, w->stream);
+            if (!e) e = mb::launch_rekey(w->P, w->n, w->pos[w->cur], w->keys, hist, w->stream);
+        }
         if (e) return cuda_fail(w, "mb_set_settings", e);
     }
     return MB_OK;
@@ -316,12 +354,13 @@ mb_status mb_set_state(mb_world* w, const float* pos_scale, const uint32_t* vfme
     // fresh sort buffers hold zeros: frame 0 sorts all-zero keys (identity order)
     if ((e = cudaMemsetAsync(w->keys, 0, sizeof(uint32_t) * w->n, w->stream)))
         return cuda_fail(w, "mb_set_state", e);
+    w->frame_done = false;
+    if ((e = recount(w))) return cuda_fail(w, "mb_set_state", e);
     if (where == MB_HOST && (e = cudaStreamSynchronize(w->stream)))
         return cuda_fail(w, "mb_set_state", e);
     w->cur = 0;
     w->time = 0;
     w->has_state = true;
-    w->frame_done = false;
     return MB_OK;
 }
 
@@ -428,9 +467,16 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
         return fail(w, MB_ERR_INVALID_ARG, "digit_bits_max must be in [4, 11]");
     if (t->collide_block < 32 || t->collide_block > 256 || (t->collide_block & 31u))
         return fail(w, MB_ERR_INVALID_ARG, "collide_block must be a multiple of 32 in [32, 256]");
+    if (t->sort_algorithm != MB_SORT_COUNTING && t->sort_algorithm != MB_SORT_ONESWEEP)
+        return fail(w, MB_ERR_INVALID_ARG, "sort_algorithm must be MB_SORT_COUNTING or MB_SORT_ONESWEEP");
     drop_graphs(w);
+    bool to_counting = t->sort_algorithm == MB_SORT_COUNTING && !counting(w);
     w->tuning = *t;
     w->sched = mb::make_schedule(w->n, w->cells, w->tuning.digit_bits_max);
+    if (to_counting && w->has_state) {  // counts were not kept while the radix sort ran
+        cudaError_t e = recount(w);
+        if (e) return cuda_fail(w, "mb_set_tuning", e);
+    }
     return MB_OK;
 }
 
@@ -501,16 +547,23 @@ mb_status mb_last_frame_times(mb_world* w, float* ms) {
     if (!w->profiling || !w->frame_done) return fail(w, MB_ERR_NOT_READY, "profiling off or no frame yet");
     cudaError_t e = cudaEventSynchronize(w->prof_ev[3]);
     if (e) return cuda_fail(w, "mb_last_frame_times", e);
+    float t[3];
     for (int i = 0; i < 3; ++i) {
-        if ((e = cudaEventElapsedTime(&ms[i], w->prof_ev[i], w->prof_ev[i + 1])))
+        if ((e = cudaEventElapsedTime(&t[i], w->prof_ev[i], w->prof_ev[i + 1])))
             return cuda_fail(w, "mb_last_frame_times", e);
     }
+    // counting mode runs the cell-offset scan before the permutation
+    ms[0] = counting(w) ? t[1] : t[0];
+    ms[1] = counting(w) ? t[0] : t[1];
+    ms[2] = t[2];
     return MB_OK;
 }
 
 uint32_t mb_kernels_per_frame(const mb_world* w) {
-    // histogram + one onesweep kernel per digit pass + cell offsets + physics
-    return w ? (uint32_t)w->sched.passes + 3u : 0u;
+    if (!w) return 0u;
+    // counting: scan + scatter + fixup + physics;
+    // onesweep: histogram + one kernel per digit pass + cell offsets + physics
+    return counting(w) ? 4u : (uint32_t)w->sched.passes + 3u;
 }
 
 const char* mb_version(void) { return "millionsball-gb300 " __DATE__ " sm_103a"; }

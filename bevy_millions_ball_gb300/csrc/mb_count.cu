@@ -1,0 +1,288 @@
+// mb_count.cu — counting sort of cell keys (the default frame sort).
+//
+// The reference sorts the cell keys with a generic 3 x 8-bit radix sort
+// (bevy_radix_sort, called at src/physics/mod.rs:880-890) and then derives each
+// cell's slot range from the sorted keys (spatial_hashing.wgsl:29-70).  Here the
+// key space *is* the cell table, so the same stable permutation comes from:
+//
+//   1. per-cell counts, accumulated by the physics pass of the previous frame as
+//      it emits the keys (one red.add per sphere);
+//   2. k_cell_scan: one single-pass exclusive scan (decoupled look-back with a
+//      32-tile window) turns the counts into the cell offsets offs[c] (= start of
+//      cell c; offs[C] = n) and a cursor copy, and zeroes the counts;
+//   3. k_cell_scatter: each sphere claims a slot of its cell with one atomic per
+//      run of equal keys in its warp (match.any), so spheres of one warp keep
+//      their order;
+//   4. k_cell_fixup: every cell's slots are put back in ascending input order
+//      (what a stable sort yields; only cells filled by several warps need it).
+//
+// The result is bit-identical to a stable sort; offs[] replaces start/close.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "mb_internal.h"
+
+namespace mb {
+namespace {
+
+constexpr uint32_t kFlagAgg = 1u, kFlagPre = 2u;
+constexpr uint32_t kValMask = (1u << 30) - 1u;
+constexpr uint32_t kSpinMax = 1u << 21;
+
+__device__ __forceinline__ void st_rlx(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_rlx(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// ---------------------------------------------------------------- scan
+__global__ void __launch_bounds__(kScanThreads)
+    k_cell_scan(uint32_t* __restrict__ hist, uint32_t cells, uint32_t* __restrict__ offs,
+                uint32_t* __restrict__ cursor, uint32_t* status, uint32_t* ticket, uint32_t* err) {
+    constexpr int W = kScanThreads / 32;
+    __shared__ uint32_t s_tile, s_warp[W], s_excl;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * kScanTile + tid * kScanItems;
+
+    uint32_t v[kScanItems];
+    if (base + kScanItems <= cells) {
+        const uint4* h4 = reinterpret_cast<const uint4*>(hist + base);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            uint4 x = __ldcg(h4 + q);
+            v[4 * q] = x.x;
+            v[4 * q + 1] = x.y;
+            v[4 * q + 2] = x.z;
+            v[4 * q + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < kScanItems; ++q) v[q] = (base + q < cells) ? __ldcg(hist + base + q) : 0u;
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) sum += v[q];
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31u) s_warp[warp] = incl;
+    __syncthreads();
+    uint32_t wexcl = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        uint32_t t = s_warp[w];
+        if ((uint32_t)w < warp) wexcl += t;
+        total += t;
+    }
+
+    // decoupled look-back over earlier tiles, 32 at a time (warp 0)
+    if (warp == 0) {
+        uint32_t excl = 0;
+        if (tile == 0) {
+            if (lane == 0) st_rlx(status, (kFlagPre << 30) | (total & kValMask));
+        } else {
+            if (lane == 0) st_rlx(status + tile, (kFlagAgg << 30) | (total & kValMask));
+            int32_t top = (int32_t)tile - 1;
+            uint32_t spins = 0;
+            bool gave_up = false;
+            while (true) {
+                int32_t idx = top - (int32_t)lane;
+                uint32_t s = idx >= 0 ? ld_rlx(status + idx) : (kFlagPre << 30);
+                uint32_t f = s >> 30;
+                uint32_t pmask = __ballot_sync(0xFFFFFFFFu, f == kFlagPre);
+                uint32_t zmask = __ballot_sync(0xFFFFFFFFu, f == 0u);
+                uint32_t first = pmask ? (uint32_t)(__ffs(pmask) - 1) : 32u;
+                uint32_t upto = first == 32u ? 0xFFFFFFFFu : ((2u << first) - 1u);
+                if (zmask & upto) {
+                    if (++spins > kSpinMax) {
+                        if (lane == 0) atomicOr(err, 2u);
+                        gave_up = true;
+                        break;
+                    }
+                    if (spins > 32u) __nanosleep(32);
+                    continue;
+                }
+                uint32_t mine = (lane <= first) ? (s & kValMask) : 0u;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xFFFFFFFFu, mine, o);
+                excl += mine;
+                if (first < 32u) break;
+                top -= 32;
+            }
+            (void)gave_up;
+            if (lane == 0) st_rlx(status + tile, (kFlagPre << 30) | ((excl + total) & kValMask));
+        }
+        if (lane == 0) s_excl = excl;
+    }
+    __syncthreads();
+    uint32_t run = s_excl + wexcl + incl - sum;
+    if (base + kScanItems <= cells) {
+        uint4* o4 = reinterpret_cast<uint4*>(offs + base);
+        uint4* c4 = reinterpret_cast<uint4*>(cursor + base);
+        uint4* h4 = reinterpret_cast<uint4*>(hist + base);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            uint4 x;
+            x.x = run; run += v[4 * q];
+            x.y = run; run += v[4 * q + 1];
+            x.z = run; run += v[4 * q + 2];
+            x.w = run; run += v[4 * q + 3];
+            o4[q] = x;
+            c4[q] = x;
+            h4[q] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        if (base + kScanItems == cells) offs[cells] = run;
+    } else {
+        for (int q = 0; q < kScanItems; ++q) {
+            uint32_t c = base + q;
+            if (c < cells) {
+                offs[c] = run;
+                cursor[c] = run;
+                hist[c] = 0u;
+                run += v[q];
+                if (c + 1u == cells) offs[cells] = run;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- scatter
+__global__ void __launch_bounds__(256)
+    k_cell_scatter(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ cursor,
+                   uint32_t* __restrict__ perm) {
+    const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        uint32_t i = i0 + threadIdx.x;
+        bool valid = i < n;
+        uint32_t k = valid ? __ldg(keys + i) : 0xFFFFFFFFu;
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+        uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+        uint32_t b = 0;
+        if (valid && lane == leader) b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
+        b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
+        if (valid) perm[b + (uint32_t)__popc(peers & lt)] = i;
+    }
+}
+
+// ---------------------------------------------------------------- fixup
+__global__ void __launch_bounds__(256)
+    k_cell_fixup(const uint32_t* __restrict__ offs, uint32_t cells, uint32_t* perm, uint32_t* status,
+                 uint32_t status_words, uint32_t* ticket) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x == 0) {  // the scan of this frame is over: reset its look-back state
+        for (uint32_t s = threadIdx.x; s < status_words; s += blockDim.x) status[s] = 0u;
+        if (threadIdx.x == 0) *ticket = 0u;
+    }
+    if (c >= cells) return;
+    const uint32_t lo = offs[c], hi = offs[c + 1u];
+    if (hi - lo < 2u) return;
+    bool sorted = true;
+    uint32_t prev = perm[lo];
+    for (uint32_t j = lo + 1u; j < hi; ++j) {
+        uint32_t x = perm[j];
+        if (x < prev) { sorted = false; break; }
+        prev = x;
+    }
+    if (sorted) return;
+    for (uint32_t a = lo + 1u; a < hi; ++a) {  // insertion sort of this cell's slots
+        uint32_t x = perm[a];
+        uint32_t b = a;
+        while (b > lo) {
+            uint32_t y = perm[b - 1u];
+            if (y <= x) break;
+            perm[b] = y;
+            --b;
+        }
+        perm[b] = x;
+    }
+}
+
+// ---------------------------------------------------------------- counting
+// hist[keys[i]] += 1 for every sphere, one atomic per run of equal keys in a warp.
+__global__ void __launch_bounds__(256)
+    k_count_keys(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        uint32_t i = i0 + threadIdx.x;
+        bool valid = i < n;
+        uint32_t k = valid ? __ldg(keys + i) : 0xFFFFFFFFu;
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+        if (valid && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(hist + k, (uint32_t)__popc(peers));
+    }
+}
+
+__global__ void k_set_word(uint32_t* p, uint32_t v) { *p = v; }
+
+}  // namespace
+
+cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells) {
+    s.max_cells = max_cells;
+    size_t padded = ((size_t)max_cells + kScanTile) & ~(size_t)15;  // uint4-aligned, room for offs[C]
+    s.status_words = (max_cells + kScanTile - 1u) / kScanTile;
+    cudaError_t e;
+    if ((e = cudaMalloc(&s.hist, sizeof(uint32_t) * padded))) return e;
+    if ((e = cudaMalloc(&s.cursor, sizeof(uint32_t) * padded))) return e;
+    if ((e = cudaMalloc(&s.status, sizeof(uint32_t) * (s.status_words + 1u)))) return e;
+    if ((e = cudaMemset(s.hist, 0, sizeof(uint32_t) * padded))) return e;
+    if ((e = cudaMemset(s.status, 0, sizeof(uint32_t) * (s.status_words + 1u)))) return e;
+    return cudaSuccess;
+}
+
+void count_scratch_free(CountScratch& s) {
+    cudaFree(s.hist);
+    cudaFree(s.cursor);
+    cudaFree(s.status);
+    s = CountScratch();
+}
+
+cudaError_t count_keys(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
+                       cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * cells, st);
+    if (e || !n) return e;
+    uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
+    k_count_keys<<<blocks, 256, 0, st>>>(keys, n, s.hist);
+    return cudaGetLastError();
+}
+
+cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * cells, st);
+    if (e) return e;
+    k_set_word<<<1, 1, 0, st>>>(s.hist, n);
+    return cudaGetLastError();
+}
+
+cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st) {
+    uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
+    k_cell_scan<<<tiles, kScanThreads, 0, st>>>(s.hist, cells, offs, s.cursor, s.status,
+                                                s.status + s.status_words, ctl + kCtlError);
+    return cudaGetLastError();
+}
+
+cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
+                          const uint32_t* offs, uint32_t* perm, cudaStream_t st) {
+    cudaError_t e;
+    if (n) {
+        uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
+        k_cell_scatter<<<blocks, 256, 0, st>>>(keys, n, s.cursor, perm);
+        if ((e = cudaGetLastError())) return e;
+    }
+    uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
+    k_cell_fixup<<<(cells + 255u) / 256u, 256, 0, st>>>(offs, cells, perm, s.status, tiles,
+                                                        s.status + s.status_words);
+    return cudaGetLastError();
+}
+
+}  // namespace mb

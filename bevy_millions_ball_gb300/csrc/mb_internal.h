@@ -94,15 +94,42 @@ struct PhysParams {
 
 PhysParams make_params(const mb_consts& c);
 
+// Physics passes.  `hist` (nullable) accumulates the per-cell counts of the
+// keys they emit, for the next frame's counting sort.
 cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t* perm,
                                 const float4* pos_in, const uint4* vfme_in, float4* pos_out,
-                                uint4* vfme_out, uint32_t* keys_out, cudaStream_t st);
+                                uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, cudaStream_t st);
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* perm,
                                 const uint32_t* offs, const float4* pos_in, const uint4* vfme_in,
-                                float4* pos_out, uint4* vfme_out, uint32_t* keys_out, int block,
+                                float4* pos_out, uint4* vfme_out, uint32_t* keys_out, uint32_t* hist,
                                 cudaStream_t st);
 cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,
-                         cudaStream_t st);
+                         uint32_t* hist, cudaStream_t st);
+
+// Counting sort of cell keys (mb_count.cu).
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;
+
+struct CountScratch {
+    uint32_t max_cells = 0;
+    uint32_t* hist = nullptr;     // [max_cells] counts of the keys of the next sort
+    uint32_t* cursor = nullptr;   // [max_cells] scatter cursors
+    uint32_t* status = nullptr;   // [status_words] scan look-back words + 1 tile ticket
+    uint32_t status_words = 0;
+};
+cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells);
+void count_scratch_free(CountScratch& s);
+// hist := counts of keys (rebuild, e.g. after an upload or a grid change).
+cudaError_t count_keys(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
+                       cudaStream_t st);
+// hist := counts of n all-zero keys (a fresh upload).
+cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, cudaStream_t st);
+// offs[0..cells] := exclusive scan of hist (offs[cells] = n), cursors := offs, hist := 0.
+cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st);
+// perm := stable permutation sorting keys by cell, from the cursors of count_scan.
+cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
+                          const uint32_t* offs, uint32_t* perm, cudaStream_t st);
 
 int device_sm_count();
 

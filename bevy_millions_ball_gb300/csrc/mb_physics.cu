@@ -162,22 +162,16 @@ __device__ __forceinline__ void cube(const PhysParams& P, Agent& a) {
     }
 }
 
-// Contacts against the candidate slots [lo, hi), skipping `skip`.
-__device__ __forceinline__ void contacts(const PhysParams& P, Agent& a, uint32_t lo, uint32_t hi,
-                                         uint32_t skip, const uint32_t* __restrict__ perm,
-                                         const float4* __restrict__ pos_in,
-                                         const uint4* __restrict__ vfme_in) {
-    if (lo >= hi) return;
-    uint32_t old = __ldg(perm + lo);
-    for (uint32_t j = lo; j < hi; ++j) {
-        uint32_t nxt = (j + 1u < hi) ? __ldg(perm + j + 1u) : 0u;
-        if (j != skip) {
-            float4 p = __ldg(pos_in + old);
-            uint4 q = __ldg(vfme_in + old);
-            sphere(P, a, unpack(p, q));
-        }
-        old = nxt;
-    }
+// solve_sphere_constraint against a packed neighbour (raw float4 + uint4).  The
+// distance test first rejects pairs whose squared distance exceeds the squared
+// edge by a 0.3% margin: sqrt is monotone and correctly rounded, so such pairs
+// can never pass `length(tpos) <= edge`, and all others take the exact path.
+__device__ __forceinline__ void sphere_raw(const PhysParams& P, Agent& a, float4 bp, uint4 bq) {
+    float edge = bp.w + a.scale;
+    V3 tpos = a.position - V3{bp.x, bp.y, bp.z};
+    float d2 = dot3(tpos, tpos);
+    if (d2 > (edge * edge) * 1.003f) return;
+    sphere(P, a, unpack(bp, bq));
 }
 
 // main, INIT pipeline (physics.wgsl:91-96): gather through perm, re-pack, emit key.
@@ -185,45 +179,126 @@ __global__ void __launch_bounds__(256)
     k_physics_init(PhysParams P, uint32_t n, const uint32_t* __restrict__ perm,
                    const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in,
                    float4* __restrict__ pos_out, uint4* __restrict__ vfme_out,
-                   uint32_t* __restrict__ keys_out) {
+                   uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint32_t old = perm[i];
+    uint32_t old = min(perm[i], n - 1u);
     float4 p = pos_in[old];
     Agent a = unpack(p, vfme_in[old]);
     uint32_t cx, cz;
     cell_of(P, a.position.x, a.position.z, cx, cz);
     pos_out[i] = make_float4(a.position.x, a.position.y, a.position.z, a.scale);
     vfme_out[i] = pack(a);
-    keys_out[i] = cz * P.N + cx;
+    uint32_t key = cz * P.N + cx;
+    keys_out[i] = key;
+    if (hist) atomicAdd(hist + key, 1u);
 }
 
-// main, LOOP pipeline (physics.wgsl:57-89), one thread per sorted slot.
-__global__ void __launch_bounds__(256)
+// Neighbour row-bands of a tile of sorted slots.  Band b (row offset b-1 = -1, 0,
+// +1) is the union of every tile sphere's candidate range in that row: since
+// slots are sorted by cell, it is one contiguous slot range.  Bands of at most
+// kBandCap slots are staged in shared memory through perm (all loads of a band
+// in flight at once); wider bands (a tile spanning a row boundary) are read from
+// global memory instead.
+constexpr int kTileThreads = 128;
+constexpr uint32_t kBandCap = 2 * kTileThreads;
+
+__device__ __forceinline__ void contacts_band(const PhysParams& P, Agent& a, uint32_t lo, uint32_t hi,
+                                              uint32_t skip, uint32_t n, uint32_t band_lo,
+                                              uint32_t band_cnt, const float4* s_pos,
+                                              const uint4* s_vfme, const uint32_t* __restrict__ perm,
+                                              const float4* __restrict__ pos_in,
+                                              const uint4* __restrict__ vfme_in) {
+    hi = min(hi, n);
+    for (uint32_t j = lo; j < hi; ++j) {
+        if (j == skip) continue;
+        uint32_t r = j - band_lo;
+        if (r < band_cnt) {
+            sphere_raw(P, a, s_pos[r], s_vfme[r]);
+        } else {
+            uint32_t o = __ldg(perm + j);
+            if (o < n) sphere_raw(P, a, __ldg(pos_in + o), __ldg(vfme_in + o));
+        }
+    }
+}
+
+// main, LOOP pipeline (physics.wgsl:57-89): one thread per sorted slot, one
+// block per tile of kTileThreads consecutive slots.
+__global__ void __launch_bounds__(kTileThreads)
     k_physics_loop(PhysParams P, uint32_t n, const uint32_t* __restrict__ perm,
                    const uint32_t* __restrict__ offs, const float4* __restrict__ pos_in,
                    const uint4* __restrict__ vfme_in, float4* __restrict__ pos_out,
-                   uint4* __restrict__ vfme_out, uint32_t* __restrict__ keys_out) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t old = __ldg(perm + i);
-    Agent a = unpack(__ldg(pos_in + old), __ldg(vfme_in + old));
-    uint32_t cx, cz;
-    cell_of(P, a.position.x, a.position.z, cx, cz);
-    const uint32_t N = P.N;
-    const uint32_t key = cz * N + cx;
-    const uint32_t l = cx > 0u ? 1u : 0u, r = cx < N - 1u ? 2u : 1u;
+                   uint4* __restrict__ vfme_out, uint32_t* __restrict__ keys_out,
+                   uint32_t* __restrict__ hist) {
+    __shared__ float4 s_pos[3][kBandCap];
+    __shared__ uint4 s_vfme[3][kBandCap];
+    __shared__ uint32_t s_lo[3], s_cnt[3], s_kf, s_kl;
 
-    // neighbour ranges (independent loads, issued before the integration math)
-    uint32_t m_lo = __ldg(offs + key - l), m_hi = __ldg(offs + key + r);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t i0 = blockIdx.x * kTileThreads;
+    const uint32_t i = i0 + tid;
+    const uint32_t ilast = min(i0 + kTileThreads, n) - 1u;
+    const bool valid = i < n;
+    const uint32_t N = P.N;
+
+    Agent a;
+    uint32_t cx = 0, cz = 0, key = 0;
+    if (valid) {
+        uint32_t old = min(__ldg(perm + i), n - 1u);
+        a = unpack(__ldg(pos_in + old), __ldg(vfme_in + old));
+        cell_of(P, a.position.x, a.position.z, cx, cz);
+        key = cz * N + cx;
+        if (i == i0) s_kf = key;
+        if (i == ilast) s_kl = key;
+    }
+    __syncthreads();
+    if (tid < 3) {
+        const uint32_t kf = s_kf, kl = s_kl;
+        uint32_t lo = 0, hi = 0;
+        if (tid == 1) {  // own row
+            lo = offs[kf - (kf % N > 0u ? 1u : 0u)];
+            hi = offs[kl + (kl % N < N - 1u ? 2u : 1u)];
+        } else if (tid == 0) {  // row below, for tile spheres with cz > 0
+            if (kl >= N) {
+                uint32_t f = max(kf, N);
+                lo = offs[f - N - (f % N > 0u ? 1u : 0u)];
+                hi = offs[kl - N + (kl % N < N - 1u ? 2u : 1u)];
+            }
+        } else {  // row above, for tile spheres with cz < N-1
+            const uint32_t top = N * (N - 1u);
+            if (kf < top) {
+                uint32_t l = min(kl, top - 1u);
+                lo = offs[kf + N - (kf % N > 0u ? 1u : 0u)];
+                hi = offs[l + N + (l % N < N - 1u ? 2u : 1u)];
+            }
+        }
+        hi = min(hi, n);
+        s_lo[tid] = lo;
+        s_cnt[tid] = (hi > lo && hi - lo <= kBandCap) ? hi - lo : 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        const uint32_t lo = s_lo[b], cnt = s_cnt[b];
+        for (uint32_t r = tid; r < cnt; r += kTileThreads) {
+            uint32_t o = min(__ldg(perm + lo + r), n - 1u);
+            s_pos[b][r] = __ldg(pos_in + o);
+            s_vfme[b][r] = __ldg(vfme_in + o);
+        }
+    }
+    __syncthreads();
+    if (!valid) return;
+
+    const uint32_t l = cx > 0u ? 1u : 0u, rr = cx < N - 1u ? 2u : 1u;
+    uint32_t m_lo = __ldg(offs + key - l), m_hi = __ldg(offs + key + rr);
     uint32_t b_lo = 0, b_hi = 0, t_lo = 0, t_hi = 0;
     if (cz > 0u) {
         b_lo = __ldg(offs + key - N - l);
-        b_hi = __ldg(offs + key - N + r);
+        b_hi = __ldg(offs + key - N + rr);
     }
     if (cz < N - 1u) {
         t_lo = __ldg(offs + key + N - l);
-        t_hi = __ldg(offs + key + N + r);
+        t_hi = __ldg(offs + key + N + rr);
     }
 
     // verlet_integration (physics.wgsl:262-266)
@@ -234,11 +309,13 @@ __global__ void __launch_bounds__(256)
     }
     a.force = splat(0.0f);
 
-    // handle_collisions (physics.wgsl:119-169)
+    // handle_collisions (physics.wgsl:119-169): own row, row below, row above
     V3 old_pos = a.position;
-    contacts(P, a, m_lo, m_hi, i, perm, pos_in, vfme_in);
-    contacts(P, a, b_lo, b_hi, 0xFFFFFFFFu, perm, pos_in, vfme_in);
-    contacts(P, a, t_lo, t_hi, 0xFFFFFFFFu, perm, pos_in, vfme_in);
+    contacts_band(P, a, m_lo, m_hi, i, n, s_lo[1], s_cnt[1], s_pos[1], s_vfme[1], perm, pos_in, vfme_in);
+    contacts_band(P, a, b_lo, b_hi, 0xFFFFFFFFu, n, s_lo[0], s_cnt[0], s_pos[0], s_vfme[0], perm, pos_in,
+                  vfme_in);
+    contacts_band(P, a, t_lo, t_hi, 0xFFFFFFFFu, n, s_lo[2], s_cnt[2], s_pos[2], s_vfme[2], perm, pos_in,
+                  vfme_in);
     V3 diff = a.position - old_pos;
     if (len3(diff) > a.scale) {
         // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337)
@@ -261,17 +338,20 @@ __global__ void __launch_bounds__(256)
     vfme_out[i] = pack(a);
     uint32_t nx, nz;
     cell_of(P, a.position.x, a.position.z, nx, nz);
-    keys_out[i] = nz * N + nx;
+    const uint32_t nk = nz * N + nx;
+    keys_out[i] = nk;
+    if (hist) atomicAdd(hist + nk, 1u);
 }
 
 __global__ void k_rekey(PhysParams P, uint32_t n, const float4* __restrict__ pos,
-                        uint32_t* __restrict__ keys) {
+                        uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 p = pos[i];
     uint32_t cx, cz;
     cell_of(P, p.x, p.z, cx, cz);
     keys[i] = cz * P.N + cx;
+    if (hist) atomicAdd(hist + keys[i], 1u);
 }
 
 }  // namespace
@@ -302,28 +382,27 @@ PhysParams make_params(const mb_consts& c) {
 
 cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t* perm,
                                 const float4* pos_in, const uint4* vfme_in, float4* pos_out,
-                                uint4* vfme_out, uint32_t* keys_out, cudaStream_t st) {
+                                uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, cudaStream_t st) {
     if (!n) return cudaSuccess;
     k_physics_init<<<(n + 255u) / 256u, 256, 0, st>>>(p, n, perm, pos_in, vfme_in, pos_out, vfme_out,
-                                                      keys_out);
+                                                      keys_out, hist);
     return cudaGetLastError();
 }
 
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* perm,
                                 const uint32_t* offs, const float4* pos_in, const uint4* vfme_in,
-                                float4* pos_out, uint4* vfme_out, uint32_t* keys_out, int block,
+                                float4* pos_out, uint4* vfme_out, uint32_t* keys_out, uint32_t* hist,
                                 cudaStream_t st) {
     if (!n) return cudaSuccess;
-    if (block <= 0 || block > 256 || (block & 31)) block = 128;
-    k_physics_loop<<<(n + (uint32_t)block - 1u) / (uint32_t)block, block, 0, st>>>(
-        p, n, perm, offs, pos_in, vfme_in, pos_out, vfme_out, keys_out);
+    k_physics_loop<<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
+        p, n, perm, offs, pos_in, vfme_in, pos_out, vfme_out, keys_out, hist);
     return cudaGetLastError();
 }
 
 cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,
-                         cudaStream_t st) {
+                         uint32_t* hist, cudaStream_t st) {
     if (!n) return cudaSuccess;
-    k_rekey<<<(n + 255u) / 256u, 256, 0, st>>>(p, n, pos, keys);
+    k_rekey<<<(n + 255u) / 256u, 256, 0, st>>>(p, n, pos, keys, hist);
     return cudaGetLastError();
 }
 

@@ -278,8 +278,10 @@ __global__ void __launch_bounds__(THREADS)
         uint32_t key = s_keys[i];
         uint32_t d = (key >> shift) & mask;
         uint32_t pos = s_goff[d] + (i - s_cnt[d]);
-        keys_out[pos] = key;
-        vals_out[pos] = s_vals[i];
+        if (pos < n) {  // always true unless a look-back wait gave up (error flagged)
+            keys_out[pos] = key;
+            vals_out[pos] = s_vals[i];
+        }
     }
 }
 

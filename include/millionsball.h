@@ -196,12 +196,20 @@ mb_status mb_sort_and_hash(mb_sort_plan* p, const uint32_t* keys, const uint32_t
                            uint32_t number_of_cells, uint32_t* sorted_keys, uint32_t* sorted_vals,
                            uint32_t* start, uint32_t* close, void* cuda_stream);
 
-/* Pick sort digit widths / block shapes for a scene size (the autotuner). */
+/* Per-world kernel choices (the autotuner's knobs). */
 typedef struct mb_tuning {
-    uint32_t digit_bits_max;   /* widest radix digit, 4..11 */
-    uint32_t collide_block;    /* threads per block of the physics kernel */
-    uint32_t reserved[6];
+    uint32_t digit_bits_max;   /* widest radix digit of the onesweep sort, 4..11 */
+    uint32_t collide_block;    /* reserved: the physics kernel's tile is fixed at 128 slots */
+    uint32_t sort_algorithm;   /* MB_SORT_COUNTING (default) or MB_SORT_ONESWEEP */
+    uint32_t reserved[5];
 } mb_tuning;
+
+/* Frame sort: both produce the identical stable permutation and cell ranges.
+ *   MB_SORT_COUNTING: per-cell counts (emitted by the previous physics pass) ->
+ *                     look-back scan = cell offsets -> scatter -> in-cell fixup
+ *   MB_SORT_ONESWEEP: onesweep LSD radix sort of the keys, then the cell-offset build */
+#define MB_SORT_COUNTING 0u
+#define MB_SORT_ONESWEEP 1u
 mb_status mb_get_tuning(const mb_world* w, mb_tuning* out);
 mb_status mb_set_tuning(mb_world* w, const mb_tuning* t);
 

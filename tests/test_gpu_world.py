@@ -101,16 +101,39 @@ def test_sparse_grid_more_cells_than_agents(built_lib, cuda):
 
 
 @pytest.mark.parametrize("digit_bits", [4, 6, 8, 11])
-def test_digit_widths_agree(built_lib, cuda, digit_bits):
+def test_onesweep_digit_widths_agree(built_lib, cuda, digit_bits):
+    """The world with the onesweep radix sort instead of the counting sort."""
     sc = scenes.plain_uniform(70_000, 256, seed=21)
     with World(sc.plugin) as w:
-        w.set_tuning(digit_bits_max=digit_bits, collide_block=64 if digit_bits == 4 else 128)
+        w.set_tuning(digit_bits_max=digit_bits, sort_algorithm=1)
         ow = oracle.OracleWorld(sc.plugin.to_c())
         w.set_state(sc.pos_scale, sc.vfme)
         ow.set_state(sc.pos_scale, sc.vfme)
         w.step(12)
         ow.step(12)
         compare(w, ow, 12)
+
+
+def test_switch_sort_algorithm_midrun(built_lib, cuda):
+    """Counting <-> onesweep switches keep the frame sequence identical."""
+    sc = scenes.plain_clustered(120_000, 256, clusters=3, sigma_xz=12.0, seed=17)
+    with World(sc.plugin) as w:
+        ow = oracle.OracleWorld(sc.plugin.to_c())
+        w.set_state(sc.pos_scale, sc.vfme)
+        ow.set_state(sc.pos_scale, sc.vfme)
+        for alg, k in [(1, 3), (0, 4), (1, 2), (0, 5)]:
+            w.set_tuning(sort_algorithm=alg)
+            w.step(k)
+            ow.step(k)
+            compare(w, ow, ow.time)
+    with World(sc.plugin) as w:  # onesweep from the upload on
+        w.set_tuning(sort_algorithm=1)
+        ow = oracle.OracleWorld(sc.plugin.to_c())
+        w.set_state(sc.pos_scale, sc.vfme)
+        ow.set_state(sc.pos_scale, sc.vfme)
+        w.step(6)
+        ow.step(6)
+        compare(w, ow, 6)
 
 
 def test_settings_change_midrun(built_lib, cuda):
@@ -220,6 +243,8 @@ def test_errors_are_reported_not_fatal(built_lib, cuda):
         w.set_settings(PhysicsPlugin(max_number_of_agents=2048))
     with pytest.raises(MbError):
         w.set_tuning(digit_bits_max=12)
+    with pytest.raises(MbError):
+        w.set_tuning(sort_algorithm=7)
     w.close()
 
 
