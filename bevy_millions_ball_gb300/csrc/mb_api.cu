@@ -135,7 +135,12 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
     cudaError_t e;
     uint32_t* hist = nullptr;
     if ((e = mark(w, 0, st, capturing))) return e;
-    if (counting(w)) {
+    if (counting(w) && init) {
+        // frame 0 after an upload sorts all-zero keys: identity order, one full cell
+        if ((e = mb::count_init_order(w->cnt, w->n, w->cells, w->scratch.offs, w->perm, st))) return e;
+        if ((e = mark(w, 1, st, capturing))) return e;
+        hist = w->cnt.hist;
+    } else if (counting(w)) {
         // cell offsets first (scan of the counts), then the permutation
         if ((e = mb::count_scan(w->cnt, w->scratch.ctl, w->cells, w->scratch.offs, st))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
@@ -245,7 +250,7 @@ mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out) {
     cudaGetDevice(&w->device);
     w->stream = (cudaStream_t)cuda_stream;
     w->n = s->max_number_of_agents;
-    w->tuning.digit_bits_max = 11;
+    w->tuning.digit_bits_max = 8;
     w->tuning.collide_block = 128;
     w->tuning.sort_algorithm = MB_SORT_COUNTING;
     apply_settings(w, *s);
@@ -483,7 +488,7 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
 // ------------------------------------------------------------------ stages
 struct mb_sort_plan {
     mb::SortScratch scratch;
-    uint32_t digit_bits_max = 11;
+    uint32_t digit_bits_max = 8;
 };
 
 mb_status mb_sort_plan_create(uint32_t max_keys, uint32_t max_cells, mb_sort_plan** out) {
@@ -561,9 +566,9 @@ mb_status mb_last_frame_times(mb_world* w, float* ms) {
 
 uint32_t mb_kernels_per_frame(const mb_world* w) {
     if (!w) return 0u;
-    // counting: scan + scatter + fixup + physics;
+    // counting: scan + scatter + fixup + big-cell fixup + physics;
     // onesweep: histogram + one kernel per digit pass + cell offsets + physics
-    return counting(w) ? 4u : (uint32_t)w->sched.passes + 3u;
+    return counting(w) ? 5u : (uint32_t)w->sched.passes + 3u;
 }
 
 const char* mb_version(void) { return "millionsball-gb300 " __DATE__ " sm_103a"; }

@@ -8,7 +8,7 @@
 //   1. per-cell counts, accumulated by the physics pass of the previous frame as
 //      it emits the keys (one red.add per sphere);
 //   2. k_cell_scan: one single-pass exclusive scan (decoupled look-back with a
-//      32-tile window) turns the counts into the cell offsets offs[c] (= start of
+//      128-tile window) turns the counts into the cell offsets offs[c] (= start of
 //      cell c; offs[C] = n) and a cursor copy, and zeroes the counts;
 //   3. k_cell_scatter: each sphere claims a slot of its cell with one atomic per
 //      run of equal keys in its warp (match.any), so spheres of one warp keep
@@ -43,13 +43,15 @@ __device__ __forceinline__ uint32_t ld_rlx(const uint32_t* p) {
 // ---------------------------------------------------------------- scan
 __global__ void __launch_bounds__(kScanThreads)
     k_cell_scan(uint32_t* __restrict__ hist, uint32_t cells, uint32_t* __restrict__ offs,
-                uint32_t* __restrict__ cursor, uint32_t* status, uint32_t* ticket, uint32_t* err) {
+                uint32_t* __restrict__ cursor, uint32_t* status, uint32_t* ticket, uint32_t* big_ctl,
+                uint32_t* err) {
     constexpr int W = kScanThreads / 32;
     __shared__ uint32_t s_tile, s_warp[W], s_excl;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(ticket, 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
+    if (tile == 0 && tid < 2) big_ctl[tid] = 0u;  // big-cell list of this frame starts empty
     const uint32_t base = tile * kScanTile + tid * kScanItems;
 
     uint32_t v[kScanItems];
@@ -97,14 +99,28 @@ __global__ void __launch_bounds__(kScanThreads)
             uint32_t spins = 0;
             bool gave_up = false;
             while (true) {
-                int32_t idx = top - (int32_t)lane;
-                uint32_t s = idx >= 0 ? ld_rlx(status + idx) : (kFlagPre << 30);
-                uint32_t f = s >> 30;
-                uint32_t pmask = __ballot_sync(0xFFFFFFFFu, f == kFlagPre);
-                uint32_t zmask = __ballot_sync(0xFFFFFFFFu, f == 0u);
+                // window of 128 predecessors: lane l holds tiles top-4l .. top-4l-3
+                uint32_t sv[4];
+                int qf = 4;  // first inclusive-prefix word of this lane
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    int32_t idx = top - (int32_t)(4u * lane) - q;
+                    sv[q] = idx >= 0 ? ld_rlx(status + idx) : (kFlagPre << 30);
+                    if (qf == 4 && (sv[q] >> 30) == kFlagPre) qf = q;
+                }
+                uint32_t pmask = __ballot_sync(0xFFFFFFFFu, qf < 4);
                 uint32_t first = pmask ? (uint32_t)(__ffs(pmask) - 1) : 32u;
-                uint32_t upto = first == 32u ? 0xFFFFFFFFu : ((2u << first) - 1u);
-                if (zmask & upto) {
+                int upto = lane < first ? 3 : (lane == first ? qf : -1);
+                bool notready = false;
+                uint32_t mine = 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (q <= upto) {
+                        if ((sv[q] >> 30) == 0u) notready = true;
+                        mine += sv[q] & kValMask;
+                    }
+                }
+                if (__any_sync(0xFFFFFFFFu, notready)) {
                     if (++spins > kSpinMax) {
                         if (lane == 0) atomicOr(err, 2u);
                         gave_up = true;
@@ -113,12 +129,11 @@ __global__ void __launch_bounds__(kScanThreads)
                     if (spins > 32u) __nanosleep(32);
                     continue;
                 }
-                uint32_t mine = (lane <= first) ? (s & kValMask) : 0u;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xFFFFFFFFu, mine, o);
                 excl += mine;
                 if (first < 32u) break;
-                top -= 32;
+                top -= 128;
             }
             (void)gave_up;
             if (lane == 0) st_rlx(status + tile, (kFlagPre << 30) | ((excl + total) & kValMask));
@@ -177,9 +192,14 @@ __global__ void __launch_bounds__(256)
 }
 
 // ---------------------------------------------------------------- fixup
+// Cells of up to kSmallCell slots are re-sorted by their own thread (insertion
+// sort, after a sortedness check); larger ones go to a list for k_cell_fixup_big.
+constexpr uint32_t kSmallCell = 32;
+constexpr uint32_t kBlockSortMax = 8192;
+
 __global__ void __launch_bounds__(256)
     k_cell_fixup(const uint32_t* __restrict__ offs, uint32_t cells, uint32_t* perm, uint32_t* status,
-                 uint32_t status_words, uint32_t* ticket) {
+                 uint32_t status_words, uint32_t* ticket, uint32_t* big_ctl, uint32_t* big) {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (blockIdx.x == 0) {  // the scan of this frame is over: reset its look-back state
         for (uint32_t s = threadIdx.x; s < status_words; s += blockDim.x) status[s] = 0u;
@@ -188,6 +208,10 @@ __global__ void __launch_bounds__(256)
     if (c >= cells) return;
     const uint32_t lo = offs[c], hi = offs[c + 1u];
     if (hi - lo < 2u) return;
+    if (hi - lo > kSmallCell) {
+        big[atomicAdd(big_ctl, 1u)] = c;
+        return;
+    }
     bool sorted = true;
     uint32_t prev = perm[lo];
     for (uint32_t j = lo + 1u; j < hi; ++j) {
@@ -206,6 +230,91 @@ __global__ void __launch_bounds__(256)
             --b;
         }
         perm[b] = x;
+    }
+}
+
+__device__ void heap_sift(uint32_t* a, uint32_t root, uint32_t end) {
+    while (true) {
+        uint32_t child = 2u * root + 1u;
+        if (child >= end) return;
+        if (child + 1u < end && a[child + 1u] > a[child]) ++child;
+        if (a[root] >= a[child]) return;
+        uint32_t t = a[root];
+        a[root] = a[child];
+        a[child] = t;
+        root = child;
+    }
+}
+
+// One block per listed cell: bitonic sort in shared memory (up to kBlockSortMax
+// slots), else an O(m log m) heapsort in place by one thread (only degenerate
+// scenes with thousands of spheres in one cell get there).
+__global__ void __launch_bounds__(256)
+    k_cell_fixup_big(const uint32_t* __restrict__ offs, uint32_t* perm, uint32_t* big_ctl,
+                     const uint32_t* __restrict__ big) {
+    __shared__ uint32_t s_v[kBlockSortMax];
+    __shared__ uint32_t s_idx, s_unsorted;
+    const uint32_t tid = threadIdx.x;
+    while (true) {
+        if (tid == 0) {
+            s_idx = atomicAdd(big_ctl + 1, 1u);
+            s_unsorted = 0u;
+        }
+        __syncthreads();
+        const uint32_t idx = s_idx;
+        if (idx >= __ldcg(big_ctl)) return;
+        const uint32_t c = __ldg(big + idx);
+        const uint32_t lo = offs[c], m = offs[c + 1u] - lo;
+        for (uint32_t j = tid + 1u; j < m; j += blockDim.x)
+            if (perm[lo + j] < perm[lo + j - 1u]) s_unsorted = 1u;
+        __syncthreads();
+        if (s_unsorted) {
+            if (m <= kBlockSortMax) {
+                uint32_t P = 2u;
+                while (P < m) P <<= 1;
+                for (uint32_t j = tid; j < P; j += blockDim.x) s_v[j] = j < m ? perm[lo + j] : 0xFFFFFFFFu;
+                __syncthreads();
+                for (uint32_t k = 2u; k <= P; k <<= 1) {
+                    for (uint32_t jj = k >> 1; jj > 0u; jj >>= 1) {
+                        for (uint32_t i = tid; i < P; i += blockDim.x) {
+                            uint32_t ixj = i ^ jj;
+                            if (ixj > i) {
+                                uint32_t a = s_v[i], b = s_v[ixj];
+                                bool up = (i & k) == 0u;
+                                if ((a > b) == up) {
+                                    s_v[i] = b;
+                                    s_v[ixj] = a;
+                                }
+                            }
+                        }
+                        __syncthreads();
+                    }
+                }
+                for (uint32_t j = tid; j < m; j += blockDim.x) perm[lo + j] = s_v[j];
+            } else if (tid == 0) {
+                uint32_t* a = perm + lo;
+                for (uint32_t r = m / 2u; r-- > 0u;) heap_sift(a, r, m);
+                for (uint32_t end = m - 1u; end > 0u; --end) {
+                    uint32_t t = a[0];
+                    a[0] = a[end];
+                    a[end] = t;
+                    heap_sift(a, 0u, end);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// INIT frame after an upload: every key is 0, so the stable order is the
+// identity and cell 0 holds everyone.  Also clears the counts (only hist[0] is set).
+__global__ void k_init_order(uint32_t n, uint32_t cells, uint32_t* perm, uint32_t* offs,
+                             uint32_t* hist) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= max(n, cells); i += stride) {
+        if (i < n) perm[i] = i;
+        if (i <= cells) offs[i] = i == 0u ? 0u : n;
+        if (i < cells) hist[i] = 0u;
     }
 }
 
@@ -235,9 +344,10 @@ cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells) {
     cudaError_t e;
     if ((e = cudaMalloc(&s.hist, sizeof(uint32_t) * padded))) return e;
     if ((e = cudaMalloc(&s.cursor, sizeof(uint32_t) * padded))) return e;
-    if ((e = cudaMalloc(&s.status, sizeof(uint32_t) * (s.status_words + 1u)))) return e;
+    if ((e = cudaMalloc(&s.status, sizeof(uint32_t) * (s.status_words + 3u)))) return e;
+    if ((e = cudaMalloc(&s.big, sizeof(uint32_t) * ((size_t)max_cells + 1u)))) return e;
     if ((e = cudaMemset(s.hist, 0, sizeof(uint32_t) * padded))) return e;
-    if ((e = cudaMemset(s.status, 0, sizeof(uint32_t) * (s.status_words + 1u)))) return e;
+    if ((e = cudaMemset(s.status, 0, sizeof(uint32_t) * (s.status_words + 3u)))) return e;
     return cudaSuccess;
 }
 
@@ -245,6 +355,7 @@ void count_scratch_free(CountScratch& s) {
     cudaFree(s.hist);
     cudaFree(s.cursor);
     cudaFree(s.status);
+    cudaFree(s.big);
     s = CountScratch();
 }
 
@@ -267,7 +378,8 @@ cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, c
 cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st) {
     uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
     k_cell_scan<<<tiles, kScanThreads, 0, st>>>(s.hist, cells, offs, s.cursor, s.status,
-                                                s.status + s.status_words, ctl + kCtlError);
+                                                s.status + s.status_words, s.status + s.status_words + 1,
+                                                ctl + kCtlError);
     return cudaGetLastError();
 }
 
@@ -280,8 +392,19 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
         if ((e = cudaGetLastError())) return e;
     }
     uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
+    uint32_t* big_ctl = s.status + s.status_words + 1;
     k_cell_fixup<<<(cells + 255u) / 256u, 256, 0, st>>>(offs, cells, perm, s.status, tiles,
-                                                        s.status + s.status_words);
+                                                        s.status + s.status_words, big_ctl, s.big);
+    if ((e = cudaGetLastError())) return e;
+    k_cell_fixup_big<<<(uint32_t)device_sm_count(), 256, 0, st>>>(offs, perm, big_ctl, s.big);
+    return cudaGetLastError();
+}
+
+cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32_t* offs, uint32_t* perm,
+                             cudaStream_t st) {
+    uint32_t m = std::max(n, cells) + 1u;
+    uint32_t blocks = std::min<uint32_t>((m + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
+    k_init_order<<<blocks, 256, 0, st>>>(n, cells, perm, offs, s.hist);
     return cudaGetLastError();
 }
 

@@ -90,6 +90,8 @@ struct PhysParams {
     float neg_c_over_dt;      // -C_AGENT / T_DELTA
     float neg_1pe_over_dt;    // -(1 + E_ENVIR) / T_DELTA
     uint32_t spring;
+    float filter_margin;      // contact-loop pre-filter margin (0 = exact loop only)
+    float pos_slack;          // rounding slack added per applied contact shift
 };
 
 PhysParams make_params(const mb_consts& c);
@@ -115,7 +117,9 @@ struct CountScratch {
     uint32_t max_cells = 0;
     uint32_t* hist = nullptr;     // [max_cells] counts of the keys of the next sort
     uint32_t* cursor = nullptr;   // [max_cells] scatter cursors
-    uint32_t* status = nullptr;   // [status_words] scan look-back words + 1 tile ticket
+    uint32_t* status = nullptr;   // [status_words] scan look-back words, then the tile
+                                  // ticket, then the big-cell list count and cursor
+    uint32_t* big = nullptr;      // cells with more than 32 spheres this frame
     uint32_t status_words = 0;
 };
 cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells);
@@ -127,6 +131,9 @@ cudaError_t count_keys(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
 cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, cudaStream_t st);
 // offs[0..cells] := exclusive scan of hist (offs[cells] = n), cursors := offs, hist := 0.
 cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st);
+// INIT frame after an upload (all keys 0): perm := identity, offs := [0, n, .., n], hist := 0.
+cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32_t* offs, uint32_t* perm,
+                             cudaStream_t st);
 // perm := stable permutation sorting keys by cell, from the cursors of count_scan.
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, cudaStream_t st);

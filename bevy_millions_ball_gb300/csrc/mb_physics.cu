@@ -96,11 +96,13 @@ __device__ __forceinline__ void cell_of(const PhysParams& P, float x, float z, u
     cz = min(cz, P.N - 1u);
 }
 
-// solve_sphere_constraint (physics.wgsl:300-331)
-__device__ __forceinline__ void sphere(const PhysParams& P, Agent& a, const Agent& b) {
+// solve_sphere_constraint (physics.wgsl:300-331).  Returns the length factor of
+// the position change it applied (0 if none): |dp| <= returned value * |norm|.
+__device__ __forceinline__ float sphere(const PhysParams& P, Agent& a, const Agent& b) {
     float edge = b.scale + a.scale;
     V3 tpos = a.position - b.position;
     float dist = len3(tpos);
+    float moved = 0.0f;
     if (dist <= edge) {
         V3 norm = normalize3(tpos);
         if (!P.spring) {
@@ -117,15 +119,20 @@ __device__ __forceinline__ void sphere(const PhysParams& P, Agent& a, const Agen
             }
             float h = 0.5f * (edge - dist);
             a.position = a.position + h * norm;
+            moved = h;
         } else {
             float makeup = edge - dist;
             V3 kforce = (P.k_agent * makeup) * norm;
             V3 cforce = P.neg_c_over_dt * a.velocity;
             a.force = a.force + (kforce + cforce);
             float limit = makeup - P.r_agent * a.scale;
-            if (limit > 0.0f) a.position = a.position + limit * norm;
+            if (limit > 0.0f) {
+                a.position = a.position + limit * norm;
+                moved = limit;
+            }
         }
     }
+    return moved;
 }
 
 // solve_cube_constraint (physics.wgsl:269-298)
@@ -166,12 +173,12 @@ __device__ __forceinline__ void cube(const PhysParams& P, Agent& a) {
 // distance test first rejects pairs whose squared distance exceeds the squared
 // edge by a 0.3% margin: sqrt is monotone and correctly rounded, so such pairs
 // can never pass `length(tpos) <= edge`, and all others take the exact path.
-__device__ __forceinline__ void sphere_raw(const PhysParams& P, Agent& a, float4 bp, uint4 bq) {
+__device__ __forceinline__ float sphere_raw(const PhysParams& P, Agent& a, float4 bp, uint4 bq) {
     float edge = bp.w + a.scale;
     V3 tpos = a.position - V3{bp.x, bp.y, bp.z};
     float d2 = dot3(tpos, tpos);
-    if (d2 > (edge * edge) * 1.003f) return;
-    sphere(P, a, unpack(bp, bq));
+    if (d2 > (edge * edge) * 1.003f) return 0.0f;
+    return sphere(P, a, unpack(bp, bq));
 }
 
 // main, INIT pipeline (physics.wgsl:91-96): gather through perm, re-pack, emit key.
@@ -203,22 +210,104 @@ __global__ void __launch_bounds__(256)
 constexpr int kTileThreads = 128;
 constexpr uint32_t kBandCap = 2 * kTileThreads;
 
-__device__ __forceinline__ void contacts_band(const PhysParams& P, Agent& a, uint32_t lo, uint32_t hi,
-                                              uint32_t skip, uint32_t n, uint32_t band_lo,
-                                              uint32_t band_cnt, const float4* s_pos,
-                                              const uint4* s_vfme, const uint32_t* __restrict__ perm,
-                                              const float4* __restrict__ pos_in,
-                                              const uint4* __restrict__ vfme_in) {
-    hi = min(hi, n);
-    for (uint32_t j = lo; j < hi; ++j) {
-        if (j == skip) continue;
-        uint32_t r = j - band_lo;
-        if (r < band_cnt) {
-            sphere_raw(P, a, s_pos[r], s_vfme[r]);
-        } else {
-            uint32_t o = __ldg(perm + j);
-            if (o < n) sphere_raw(P, a, __ldg(pos_in + o), __ldg(vfme_in + o));
+// The candidates of one sphere, in the reference's order (physics.wgsl:119-160):
+// own row without itself, row below, row above.  Ordinal o maps to a slot j and
+// the shared-memory band holding it (if that band was staged).
+struct Cands {
+    uint32_t m_lo, n_mid, b_lo, n_bot, t_lo, n_top, self;
+    __device__ __forceinline__ uint32_t total() const { return n_mid + n_bot + n_top; }
+    __device__ __forceinline__ uint32_t slot(uint32_t o, int& band) const {
+        if (o < n_mid) {
+            band = 1;
+            uint32_t j = m_lo + o;
+            return j >= self ? j + 1u : j;
         }
+        o -= n_mid;
+        if (o < n_bot) {
+            band = 0;
+            return b_lo + o;
+        }
+        band = 2;
+        return t_lo + (o - n_bot);
+    }
+};
+
+struct Bands {
+    const float4 (*pos)[kBandCap];
+    const uint4 (*vfme)[kBandCap];
+    const uint32_t* lo;
+    const uint32_t* cnt;
+};
+
+__device__ __forceinline__ float4 cand_pos(const Bands& B, int band, uint32_t j, uint32_t n,
+                                           const uint32_t* __restrict__ perm,
+                                           const float4* __restrict__ pos_in) {
+    uint32_t r = j - B.lo[band];
+    if (r < B.cnt[band]) return B.pos[band][r];
+    return __ldg(pos_in + min(__ldg(perm + j), n - 1u));
+}
+__device__ __forceinline__ uint4 cand_vfme(const Bands& B, int band, uint32_t j, uint32_t n,
+                                          const uint32_t* __restrict__ perm,
+                                          const uint4* __restrict__ vfme_in) {
+    uint32_t r = j - B.lo[band];
+    if (r < B.cnt[band]) return B.vfme[band][r];
+    return __ldg(vfme_in + min(__ldg(perm + j), n - 1u));
+}
+
+// handle_collisions' contact loop (physics.wgsl:122-160), in two phases that give
+// the same result as the plain sequential loop:
+//  1. the first 64 candidates are classified against the position p0 at loop
+//     entry: "near" if within edge + margin (squared test with slack);
+//  2. contacts run in candidate order over the near ones only, while a bound on
+//     |p - p0| (sum of applied shifts, with rounding slack) stays below the
+//     margin: then every skipped candidate is farther than edge from p and
+//     would have been a no-op.  If the bound is exceeded, or beyond ordinal 63,
+//     the remaining candidates run through the exact loop.
+__device__ __forceinline__ void collide_all(const PhysParams& P, Agent& a, const Cands& C,
+                                            const Bands& B, uint32_t n,
+                                            const uint32_t* __restrict__ perm,
+                                            const float4* __restrict__ pos_in,
+                                            const uint4* __restrict__ vfme_in) {
+    const uint32_t total = C.total();
+    uint32_t start = 0;  // ordinals from here on take the exact loop
+    // the rounding slack below assumes |coordinate| <= 8192 (ulp <= 2^-10)
+    const bool small = fabsf(a.position.x) <= 8192.0f && fabsf(a.position.y) <= 8192.0f &&
+                       fabsf(a.position.z) <= 8192.0f;
+    if (P.filter_margin > 0.0f && small) {
+        uint64_t near = 0;
+        const uint32_t nf = min(total, 64u);
+        for (uint32_t o = 0; o < nf; ++o) {
+            int band;
+            uint32_t j = C.slot(o, band);
+            float4 bp = cand_pos(B, band, j, n, perm, pos_in);
+            float em = (bp.w + a.scale) + P.filter_margin;
+            V3 tpos = a.position - V3{bp.x, bp.y, bp.z};
+            float d2 = dot3(tpos, tpos);
+            if (!(d2 > (em * em) * 1.0001f)) near |= 1ull << o;
+        }
+        float disp = 0.0f;
+        const float limit = P.filter_margin - 0.02f;
+        start = nf;
+        while (near) {
+            uint32_t o = (uint32_t)(__ffsll((long long)near) - 1);
+            near &= near - 1ull;
+            int band;
+            uint32_t j = C.slot(o, band);
+            float mv = sphere_raw(P, a, cand_pos(B, band, j, n, perm, pos_in),
+                                  cand_vfme(B, band, j, n, perm, vfme_in));
+            if (mv != 0.0f) {
+                disp = disp + (mv * 1.001f + P.pos_slack);
+                if (!(disp <= limit)) {  // moved too far: later skips would not be safe
+                    start = o + 1u;
+                    break;
+                }
+            }
+        }
+    }
+    for (uint32_t o = start; o < total; ++o) {
+        int band;
+        uint32_t j = C.slot(o, band);
+        sphere_raw(P, a, cand_pos(B, band, j, n, perm, pos_in), cand_vfme(B, band, j, n, perm, vfme_in));
     }
 }
 
@@ -290,16 +379,26 @@ __global__ void __launch_bounds__(kTileThreads)
     if (!valid) return;
 
     const uint32_t l = cx > 0u ? 1u : 0u, rr = cx < N - 1u ? 2u : 1u;
-    uint32_t m_lo = __ldg(offs + key - l), m_hi = __ldg(offs + key + rr);
-    uint32_t b_lo = 0, b_hi = 0, t_lo = 0, t_hi = 0;
+    Cands C;
+    C.self = i;
+    C.m_lo = __ldg(offs + key - l);
+    {
+        uint32_t hi = min(__ldg(offs + key + rr), n);
+        C.n_mid = (hi > C.m_lo && i >= C.m_lo && i < hi) ? hi - C.m_lo - 1u : 0u;  // own cell holds i
+    }
+    C.b_lo = C.t_lo = 0;
+    C.n_bot = C.n_top = 0;
     if (cz > 0u) {
-        b_lo = __ldg(offs + key - N - l);
-        b_hi = __ldg(offs + key - N + rr);
+        C.b_lo = __ldg(offs + key - N - l);
+        uint32_t hi = min(__ldg(offs + key - N + rr), n);
+        C.n_bot = hi > C.b_lo ? hi - C.b_lo : 0u;
     }
     if (cz < N - 1u) {
-        t_lo = __ldg(offs + key + N - l);
-        t_hi = __ldg(offs + key + N + rr);
+        C.t_lo = __ldg(offs + key + N - l);
+        uint32_t hi = min(__ldg(offs + key + N + rr), n);
+        C.n_top = hi > C.t_lo ? hi - C.t_lo : 0u;
     }
+    Bands B{s_pos, s_vfme, s_lo, s_cnt};
 
     // verlet_integration (physics.wgsl:262-266)
     {
@@ -311,11 +410,7 @@ __global__ void __launch_bounds__(kTileThreads)
 
     // handle_collisions (physics.wgsl:119-169): own row, row below, row above
     V3 old_pos = a.position;
-    contacts_band(P, a, m_lo, m_hi, i, n, s_lo[1], s_cnt[1], s_pos[1], s_vfme[1], perm, pos_in, vfme_in);
-    contacts_band(P, a, b_lo, b_hi, 0xFFFFFFFFu, n, s_lo[0], s_cnt[0], s_pos[0], s_vfme[0], perm, pos_in,
-                  vfme_in);
-    contacts_band(P, a, t_lo, t_hi, 0xFFFFFFFFu, n, s_lo[2], s_cnt[2], s_pos[2], s_vfme[2], perm, pos_in,
-                  vfme_in);
+    collide_all(P, a, C, B, n, perm, pos_in, vfme_in);
     V3 diff = a.position - old_pos;
     if (len3(diff) > a.scale) {
         // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337)
@@ -377,6 +472,10 @@ PhysParams make_params(const mb_consts& c) {
     p.neg_c_over_dt = nc / c.time_delta;
     p.neg_1pe_over_dt = n1pe / c.time_delta;
     p.spring = c.enable_spring;
+    // contact-loop filter margin (collide_all): disabled on maps so large that
+    // f32 rounding of positions approaches the margin
+    p.filter_margin = c.half_map_size <= 4096.0f ? 0.25f : 0.0f;
+    p.pos_slack = 1e-3f;
     return p;
 }
 

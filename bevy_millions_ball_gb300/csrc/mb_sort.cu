@@ -32,6 +32,7 @@ constexpr uint32_t kFlagAggregate = 1u;
 constexpr uint32_t kFlagPrefix = 2u;
 constexpr uint32_t kValueMask = (1u << 28) - 1u;
 constexpr uint32_t kSpinLimit = 1u << 21;
+constexpr int kWindow = 16;  // look-back words loaded per step
 
 __device__ __forceinline__ uint32_t lb_pack(uint32_t flag, uint32_t epoch, uint32_t value) {
     return (flag << 30) | ((epoch & 3u) << 28) | (value & kValueMask);
@@ -204,29 +205,46 @@ __global__ void __launch_bounds__(THREADS)
     }
     __syncthreads();
 
-    // decoupled look-back: exclusive prefix of this digit over all earlier tiles
+    // decoupled look-back: exclusive prefix of this digit over all earlier tiles,
+    // reading a window of kWindow predecessor words at once (independent loads)
     bool gave_up = false;
     for (uint32_t d = tid; d < R; d += THREADS) {
         uint32_t cnt = s_cnt[d];
         uint32_t excl = 0;
         if (tile > 0) {
-            int32_t t = (int32_t)tile - 1;
+            int32_t top = (int32_t)tile - 1;
             uint32_t spins = 0;
-            while (t >= 0) {
-                uint32_t e = ld_relaxed(lookback + (size_t)t * R + d);
-                uint32_t f = e >> 30;
-                if (f == 0u || ((e >> 28) & 3u) != (epoch & 3u)) {
-                    if (gave_up || ++spins > kSpinLimit) {
-                        if (!gave_up) atomicOr(err, 1u);
-                        gave_up = true;
-                        break;
+            while (top >= 0 && !gave_up) {
+                uint32_t e[kWindow];
+#pragma unroll
+                for (int q = 0; q < kWindow; ++q)
+                    e[q] = (top - q >= 0) ? ld_relaxed(lookback + (size_t)(top - q) * R + d)
+                                          : lb_pack(kFlagPrefix, epoch, 0u);
+                uint32_t sum = 0;
+                bool ready = true, found = false;
+#pragma unroll
+                for (int q = 0; q < kWindow; ++q) {
+                    if (!ready || found) continue;
+                    uint32_t f = e[q] >> 30;
+                    if (f == 0u || ((e[q] >> 28) & 3u) != (epoch & 3u)) {
+                        ready = false;
+                        continue;
                     }
-                    if (spins > 64u) __nanosleep(64);
+                    sum += e[q] & kValueMask;
+                    if (f == kFlagPrefix) found = true;
+                }
+                if (!ready) {  // a predecessor has not published yet: retry this window
+                    if (++spins > kSpinLimit) {
+                        atomicOr(err, 1u);
+                        gave_up = true;
+                    } else if (spins > 16u) {
+                        __nanosleep(64);
+                    }
                     continue;
                 }
-                excl += e & kValueMask;
-                if (f == kFlagPrefix) break;
-                --t;
+                excl += sum;
+                if (found) break;
+                top -= kWindow;
             }
             st_relaxed(lb_tile + d, lb_pack(kFlagPrefix, epoch, excl + cnt));
         }

@@ -156,6 +156,18 @@ def test_settings_change_midrun(built_lib, cuda):
             compare(w, ow, ow.time)
 
 
+def test_crowded_cells_block_sort(built_lib, cuda):
+    """~200 spheres per cell: cells re-sorted by the block bitonic path."""
+    sc = scenes.plain_uniform(51_200, 16, grid_size=1, half_map_height=8, seed=31)
+    run_pair(sc, 4, [1, 2, 4])
+
+
+def test_degenerate_cells_heapsort(built_lib, cuda):
+    """~9,000 spheres per cell (N=2): the bounded single-thread heapsort path."""
+    sc = scenes.plain_uniform(36_000, 2, grid_size=4, half_map_height=8, seed=32)
+    run_pair(sc, 3, [1, 2, 3])
+
+
 def test_full_size_1m_frames_bit_exact(built_lib, cuda):
     """1,048,576 spheres, N=1024: the benchmark workload, 3 frames against the oracle."""
     sc = scenes.workload("P-1M")
