@@ -54,6 +54,8 @@ struct mb_world {
     cudaStream_t cap_stream = nullptr; // private stream used only to capture graphs
     float4* pos[2] = {nullptr, nullptr};
     uint4* vfme[2] = {nullptr, nullptr};
+    float4* spos = nullptr;            // state in sorted order (input of the LOOP pass)
+    uint4* svfme = nullptr;
     uint32_t* keys = nullptr;          // unsorted keys emitted by the last physics pass
     uint32_t* sorted_keys = nullptr;
     uint32_t* perm = nullptr;
@@ -134,31 +136,38 @@ bool counting(const mb_world* w) { return w->tuning.sort_algorithm == MB_SORT_CO
 cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool capturing = false) {
     cudaError_t e;
     uint32_t* hist = nullptr;
+    uint32_t* coarse = nullptr;
     if ((e = mark(w, 0, st, capturing))) return e;
     if (counting(w) && init) {
         // frame 0 after an upload sorts all-zero keys: identity order, one full cell
         if ((e = mb::count_init_order(w->cnt, w->n, w->cells, w->scratch.offs, w->perm, st))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
         hist = w->cnt.hist;
+        coarse = w->cnt.coarse;
     } else if (counting(w)) {
         // cell offsets first (scan of the counts), then the permutation
         if ((e = mb::count_scan(w->cnt, w->scratch.ctl, w->cells, w->scratch.offs, st))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
-        if ((e = mb::count_scatter(w->cnt, w->keys, w->n, w->cells, w->scratch.offs, w->perm, st))) return e;
+        if ((e = mb::count_scatter(w->cnt, w->keys, w->n, w->cells, w->scratch.offs, w->perm, w->pos[cur],
+                                   w->vfme[cur], w->spos, w->svfme, st)))
+            return e;
         hist = w->cnt.hist;
+        coarse = w->cnt.coarse;
     } else {
         if ((e = mb::sort_pairs(w->scratch, w->sched, w->keys, nullptr, w->sorted_keys, w->perm, st))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
         if ((e = mb::cell_offsets(w->scratch, w->sched, w->sorted_keys, st))) return e;
+        if (!init && (e = mb::gather_state(w->perm, w->n, w->pos[cur], w->vfme[cur], w->spos, w->svfme, st)))
+            return e;
     }
     if ((e = mark(w, 2, st, capturing))) return e;
     int nxt = cur ^ 1;
     if (init)
         e = mb::launch_physics_init(w->P, w->n, w->perm, w->pos[cur], w->vfme[cur], w->pos[nxt],
-                                    w->vfme[nxt], w->keys, hist, st);
+                                    w->vfme[nxt], w->keys, hist, coarse, st);
     else
-        e = mb::launch_physics_loop(w->P, w->n, w->perm, w->scratch.offs, w->pos[cur], w->vfme[cur],
-                                    w->pos[nxt], w->vfme[nxt], w->keys, hist, st);
+        e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->spos, w->svfme, w->pos[nxt], w->vfme[nxt],
+                                    w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError, st);
     if (e) return e;
     return mark(w, 3, st, capturing);
 }
@@ -262,6 +271,8 @@ mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out) {
             if ((e = cudaMalloc(&w->pos[i], sizeof(float4) * n))) return e;
             if ((e = cudaMalloc(&w->vfme[i], sizeof(uint4) * n))) return e;
         }
+        if ((e = cudaMalloc(&w->spos, sizeof(float4) * n))) return e;
+        if ((e = cudaMalloc(&w->svfme, sizeof(uint4) * n))) return e;
         if ((e = cudaMalloc(&w->keys, sizeof(uint32_t) * n))) return e;
         if ((e = cudaMalloc(&w->sorted_keys, sizeof(uint32_t) * n))) return e;
         if ((e = cudaMalloc(&w->perm, sizeof(uint32_t) * n))) return e;
@@ -286,6 +297,8 @@ mb_status mb_destroy(mb_world* w) {
         cudaFree(w->pos[i]);
         cudaFree(w->vfme[i]);
     }
+    cudaFree(w->spos);
+    cudaFree(w->svfme);
     cudaFree(w->keys);
     cudaFree(w->sorted_keys);
     cudaFree(w->perm);
@@ -334,8 +347,9 @@ mb_status mb_set_settings(mb_world* w, const mb_settings* s) {
             e = recount(w);  // still the all-zero keys of the upload
         } else {
             uint32_t* hist = counting(w) ? w->cnt.hist : nullptr;
-            if (hist) e = cudaMemsetAsync(hist, 0, sizeof(uint32_t) * w->cells, w->stream);
-            if (!e) e = mb::launch_rekey(w->P, w->n, w->pos[w->cur], w->keys, hist, w->stream);
+            uint32_t* coarse = counting(w) ? w->cnt.coarse : nullptr;
+            if (hist) e = mb::count_clear(w->cnt, w->cells, w->stream);
+            if (!e) e = mb::launch_rekey(w->P, w->n, w->pos[w->cur], w->keys, hist, coarse, w->stream);
         }
         if (e) return cuda_fail(w, "mb_set_settings", e);
     }
@@ -413,7 +427,12 @@ mb_status mb_sync(mb_world* w) {
         cudaMemset(w->scratch.ctl + mb::kCtlError, 0, sizeof(uint32_t));
         w->scratch.last_tiles = 0;  // force a clean look-back table next sort
         drop_graphs(w);
-        return fail(w, MB_ERR_TIMEOUT, "sort look-back wait gave up; results of that frame are invalid");
+        char msg[160];
+        std::snprintf(msg, sizeof msg,
+                      "a bounded device-side wait gave up (flags 0x%x: 1 sort look-back, 4 band copy); "
+                      "results since the last sync are invalid",
+                      flag);
+        return fail(w, MB_ERR_TIMEOUT, msg);
     }
     return MB_OK;
 }
@@ -567,8 +586,8 @@ mb_status mb_last_frame_times(mb_world* w, float* ms) {
 uint32_t mb_kernels_per_frame(const mb_world* w) {
     if (!w) return 0u;
     // counting: scan + scatter + fixup + big-cell fixup + physics;
-    // onesweep: histogram + one kernel per digit pass + cell offsets + physics
-    return counting(w) ? 5u : (uint32_t)w->sched.passes + 3u;
+    // onesweep: histogram + one kernel per digit pass + cell offsets + gather + physics
+    return counting(w) ? 5u : (uint32_t)w->sched.passes + 4u;
 }
 
 const char* mb_version(void) { return "millionsball-gb300 " __DATE__ " sm_103a"; }

@@ -7,14 +7,16 @@
 //
 //   1. per-cell counts, accumulated by the physics pass of the previous frame as
 //      it emits the keys (one red.add per sphere);
-//   2. k_cell_scan: one single-pass exclusive scan (decoupled look-back with a
-//      128-tile window) turns the counts into the cell offsets offs[c] (= start of
-//      cell c; offs[C] = n) and a cursor copy, and zeroes the counts;
+//   2. k_cell_scan: one exclusive scan turns the counts into the cell offsets
+//      offs[c] (= start of cell c; offs[C] = n) and a cursor copy, and zeroes the
+//      counts; each 4096-cell tile takes its base from per-tile counts emitted
+//      with the per-cell ones, so tiles never wait on each other;
 //   3. k_cell_scatter: each sphere claims a slot of its cell with one atomic per
 //      run of equal keys in its warp (match.any), so spheres of one warp keep
-//      their order;
+//      their order, and its 32-byte state is copied to that slot;
 //   4. k_cell_fixup: every cell's slots are put back in ascending input order
-//      (what a stable sort yields; only cells filled by several warps need it).
+//      (what a stable sort yields; only cells filled by several warps need it),
+//      re-gathering the state copy of the cells it reorders.
 //
 // The result is bit-identical to a stable sort; offs[] replaces start/close.
 
@@ -27,32 +29,23 @@
 namespace mb {
 namespace {
 
-constexpr uint32_t kFlagAgg = 1u, kFlagPre = 2u;
-constexpr uint32_t kValMask = (1u << 30) - 1u;
-constexpr uint32_t kSpinMax = 1u << 21;
-
-__device__ __forceinline__ void st_rlx(uint32_t* p, uint32_t v) {
-    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ uint32_t ld_rlx(const uint32_t* p) {
-    uint32_t v;
-    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
 // ---------------------------------------------------------------- scan
+// Tile t of the scan covers cells [4096 t, 4096 t + 4096).  coarse[t] holds the
+// number of spheres in those cells (emitted with the per-cell counts), so a tile
+// finds its base by summing coarse[0..t) - no look-back, no waiting on other tiles.
 __global__ void __launch_bounds__(kScanThreads)
-    k_cell_scan(uint32_t* __restrict__ hist, uint32_t cells, uint32_t* __restrict__ offs,
-                uint32_t* __restrict__ cursor, uint32_t* status, uint32_t* ticket, uint32_t* big_ctl,
-                uint32_t* err) {
+    k_cell_scan(uint32_t* __restrict__ hist, const uint32_t* __restrict__ coarse, uint32_t cells,
+                uint32_t* __restrict__ offs, uint32_t* __restrict__ cursor, uint32_t* big_ctl) {
     constexpr int W = kScanThreads / 32;
-    __shared__ uint32_t s_tile, s_warp[W], s_excl;
+    __shared__ uint32_t s_warp[W], s_base[W];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    if (tid == 0) s_tile = atomicAdd(ticket, 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
+    const uint32_t tile = blockIdx.x;
     if (tile == 0 && tid < 2) big_ctl[tid] = 0u;  // big-cell list of this frame starts empty
     const uint32_t base = tile * kScanTile + tid * kScanItems;
+
+    // exclusive base of this tile: sum of the coarse counts of all earlier tiles
+    uint32_t bsum = 0;
+    for (uint32_t t = tid; t < tile; t += kScanThreads) bsum += __ldg(coarse + t);
 
     uint32_t v[kScanItems];
     if (base + kScanItems <= cells) {
@@ -78,70 +71,17 @@ __global__ void __launch_bounds__(kScanThreads)
         uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
         if (lane >= (uint32_t)o) incl += y;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) bsum += __shfl_xor_sync(0xFFFFFFFFu, bsum, o);
     if (lane == 31u) s_warp[warp] = incl;
+    if (lane == 0u) s_base[warp] = bsum;
     __syncthreads();
-    uint32_t wexcl = 0, total = 0;
+    uint32_t run = incl - sum;
 #pragma unroll
     for (int w = 0; w < W; ++w) {
-        uint32_t t = s_warp[w];
-        if ((uint32_t)w < warp) wexcl += t;
-        total += t;
+        if ((uint32_t)w < warp) run += s_warp[w];
+        run += s_base[w];
     }
-
-    // decoupled look-back over earlier tiles, 32 at a time (warp 0)
-    if (warp == 0) {
-        uint32_t excl = 0;
-        if (tile == 0) {
-            if (lane == 0) st_rlx(status, (kFlagPre << 30) | (total & kValMask));
-        } else {
-            if (lane == 0) st_rlx(status + tile, (kFlagAgg << 30) | (total & kValMask));
-            int32_t top = (int32_t)tile - 1;
-            uint32_t spins = 0;
-            bool gave_up = false;
-            while (true) {
-                // window of 128 predecessors: lane l holds tiles top-4l .. top-4l-3
-                uint32_t sv[4];
-                int qf = 4;  // first inclusive-prefix word of this lane
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    int32_t idx = top - (int32_t)(4u * lane) - q;
-                    sv[q] = idx >= 0 ? ld_rlx(status + idx) : (kFlagPre << 30);
-                    if (qf == 4 && (sv[q] >> 30) == kFlagPre) qf = q;
-                }
-                uint32_t pmask = __ballot_sync(0xFFFFFFFFu, qf < 4);
-                uint32_t first = pmask ? (uint32_t)(__ffs(pmask) - 1) : 32u;
-                int upto = lane < first ? 3 : (lane == first ? qf : -1);
-                bool notready = false;
-                uint32_t mine = 0;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (q <= upto) {
-                        if ((sv[q] >> 30) == 0u) notready = true;
-                        mine += sv[q] & kValMask;
-                    }
-                }
-                if (__any_sync(0xFFFFFFFFu, notready)) {
-                    if (++spins > kSpinMax) {
-                        if (lane == 0) atomicOr(err, 2u);
-                        gave_up = true;
-                        break;
-                    }
-                    if (spins > 32u) __nanosleep(32);
-                    continue;
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xFFFFFFFFu, mine, o);
-                excl += mine;
-                if (first < 32u) break;
-                top -= 128;
-            }
-            (void)gave_up;
-            if (lane == 0) st_rlx(status + tile, (kFlagPre << 30) | ((excl + total) & kValMask));
-        }
-        if (lane == 0) s_excl = excl;
-    }
-    __syncthreads();
-    uint32_t run = s_excl + wexcl + incl - sum;
     if (base + kScanItems <= cells) {
         uint4* o4 = reinterpret_cast<uint4*>(offs + base);
         uint4* c4 = reinterpret_cast<uint4*>(cursor + base);
@@ -173,21 +113,35 @@ __global__ void __launch_bounds__(kScanThreads)
 }
 
 // ---------------------------------------------------------------- scatter
+// Also moves each sphere's state to its slot (sorted copy for the physics pass).
 __global__ void __launch_bounds__(256)
     k_cell_scatter(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ cursor,
-                   uint32_t* __restrict__ perm) {
+                   uint32_t* __restrict__ perm, const float4* __restrict__ pos_in,
+                   const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
+                   uint4* __restrict__ svfme) {
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
         uint32_t i = i0 + threadIdx.x;
         bool valid = i < n;
         uint32_t k = valid ? __ldg(keys + i) : 0xFFFFFFFFu;
+        float4 p;
+        uint4 q;
+        if (valid) {
+            p = __ldg(pos_in + i);
+            q = __ldg(vfme_in + i);
+        }
         uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
         uint32_t leader = (uint32_t)(__ffs(peers) - 1);
         uint32_t b = 0;
         if (valid && lane == leader) b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
-        if (valid) perm[b + (uint32_t)__popc(peers & lt)] = i;
+        if (valid) {
+            const uint32_t dst = b + (uint32_t)__popc(peers & lt);
+            perm[dst] = i;
+            spos[dst] = p;
+            svfme[dst] = q;
+        }
     }
 }
 
@@ -198,13 +152,12 @@ constexpr uint32_t kSmallCell = 32;
 constexpr uint32_t kBlockSortMax = 8192;
 
 __global__ void __launch_bounds__(256)
-    k_cell_fixup(const uint32_t* __restrict__ offs, uint32_t cells, uint32_t* perm, uint32_t* status,
-                 uint32_t status_words, uint32_t* ticket, uint32_t* big_ctl, uint32_t* big) {
+    k_cell_fixup(const uint32_t* __restrict__ offs, uint32_t cells, uint32_t* perm, uint32_t* coarse,
+                 uint32_t tiles, uint32_t* big_ctl, uint32_t* big, const float4* __restrict__ pos_in,
+                 const uint4* __restrict__ vfme_in, float4* __restrict__ spos, uint4* __restrict__ svfme) {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (blockIdx.x == 0) {  // the scan of this frame is over: reset its look-back state
-        for (uint32_t s = threadIdx.x; s < status_words; s += blockDim.x) status[s] = 0u;
-        if (threadIdx.x == 0) *ticket = 0u;
-    }
+    if (blockIdx.x == 0)  // the scan of this frame is over: clear the tile counts for the next one
+        for (uint32_t t = threadIdx.x; t < tiles; t += blockDim.x) coarse[t] = 0u;
     if (c >= cells) return;
     const uint32_t lo = offs[c], hi = offs[c + 1u];
     if (hi - lo < 2u) return;
@@ -231,6 +184,11 @@ __global__ void __launch_bounds__(256)
         }
         perm[b] = x;
     }
+    for (uint32_t j = lo; j < hi; ++j) {  // the sorted state copy follows the new order
+        const uint32_t o = perm[j];
+        spos[j] = __ldg(pos_in + o);
+        svfme[j] = __ldg(vfme_in + o);
+    }
 }
 
 __device__ void heap_sift(uint32_t* a, uint32_t root, uint32_t end) {
@@ -251,7 +209,9 @@ __device__ void heap_sift(uint32_t* a, uint32_t root, uint32_t end) {
 // scenes with thousands of spheres in one cell get there).
 __global__ void __launch_bounds__(256)
     k_cell_fixup_big(const uint32_t* __restrict__ offs, uint32_t* perm, uint32_t* big_ctl,
-                     const uint32_t* __restrict__ big) {
+                     const uint32_t* __restrict__ big, const float4* __restrict__ pos_in,
+                     const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
+                     uint4* __restrict__ svfme) {
     __shared__ uint32_t s_v[kBlockSortMax];
     __shared__ uint32_t s_idx, s_unsorted;
     const uint32_t tid = threadIdx.x;
@@ -301,6 +261,12 @@ __global__ void __launch_bounds__(256)
                     heap_sift(a, 0u, end);
                 }
             }
+            __syncthreads();
+            for (uint32_t j = tid; j < m; j += blockDim.x) {  // sorted state copy follows
+                const uint32_t o = perm[lo + j];
+                spos[lo + j] = __ldg(pos_in + o);
+                svfme[lo + j] = __ldg(vfme_in + o);
+            }
         }
         __syncthreads();
     }
@@ -309,19 +275,21 @@ __global__ void __launch_bounds__(256)
 // INIT frame after an upload: every key is 0, so the stable order is the
 // identity and cell 0 holds everyone.  Also clears the counts (only hist[0] is set).
 __global__ void k_init_order(uint32_t n, uint32_t cells, uint32_t* perm, uint32_t* offs,
-                             uint32_t* hist) {
+                             uint32_t* hist, uint32_t* coarse, uint32_t tiles) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= max(n, cells); i += stride) {
         if (i < n) perm[i] = i;
         if (i <= cells) offs[i] = i == 0u ? 0u : n;
         if (i < cells) hist[i] = 0u;
+        if (i < tiles) coarse[i] = 0u;
     }
 }
 
 // ---------------------------------------------------------------- counting
 // hist[keys[i]] += 1 for every sphere, one atomic per run of equal keys in a warp.
 __global__ void __launch_bounds__(256)
-    k_count_keys(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist) {
+    k_count_keys(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
+                 uint32_t* __restrict__ coarse) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
@@ -330,73 +298,88 @@ __global__ void __launch_bounds__(256)
         uint32_t k = valid ? __ldg(keys + i) : 0xFFFFFFFFu;
         uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
         if (valid && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(hist + k, (uint32_t)__popc(peers));
+        uint32_t t = valid ? k / kScanTile : 0xFFFFFFFFu;
+        uint32_t tp = __match_any_sync(0xFFFFFFFFu, t);
+        if (valid && lane == (uint32_t)(__ffs(tp) - 1)) atomicAdd(coarse + t, (uint32_t)__popc(tp));
     }
 }
 
-__global__ void k_set_word(uint32_t* p, uint32_t v) { *p = v; }
+__global__ void k_set_word(uint32_t* p, uint32_t v, uint32_t* q) {
+    *p = v;
+    *q = v;
+}
 
 }  // namespace
 
 cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells) {
     s.max_cells = max_cells;
     size_t padded = ((size_t)max_cells + kScanTile) & ~(size_t)15;  // uint4-aligned, room for offs[C]
-    s.status_words = (max_cells + kScanTile - 1u) / kScanTile;
+    s.tiles = (max_cells + kScanTile - 1u) / kScanTile;
     cudaError_t e;
     if ((e = cudaMalloc(&s.hist, sizeof(uint32_t) * padded))) return e;
     if ((e = cudaMalloc(&s.cursor, sizeof(uint32_t) * padded))) return e;
-    if ((e = cudaMalloc(&s.status, sizeof(uint32_t) * (s.status_words + 3u)))) return e;
+    if ((e = cudaMalloc(&s.coarse, sizeof(uint32_t) * (s.tiles + 1u)))) return e;
+    if ((e = cudaMalloc(&s.big_ctl, sizeof(uint32_t) * 2u))) return e;
     if ((e = cudaMalloc(&s.big, sizeof(uint32_t) * ((size_t)max_cells + 1u)))) return e;
     if ((e = cudaMemset(s.hist, 0, sizeof(uint32_t) * padded))) return e;
-    if ((e = cudaMemset(s.status, 0, sizeof(uint32_t) * (s.status_words + 3u)))) return e;
+    if ((e = cudaMemset(s.coarse, 0, sizeof(uint32_t) * (s.tiles + 1u)))) return e;
+    if ((e = cudaMemset(s.big_ctl, 0, sizeof(uint32_t) * 2u))) return e;
     return cudaSuccess;
 }
 
 void count_scratch_free(CountScratch& s) {
     cudaFree(s.hist);
     cudaFree(s.cursor);
-    cudaFree(s.status);
+    cudaFree(s.coarse);
+    cudaFree(s.big_ctl);
     cudaFree(s.big);
     s = CountScratch();
 }
 
+cudaError_t count_clear(CountScratch& s, uint32_t cells, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * cells, st);
+    if (e) return e;
+    return cudaMemsetAsync(s.coarse, 0, sizeof(uint32_t) * ((cells + kScanTile - 1u) / kScanTile), st);
+}
+
 cudaError_t count_keys(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                        cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * cells, st);
+    cudaError_t e = count_clear(s, cells, st);
     if (e || !n) return e;
     uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
-    k_count_keys<<<blocks, 256, 0, st>>>(keys, n, s.hist);
+    k_count_keys<<<blocks, 256, 0, st>>>(keys, n, s.hist, s.coarse);
     return cudaGetLastError();
 }
 
 cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * cells, st);
+    cudaError_t e = count_clear(s, cells, st);
     if (e) return e;
-    k_set_word<<<1, 1, 0, st>>>(s.hist, n);
+    k_set_word<<<1, 1, 0, st>>>(s.hist, n, s.coarse);
     return cudaGetLastError();
 }
 
 cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st) {
+    (void)ctl;
     uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
-    k_cell_scan<<<tiles, kScanThreads, 0, st>>>(s.hist, cells, offs, s.cursor, s.status,
-                                                s.status + s.status_words, s.status + s.status_words + 1,
-                                                ctl + kCtlError);
+    k_cell_scan<<<tiles, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.big_ctl);
     return cudaGetLastError();
 }
 
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
-                          const uint32_t* offs, uint32_t* perm, cudaStream_t st) {
+                          const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
+                          float4* spos, uint4* svfme, cudaStream_t st) {
     cudaError_t e;
     if (n) {
         uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
-        k_cell_scatter<<<blocks, 256, 0, st>>>(keys, n, s.cursor, perm);
+        k_cell_scatter<<<blocks, 256, 0, st>>>(keys, n, s.cursor, perm, pos_in, vfme_in, spos, svfme);
         if ((e = cudaGetLastError())) return e;
     }
     uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
-    uint32_t* big_ctl = s.status + s.status_words + 1;
-    k_cell_fixup<<<(cells + 255u) / 256u, 256, 0, st>>>(offs, cells, perm, s.status, tiles,
-                                                        s.status + s.status_words, big_ctl, s.big);
+    k_cell_fixup<<<(cells + 255u) / 256u, 256, 0, st>>>(offs, cells, perm, s.coarse, tiles, s.big_ctl, s.big,
+                                                        pos_in, vfme_in, spos, svfme);
     if ((e = cudaGetLastError())) return e;
-    k_cell_fixup_big<<<(uint32_t)device_sm_count(), 256, 0, st>>>(offs, perm, big_ctl, s.big);
+    k_cell_fixup_big<<<(uint32_t)device_sm_count(), 256, 0, st>>>(offs, perm, s.big_ctl, s.big, pos_in,
+                                                                  vfme_in, spos, svfme);
     return cudaGetLastError();
 }
 
@@ -404,7 +387,8 @@ cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32
                              cudaStream_t st) {
     uint32_t m = std::max(n, cells) + 1u;
     uint32_t blocks = std::min<uint32_t>((m + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
-    k_init_order<<<blocks, 256, 0, st>>>(n, cells, perm, offs, s.hist);
+    k_init_order<<<blocks, 256, 0, st>>>(n, cells, perm, offs, s.hist, s.coarse,
+                                         (cells + kScanTile - 1u) / kScanTile);
     return cudaGetLastError();
 }
 

@@ -92,21 +92,25 @@ struct PhysParams {
     uint32_t spring;
     float filter_margin;      // contact-loop pre-filter margin (0 = exact loop only)
     float pos_slack;          // rounding slack added per applied contact shift
+    uint32_t div_m, div_s1, div_s2;  // exact n / grid_size by multiply-shift
 };
 
 PhysParams make_params(const mb_consts& c);
 
-// Physics passes.  `hist` (nullable) accumulates the per-cell counts of the
-// keys they emit, for the next frame's counting sort.
+// Physics passes.  `hist` / `coarse` (nullable together) accumulate the per-cell
+// and per-4096-cell-tile counts of the keys they emit, for the next frame's
+// counting sort.
 cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t* perm,
                                 const float4* pos_in, const uint4* vfme_in, float4* pos_out,
-                                uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, cudaStream_t st);
-cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* perm,
-                                const uint32_t* offs, const float4* pos_in, const uint4* vfme_in,
-                                float4* pos_out, uint4* vfme_out, uint32_t* keys_out, uint32_t* hist,
+                                uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse,
+                                cudaStream_t st);
+// LOOP pass over the state in sorted order (spos/svfme, slot j = sorted slot j).
+cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs,
+                                const float4* spos, const uint4* svfme, float4* pos_out, uint4* vfme_out,
+                                uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
                                 cudaStream_t st);
 cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,
-                         uint32_t* hist, cudaStream_t st);
+                         uint32_t* hist, uint32_t* coarse, cudaStream_t st);
 
 // Counting sort of cell keys (mb_count.cu).
 constexpr int kScanThreads = 256;
@@ -117,13 +121,15 @@ struct CountScratch {
     uint32_t max_cells = 0;
     uint32_t* hist = nullptr;     // [max_cells] counts of the keys of the next sort
     uint32_t* cursor = nullptr;   // [max_cells] scatter cursors
-    uint32_t* status = nullptr;   // [status_words] scan look-back words, then the tile
-                                  // ticket, then the big-cell list count and cursor
+    uint32_t* coarse = nullptr;   // [tiles] counts per 4096-cell scan tile
+    uint32_t* big_ctl = nullptr;  // [2] big-cell list count and cursor
     uint32_t* big = nullptr;      // cells with more than 32 spheres this frame
-    uint32_t status_words = 0;
+    uint32_t tiles = 0;
 };
 cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells);
 void count_scratch_free(CountScratch& s);
+// hist := 0, coarse := 0 for `cells` cells.
+cudaError_t count_clear(CountScratch& s, uint32_t cells, cudaStream_t st);
 // hist := counts of keys (rebuild, e.g. after an upload or a grid change).
 cudaError_t count_keys(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                        cudaStream_t st);
@@ -134,9 +140,14 @@ cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t*
 // INIT frame after an upload (all keys 0): perm := identity, offs := [0, n, .., n], hist := 0.
 cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32_t* offs, uint32_t* perm,
                              cudaStream_t st);
-// perm := stable permutation sorting keys by cell, from the cursors of count_scan.
+// perm := stable permutation sorting keys by cell, from the cursors of count_scan;
+// spos/svfme := the state in that order (spos[j] = pos_in[perm[j]]).
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
-                          const uint32_t* offs, uint32_t* perm, cudaStream_t st);
+                          const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
+                          float4* spos, uint4* svfme, cudaStream_t st);
+// spos/svfme := pos_in/vfme_in gathered through perm (after the onesweep sort).
+cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in, const uint4* vfme_in,
+                         float4* spos, uint4* svfme, cudaStream_t st);
 
 int device_sm_count();
 

@@ -38,18 +38,13 @@ __device__ __forceinline__ float dot3(V3 a, V3 b) {
 __device__ __forceinline__ float len3(V3 a) { return sqrtf(dot3(a, a)); }
 __device__ __forceinline__ V3 normalize3(V3 a) { return a / len3(a); }
 
-// WGSL min/max: "e2 if e2 < e1 (resp. >), else e1; a NaN operand yields the other".
-__device__ __forceinline__ float wmin(float a, float b) {
-    if (isnan(a)) return b;
-    if (isnan(b)) return a;
-    return b < a ? b : a;
-}
-__device__ __forceinline__ float wmax(float a, float b) {
-    if (isnan(a)) return b;
-    if (isnan(b)) return a;
-    return b > a ? b : a;
-}
-__device__ __forceinline__ float wclamp(float e, float lo, float hi) { return wmin(wmax(e, lo), hi); }
+// WGSL clamp(e, lo, hi) = min(max(e, lo), hi), with min/max defined as "e2 if
+// e2 < e1 (resp. >), else e1; a NaN operand yields the other".  The hardware
+// min/max (fminf/fmaxf) return the same value at every call site here: they
+// also return the non-NaN operand, and they differ only for min(+0, -0) and
+// max(-0, +0), argument orders that cannot occur with the bounds used below
+// (+-65504, [-(r*R_AGENT), +0], +-edge with edge >= +0).
+__device__ __forceinline__ float wclamp(float e, float lo, float hi) { return fminf(fmaxf(e, lo), hi); }
 __device__ __forceinline__ float wsign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
 
 struct Agent {  // physics.wgsl:208-215
@@ -86,12 +81,19 @@ __device__ __forceinline__ uint4 pack(const Agent& a) {
     return q;
 }
 
+// n / d for the grid size d, exact for every u32 n (Granlund-Montgomery
+// multiply-shift with a 33-bit magic, as set up by make_params).
+__device__ __forceinline__ uint32_t div_grid(const PhysParams& P, uint32_t n) {
+    uint32_t t = __umulhi(P.div_m, n);
+    return (t + ((n - t) >> P.div_s1)) >> P.div_s2;
+}
+
 // get_collision_grid_id (physics.wgsl:107-109): saturating f32->u32, integer
 // division by GRID_SIZE; clamped to the border cell for positions off the map.
 __device__ __forceinline__ void cell_of(const PhysParams& P, float x, float z, uint32_t& cx,
                                         uint32_t& cz) {
-    cx = __float2uint_rz(x + P.half_map_size) / P.grid_size;
-    cz = __float2uint_rz(z + P.half_map_size) / P.grid_size;
+    cx = div_grid(P, __float2uint_rz(x + P.half_map_size));
+    cz = div_grid(P, __float2uint_rz(z + P.half_map_size));
     cx = min(cx, P.N - 1u);
     cz = min(cz, P.N - 1u);
 }
@@ -181,12 +183,24 @@ __device__ __forceinline__ float sphere_raw(const PhysParams& P, Agent& a, float
     return sphere(P, a, unpack(bp, bq));
 }
 
+// Counts of the emitted key for the next frame's counting sort: the cell, and the
+// 4096-cell scan tile (one atomic per run of equal tiles among the active lanes).
+__device__ __forceinline__ void emit_count(uint32_t* hist, uint32_t* coarse, uint32_t key) {
+    if (!hist) return;
+    atomicAdd(hist + key, 1u);
+    const uint32_t t = key >> 12;  // kScanTile = 4096
+    const uint32_t am = __activemask();
+    const uint32_t peers = __match_any_sync(am, t);
+    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(coarse + t, (uint32_t)__popc(peers));
+}
+
 // main, INIT pipeline (physics.wgsl:91-96): gather through perm, re-pack, emit key.
 __global__ void __launch_bounds__(256)
     k_physics_init(PhysParams P, uint32_t n, const uint32_t* __restrict__ perm,
                    const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in,
                    float4* __restrict__ pos_out, uint4* __restrict__ vfme_out,
-                   uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist) {
+                   uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist,
+                   uint32_t* __restrict__ coarse) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t old = min(perm[i], n - 1u);
@@ -198,130 +212,172 @@ __global__ void __launch_bounds__(256)
     vfme_out[i] = pack(a);
     uint32_t key = cz * P.N + cx;
     keys_out[i] = key;
-    if (hist) atomicAdd(hist + key, 1u);
+    emit_count(hist, coarse, key);
 }
 
 // Neighbour row-bands of a tile of sorted slots.  Band b (row offset b-1 = -1, 0,
 // +1) is the union of every tile sphere's candidate range in that row: since
-// slots are sorted by cell, it is one contiguous slot range.  Bands of at most
-// kBandCap slots are staged in shared memory through perm (all loads of a band
-// in flight at once); wider bands (a tile spanning a row boundary) are read from
-// global memory instead.
+// slots are sorted by cell, it is one contiguous slot range of the sorted state.
+// Bands of at most kBandCap slots are copied to shared memory with TMA bulk
+// copies (cp.async.bulk, completion on one mbarrier); wider bands (a tile
+// spanning a row boundary) are read from global memory instead.
 constexpr int kTileThreads = 128;
 constexpr uint32_t kBandCap = 2 * kTileThreads;
+constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier wait (error flag on expiry)
 
-// The candidates of one sphere, in the reference's order (physics.wgsl:119-160):
-// own row without itself, row below, row above.  Ordinal o maps to a slot j and
-// the shared-memory band holding it (if that band was staged).
-struct Cands {
-    uint32_t m_lo, n_mid, b_lo, n_bot, t_lo, n_top, self;
-    __device__ __forceinline__ uint32_t total() const { return n_mid + n_bot + n_top; }
-    __device__ __forceinline__ uint32_t slot(uint32_t o, int& band) const {
-        if (o < n_mid) {
-            band = 1;
-            uint32_t j = m_lo + o;
-            return j >= self ? j + 1u : j;
-        }
-        o -= n_mid;
-        if (o < n_bot) {
-            band = 0;
-            return b_lo + o;
-        }
-        band = 2;
-        return t_lo + (o - n_bot);
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// One row of one sphere's candidates: sorted slots [lo, lo + cnt), read from
+// shared memory when the whole range was staged (sp/sq indexed by slot - slo).
+struct Row {
+    uint32_t lo, cnt;
+    const float4* sp;
+    const uint4* sq;
+    uint32_t slo;
+    bool smem;
+};
+
+__device__ __forceinline__ float4 row_pos(const Row& R, uint32_t j, const float4* __restrict__ spos) {
+    return R.smem ? R.sp[j - R.slo] : __ldg(spos + j);
+}
+__device__ __forceinline__ uint4 row_vfme(const Row& R, uint32_t j, const uint4* __restrict__ svfme) {
+    return R.smem ? R.sq[j - R.slo] : __ldg(svfme + j);
+}
+
+// Phase-1 classification of one row (see collide_rows): bit q of the result is
+// set when candidate lo+q (q < 32) lies within edge + margin of p0.
+template <bool kOwnRow>
+__device__ __forceinline__ uint32_t classify_row(const Row& R, const V3& p0, float scale_m, uint32_t self,
+                                                 const float4* __restrict__ spos) {
+    const uint32_t lim = min(R.cnt, 32u);
+    const float4* src = R.smem ? R.sp + (R.lo - R.slo) : spos + R.lo;
+    uint32_t m = 0;
+    for (uint32_t q = 0; q < lim; ++q) {
+        if (kOwnRow && R.lo + q == self) continue;
+        const float4 bp = src[q];
+        const float em = bp.w + scale_m;
+        const float dx = p0.x - bp.x, dy = p0.y - bp.y, dz = p0.z - bp.z;
+        const float d2 = (dx * dx + dy * dy) + dz * dz;
+        if (!(d2 > (em * em) * 1.0001f)) m |= 1u << q;
     }
-};
-
-struct Bands {
-    const float4 (*pos)[kBandCap];
-    const uint4 (*vfme)[kBandCap];
-    const uint32_t* lo;
-    const uint32_t* cnt;
-};
-
-__device__ __forceinline__ float4 cand_pos(const Bands& B, int band, uint32_t j, uint32_t n,
-                                           const uint32_t* __restrict__ perm,
-                                           const float4* __restrict__ pos_in) {
-    uint32_t r = j - B.lo[band];
-    if (r < B.cnt[band]) return B.pos[band][r];
-    return __ldg(pos_in + min(__ldg(perm + j), n - 1u));
-}
-__device__ __forceinline__ uint4 cand_vfme(const Bands& B, int band, uint32_t j, uint32_t n,
-                                          const uint32_t* __restrict__ perm,
-                                          const uint4* __restrict__ vfme_in) {
-    uint32_t r = j - B.lo[band];
-    if (r < B.cnt[band]) return B.vfme[band][r];
-    return __ldg(vfme_in + min(__ldg(perm + j), n - 1u));
+    return m;
 }
 
-// handle_collisions' contact loop (physics.wgsl:122-160), in two phases that give
-// the same result as the plain sequential loop:
-//  1. the first 64 candidates are classified against the position p0 at loop
-//     entry: "near" if within edge + margin (squared test with slack);
-//  2. contacts run in candidate order over the near ones only, while a bound on
-//     |p - p0| (sum of applied shifts, with rounding slack) stays below the
-//     margin: then every skipped candidate is farther than edge from p and
-//     would have been a no-op.  If the bound is exceeded, or beyond ordinal 63,
-//     the remaining candidates run through the exact loop.
-__device__ __forceinline__ void collide_all(const PhysParams& P, Agent& a, const Cands& C,
-                                            const Bands& B, uint32_t n,
-                                            const uint32_t* __restrict__ perm,
-                                            const float4* __restrict__ pos_in,
-                                            const uint4* __restrict__ vfme_in) {
-    const uint32_t total = C.total();
-    uint32_t start = 0;  // ordinals from here on take the exact loop
-    // the rounding slack below assumes |coordinate| <= 8192 (ulp <= 2^-10)
-    const bool small = fabsf(a.position.x) <= 8192.0f && fabsf(a.position.y) <= 8192.0f &&
-                       fabsf(a.position.z) <= 8192.0f;
-    if (P.filter_margin > 0.0f && small) {
-        uint64_t near = 0;
-        const uint32_t nf = min(total, 64u);
-        for (uint32_t o = 0; o < nf; ++o) {
-            int band;
-            uint32_t j = C.slot(o, band);
-            float4 bp = cand_pos(B, band, j, n, perm, pos_in);
-            float em = (bp.w + a.scale) + P.filter_margin;
-            V3 tpos = a.position - V3{bp.x, bp.y, bp.z};
-            float d2 = dot3(tpos, tpos);
-            if (!(d2 > (em * em) * 1.0001f)) near |= 1ull << o;
-        }
-        float disp = 0.0f;
-        const float limit = P.filter_margin - 0.02f;
-        start = nf;
+// Phase 2 of one row: near candidates in order while the displacement bound
+// holds, then the exact loop from wherever the bound broke (or from q = 32).
+template <bool kOwnRow>
+__device__ __forceinline__ void contact_row(const PhysParams& P, Agent& a, const Row& R, uint32_t near,
+                                            bool& exact, float& disp, float limit, uint32_t self,
+                                            const float4* __restrict__ spos, const uint4* __restrict__ svfme) {
+    uint32_t q0 = 0;
+    if (!exact) {
+        q0 = min(R.cnt, 32u);
         while (near) {
-            uint32_t o = (uint32_t)(__ffsll((long long)near) - 1);
-            near &= near - 1ull;
-            int band;
-            uint32_t j = C.slot(o, band);
-            float mv = sphere_raw(P, a, cand_pos(B, band, j, n, perm, pos_in),
-                                  cand_vfme(B, band, j, n, perm, vfme_in));
+            const uint32_t q = (uint32_t)(__ffs(near) - 1);
+            near &= near - 1u;
+            const uint32_t j = R.lo + q;
+            float mv = sphere_raw(P, a, row_pos(R, j, spos), row_vfme(R, j, svfme));
             if (mv != 0.0f) {
                 disp = disp + (mv * 1.001f + P.pos_slack);
                 if (!(disp <= limit)) {  // moved too far: later skips would not be safe
-                    start = o + 1u;
+                    exact = true;
+                    q0 = q + 1u;
                     break;
                 }
             }
         }
     }
-    for (uint32_t o = start; o < total; ++o) {
-        int band;
-        uint32_t j = C.slot(o, band);
-        sphere_raw(P, a, cand_pos(B, band, j, n, perm, pos_in), cand_vfme(B, band, j, n, perm, vfme_in));
+    for (uint32_t q = q0; q < R.cnt; ++q) {
+        const uint32_t j = R.lo + q;
+        if (kOwnRow && j == self) continue;
+        float mv = sphere_raw(P, a, row_pos(R, j, spos), row_vfme(R, j, svfme));
+        // shifts applied here count too: later rows still skip by the bound
+        if (mv != 0.0f && !exact) {
+            disp = disp + (mv * 1.001f + P.pos_slack);
+            if (!(disp <= limit)) exact = true;
+        }
     }
 }
 
+// handle_collisions' contact loop (physics.wgsl:122-160) over the rows in the
+// reference's order (own row without itself, row below, row above), in two
+// phases that give exactly the result of the plain sequential loop:
+//  1. the first 32 candidates of each row are classified against the position
+//     p0 at loop entry: "near" if within edge + margin (squared test, slack);
+//  2. contacts run in candidate order over the near ones only while a bound on
+//     |p - p0| (sum of applied shifts plus rounding slack) stays below the
+//     margin minus 0.02: every skipped candidate is then farther than edge from
+//     p and would have been a no-op.  Once the bound is exceeded, and beyond the
+//     32nd candidate of a row, candidates run through the exact loop.
+__device__ __forceinline__ void collide_rows(const PhysParams& P, Agent& a, const Row (&rows)[3],
+                                             uint32_t self, const float4* __restrict__ spos,
+                                             const uint4* __restrict__ svfme) {
+    // the rounding slack assumes |coordinate| <= 8192 (ulp <= 2^-10)
+    bool exact = !(P.filter_margin > 0.0f && fabsf(a.position.x) <= 8192.0f &&
+                   fabsf(a.position.y) <= 8192.0f && fabsf(a.position.z) <= 8192.0f);
+    uint32_t n0 = 0, n1 = 0, n2 = 0;
+    if (!exact) {
+        const float scale_m = a.scale + P.filter_margin;
+        n0 = classify_row<true>(rows[0], a.position, scale_m, self, spos);
+        n1 = classify_row<false>(rows[1], a.position, scale_m, self, spos);
+        n2 = classify_row<false>(rows[2], a.position, scale_m, self, spos);
+    }
+    float disp = 0.0f;
+    const float limit = P.filter_margin - 0.02f;
+    contact_row<true>(P, a, rows[0], n0, exact, disp, limit, self, spos, svfme);
+    contact_row<false>(P, a, rows[1], n1, exact, disp, limit, self, spos, svfme);
+    contact_row<false>(P, a, rows[2], n2, exact, disp, limit, self, spos, svfme);
+}
+
+// Key of a position (physics.wgsl:115-117).
+__device__ __forceinline__ uint32_t key_of(const PhysParams& P, float4 p) {
+    uint32_t cx, cz;
+    cell_of(P, p.x, p.z, cx, cz);
+    return cz * P.N + cx;
+}
+
 // main, LOOP pipeline (physics.wgsl:57-89): one thread per sorted slot, one
-// block per tile of kTileThreads consecutive slots.
+// block per tile of kTileThreads consecutive slots.  spos/svfme hold the state in
+// sorted order (agent_new(agent_index_sorted[i]) of the reference is spos[i]).
 __global__ void __launch_bounds__(kTileThreads)
-    k_physics_loop(PhysParams P, uint32_t n, const uint32_t* __restrict__ perm,
-                   const uint32_t* __restrict__ offs, const float4* __restrict__ pos_in,
-                   const uint4* __restrict__ vfme_in, float4* __restrict__ pos_out,
-                   uint4* __restrict__ vfme_out, uint32_t* __restrict__ keys_out,
-                   uint32_t* __restrict__ hist) {
-    __shared__ float4 s_pos[3][kBandCap];
-    __shared__ uint4 s_vfme[3][kBandCap];
-    __shared__ uint32_t s_lo[3], s_cnt[3], s_kf, s_kl;
+    k_physics_loop(PhysParams P, uint32_t n, const uint32_t* __restrict__ offs,
+                   const float4* __restrict__ spos, const uint4* __restrict__ svfme,
+                   float4* __restrict__ pos_out, uint4* __restrict__ vfme_out,
+                   uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist,
+                   uint32_t* __restrict__ coarse, uint32_t* __restrict__ err) {
+    __shared__ __align__(16) float4 s_pos[3][kBandCap];
+    __shared__ __align__(16) uint4 s_vfme[3][kBandCap];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ uint32_t s_lo[3], s_cnt[3];
 
     const uint32_t tid = threadIdx.x;
     const uint32_t i0 = blockIdx.x * kTileThreads;
@@ -330,75 +386,98 @@ __global__ void __launch_bounds__(kTileThreads)
     const bool valid = i < n;
     const uint32_t N = P.N;
 
-    Agent a;
-    uint32_t cx = 0, cz = 0, key = 0;
-    if (valid) {
-        uint32_t old = min(__ldg(perm + i), n - 1u);
-        a = unpack(__ldg(pos_in + old), __ldg(vfme_in + old));
-        cell_of(P, a.position.x, a.position.z, cx, cz);
-        key = cz * N + cx;
-        if (i == i0) s_kf = key;
-        if (i == ilast) s_kl = key;
-    }
-    __syncthreads();
-    if (tid < 3) {
-        const uint32_t kf = s_kf, kl = s_kl;
+    if (tid == 0) mbar_init(&s_bar, 1u);
+    if (tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
+        const uint32_t kf = key_of(P, __ldg(spos + i0)), kl = key_of(P, __ldg(spos + ilast));
+        const uint32_t cxf = kf - (kf / N) * N, cxl = kl - (kl / N) * N;
         uint32_t lo = 0, hi = 0;
         if (tid == 1) {  // own row
-            lo = offs[kf - (kf % N > 0u ? 1u : 0u)];
-            hi = offs[kl + (kl % N < N - 1u ? 2u : 1u)];
+            lo = offs[kf - (cxf > 0u ? 1u : 0u)];
+            hi = offs[kl + (cxl < N - 1u ? 2u : 1u)];
         } else if (tid == 0) {  // row below, for tile spheres with cz > 0
             if (kl >= N) {
                 uint32_t f = max(kf, N);
-                lo = offs[f - N - (f % N > 0u ? 1u : 0u)];
-                hi = offs[kl - N + (kl % N < N - 1u ? 2u : 1u)];
+                uint32_t cf = f - (f / N) * N;
+                lo = offs[f - N - (cf > 0u ? 1u : 0u)];
+                hi = offs[kl - N + (cxl < N - 1u ? 2u : 1u)];
             }
         } else {  // row above, for tile spheres with cz < N-1
             const uint32_t top = N * (N - 1u);
             if (kf < top) {
                 uint32_t l = min(kl, top - 1u);
-                lo = offs[kf + N - (kf % N > 0u ? 1u : 0u)];
-                hi = offs[l + N + (l % N < N - 1u ? 2u : 1u)];
+                uint32_t cl = l - (l / N) * N;
+                lo = offs[kf + N - (cxf > 0u ? 1u : 0u)];
+                hi = offs[l + N + (cl < N - 1u ? 2u : 1u)];
             }
         }
         hi = min(hi, n);
         s_lo[tid] = lo;
         s_cnt[tid] = (hi > lo && hi - lo <= kBandCap) ? hi - lo : 0u;
     }
-    __syncthreads();
-#pragma unroll
-    for (int b = 0; b < 3; ++b) {
-        const uint32_t lo = s_lo[b], cnt = s_cnt[b];
-        for (uint32_t r = tid; r < cnt; r += kTileThreads) {
-            uint32_t o = min(__ldg(perm + lo + r), n - 1u);
-            s_pos[b][r] = __ldg(pos_in + o);
-            s_vfme[b][r] = __ldg(vfme_in + o);
+
+    // own sphere and its candidate rows (overlaps the band set-up above)
+    Agent a;
+    uint32_t cx = 0, cz = 0, key = 0;
+    uint32_t lo[3] = {0u, 0u, 0u}, hi[3] = {0u, 0u, 0u};
+    if (valid) {
+        a = unpack(__ldg(spos + i), __ldg(svfme + i));
+        cell_of(P, a.position.x, a.position.z, cx, cz);
+        key = cz * N + cx;
+        const uint32_t l = cx > 0u ? 1u : 0u, rr = cx < N - 1u ? 2u : 1u;
+        lo[0] = __ldg(offs + key - l);
+        hi[0] = __ldg(offs + key + rr);
+        if (cz > 0u) {
+            lo[1] = __ldg(offs + key - N - l);
+            hi[1] = __ldg(offs + key - N + rr);
+        }
+        if (cz < N - 1u) {
+            lo[2] = __ldg(offs + key + N - l);
+            hi[2] = __ldg(offs + key + N + rr);
         }
     }
     __syncthreads();
+    if (tid == 0) {
+        uint32_t bytes = 0;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) bytes += s_cnt[b] * 32u;
+        mbar_arrive_expect_tx(&s_bar, bytes);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            if (s_cnt[b]) {
+                bulk_g2s(s_pos[b], spos + s_lo[b], s_cnt[b] * 16u, &s_bar);
+                bulk_g2s(s_vfme[b], svfme + s_lo[b], s_cnt[b] * 16u, &s_bar);
+            }
+        }
+    }
+    {  // bounded wait for the bands (every thread, so all copies land before exit)
+        uint32_t spins = 0;
+        while (!mbar_try_wait(&s_bar, 0u)) {
+            if (++spins > kWaitLimit) {
+                if (tid == 0) atomicOr(err, 4u);
+                break;
+            }
+        }
+    }
     if (!valid) return;
 
-    const uint32_t l = cx > 0u ? 1u : 0u, rr = cx < N - 1u ? 2u : 1u;
-    Cands C;
-    C.self = i;
-    C.m_lo = __ldg(offs + key - l);
+    // candidate rows in the reference's order: own row (band 1), below (0), above (2)
+    Row rows[3];
     {
-        uint32_t hi = min(__ldg(offs + key + rr), n);
-        C.n_mid = (hi > C.m_lo && i >= C.m_lo && i < hi) ? hi - C.m_lo - 1u : 0u;  // own cell holds i
+        const int band[3] = {1, 0, 2};
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const int b = band[r];
+            const uint32_t h = min(hi[r], n);
+            rows[r].lo = lo[r];
+            rows[r].cnt = h > lo[r] ? h - lo[r] : 0u;
+            rows[r].sp = s_pos[b];
+            rows[r].sq = s_vfme[b];
+            rows[r].slo = s_lo[b];
+            rows[r].smem = lo[r] >= s_lo[b] && h <= s_lo[b] + s_cnt[b];
+        }
+        // own cell holds i; a range that does not (inconsistent input) is dropped
+        if (!(i >= rows[0].lo && i < rows[0].lo + rows[0].cnt)) rows[0].cnt = 0;
     }
-    C.b_lo = C.t_lo = 0;
-    C.n_bot = C.n_top = 0;
-    if (cz > 0u) {
-        C.b_lo = __ldg(offs + key - N - l);
-        uint32_t hi = min(__ldg(offs + key - N + rr), n);
-        C.n_bot = hi > C.b_lo ? hi - C.b_lo : 0u;
-    }
-    if (cz < N - 1u) {
-        C.t_lo = __ldg(offs + key + N - l);
-        uint32_t hi = min(__ldg(offs + key + N + rr), n);
-        C.n_top = hi > C.t_lo ? hi - C.t_lo : 0u;
-    }
-    Bands B{s_pos, s_vfme, s_lo, s_cnt};
 
     // verlet_integration (physics.wgsl:262-266)
     {
@@ -408,9 +487,9 @@ __global__ void __launch_bounds__(kTileThreads)
     }
     a.force = splat(0.0f);
 
-    // handle_collisions (physics.wgsl:119-169): own row, row below, row above
+    // handle_collisions (physics.wgsl:119-169)
     V3 old_pos = a.position;
-    collide_all(P, a, C, B, n, perm, pos_in, vfme_in);
+    collide_rows(P, a, rows, i, spos, svfme);
     V3 diff = a.position - old_pos;
     if (len3(diff) > a.scale) {
         // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337)
@@ -435,18 +514,19 @@ __global__ void __launch_bounds__(kTileThreads)
     cell_of(P, a.position.x, a.position.z, nx, nz);
     const uint32_t nk = nz * N + nx;
     keys_out[i] = nk;
-    if (hist) atomicAdd(hist + nk, 1u);
+    emit_count(hist, coarse, nk);
 }
 
 __global__ void k_rekey(PhysParams P, uint32_t n, const float4* __restrict__ pos,
-                        uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
+                        uint32_t* __restrict__ keys, uint32_t* __restrict__ hist,
+                        uint32_t* __restrict__ coarse) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 p = pos[i];
     uint32_t cx, cz;
     cell_of(P, p.x, p.z, cx, cz);
     keys[i] = cz * P.N + cx;
-    if (hist) atomicAdd(hist + keys[i], 1u);
+    emit_count(hist, coarse, keys[i]);
 }
 
 }  // namespace
@@ -475,33 +555,40 @@ PhysParams make_params(const mb_consts& c) {
     // contact-loop filter margin (collide_all): disabled on maps so large that
     // f32 rounding of positions approaches the margin
     p.filter_margin = c.half_map_size <= 4096.0f ? 0.25f : 0.0f;
+    // magic numbers of n / grid_size (Hacker's Delight 10-8, 33-bit multiplier)
+    uint32_t d = c.grid_size ? c.grid_size : 1u, lg = 0;
+    while (lg < 32u && (1ull << lg) < d) ++lg;
+    p.div_m = (uint32_t)(((1ull << 32) * ((1ull << lg) - d)) / d + 1ull);
+    p.div_s1 = lg > 0u ? 1u : 0u;
+    p.div_s2 = lg > 0u ? lg - 1u : 0u;
     p.pos_slack = 1e-3f;
     return p;
 }
 
 cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t* perm,
                                 const float4* pos_in, const uint4* vfme_in, float4* pos_out,
-                                uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, cudaStream_t st) {
+                                uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse,
+                                cudaStream_t st) {
     if (!n) return cudaSuccess;
     k_physics_init<<<(n + 255u) / 256u, 256, 0, st>>>(p, n, perm, pos_in, vfme_in, pos_out, vfme_out,
-                                                      keys_out, hist);
+                                                      keys_out, hist, coarse);
     return cudaGetLastError();
 }
 
-cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* perm,
-                                const uint32_t* offs, const float4* pos_in, const uint4* vfme_in,
-                                float4* pos_out, uint4* vfme_out, uint32_t* keys_out, uint32_t* hist,
+cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs,
+                                const float4* spos, const uint4* svfme, float4* pos_out, uint4* vfme_out,
+                                uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
                                 cudaStream_t st) {
     if (!n) return cudaSuccess;
     k_physics_loop<<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
-        p, n, perm, offs, pos_in, vfme_in, pos_out, vfme_out, keys_out, hist);
+        p, n, offs, spos, svfme, pos_out, vfme_out, keys_out, hist, coarse, err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,
-                         uint32_t* hist, cudaStream_t st) {
+                         uint32_t* hist, uint32_t* coarse, cudaStream_t st) {
     if (!n) return cudaSuccess;
-    k_rekey<<<(n + 255u) / 256u, 256, 0, st>>>(p, n, pos, keys, hist);
+    k_rekey<<<(n + 255u) / 256u, 256, 0, st>>>(p, n, pos, keys, hist, coarse);
     return cudaGetLastError();
 }
 

@@ -349,6 +349,16 @@ __global__ void k_offs_to_start_close(const uint32_t* __restrict__ offs, uint32_
     if (close) close[c] = full ? b - 1u : kInvalid;
 }
 
+__global__ void __launch_bounds__(256)
+    k_gather_state(const uint32_t* __restrict__ perm, uint32_t n, const float4* __restrict__ pos_in,
+                   const uint4* __restrict__ vfme_in, float4* __restrict__ spos, uint4* __restrict__ svfme) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = min(__ldg(perm + i), n - 1u);
+    spos[i] = __ldg(pos_in + o);
+    svfme[i] = __ldg(vfme_in + o);
+}
+
 size_t onesweep_smem(uint32_t R) {
     return sizeof(uint32_t) * (2u * kSortTile + 2u * R) + sizeof(uint16_t) * (kSortThreads / 32) * R;
 }
@@ -496,6 +506,13 @@ cudaError_t sort_and_offsets(SortScratch& s, const SortSchedule& sch, const uint
     cudaError_t e = sort_pairs(s, sch, keys, vals, sorted_keys, sorted_vals, st);
     if (e) return e;
     return cell_offsets(s, sch, sorted_keys, st);
+}
+
+cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in, const uint4* vfme_in,
+                         float4* spos, uint4* svfme, cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    k_gather_state<<<(n + 255u) / 256u, 256, 0, st>>>(perm, n, pos_in, vfme_in, spos, svfme);
+    return cudaGetLastError();
 }
 
 cudaError_t offsets_to_start_close(const uint32_t* offs, uint32_t cells, uint32_t* start,

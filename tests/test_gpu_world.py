@@ -94,6 +94,13 @@ def test_nonpow2_grid_and_grid_size(built_lib, cuda):
     run_pair(sc, 30, [1, 2, 11, 30])
 
 
+@pytest.mark.parametrize("grid_size", [3, 7])
+def test_odd_grid_sizes(built_lib, cuda, grid_size):
+    """Cell index = u32(x + H_s) / grid_size for divisors that are not powers of two."""
+    sc = scenes.plain_uniform(20_000, 64, grid_size=grid_size, half_map_height=4, seed=40 + grid_size)
+    run_pair(sc, 12, [1, 2, 12])
+
+
 def test_sparse_grid_more_cells_than_agents(built_lib, cuda):
     """C = N*N > n: every cell cleared, not just n (the reference needs n >= N*N)."""
     sc = scenes.plain_uniform(5_000, 512, seed=13)
