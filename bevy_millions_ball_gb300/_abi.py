@@ -96,6 +96,7 @@ SIGNATURES = {
     "mb_sort_plan_create": (C.c_int, [u32, u32, C.POINTER(vp)]),
     "mb_sort_plan_destroy": (C.c_int, [vp]),
     "mb_sort_and_hash": (C.c_int, [vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]),
+    "mb_sort_and_hash_static": (C.c_int, [vp, vp, u32, u32, vp, vp, vp, vp, vp]),
     "mb_get_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),
     "mb_set_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),
     "mb_set_profiling": (C.c_int, [vp, C.c_int]),

@@ -43,6 +43,8 @@ uint32_t q_u32(float x) {
 
 }  // namespace
 
+void mb::set_process_error(const std::string& msg) { g_last_error = msg; }
+
 struct mb_world {
     mb_settings s{};
     mb_consts c{};

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "../../include/millionsball.h"
 
 namespace mb {
@@ -150,5 +152,8 @@ cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in,
                          float4* spos, uint4* svfme, cudaStream_t st);
 
 int device_sm_count();
+
+// Sets the message mb_last_error(NULL) returns on this thread.
+void set_process_error(const std::string& msg);
 
 }  // namespace mb

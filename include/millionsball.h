@@ -196,6 +196,29 @@ mb_status mb_sort_and_hash(mb_sort_plan* p, const uint32_t* keys, const uint32_t
                            uint32_t number_of_cells, uint32_t* sorted_keys, uint32_t* sorted_vals,
                            uint32_t* start, uint32_t* close, void* cuda_stream);
 
+/*
+ * mb_sort_and_hash without any device allocation (no counterpart in the
+ * reference).  For callers that may not allocate device memory where they issue
+ * GPU work: a frame loop that forbids allocation after start-up (allocator
+ * stalls cause frame-time spikes and break fixed memory budgets), or code
+ * recording into a CUDA stream capture, where cudaMalloc cannot be recorded.
+ * Same arguments and results as mb_sort_and_hash minus the plan: the scratch is
+ * one fixed array inside the library (about 3.5 MB on every GPU that loads it).
+ *   - n <= MB_STATIC_MAX_KEYS and 1 <= number_of_cells <= MB_STATIC_MAX_CELLS,
+ *     else MB_ERR_INVALID_ARG (message via mb_last_error(NULL));
+ *   - the first call on a device sets the scratch up (looks up its device
+ *     address and zeroes it on `cuda_stream`): make that first call before any
+ *     stream capture;
+ *   - all calls on a device share the scratch and it keeps the last call's
+ *     contents: calls that overlap on the GPU race and corrupt each other, so
+ *     order them (e.g. issue them on one stream).
+ */
+#define MB_STATIC_MAX_KEYS 262144u
+#define MB_STATIC_MAX_CELLS 262144u
+mb_status mb_sort_and_hash_static(const uint32_t* keys, const uint32_t* vals, uint32_t n,
+                                  uint32_t number_of_cells, uint32_t* sorted_keys, uint32_t* sorted_vals,
+                                  uint32_t* start, uint32_t* close, void* cuda_stream);
+
 /* Per-world kernel choices (the autotuner's knobs). */
 typedef struct mb_tuning {
     uint32_t digit_bits_max;   /* widest radix digit of the onesweep sort, 4..11 */
