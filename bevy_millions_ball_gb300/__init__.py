@@ -22,13 +22,15 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _abi
-from ._abi import MB_DEVICE, MB_HOST, MbConsts, MbError, MbSettings, MbTuning
+from ._abi import MB_DEVICE, MB_HOST, MbConsts, MbError, MbServerConfig, MbServerStats, MbSettings, MbTuning
 
 __all__ = [
     "PhysicsPlugin",
     "PhysicsSettings",
     "World",
     "SortPlan",
+    "Batch",
+    "Server",
     "MbError",
     "pack_vfme",
     "unpack_vfme",
@@ -297,6 +299,147 @@ class SortPlan:
         if self._h:
             self._lib.mb_sort_plan_destroy(self._h)
             self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent scenes stepped together (mb_batch_*); each evolves exactly as alone."""
+
+    def __init__(self, plugins, capacity_agents: int = 0, capacity_cells: int = 0, capacity_scenes: int = 0,
+                 stream=None):
+        self._lib = library()
+        arr = (MbSettings * max(len(plugins), 1))(*[p.to_c() for p in plugins])
+        self._h = C.c_void_p()
+        self.sizes = [int(p.max_number_of_agents) for p in plugins]
+        self.cells = [int(p.number_of_grids_one_dimension) ** 2 for p in plugins]
+        _abi.check(self._lib, self._lib.mb_batch_create(arr, len(plugins), capacity_agents, capacity_cells,
+                                                        capacity_scenes, _stream_handle(stream), C.byref(self._h)))
+
+    def _check(self, st):
+        _abi.check(self._lib, st)
+
+    def add_scene(self, plugin: PhysicsPlugin) -> int:
+        idx = C.c_uint32()
+        self._check(self._lib.mb_batch_add_scene(self._h, C.byref(plugin.to_c()), C.byref(idx)))
+        self.sizes.append(int(plugin.max_number_of_agents))
+        self.cells.append(int(plugin.number_of_grids_one_dimension) ** 2)
+        return idx.value
+
+    def set_state(self, scene: int, pos_scale: np.ndarray, vfme: np.ndarray) -> None:
+        p = np.ascontiguousarray(pos_scale, np.float32)
+        q = np.ascontiguousarray(vfme, np.uint32)
+        self._check(self._lib.mb_batch_set_state(self._h, scene, p.ctypes.data, q.ctypes.data, MB_HOST))
+
+    def get_state(self, scene: int):
+        n = self.sizes[scene]
+        p = np.empty((n, 4), np.float32)
+        q = np.empty((n, 4), np.uint32)
+        self._check(self._lib.mb_batch_get_state(self._h, scene, p.ctypes.data, q.ctypes.data, MB_HOST))
+        return p, q
+
+    def set_active(self, scene: int, active: bool) -> None:
+        self._check(self._lib.mb_batch_set_active(self._h, scene, 1 if active else 0))
+
+    def step(self, k: int = 1) -> None:
+        self._check(self._lib.mb_batch_step(self._h, int(k)))
+
+    def sync(self) -> None:
+        self._check(self._lib.mb_batch_sync(self._h))
+
+    def time(self, scene: int) -> int:
+        return int(self._lib.mb_batch_time(self._h, scene))
+
+    def debug(self, scene: int):
+        n, c = self.sizes[scene], self.cells[scene]
+        keys, perm = np.empty(n, np.uint32), np.empty(n, np.uint32)
+        start, close = np.empty(c, np.uint32), np.empty(c, np.uint32)
+        self._check(self._lib.mb_batch_get_debug(self._h, scene, keys.ctypes.data, perm.ctypes.data,
+                                                 start.ctypes.data, close.ctypes.data, MB_HOST))
+        return {"keys": keys, "perm": perm, "start": start, "close": close}
+
+    def memory(self) -> int:
+        b = C.c_uint64()
+        self._check(self._lib.mb_batch_memory(self._h, C.byref(b)))
+        return b.value
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.mb_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request-serving loop over one batch pool (mb_server_*)."""
+
+    def __init__(self, budget_bytes: int, max_scenes: int = 4096, max_agents: int = 0, max_cells: int = 0,
+                 stream=None):
+        self._lib = library()
+        cfg = MbServerConfig(budget_bytes=int(budget_bytes), max_scenes=max_scenes, max_agents=max_agents,
+                             max_cells=max_cells)
+        self._h = C.c_void_p()
+        self.sizes = {}
+        _abi.check(self._lib, self._lib.mb_server_create(C.byref(cfg), _stream_handle(stream), C.byref(self._h)))
+
+    def create(self, plugin: PhysicsPlugin, pos_scale: np.ndarray, vfme: np.ndarray):
+        """Submit a create-scene request: returns (scene handle, request id)."""
+        p = np.ascontiguousarray(pos_scale, np.float32)
+        q = np.ascontiguousarray(vfme, np.uint32)
+        sc, rq = C.c_uint32(), C.c_uint64()
+        _abi.check(self._lib, self._lib.mb_server_submit_create(self._h, C.byref(plugin.to_c()), p.ctypes.data,
+                                                                q.ctypes.data, C.byref(sc), C.byref(rq)))
+        self.sizes[sc.value] = int(plugin.max_number_of_agents)
+        return sc.value, rq.value
+
+    def advance(self, scene: int, k: int) -> int:
+        rq = C.c_uint64()
+        _abi.check(self._lib, self._lib.mb_server_submit_advance(self._h, scene, int(k), C.byref(rq)))
+        return rq.value
+
+    def wait(self, request: int, timeout: float = 600.0) -> float:
+        """Block until the request is done; returns its latency in seconds."""
+        lat = C.c_double()
+        _abi.check(self._lib, self._lib.mb_server_wait(self._h, request, timeout, C.byref(lat)))
+        return lat.value
+
+    def get_state(self, scene: int):
+        n = self.sizes[scene]
+        p = np.empty((n, 4), np.float32)
+        q = np.empty((n, 4), np.uint32)
+        _abi.check(self._lib, self._lib.mb_server_get_state(self._h, scene, p.ctypes.data, q.ctypes.data))
+        return p, q
+
+    def stats(self) -> MbServerStats:
+        st = MbServerStats()
+        _abi.check(self._lib, self._lib.mb_server_get_stats(self._h, C.byref(st)))
+        return st
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.mb_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def __del__(self):
         try:

@@ -65,6 +65,16 @@ class MbTuning(C.Structure):
 MB_SORT_COUNTING, MB_SORT_ONESWEEP = 0, 1
 
 
+class MbServerConfig(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("max_scenes", u32), ("max_agents", u32), ("max_cells", u32),
+                ("reserved", u32 * 3)]
+
+
+class MbServerStats(C.Structure):
+    _fields_ = [("requests_done", C.c_uint64), ("frames", C.c_uint64), ("agent_steps", C.c_uint64),
+                ("busy_seconds", C.c_double), ("scenes", u32), ("reserved", u32 * 3)]
+
+
 MB_OK = 0
 STATUS_NAMES = {
     0: "MB_OK",
@@ -102,6 +112,25 @@ SIGNATURES = {
     "mb_set_profiling": (C.c_int, [vp, C.c_int]),
     "mb_last_frame_times": (C.c_int, [vp, C.POINTER(C.c_float)]),
     "mb_kernels_per_frame": (u32, [vp]),
+    "mb_batch_create": (C.c_int, [C.POINTER(MbSettings), u32, u32, u32, u32, vp, C.POINTER(vp)]),
+    "mb_batch_add_scene": (C.c_int, [vp, C.POINTER(MbSettings), C.POINTER(u32)]),
+    "mb_batch_destroy": (C.c_int, [vp]),
+    "mb_batch_num_scenes": (u32, [vp]),
+    "mb_batch_memory": (C.c_int, [vp, C.POINTER(C.c_uint64)]),
+    "mb_batch_set_state": (C.c_int, [vp, u32, vp, vp, C.c_int]),
+    "mb_batch_get_state": (C.c_int, [vp, u32, vp, vp, C.c_int]),
+    "mb_batch_set_active": (C.c_int, [vp, u32, C.c_int]),
+    "mb_batch_step": (C.c_int, [vp, u32]),
+    "mb_batch_sync": (C.c_int, [vp]),
+    "mb_batch_time": (i64, [vp, u32]),
+    "mb_batch_get_debug": (C.c_int, [vp, u32, vp, vp, vp, vp, C.c_int]),
+    "mb_server_create": (C.c_int, [C.POINTER(MbServerConfig), vp, C.POINTER(vp)]),
+    "mb_server_destroy": (C.c_int, [vp]),
+    "mb_server_submit_create": (C.c_int, [vp, C.POINTER(MbSettings), vp, vp, C.POINTER(u32), C.POINTER(C.c_uint64)]),
+    "mb_server_submit_advance": (C.c_int, [vp, u32, u32, C.POINTER(C.c_uint64)]),
+    "mb_server_wait": (C.c_int, [vp, C.c_uint64, C.c_double, C.POINTER(C.c_double)]),
+    "mb_server_get_state": (C.c_int, [vp, u32, vp, vp]),
+    "mb_server_get_stats": (C.c_int, [vp, C.POINTER(MbServerStats)]),
     "mb_version": (C.c_char_p, []),
 }
 

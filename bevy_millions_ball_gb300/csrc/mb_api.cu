@@ -86,7 +86,9 @@ mb_status cuda_fail(mb_world* w, const char* what, cudaError_t e) {
     return fail(w, e == cudaErrorMemoryAllocation ? MB_ERR_OOM : MB_ERR_CUDA, cuda_msg(what, e));
 }
 
-bool settings_valid(const mb_settings* s, std::string& why) {
+}  // namespace
+
+bool mb::settings_valid(const mb_settings* s, std::string& why) {
     if (!s) { why = "settings is NULL"; return false; }
     if (s->max_number_of_agents == 0 || s->max_number_of_agents > mb::kMaxAgents) {
         why = "max_number_of_agents must be in [1, 2^28-1]";
@@ -107,6 +109,9 @@ bool settings_valid(const mb_settings* s, std::string& why) {
     if (!(c.time_delta > 0.0f)) { why = "time_delta quantises to 0 (needs >= 0.001)"; return false; }
     return true;
 }
+
+namespace {
+using mb::settings_valid;
 
 void drop_graphs(mb_world* w) {
     for (auto& g : w->graph) {

@@ -1,0 +1,757 @@
+// mb_batch.cu — many independent scenes stepped by one set of launches per
+// frame (batching), and a request-serving loop on top of it (serving).
+//
+// No counterpart in the reference, which runs one scene per app.  Layout: scene
+// s owns sorted slots [agent_base, agent_base + n) and cells
+// [cell_base, cell_base + N*N) of one flattened key space.  A frame is the same
+// three stages as a single world's - count scan, scatter + fixup, physics - run
+// once over all scenes: keys of different scenes never mix, so each scene's
+// stable order, cell ranges and physics are exactly what it gets alone.  Each
+// scene runs its own mode per frame (LOOP, INIT after an upload, or HOLD when
+// it has no step to take); the per-scene table is a device buffer that the host
+// rewrites between launches, so one captured graph per frame parity serves any
+// mix of modes.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "mb_internal.h"
+
+namespace {
+
+constexpr uint32_t kTile = mb::kPhysicsTile;
+
+__global__ void k_fill_keys(uint32_t* keys, uint32_t n, uint32_t value) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) keys[i] = value;
+}
+
+// slot-local debug views of one scene
+__global__ void k_local_debug(const uint32_t* keys, const uint32_t* perm, const uint32_t* offs, uint32_t n,
+                              uint32_t cells, uint32_t agent_base, uint32_t cell_base, uint32_t* okeys,
+                              uint32_t* operm, uint32_t* ostart, uint32_t* oclose) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        if (okeys) okeys[i] = (keys[agent_base + i] & ~mb::kInitKeyBit) - cell_base;
+        if (operm) operm[i] = perm[agent_base + i] - agent_base;
+    }
+    if (i < cells) {
+        uint32_t a = offs[cell_base + i], b = offs[cell_base + i + 1u];
+        bool full = b > a;
+        if (ostart) ostart[i] = full ? a - agent_base : mb::kInvalid;
+        if (oclose) oclose[i] = full ? b - 1u - agent_base : mb::kInvalid;
+    }
+}
+
+struct SceneHost {
+    mb_settings s{};
+    mb_consts c{};
+    uint32_t agent_base = 0, n = 0, cell_base = 0, cells = 0;
+    bool has_state = false;
+    bool init_pending = false;
+    bool active = true;
+    bool frame_done = false;
+    int64_t time = -1;
+};
+
+}  // namespace
+
+struct mb_batch {
+    uint32_t cap_agents = 0, cap_cells = 0, cap_scenes = 0;
+    cudaStream_t stream = nullptr, cap_stream = nullptr;
+    float4* pos[2] = {nullptr, nullptr};
+    uint4* vfme[2] = {nullptr, nullptr};
+    float4* spos = nullptr;
+    uint4* svfme = nullptr;
+    uint32_t *keys = nullptr, *perm = nullptr, *offs = nullptr, *ctl = nullptr, *d_tile_scene = nullptr;
+    mb::SceneDev* d_scenes = nullptr;
+    mb::SceneDev* h_scenes = nullptr;     // pinned mirror of the scene table
+    uint32_t* h_tile_scene = nullptr;     // pinned
+    cudaEvent_t table_ev = nullptr;       // last table upload has been read
+    mb::CountScratch cnt;
+    std::vector<SceneHost> scenes;
+    uint32_t n_total = 0, cells_total = 0;
+    int cur = 0;
+    bool counts_valid = true;             // hist/coarse match keys
+    bool layout_dirty = true;             // scene ranges changed: re-upload tiles, re-capture
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    std::vector<uint32_t> last_modes;
+    std::string err;
+};
+
+namespace {
+
+mb_status bfail(mb_batch* b, mb_status st, const std::string& msg) {
+    if (b) b->err = msg;
+    mb::set_process_error(msg);
+    return st;
+}
+mb_status bcuda(mb_batch* b, const char* what, cudaError_t e) {
+    return bfail(b, e == cudaErrorMemoryAllocation ? MB_ERR_OOM : MB_ERR_CUDA,
+                 std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+void drop_graphs(mb_batch* b) {
+    for (auto& g : b->graph) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
+}
+
+uint64_t bytes_for(uint64_t agents, uint64_t cells, uint64_t scenes) {
+    // state x2, sorted copy, keys, perm; offs, counts, cursors, big list; tables
+    return agents * (32u * 3u + 8u) + cells * 16u + scenes * sizeof(mb::SceneDev) + (agents / kTile + 1u) * 4u +
+           (cells / mb::kScanTile + 2u) * 4u + 64u * 1024u;
+}
+
+cudaError_t alloc_pool(mb_batch* b) {
+    const size_t A = std::max<uint32_t>(b->cap_agents, 1u), Cc = std::max<uint32_t>(b->cap_cells, 1u);
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking))) return e;
+    for (int i = 0; i < 2; ++i) {
+        if ((e = cudaMalloc(&b->pos[i], sizeof(float4) * A))) return e;
+        if ((e = cudaMalloc(&b->vfme[i], sizeof(uint4) * A))) return e;
+    }
+    if ((e = cudaMalloc(&b->spos, sizeof(float4) * A))) return e;
+    if ((e = cudaMalloc(&b->svfme, sizeof(uint4) * A))) return e;
+    if ((e = cudaMalloc(&b->keys, sizeof(uint32_t) * A))) return e;
+    if ((e = cudaMalloc(&b->perm, sizeof(uint32_t) * A))) return e;
+    if ((e = cudaMalloc(&b->offs, sizeof(uint32_t) * (Cc + 1u)))) return e;
+    if ((e = cudaMalloc(&b->ctl, sizeof(uint32_t) * mb::kCtlWords))) return e;
+    if ((e = cudaMemset(b->ctl, 0, sizeof(uint32_t) * mb::kCtlWords))) return e;
+    if ((e = cudaMalloc(&b->d_tile_scene, sizeof(uint32_t) * (A / kTile + 1u)))) return e;
+    if ((e = cudaMalloc(&b->d_scenes, sizeof(mb::SceneDev) * std::max<uint32_t>(b->cap_scenes, 1u)))) return e;
+    if ((e = cudaMallocHost(&b->h_scenes, sizeof(mb::SceneDev) * std::max<uint32_t>(b->cap_scenes, 1u)))) return e;
+    if ((e = cudaMallocHost(&b->h_tile_scene, sizeof(uint32_t) * (A / kTile + 1u)))) return e;
+    if ((e = cudaEventCreateWithFlags(&b->table_ev, cudaEventDisableTiming))) return e;
+    if ((e = cudaMemset(b->keys, 0, sizeof(uint32_t) * A))) return e;
+    return mb::count_scratch_alloc(b->cnt, (uint32_t)Cc);
+}
+
+void free_pool(mb_batch* b) {
+    drop_graphs(b);
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(b->pos[i]);
+        cudaFree(b->vfme[i]);
+    }
+    cudaFree(b->spos);
+    cudaFree(b->svfme);
+    cudaFree(b->keys);
+    cudaFree(b->perm);
+    cudaFree(b->offs);
+    cudaFree(b->ctl);
+    cudaFree(b->d_tile_scene);
+    cudaFree(b->d_scenes);
+    if (b->h_scenes) cudaFreeHost(b->h_scenes);
+    if (b->h_tile_scene) cudaFreeHost(b->h_tile_scene);
+    if (b->table_ev) cudaEventDestroy(b->table_ev);
+    mb::count_scratch_free(b->cnt);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+}
+
+mb_status add_scene(mb_batch* b, const mb_settings* s, uint32_t* index) {
+    std::string why;
+    if (!mb::settings_valid(s, why)) return bfail(b, MB_ERR_INVALID_ARG, why);
+    const uint64_t cells = (uint64_t)s->number_of_grids_one_dimension * s->number_of_grids_one_dimension;
+    if (b->scenes.size() >= b->cap_scenes || (uint64_t)b->n_total + s->max_number_of_agents > b->cap_agents ||
+        (uint64_t)b->cells_total + cells > b->cap_cells)
+        return bfail(b, MB_ERR_BUDGET_EXCEEDED, "batch capacity exhausted (scenes, spheres or cells)");
+    SceneHost h;
+    h.s = *s;
+    mb_quantize_settings(s, &h.c);
+    h.agent_base = b->n_total;
+    h.n = s->max_number_of_agents;
+    h.cell_base = b->cells_total;
+    h.cells = (uint32_t)cells;
+    b->scenes.push_back(h);
+    b->n_total += h.n;
+    b->cells_total += h.cells;
+    b->layout_dirty = true;
+    b->counts_valid = false;
+    if (index) *index = (uint32_t)(b->scenes.size() - 1u);
+    return MB_OK;
+}
+
+// Upload the scene table (and tile table after a layout change) if it differs
+// from what the device holds.
+cudaError_t sync_tables(mb_batch* b, const std::vector<uint32_t>& modes) {
+    const bool layout = b->layout_dirty;
+    if (!layout && modes == b->last_modes) return cudaSuccess;
+    cudaError_t e = cudaEventSynchronize(b->table_ev);  // pinned mirrors free to rewrite
+    if (e) return e;
+    const uint32_t S = (uint32_t)b->scenes.size();
+    for (uint32_t i = 0; i < S; ++i) {
+        const SceneHost& h = b->scenes[i];
+        mb::SceneDev& d = b->h_scenes[i];
+        d.P = mb::make_params(h.c);
+        d.agent_base = h.agent_base;
+        d.agent_end = h.agent_base + h.n;
+        d.cell_base = h.cell_base;
+        d.mode = modes[i];
+    }
+    if ((e = cudaMemcpyAsync(b->d_scenes, b->h_scenes, sizeof(mb::SceneDev) * S, cudaMemcpyHostToDevice,
+                             b->stream)))
+        return e;
+    if (layout) {
+        const uint32_t tiles = (b->n_total + kTile - 1u) / kTile;
+        uint32_t sc = 0;
+        for (uint32_t t = 0; t < tiles; ++t) {
+            while (sc + 1u < S && t * kTile >= b->scenes[sc].agent_base + b->scenes[sc].n) ++sc;
+            b->h_tile_scene[t] = sc;
+        }
+        if ((e = cudaMemcpyAsync(b->d_tile_scene, b->h_tile_scene, sizeof(uint32_t) * std::max(tiles, 1u),
+                                 cudaMemcpyHostToDevice, b->stream)))
+            return e;
+        drop_graphs(b);
+        b->layout_dirty = false;
+    }
+    b->last_modes = modes;
+    return cudaEventRecord(b->table_ev, b->stream);
+}
+
+cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st, int cur) {
+    cudaError_t e;
+    if ((e = mb::count_scan(b->cnt, b->ctl, b->cells_total, b->offs, st))) return e;
+    if ((e = mb::count_scatter(b->cnt, b->keys, b->n_total, b->cells_total, b->offs, b->perm, b->pos[cur],
+                               b->vfme[cur], b->spos, b->svfme, st)))
+        return e;
+    return mb::launch_physics_batch(b->d_scenes, b->d_tile_scene, b->n_total, b->offs, b->spos, b->svfme,
+                                    b->pos[cur], b->vfme[cur], b->pos[cur ^ 1], b->vfme[cur ^ 1], b->keys,
+                                    b->cnt.hist, b->cnt.coarse, b->ctl + mb::kCtlError, st);
+}
+
+cudaError_t build_graph(mb_batch* b, int cur) {
+    cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
+    if (e) return e;
+    cudaError_t fe = enqueue_frame(b, b->cap_stream, cur);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(b->cap_stream, &g);
+    if (fe) {
+        if (g) cudaGraphDestroy(g);
+        return fe;
+    }
+    if (e) return e;
+    e = cudaGraphInstantiate(&b->graph[cur], g, 0);
+    cudaGraphDestroy(g);
+    return e;
+}
+
+// Rebuild per-cell counts from the keys of every scene (after an upload).
+cudaError_t recount(mb_batch* b) {
+    cudaError_t e = mb::count_keys(b->cnt, b->keys, b->n_total, b->cells_total, b->stream);
+    if (!e) b->counts_valid = true;
+    return e;
+}
+
+// One frame over every scene; modes[i] is scene i's mode for this frame.
+mb_status run_frame(mb_batch* b, const std::vector<uint32_t>& modes) {
+    cudaError_t e;
+    if (!b->counts_valid && (e = recount(b))) return bcuda(b, "batch recount", e);
+    if ((e = sync_tables(b, modes))) return bcuda(b, "batch tables", e);
+    if (!b->graph[b->cur] && (e = build_graph(b, b->cur))) return bcuda(b, "batch capture", e);
+    if ((e = cudaGraphLaunch(b->graph[b->cur], b->stream))) return bcuda(b, "batch frame", e);
+    for (size_t i = 0; i < b->scenes.size(); ++i) {
+        SceneHost& h = b->scenes[i];
+        if (modes[i] != mb::kModeHold) {
+            h.time += 1;
+            h.frame_done = true;
+        }
+        if (modes[i] == mb::kModeInit) h.init_pending = false;
+    }
+    b->cur ^= 1;
+    return MB_OK;
+}
+
+// Copy a scene's state in the pool's current buffers (every scene lives in the
+// same parity).
+mb_status set_scene_state(mb_batch* b, uint32_t si, const float* pos, const uint32_t* vfme, mb_memory where) {
+    if (si >= b->scenes.size()) return bfail(b, MB_ERR_INVALID_ARG, "scene index out of range");
+    if (!pos || !vfme) return bfail(b, MB_ERR_INVALID_ARG, "NULL state");
+    SceneHost& h = b->scenes[si];
+    cudaMemcpyKind kind = where == MB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(b->pos[b->cur] + h.agent_base, pos, sizeof(float4) * h.n, kind, b->stream)))
+        return bcuda(b, "batch set_state", e);
+    if ((e = cudaMemcpyAsync(b->vfme[b->cur] + h.agent_base, vfme, sizeof(uint4) * h.n, kind, b->stream)))
+        return bcuda(b, "batch set_state", e);
+    k_fill_keys<<<(h.n + 255u) / 256u, 256, 0, b->stream>>>(b->keys + h.agent_base, h.n,
+                                                             h.cell_base | mb::kInitKeyBit);
+    if ((e = cudaGetLastError())) return bcuda(b, "batch set_state", e);
+    if (where == MB_HOST && (e = cudaStreamSynchronize(b->stream))) return bcuda(b, "batch set_state", e);
+    h.has_state = true;
+    h.init_pending = true;
+    h.frame_done = false;
+    h.time = 0;
+    b->counts_valid = false;
+    return MB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mb_status mb_batch_create(const mb_settings* scenes, uint32_t num_scenes, uint32_t capacity_agents,
+                          uint32_t capacity_cells, uint32_t capacity_scenes, void* cuda_stream, mb_batch** out) {
+    if (!out) return bfail(nullptr, MB_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (num_scenes && !scenes) return bfail(nullptr, MB_ERR_INVALID_ARG, "scenes is NULL");
+    uint64_t agents = 0, cells = 0;
+    std::string why;
+    for (uint32_t i = 0; i < num_scenes; ++i) {
+        if (!mb::settings_valid(&scenes[i], why)) return bfail(nullptr, MB_ERR_INVALID_ARG, why);
+        agents += scenes[i].max_number_of_agents;
+        cells += (uint64_t)scenes[i].number_of_grids_one_dimension * scenes[i].number_of_grids_one_dimension;
+    }
+    agents = std::max<uint64_t>(agents, capacity_agents);
+    cells = std::max<uint64_t>(cells, capacity_cells);
+    if (agents > mb::kMaxAgents || cells > mb::kMaxCells)
+        return bfail(nullptr, MB_ERR_INVALID_ARG, "batch exceeds 2^28 spheres or cells");
+    mb_batch* b = new (std::nothrow) mb_batch();
+    if (!b) return bfail(nullptr, MB_ERR_OOM, "host allocation failed");
+    b->cap_agents = (uint32_t)agents;
+    b->cap_cells = (uint32_t)cells;
+    b->cap_scenes = std::max(num_scenes, capacity_scenes);
+    b->stream = (cudaStream_t)cuda_stream;
+    cudaError_t e = alloc_pool(b);
+    if (e) {
+        mb_status st = bcuda(nullptr, "mb_batch_create", e);
+        free_pool(b);
+        delete b;
+        return st;
+    }
+    for (uint32_t i = 0; i < num_scenes; ++i) add_scene(b, &scenes[i], nullptr);
+    *out = b;
+    return MB_OK;
+}
+
+mb_status mb_batch_add_scene(mb_batch* b, const mb_settings* s, uint32_t* index) {
+    if (!b) return bfail(nullptr, MB_ERR_INVALID_ARG, "batch is NULL");
+    return add_scene(b, s, index);
+}
+
+mb_status mb_batch_destroy(mb_batch* b) {
+    if (!b) return MB_OK;
+    cudaStreamSynchronize(b->stream);
+    free_pool(b);
+    delete b;
+    return MB_OK;
+}
+
+uint32_t mb_batch_num_scenes(const mb_batch* b) { return b ? (uint32_t)b->scenes.size() : 0u; }
+
+mb_status mb_batch_memory(const mb_batch* b, uint64_t* bytes) {
+    if (!b || !bytes) return MB_ERR_INVALID_ARG;
+    *bytes = bytes_for(b->cap_agents, b->cap_cells, b->cap_scenes);
+    return MB_OK;
+}
+
+mb_status mb_batch_set_state(mb_batch* b, uint32_t scene, const float* pos_scale, const uint32_t* vfme,
+                             mb_memory where) {
+    if (!b) return bfail(nullptr, MB_ERR_INVALID_ARG, "batch is NULL");
+    return set_scene_state(b, scene, pos_scale, vfme, where);
+}
+
+mb_status mb_batch_get_state(mb_batch* b, uint32_t scene, float* pos_scale, uint32_t* vfme, mb_memory where) {
+    if (!b) return bfail(nullptr, MB_ERR_INVALID_ARG, "batch is NULL");
+    if (scene >= b->scenes.size()) return bfail(b, MB_ERR_INVALID_ARG, "scene index out of range");
+    const SceneHost& h = b->scenes[scene];
+    if (!h.has_state) return bfail(b, MB_ERR_NOT_READY, "scene has no state");
+    cudaMemcpyKind kind = where == MB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    cudaError_t e;
+    if (pos_scale &&
+        (e = cudaMemcpyAsync(pos_scale, b->pos[b->cur] + h.agent_base, sizeof(float4) * h.n, kind, b->stream)))
+        return bcuda(b, "batch get_state", e);
+    if (vfme && (e = cudaMemcpyAsync(vfme, b->vfme[b->cur] + h.agent_base, sizeof(uint4) * h.n, kind, b->stream)))
+        return bcuda(b, "batch get_state", e);
+    if (where == MB_HOST && (e = cudaStreamSynchronize(b->stream))) return bcuda(b, "batch get_state", e);
+    return MB_OK;
+}
+
+mb_status mb_batch_set_active(mb_batch* b, uint32_t scene, int active) {
+    if (!b) return bfail(nullptr, MB_ERR_INVALID_ARG, "batch is NULL");
+    if (scene >= b->scenes.size()) return bfail(b, MB_ERR_INVALID_ARG, "scene index out of range");
+    b->scenes[scene].active = active != 0;
+    return MB_OK;
+}
+
+mb_status mb_batch_step(mb_batch* b, uint32_t k) {
+    if (!b) return bfail(nullptr, MB_ERR_INVALID_ARG, "batch is NULL");
+    for (const SceneHost& h : b->scenes)
+        if (!h.has_state) return bfail(b, MB_ERR_NOT_READY, "every scene needs a state before stepping");
+    std::vector<uint32_t> modes(b->scenes.size());
+    for (uint32_t f = 0; f < k; ++f) {
+        for (size_t i = 0; i < b->scenes.size(); ++i) {
+            const SceneHost& h = b->scenes[i];
+            const bool run = h.active && h.s.enable_simulation;
+            modes[i] = !run ? mb::kModeHold : (h.init_pending ? mb::kModeInit : mb::kModeLoop);
+        }
+        mb_status st = run_frame(b, modes);
+        if (st != MB_OK) return st;
+    }
+    return MB_OK;
+}
+
+mb_status mb_batch_sync(mb_batch* b) {
+    if (!b) return bfail(nullptr, MB_ERR_INVALID_ARG, "batch is NULL");
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e) return bcuda(b, "mb_batch_sync", e);
+    uint32_t flag = 0;
+    if ((e = cudaMemcpy(&flag, b->ctl + mb::kCtlError, sizeof(uint32_t), cudaMemcpyDeviceToHost)))
+        return bcuda(b, "mb_batch_sync", e);
+    if (flag) {
+        cudaMemset(b->ctl + mb::kCtlError, 0, sizeof(uint32_t));
+        return bfail(b, MB_ERR_TIMEOUT, "a bounded device-side wait gave up; results since the last sync are invalid");
+    }
+    return MB_OK;
+}
+
+int64_t mb_batch_time(const mb_batch* b, uint32_t scene) {
+    return (b && scene < b->scenes.size()) ? b->scenes[scene].time : -1;
+}
+
+mb_status mb_batch_get_debug(mb_batch* b, uint32_t scene, uint32_t* keys, uint32_t* perm, uint32_t* start,
+                             uint32_t* close, mb_memory where) {
+    if (!b) return bfail(nullptr, MB_ERR_INVALID_ARG, "batch is NULL");
+    if (scene >= b->scenes.size()) return bfail(b, MB_ERR_INVALID_ARG, "scene index out of range");
+    const SceneHost& h = b->scenes[scene];
+    if (!h.frame_done) return bfail(b, MB_ERR_NOT_READY, "no frame has run for this scene since its upload");
+    const uint32_t m = std::max(h.n, h.cells);
+    uint32_t* tmp = nullptr;  // device staging for host requests
+    cudaError_t e;
+    uint32_t *dk = keys, *dp = perm, *ds = start, *dc = close;
+    if (where == MB_HOST) {
+        if ((e = cudaMalloc(&tmp, sizeof(uint32_t) * (2u * (size_t)h.n + 2u * (size_t)h.cells))))
+            return bcuda(b, "batch debug", e);
+        dk = keys ? tmp : nullptr;
+        dp = perm ? tmp + h.n : nullptr;
+        ds = start ? tmp + 2u * h.n : nullptr;
+        dc = close ? tmp + 2u * h.n + h.cells : nullptr;
+    }
+    k_local_debug<<<(m + 255u) / 256u, 256, 0, b->stream>>>(b->keys, b->perm, b->offs, h.n, h.cells,
+                                                             h.agent_base, h.cell_base, dk, dp, ds, dc);
+    e = cudaGetLastError();
+    if (!e && where == MB_HOST) {
+        if (keys) e = cudaMemcpyAsync(keys, dk, sizeof(uint32_t) * h.n, cudaMemcpyDeviceToHost, b->stream);
+        if (!e && perm) e = cudaMemcpyAsync(perm, dp, sizeof(uint32_t) * h.n, cudaMemcpyDeviceToHost, b->stream);
+        if (!e && start) e = cudaMemcpyAsync(start, ds, sizeof(uint32_t) * h.cells, cudaMemcpyDeviceToHost, b->stream);
+        if (!e && close) e = cudaMemcpyAsync(close, dc, sizeof(uint32_t) * h.cells, cudaMemcpyDeviceToHost, b->stream);
+        if (!e) e = cudaStreamSynchronize(b->stream);
+        cudaFree(tmp);
+    }
+    if (e) return bcuda(b, "batch debug", e);
+    return MB_OK;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Serving: a request loop over one batch pool.
+//
+// create-scene requests are admitted in arrival order while the pool's memory
+// budget (spheres, cells, scenes reserved at start-up) has room; scenes stay
+// resident, so a create that does not fit is rejected (MB_ERR_BUDGET_EXCEEDED)
+// and so are later requests on it.  Advance requests add steps to their scene.  A worker thread runs frames over the
+// pool: every scene with a pending step runs LOOP (INIT first after an
+// upload), the others HOLD.  Requests that arrive while frames are on the GPU
+// join at the next frame.  A request completes when its scene has taken all
+// its steps; its latency is completion minus submission (host clock).
+// ============================================================================
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    uint64_t id = 0;
+    bool create = false;
+    uint32_t scene = 0;
+    uint32_t steps = 0;
+    mb_settings settings{};
+    std::vector<float> pos;
+    std::vector<uint32_t> vfme;
+    Clock::time_point submitted;
+    int64_t target_time = -1;  // scene time at which the request is done
+    bool done = false;
+    double latency = 0.0;
+    mb_status status = MB_OK;
+};
+
+struct ServerScene {
+    bool admitted = false;
+    bool rejected = false;
+    uint32_t pool = 0;          // index of the scene in the batch pool
+    int64_t pending = 0;        // steps owed (incl. INIT)
+    int64_t scheduled_time = 0; // scene time after every step owed so far
+};
+
+}  // namespace
+
+struct mb_server {
+    mb_batch* pool = nullptr;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request*> incoming;        // not yet seen by the worker
+    std::unordered_map<uint64_t, Request*> requests;
+    std::vector<ServerScene> sscenes;     // by scene handle (submission order)
+    std::vector<uint32_t> pool_handle;    // scene handle of each pool scene
+    std::vector<Request*> in_flight;      // advance/create requests not yet complete
+    uint64_t next_id = 1;
+    uint32_t next_scene = 0;              // scene handles handed out (admission order)
+    bool stop = false;
+    mb_server_stats stats{};
+    std::string err;
+};
+
+namespace {
+
+void complete(mb_server* s, Request* r, Clock::time_point now) {
+    r->done = true;
+    r->latency = std::chrono::duration<double>(now - r->submitted).count();
+    s->stats.requests_done += 1;
+}
+
+void worker_loop(mb_server* s) {
+    mb_batch* b = s->pool;
+    std::vector<uint32_t> modes;
+    std::unique_lock<std::mutex> lk(s->mu);
+    while (true) {
+        bool idle = true;
+        for (const ServerScene& sc : s->sscenes)
+            if (sc.admitted && sc.pending > 0) idle = false;
+        if (idle && s->incoming.empty()) s->cv_work.wait(lk, [&] { return s->stop || !s->incoming.empty(); });
+        if (s->stop) return;
+        // admit creates in arrival order; queue advances on their scenes
+        std::deque<Request*> fresh;
+        fresh.swap(s->incoming);
+        for (Request* r : fresh) {
+            if (s->sscenes.size() <= r->scene) s->sscenes.resize(r->scene + 1u);
+            ServerScene& sc = s->sscenes[r->scene];
+            if (r->create) {
+                uint32_t idx = 0;
+                mb_status st = add_scene(b, &r->settings, &idx);
+                if (st == MB_OK) st = set_scene_state(b, idx, r->pos.data(), r->vfme.data(), MB_HOST);
+                r->pos = std::vector<float>();
+                r->vfme = std::vector<uint32_t>();
+                if (st != MB_OK) {  // no room (scenes stay resident) or bad input: rejected
+                    r->status = st;
+                    sc.rejected = true;
+                    complete(s, r, Clock::now());
+                    continue;
+                }
+                if (s->pool_handle.size() <= idx) s->pool_handle.resize(idx + 1u);
+                s->pool_handle[idx] = r->scene;
+                sc.admitted = true;
+                sc.pool = idx;
+                sc.pending = 1;  // the INIT frame
+                sc.scheduled_time = 1;
+                r->target_time = 1;
+                s->in_flight.push_back(r);
+            } else {
+                if (sc.rejected || !sc.admitted) {
+                    r->status = sc.rejected ? MB_ERR_BUDGET_EXCEEDED : MB_ERR_INVALID_ARG;
+                    complete(s, r, Clock::now());
+                    continue;
+                }
+                sc.pending += r->steps;
+                sc.scheduled_time += r->steps;
+                r->target_time = sc.scheduled_time;
+                s->in_flight.push_back(r);
+            }
+        }
+        s->cv_done.notify_all();
+        // frames while the active set is unchanged (up to 16, INIT frames alone)
+        const size_t S = b->scenes.size();
+        int64_t frames = 0;
+        {
+            int64_t m = 16;
+            bool any = false;
+            for (size_t i = 0; i < S; ++i) {
+                const ServerScene& sc = s->sscenes[s->pool_handle[i]];
+                if (!sc.admitted || sc.pending <= 0) continue;
+                any = true;
+                m = std::min<int64_t>(m, b->scenes[i].init_pending ? 1 : sc.pending);
+            }
+            frames = any ? m : 0;
+        }
+        if (frames == 0) continue;
+        const auto t0 = Clock::now();
+        uint64_t agent_steps = 0;
+        modes.assign(S, mb::kModeHold);
+        for (int64_t f = 0; f < frames; ++f) {
+            for (size_t i = 0; i < S; ++i) {
+                const ServerScene& sc = s->sscenes[s->pool_handle[i]];
+                const bool run = sc.admitted && sc.pending > 0 && b->scenes[i].s.enable_simulation;
+                modes[i] = !run ? mb::kModeHold : (b->scenes[i].init_pending ? mb::kModeInit : mb::kModeLoop);
+                if (modes[i] == mb::kModeLoop) agent_steps += b->scenes[i].n;
+            }
+            if (run_frame(b, modes) != MB_OK) {
+                s->err = b->err;
+                break;
+            }
+            for (size_t i = 0; i < S; ++i)
+                if (modes[i] != mb::kModeHold) s->sscenes[s->pool_handle[i]].pending -= 1;
+        }
+        lk.unlock();  // submitters keep queueing while the GPU works
+        cudaStreamSynchronize(b->stream);
+        const auto t1 = Clock::now();
+        lk.lock();
+        s->stats.frames += (uint64_t)frames;
+        s->stats.agent_steps += agent_steps;
+        s->stats.busy_seconds += std::chrono::duration<double>(t1 - t0).count();
+        for (auto it = s->in_flight.begin(); it != s->in_flight.end();) {
+            Request* r = *it;
+            if (b->scenes[s->sscenes[r->scene].pool].time >= r->target_time) {
+                complete(s, r, t1);
+                it = s->in_flight.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        s->cv_done.notify_all();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+mb_status mb_server_create(const mb_server_config* cfg, void* cuda_stream, mb_server** out) {
+    if (!out || !cfg) return bfail(nullptr, MB_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    // split the budget: per sphere ~104 B, per cell 16 B (cells ~ 2 x spheres)
+    uint64_t budget = cfg->budget_bytes;
+    uint64_t agents = cfg->max_agents, cells = cfg->max_cells;
+    if (!agents || !cells) {
+        const uint64_t fixed = bytes_for(0, 0, cfg->max_scenes);
+        const uint64_t per = 104u + 2u * 16u + 1u;  // a sphere and two cells, plus tile tables
+        agents = budget > fixed ? std::min<uint64_t>((budget - fixed) / per, mb::kMaxAgents) : 0u;
+        cells = std::min<uint64_t>(2u * agents, mb::kMaxCells);
+    }
+    if (bytes_for(agents, cells, cfg->max_scenes) > budget)
+        return bfail(nullptr, MB_ERR_BUDGET_EXCEEDED, "configured capacity exceeds the memory budget");
+    mb_server* s = new (std::nothrow) mb_server();
+    if (!s) return bfail(nullptr, MB_ERR_OOM, "host allocation failed");
+    mb_status st = mb_batch_create(nullptr, 0, (uint32_t)agents, (uint32_t)cells,
+                                   std::max<uint32_t>(cfg->max_scenes, 1u), cuda_stream, &s->pool);
+    if (st != MB_OK) {
+        delete s;
+        return st;
+    }
+    s->worker = std::thread(worker_loop, s);
+    *out = s;
+    return MB_OK;
+}
+
+mb_status mb_server_destroy(mb_server* s) {
+    if (!s) return MB_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    mb_batch_destroy(s->pool);
+    for (auto& kv : s->requests) delete kv.second;
+    delete s;
+    return MB_OK;
+}
+
+mb_status mb_server_submit_create(mb_server* s, const mb_settings* settings, const float* pos_scale,
+                                  const uint32_t* vfme, uint32_t* scene, uint64_t* request) {
+    if (!s || !settings || !pos_scale || !vfme) return bfail(nullptr, MB_ERR_INVALID_ARG, "NULL argument");
+    std::string why;
+    if (!mb::settings_valid(settings, why)) return bfail(nullptr, MB_ERR_INVALID_ARG, why);
+    Request* r = new (std::nothrow) Request();
+    if (!r) return bfail(nullptr, MB_ERR_OOM, "host allocation failed");
+    r->create = true;
+    r->settings = *settings;
+    const size_t n = settings->max_number_of_agents;
+    r->pos.assign(pos_scale, pos_scale + 4u * n);
+    r->vfme.assign(vfme, vfme + 4u * n);
+    r->submitted = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        r->id = s->next_id++;
+        r->scene = s->next_scene++;
+        s->requests[r->id] = r;
+        s->incoming.push_back(r);
+    }
+    s->cv_work.notify_all();
+    if (scene) *scene = r->scene;
+    if (request) *request = r->id;
+    return MB_OK;
+}
+
+mb_status mb_server_submit_advance(mb_server* s, uint32_t scene, uint32_t k, uint64_t* request) {
+    if (!s) return bfail(nullptr, MB_ERR_INVALID_ARG, "server is NULL");
+    Request* r = new (std::nothrow) Request();
+    if (!r) return bfail(nullptr, MB_ERR_OOM, "host allocation failed");
+    r->scene = scene;
+    r->steps = k;
+    r->submitted = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (scene >= s->next_scene) {
+            delete r;
+            return bfail(nullptr, MB_ERR_INVALID_ARG, "unknown scene");
+        }
+        r->id = s->next_id++;
+        s->requests[r->id] = r;
+        s->incoming.push_back(r);
+    }
+    s->cv_work.notify_all();
+    if (request) *request = r->id;
+    return MB_OK;
+}
+
+mb_status mb_server_wait(mb_server* s, uint64_t request, double timeout_s, double* latency_s) {
+    if (!s) return bfail(nullptr, MB_ERR_INVALID_ARG, "server is NULL");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->requests.find(request);
+    if (it == s->requests.end()) return bfail(nullptr, MB_ERR_INVALID_ARG, "unknown request");
+    Request* r = it->second;
+    bool ok = s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), [&] { return r->done; });
+    if (!ok) return MB_ERR_NOT_READY;
+    if (latency_s) *latency_s = r->latency;
+    mb_status st = r->status;
+    s->requests.erase(it);
+    delete r;
+    return st;
+}
+
+mb_status mb_server_get_state(mb_server* s, uint32_t scene, float* pos_scale, uint32_t* vfme) {
+    if (!s) return bfail(nullptr, MB_ERR_INVALID_ARG, "server is NULL");
+    // wait until the scene owes no step, then copy under the lock (frames are
+    // only launched by the worker, which takes the lock between rounds)
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (scene >= s->next_scene) return bfail(nullptr, MB_ERR_INVALID_ARG, "unknown scene");
+    s->cv_done.wait(lk, [&] {
+        if (scene >= s->sscenes.size()) return false;
+        const ServerScene& sc = s->sscenes[scene];
+        return sc.rejected || (sc.admitted && sc.pending == 0);
+    });
+    if (s->sscenes[scene].rejected) return bfail(nullptr, MB_ERR_BUDGET_EXCEEDED, "scene was not admitted");
+    return mb_batch_get_state(s->pool, s->sscenes[scene].pool, pos_scale, vfme, MB_HOST);
+}
+
+mb_status mb_server_get_stats(mb_server* s, mb_server_stats* out) {
+    if (!s || !out) return MB_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
+    out->scenes = (uint32_t)s->pool->scenes.size();
+    return MB_OK;
+}
+
+}  // extern "C"

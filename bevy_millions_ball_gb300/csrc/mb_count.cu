@@ -131,13 +131,16 @@ __global__ void __launch_bounds__(256)
             p = __ldg(pos_in + i);
             q = __ldg(vfme_in + i);
         }
-        uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+        // a key flagged kInitKeyBit belongs to a scene in its INIT frame: all its
+        // keys are equal, so its stable order is the identity and the slot is i
+        const bool ident = valid && (k & kInitKeyBit);
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k);
         uint32_t leader = (uint32_t)(__ffs(peers) - 1);
         uint32_t b = 0;
-        if (valid && lane == leader) b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
+        if (valid && !ident && lane == leader) b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
         if (valid) {
-            const uint32_t dst = b + (uint32_t)__popc(peers & lt);
+            const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
             perm[dst] = i;
             spos[dst] = p;
             svfme[dst] = q;
@@ -295,7 +298,7 @@ __global__ void __launch_bounds__(256)
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
         uint32_t i = i0 + threadIdx.x;
         bool valid = i < n;
-        uint32_t k = valid ? __ldg(keys + i) : 0xFFFFFFFFu;
+        uint32_t k = valid ? (__ldg(keys + i) & ~kInitKeyBit) : 0xFFFFFFFFu;
         uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
         if (valid && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(hist + k, (uint32_t)__popc(peers));
         uint32_t t = valid ? k / kScanTile : 0xFFFFFFFFu;

@@ -16,6 +16,8 @@ constexpr uint32_t kMaxDigitBits = 11;
 constexpr uint32_t kMaxRadix = 1u << kMaxDigitBits;
 constexpr uint32_t kMaxAgents = (1u << 28) - 1u;   // look-back words keep 28 value bits
 constexpr uint32_t kMaxCells = 1u << 28;
+// Flag on a cell key of a batched scene in its INIT frame (keys are < 2^28).
+constexpr uint32_t kInitKeyBit = 0x80000000u;
 
 // Onesweep tile shape: 256 threads x 16 keys.
 constexpr int kSortThreads = 256;
@@ -99,6 +101,16 @@ struct PhysParams {
 
 PhysParams make_params(const mb_consts& c);
 
+// One scene of a batch (many scenes in one flattened key space).
+enum : uint32_t { kModeHold = 0, kModeInit = 1, kModeLoop = 2 };
+struct SceneDev {
+    PhysParams P;
+    uint32_t agent_base, agent_end;  // sorted slots [agent_base, agent_end)
+    uint32_t cell_base;              // cells [cell_base, cell_base + N*N)
+    uint32_t mode;                   // kModeHold / kModeInit / kModeLoop
+};
+constexpr uint32_t kPhysicsTile = 128;  // slots per block of the physics pass
+
 // Physics passes.  `hist` / `coarse` (nullable together) accumulate the per-cell
 // and per-4096-cell-tile counts of the keys they emit, for the next frame's
 // counting sort.
@@ -113,6 +125,13 @@ cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t*
                                 cudaStream_t st);
 cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,
                          uint32_t* hist, uint32_t* coarse, cudaStream_t st);
+
+// Batched LOOP/INIT/HOLD pass: tile_scene[t] = scene of slot t*kPhysicsTile.
+// pos_in/vfme_in: the frame's input state in input order (HOLD scenes copy it).
+cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
+                                 const uint32_t* offs, const float4* spos, const uint4* svfme, const float4* pos_in,
+                                 const uint4* vfme_in, float4* pos_out, uint4* vfme_out, uint32_t* keys_out,
+                                 uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st);
 
 // Counting sort of cell keys (mb_count.cu).
 constexpr int kScanThreads = 256;
@@ -152,6 +171,9 @@ cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in,
                          float4* spos, uint4* svfme, cudaStream_t st);
 
 int device_sm_count();
+
+// Settings checks shared by worlds and batches ("" = valid).
+bool settings_valid(const mb_settings* s, std::string& why);
 
 // Sets the message mb_last_error(NULL) returns on this thread.
 void set_process_error(const std::string& msg);

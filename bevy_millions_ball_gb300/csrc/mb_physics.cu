@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256)
 // Bands of at most kBandCap slots are copied to shared memory with TMA bulk
 // copies (cp.async.bulk, completion on one mbarrier); wider bands (a tile
 // spanning a row boundary) are read from global memory instead.
-constexpr int kTileThreads = 128;
+constexpr int kTileThreads = kPhysicsTile;
 constexpr uint32_t kBandCap = 2 * kTileThreads;
 constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier wait (error flag on expiry)
 
@@ -365,15 +365,31 @@ __device__ __forceinline__ uint32_t key_of(const PhysParams& P, float4 p) {
     return cz * P.N + cx;
 }
 
-// main, LOOP pipeline (physics.wgsl:57-89): one thread per sorted slot, one
-// block per tile of kTileThreads consecutive slots.  spos/svfme hold the state in
-// sorted order (agent_new(agent_index_sorted[i]) of the reference is spos[i]).
+// Scene of sorted slot i: start from the first scene of the tile.
+__device__ __forceinline__ uint32_t scene_of(const SceneDev* __restrict__ scenes, uint32_t first, uint32_t i) {
+    uint32_t s = first;
+    while (i >= __ldg(&scenes[s].agent_end)) ++s;
+    return s;
+}
+
+// main (physics.wgsl:57-97) for one tile of kTileThreads consecutive sorted
+// slots, one thread per slot.  spos/svfme hold the state in sorted order
+// (agent_new(agent_index_sorted[i]) of the reference is spos[i]).
+//
+// kBatched = false: one scene, parameters P, LOOP pipeline.
+// kBatched = true: many scenes in one flattened key space (scene s owns slots
+// [agent_base, agent_end) and cells [cell_base, cell_base + N*N)); each slot runs
+// its scene's mode: LOOP, INIT (re-pack, emit key) or HOLD (state carried over
+// unchanged, key re-emitted).  Slot indices inside a scene (the jitter hash)
+// are local, so every scene evolves exactly as it would alone.
+template <bool kBatched>
 __global__ void __launch_bounds__(kTileThreads)
-    k_physics_loop(PhysParams P, uint32_t n, const uint32_t* __restrict__ offs,
-                   const float4* __restrict__ spos, const uint4* __restrict__ svfme,
-                   float4* __restrict__ pos_out, uint4* __restrict__ vfme_out,
-                   uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist,
-                   uint32_t* __restrict__ coarse, uint32_t* __restrict__ err) {
+    k_physics_frame(PhysParams P1, const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
+                    uint32_t n, const uint32_t* __restrict__ offs, const float4* __restrict__ spos,
+                    const uint4* __restrict__ svfme, const float4* __restrict__ pos_in,
+                    const uint4* __restrict__ vfme_in, float4* __restrict__ pos_out, uint4* __restrict__ vfme_out,
+                    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
+                    uint32_t* __restrict__ err) {
     __shared__ __align__(16) float4 s_pos[3][kBandCap];
     __shared__ __align__(16) uint4 s_vfme[3][kBandCap];
     __shared__ __align__(8) uint64_t s_bar;
@@ -384,30 +400,55 @@ __global__ void __launch_bounds__(kTileThreads)
     const uint32_t i = i0 + tid;
     const uint32_t ilast = min(i0 + kTileThreads, n) - 1u;
     const bool valid = i < n;
-    const uint32_t N = P.N;
+
+    // this slot's scene
+    uint32_t sc = 0, base_a = 0, base_c = 0, mode = kModeLoop;
+    PhysParams P = P1;
+    if (kBatched) {
+        const uint32_t first = __ldg(tile_scene + blockIdx.x);
+        sc = scene_of(scenes, first, valid ? i : ilast);
+        P = scenes[sc].P;
+        base_a = scenes[sc].agent_base;
+        base_c = scenes[sc].cell_base;
+        mode = scenes[sc].mode;
+    }
 
     if (tid == 0) mbar_init(&s_bar, 1u);
     if (tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
-        const uint32_t kf = key_of(P, __ldg(spos + i0)), kl = key_of(P, __ldg(spos + ilast));
-        const uint32_t cxf = kf - (kf / N) * N, cxl = kl - (kl / N) * N;
         uint32_t lo = 0, hi = 0;
-        if (tid == 1) {  // own row
-            lo = offs[kf - (cxf > 0u ? 1u : 0u)];
-            hi = offs[kl + (cxl < N - 1u ? 2u : 1u)];
-        } else if (tid == 0) {  // row below, for tile spheres with cz > 0
-            if (kl >= N) {
-                uint32_t f = max(kf, N);
-                uint32_t cf = f - (f / N) * N;
-                lo = offs[f - N - (cf > 0u ? 1u : 0u)];
-                hi = offs[kl - N + (cxl < N - 1u ? 2u : 1u)];
-            }
-        } else {  // row above, for tile spheres with cz < N-1
-            const uint32_t top = N * (N - 1u);
-            if (kf < top) {
-                uint32_t l = min(kl, top - 1u);
-                uint32_t cl = l - (l / N) * N;
-                lo = offs[kf + N - (cxf > 0u ? 1u : 0u)];
-                hi = offs[l + N + (cl < N - 1u ? 2u : 1u)];
+        bool stage = true;
+        PhysParams Q = P;
+        uint32_t qc = base_c;
+        if (kBatched) {  // stage only tiles inside one LOOP scene
+            const uint32_t first = __ldg(tile_scene + blockIdx.x);
+            const uint32_t sf = scene_of(scenes, first, i0), sl = scene_of(scenes, first, ilast);
+            stage = sf == sl && scenes[sf].mode == kModeLoop;
+            Q = scenes[sf].P;
+            qc = scenes[sf].cell_base;
+        }
+        if (stage) {
+            const uint32_t N = Q.N;
+            const uint32_t kf = key_of(Q, __ldg(spos + i0)), kl = key_of(Q, __ldg(spos + ilast));
+            const uint32_t cxf = kf - (kf / N) * N, cxl = kl - (kl / N) * N;
+            const uint32_t* of = offs + qc;
+            if (tid == 1) {  // own row
+                lo = of[kf - (cxf > 0u ? 1u : 0u)];
+                hi = of[kl + (cxl < N - 1u ? 2u : 1u)];
+            } else if (tid == 0) {  // row below, for tile spheres with cz > 0
+                if (kl >= N) {
+                    uint32_t f = max(kf, N);
+                    uint32_t cf = f - (f / N) * N;
+                    lo = of[f - N - (cf > 0u ? 1u : 0u)];
+                    hi = of[kl - N + (cxl < N - 1u ? 2u : 1u)];
+                }
+            } else {  // row above, for tile spheres with cz < N-1
+                const uint32_t top = N * (N - 1u);
+                if (kf < top) {
+                    uint32_t l = min(kl, top - 1u);
+                    uint32_t cl = l - (l / N) * N;
+                    lo = of[kf + N - (cxf > 0u ? 1u : 0u)];
+                    hi = of[l + N + (cl < N - 1u ? 2u : 1u)];
+                }
             }
         }
         hi = min(hi, n);
@@ -416,23 +457,31 @@ __global__ void __launch_bounds__(kTileThreads)
     }
 
     // own sphere and its candidate rows (overlaps the band set-up above)
+    const uint32_t N = P.N;
     Agent a;
+    float4 own_p;
+    uint4 own_q;
     uint32_t cx = 0, cz = 0, key = 0;
     uint32_t lo[3] = {0u, 0u, 0u}, hi[3] = {0u, 0u, 0u};
     if (valid) {
-        a = unpack(__ldg(spos + i), __ldg(svfme + i));
+        own_p = __ldg(spos + i);
+        own_q = __ldg(svfme + i);
+        a = unpack(own_p, own_q);
         cell_of(P, a.position.x, a.position.z, cx, cz);
         key = cz * N + cx;
-        const uint32_t l = cx > 0u ? 1u : 0u, rr = cx < N - 1u ? 2u : 1u;
-        lo[0] = __ldg(offs + key - l);
-        hi[0] = __ldg(offs + key + rr);
-        if (cz > 0u) {
-            lo[1] = __ldg(offs + key - N - l);
-            hi[1] = __ldg(offs + key - N + rr);
-        }
-        if (cz < N - 1u) {
-            lo[2] = __ldg(offs + key + N - l);
-            hi[2] = __ldg(offs + key + N + rr);
+        if (mode == kModeLoop) {
+            const uint32_t l = cx > 0u ? 1u : 0u, rr = cx < N - 1u ? 2u : 1u;
+            const uint32_t* of = offs + base_c;
+            lo[0] = __ldg(of + key - l);
+            hi[0] = __ldg(of + key + rr);
+            if (cz > 0u) {
+                lo[1] = __ldg(of + key - N - l);
+                hi[1] = __ldg(of + key - N + rr);
+            }
+            if (cz < N - 1u) {
+                lo[2] = __ldg(of + key + N - l);
+                hi[2] = __ldg(of + key + N + rr);
+            }
         }
     }
     __syncthreads();
@@ -459,6 +508,23 @@ __global__ void __launch_bounds__(kTileThreads)
         }
     }
     if (!valid) return;
+
+    if (kBatched && mode == kModeInit) {  // INIT (physics.wgsl:91-96): re-pack, emit key
+        pos_out[i] = own_p;
+        vfme_out[i] = pack(a);
+        keys_out[i] = base_c + key;
+        emit_count(hist, coarse, base_c + key);
+        return;
+    }
+    if (kBatched && mode == kModeHold) {
+        // a scene without a pending step keeps its state in its own slot order
+        // (input order, not this frame's sorted copy) and its key, which is
+        // counted again for the next frame's sort
+        pos_out[i] = __ldg(pos_in + i);
+        vfme_out[i] = __ldg(vfme_in + i);
+        emit_count(hist, coarse, keys_out[i] & ~kInitKeyBit);
+        return;
+    }
 
     // candidate rows in the reference's order: own row (band 1), below (0), above (2)
     Row rows[3];
@@ -492,8 +558,10 @@ __global__ void __launch_bounds__(kTileThreads)
     collide_rows(P, a, rows, i, spos, svfme);
     V3 diff = a.position - old_pos;
     if (len3(diff) > a.scale) {
-        // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337)
-        uint32_t v = i * (i ^ (i >> 15));
+        // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337); the
+        // index is the slot inside the sphere's own scene
+        const uint32_t li = i - base_a;
+        uint32_t v = li * (li ^ (li >> 15));
         const float d = 4294967296.0f;
         V3 h = {__uint2float_rn(v * 0x1u) / d, __uint2float_rn(v * 0x1FFu) / d,
                 __uint2float_rn(v * 0x3FFFFu) / d};
@@ -512,7 +580,7 @@ __global__ void __launch_bounds__(kTileThreads)
     vfme_out[i] = pack(a);
     uint32_t nx, nz;
     cell_of(P, a.position.x, a.position.z, nx, nz);
-    const uint32_t nk = nz * N + nx;
+    const uint32_t nk = base_c + nz * N + nx;
     keys_out[i] = nk;
     emit_count(hist, coarse, nk);
 }
@@ -580,8 +648,20 @@ cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t*
                                 uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
                                 cudaStream_t st) {
     if (!n) return cudaSuccess;
-    k_physics_loop<<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
-        p, n, offs, spos, svfme, pos_out, vfme_out, keys_out, hist, coarse, err);
+    k_physics_frame<false><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
+        p, nullptr, nullptr, n, offs, spos, svfme, nullptr, nullptr, pos_out, vfme_out, keys_out, hist, coarse, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
+                                 const uint32_t* offs, const float4* spos, const uint4* svfme, const float4* pos_in,
+                                 const uint4* vfme_in, float4* pos_out, uint4* vfme_out, uint32_t* keys_out,
+                                 uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    PhysParams unused{};
+    k_physics_frame<true><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
+        unused, scenes, tile_scene, n, offs, spos, svfme, pos_in, vfme_in, pos_out, vfme_out, keys_out, hist,
+        coarse, err);
     return cudaGetLastError();
 }
 

@@ -250,6 +250,88 @@ mb_status mb_last_frame_times(mb_world* w, float* stage_ms3);
 /* Kernels one frame launches (graph nodes that are kernels). */
 uint32_t mb_kernels_per_frame(const mb_world* w);
 
+/* ------------------------------------------------------------------------- */
+/* Batching: many independent scenes, one set of launches per frame.         */
+/* No counterpart in the reference (one scene per app).                       */
+/* ------------------------------------------------------------------------- */
+/*
+ * A batch is a pool of scenes sharing device buffers; every frame sorts, builds
+ * cell ranges and runs physics for all of them at once, and each scene evolves
+ * exactly as it would in its own mb_world (same state, keys, order, bit for
+ * bit).  Per frame each scene runs its own mode: LOOP, INIT (its first frame
+ * after mb_batch_set_state) or HOLD (inactive: state kept, nothing advances).
+ *
+ *   mb_batch_create    scenes[0..num_scenes) plus room for later
+ *                      mb_batch_add_scene calls (capacity_* >= the initial sum;
+ *                      0 = just the initial scenes)
+ *   mb_batch_step      k frames for every active scene with a state
+ *   mb_batch_get_debug slot-local keys / perm / start / close of one scene; the
+ *                      pool sorts every frame, so for a scene that was held in
+ *                      the last frame perm / start / close are the ones its next
+ *                      frame will use (its state and keys are unchanged)
+ */
+typedef struct mb_batch mb_batch;
+mb_status mb_batch_create(const mb_settings* scenes, uint32_t num_scenes, uint32_t capacity_agents,
+                          uint32_t capacity_cells, uint32_t capacity_scenes, void* cuda_stream,
+                          mb_batch** out);
+mb_status mb_batch_add_scene(mb_batch* b, const mb_settings* s, uint32_t* scene_index);
+mb_status mb_batch_destroy(mb_batch* b);
+uint32_t mb_batch_num_scenes(const mb_batch* b);
+mb_status mb_batch_memory(const mb_batch* b, uint64_t* device_bytes);
+mb_status mb_batch_set_state(mb_batch* b, uint32_t scene, const float* pos_scale, const uint32_t* vfme,
+                             mb_memory where);
+mb_status mb_batch_get_state(mb_batch* b, uint32_t scene, float* pos_scale, uint32_t* vfme, mb_memory where);
+mb_status mb_batch_set_active(mb_batch* b, uint32_t scene, int active);
+mb_status mb_batch_step(mb_batch* b, uint32_t k);
+mb_status mb_batch_sync(mb_batch* b);
+int64_t mb_batch_time(const mb_batch* b, uint32_t scene);
+mb_status mb_batch_get_debug(mb_batch* b, uint32_t scene, uint32_t* keys, uint32_t* perm, uint32_t* start,
+                             uint32_t* close, mb_memory where);
+
+/* ------------------------------------------------------------------------- */
+/* Serving: a request loop over one batch pool (no counterpart in the         */
+/* reference).                                                                */
+/* ------------------------------------------------------------------------- */
+/*
+ * Requests are submitted from any thread and run by a worker thread:
+ *   create  - admitted in arrival order while the memory budget has room (the
+ *             pool's spheres / cells / scenes are reserved at mb_server_create);
+ *             scenes stay resident, so one that does not fit is rejected
+ *             (MB_ERR_BUDGET_EXCEEDED), and so are later requests on it;
+ *   advance - k more frames for a scene.
+ * Requests that arrive while frames run join at the next frame (continuous
+ * batching); each frame advances every scene that owes a step.  A request is
+ * done when its scene has taken its steps; latency = done - submitted.
+ */
+typedef struct mb_server_config {
+    uint64_t budget_bytes;   /* device memory the pool may take */
+    uint32_t max_scenes;
+    uint32_t max_agents;     /* 0: derived from the budget */
+    uint32_t max_cells;      /* 0: derived from the budget */
+    uint32_t reserved[3];
+} mb_server_config;
+
+typedef struct mb_server_stats {
+    uint64_t requests_done;
+    uint64_t frames;
+    uint64_t agent_steps;    /* sphere-steps taken by LOOP frames */
+    double busy_seconds;     /* wall time with frames on the GPU */
+    uint32_t scenes;
+    uint32_t reserved[3];
+} mb_server_stats;
+
+typedef struct mb_server mb_server;
+mb_status mb_server_create(const mb_server_config* cfg, void* cuda_stream, mb_server** out);
+mb_status mb_server_destroy(mb_server* s);
+mb_status mb_server_submit_create(mb_server* s, const mb_settings* settings, const float* pos_scale,
+                                  const uint32_t* vfme, uint32_t* scene, uint64_t* request);
+mb_status mb_server_submit_advance(mb_server* s, uint32_t scene, uint32_t k, uint64_t* request);
+/* MB_ERR_NOT_READY if the request is not done within timeout_s (it stays queued). */
+mb_status mb_server_wait(mb_server* s, uint64_t request, double timeout_s, double* latency_s);
+/* Waits until the scene owes no step, then copies its state to host memory. */
+mb_status mb_server_get_state(mb_server* s, uint32_t scene, float* pos_scale, uint32_t* vfme);
+mb_status mb_server_get_stats(mb_server* s, mb_server_stats* out);
+
 /* Library version string (build id). */
 const char* mb_version(void);
 
