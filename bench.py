@@ -295,9 +295,9 @@ def run_ours(args, rank, world_size, local_rank):
     achieved = phys_bytes / (phys_ms * 1e-3) / 1e9
     frame_bytes = FRAME_BYTES_PER_AGENT * n + FRAME_BYTES_PER_CELL * cells
     roofline = {
-        "bound": "hbm", "kernel": "k_physics_loop", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+        "bound": "hbm", "kernel": "k_physics_frame", "achieved": achieved, "peak": hbm, "unit": "GB/s",
         "frac": achieved / hbm, "peak_kind": peak_kind,
-        "traffic": ncu_traffic("k_physics_loop", args.workload),
+        "traffic": ncu_traffic("k_physics_frame", args.workload),
         "algorithmic_bytes_per_launch": phys_bytes,
         "frame": {"algorithmic_bytes": frame_bytes,
                   "achieved_gbs": frame_bytes / (total_ms / args.steps * 1e-3) / 1e9,
@@ -332,13 +332,162 @@ def run_ours(args, rank, world_size, local_rank):
     return 0
 
 
+def run_batch(args):
+    """Batching workload: independent scenes (log-uniform sizes) stepped together vs one at a time."""
+    import numpy as np
+    import torch
+
+    from bevy_millions_ball_gb300 import Batch, World, scenes
+
+    torch.cuda.set_device(0)
+    scs = scenes.batch(count=args.batch_scenes, seed=0)
+    total = sum(s.n for s in scs)
+    stream = torch.cuda.current_stream()
+    K = args.steps
+    b = Batch([s.plugin for s in scs], stream=stream.cuda_stream)
+    for i, s in enumerate(scs):
+        b.set_state(i, s.pos_scale, s.vfme)
+    b.step(1 + max(args.warmup, 3))
+    b.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(K)
+    e1.record(stream)
+    b.sync()
+    t_batch = e0.elapsed_time(e1) * 1e-3
+    mem = b.memory()
+    b.close()
+    # the plain loop: each scene in its own world, one after the other
+    worlds = []
+    for s in scs:
+        w = World(s.plugin, stream=stream.cuda_stream)
+        w.set_state(s.pos_scale, s.vfme)
+        w.step(1 + max(args.warmup, 3))
+        worlds.append(w)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for w in worlds:
+        w.step(K)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = e0.elapsed_time(e1) * 1e-3
+    for w in worlds:
+        w.close()
+    sizes = np.array([s.n for s in scs])
+    line = {
+        "metric": "agent-steps/s (batched scenes)", "value": total * K / t_batch, "unit": "agent-steps/s",
+        "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": 1e3 * t_batch / K,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batch: {len(scs)} scenes, n log-uniform [1024, 262144], total {total:,} spheres, "
+                               "N = next_pow2(sqrt n), H in {4,8,16}, e in [0.5,0.95], half spring",
+                   "spheres_total": int(total), "median_scene": int(np.median(sizes)), "pool_bytes": int(mem),
+                   "l2": "pool larger than L2"},
+        "plain_loop": {"value": total * K / t_plain, "ms_per_step": 1e3 * t_plain / K,
+                       "what": "same scenes, each in its own world, stepped one after the other"},
+        "speedup_vs_plain_loop": t_plain / t_batch,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serving(args):
+    """Serving workload: Poisson arrivals of create / advance(k) requests; latency p50/p99."""
+    import math
+    import threading as th
+
+    import numpy as np
+    import torch
+
+    from bevy_millions_ball_gb300 import Server, World, scenes
+
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(1)
+    R, rate = args.serve_requests, args.serve_rate
+    # request stream: the first creates, then 25% creates / 75% advances
+    reqs, n_scenes = [], 0
+    t = 0.0
+    for r in range(R):
+        t += rng.exponential(1.0 / rate)
+        if n_scenes < 4 or rng.random() < 0.25:
+            n = int(round(math.exp(rng.uniform(math.log(4096), math.log(1 << 20)))))
+            grids = scenes.next_pow2(math.isqrt(n - 1) + 1)
+            sc = scenes.plain_uniform(n, grids, half_map_height=int(rng.choice([4, 8, 16])),
+                                      seed=int(rng.integers(0, 2**31)), spring=bool(rng.integers(0, 2)),
+                                      e=float(rng.uniform(0.5, 0.95)))
+            reqs.append(("create", t, sc))
+            n_scenes += 1
+        else:
+            reqs.append(("advance", t, int(rng.integers(0, n_scenes)), int(rng.integers(1, 65))))
+    # batched server
+    srv = Server(budget_bytes=120 << 30, max_scenes=max(64, n_scenes))
+    lat = [None] * R
+    handles = {}
+    ids = [None] * R
+    t0 = time.perf_counter()
+    for i, rq in enumerate(reqs):
+        now = time.perf_counter() - t0
+        if rq[1] > now:
+            time.sleep(rq[1] - now)
+        if rq[0] == "create":
+            handles[len(handles)], ids[i] = srv.create(rq[2].plugin, rq[2].pos_scale, rq[2].vfme)
+        else:
+            ids[i] = srv.advance(handles[rq[2]], rq[3])
+    for i in range(R):
+        lat[i] = srv.wait(ids[i])
+    t_end = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    serve_value = st.agent_steps / t_end
+    # plain loop: the same stream served one request at a time, each scene its own world
+    worlds, plain_lat, clock, steps_done = {}, [], 0.0, 0
+    stream = torch.cuda.current_stream()
+    tp0 = time.perf_counter()
+    for rq in reqs:
+        clock = max(clock, rq[1])
+        s0 = time.perf_counter()
+        if rq[0] == "create":
+            w = World(rq[2].plugin, stream=stream.cuda_stream)
+            w.set_state(rq[2].pos_scale, rq[2].vfme)
+            w.step(1)
+            worlds[len(worlds)] = w
+        else:
+            w = worlds[rq[2]]
+            w.step(rq[3])
+            steps_done += w.n * rq[3]
+        torch.cuda.synchronize()
+        clock += time.perf_counter() - s0
+        plain_lat.append(clock - rq[1])
+    t_plain = clock
+    for w in worlds.values():
+        w.close()
+    line = {
+        "metric": "agent-steps/s (serving)", "value": serve_value, "unit": "agent-steps/s", "n_gpus": 1,
+        "steps": R, "warmup": 0, "ms_per_step": 1e3 * t_end / R, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"serving: {R} Poisson requests at {rate}/s, creates n log-uniform "
+                               "[4096, 1048576], advances k ~ U{1..64}, 120 GB budget",
+                   "scenes": n_scenes},
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "plain_loop": {"value": steps_done / t_plain,
+                       "latency_s": {"p50": float(np.percentile(plain_lat, 50)),
+                                     "p99": float(np.percentile(plain_lat, 99))},
+                       "what": "same request stream served one at a time, each scene in its own world"},
+        "speedup_vs_plain_loop": serve_value / (steps_done / t_plain),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="P-1M", choices=["P-small", "P-1M", "P-4M"])
+    ap.add_argument("--workload", default="P-1M", choices=["P-small", "P-1M", "P-4M", "batch", "serving"])
+    ap.add_argument("--batch-scenes", type=int, default=512)
+    ap.add_argument("--serve-requests", type=int, default=300)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--reference-seconds", type=float, default=120.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -347,10 +496,18 @@ def main():
     args = ap.parse_args()
     rank, world_size, local_rank = env_rank()
     if args.impl == "reference":
+        if args.workload in ("batch", "serving"):
+            print(json.dumps({"impl": "reference", "unavailable": "the reference runs one scene per app; "
+                              "batching/serving have no reference implementation"}))
+            return 0
         return run_reference(args, rank, world_size)
     from __graft_entry__ import build
 
     build()
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "serving":
+        return run_serving(args)
     return run_ours(args, rank, world_size, local_rank)
 
 
