@@ -37,6 +37,17 @@ __global__ void k_fill_keys(uint32_t* keys, uint32_t n, uint32_t value) {
     if (i < n) keys[i] = value;
 }
 
+// after a frame: every scene that ran now holds its state in the other buffer
+__global__ void k_flip_parity(mb::SceneDev* scenes, uint32_t count) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < count && scenes[s].mode != mb::kModeHold) scenes[s].parity ^= 1u;
+}
+
+// cells of a scene are padded to whole scan tiles, so every tile has one scene
+uint32_t padded_cells(uint64_t cells) {
+    return (uint32_t)((cells + mb::kScanTile - 1u) / mb::kScanTile * mb::kScanTile);
+}
+
 // slot-local debug views of one scene
 __global__ void k_local_debug(const uint32_t* keys, const uint32_t* perm, const uint32_t* offs, uint32_t n,
                               uint32_t cells, uint32_t agent_base, uint32_t cell_base, uint32_t* okeys,
@@ -62,6 +73,7 @@ struct SceneHost {
     bool init_pending = false;
     bool active = true;
     bool frame_done = false;
+    uint32_t parity = 0;   // state buffer holding the current state
     int64_t time = -1;
 };
 
@@ -75,14 +87,15 @@ struct mb_batch {
     float4* spos = nullptr;
     uint4* svfme = nullptr;
     uint32_t *keys = nullptr, *perm = nullptr, *offs = nullptr, *ctl = nullptr, *d_tile_scene = nullptr;
+    uint32_t* d_cell_tile_scene = nullptr;  // scene of each 4096-cell scan tile
+    uint32_t* h_cell_tile_scene = nullptr;  // pinned
     mb::SceneDev* d_scenes = nullptr;
     mb::SceneDev* h_scenes = nullptr;     // pinned mirror of the scene table
     uint32_t* h_tile_scene = nullptr;     // pinned
     cudaEvent_t table_ev = nullptr;       // last table upload has been read
     mb::CountScratch cnt;
     std::vector<SceneHost> scenes;
-    uint32_t n_total = 0, cells_total = 0;
-    int cur = 0;
+    uint32_t n_total = 0, cells_total = 0;  // cells_total: padded to whole scan tiles
     bool counts_valid = true;             // hist/coarse match keys
     bool layout_dirty = true;             // scene ranges changed: re-upload tiles, re-capture
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -131,6 +144,8 @@ cudaError_t alloc_pool(mb_batch* b) {
     if ((e = cudaMalloc(&b->ctl, sizeof(uint32_t) * mb::kCtlWords))) return e;
     if ((e = cudaMemset(b->ctl, 0, sizeof(uint32_t) * mb::kCtlWords))) return e;
     if ((e = cudaMalloc(&b->d_tile_scene, sizeof(uint32_t) * (A / kTile + 1u)))) return e;
+    if ((e = cudaMalloc(&b->d_cell_tile_scene, sizeof(uint32_t) * (Cc / mb::kScanTile + 1u)))) return e;
+    if ((e = cudaMallocHost(&b->h_cell_tile_scene, sizeof(uint32_t) * (Cc / mb::kScanTile + 1u)))) return e;
     if ((e = cudaMalloc(&b->d_scenes, sizeof(mb::SceneDev) * std::max<uint32_t>(b->cap_scenes, 1u)))) return e;
     if ((e = cudaMallocHost(&b->h_scenes, sizeof(mb::SceneDev) * std::max<uint32_t>(b->cap_scenes, 1u)))) return e;
     if ((e = cudaMallocHost(&b->h_tile_scene, sizeof(uint32_t) * (A / kTile + 1u)))) return e;
@@ -152,6 +167,8 @@ void free_pool(mb_batch* b) {
     cudaFree(b->offs);
     cudaFree(b->ctl);
     cudaFree(b->d_tile_scene);
+    cudaFree(b->d_cell_tile_scene);
+    if (b->h_cell_tile_scene) cudaFreeHost(b->h_cell_tile_scene);
     cudaFree(b->d_scenes);
     if (b->h_scenes) cudaFreeHost(b->h_scenes);
     if (b->h_tile_scene) cudaFreeHost(b->h_tile_scene);
@@ -165,7 +182,7 @@ mb_status add_scene(mb_batch* b, const mb_settings* s, uint32_t* index) {
     if (!mb::settings_valid(s, why)) return bfail(b, MB_ERR_INVALID_ARG, why);
     const uint64_t cells = (uint64_t)s->number_of_grids_one_dimension * s->number_of_grids_one_dimension;
     if (b->scenes.size() >= b->cap_scenes || (uint64_t)b->n_total + s->max_number_of_agents > b->cap_agents ||
-        (uint64_t)b->cells_total + cells > b->cap_cells)
+        (uint64_t)b->cells_total + padded_cells(cells) > b->cap_cells)
         return bfail(b, MB_ERR_BUDGET_EXCEEDED, "batch capacity exhausted (scenes, spheres or cells)");
     SceneHost h;
     h.s = *s;
@@ -176,7 +193,7 @@ mb_status add_scene(mb_batch* b, const mb_settings* s, uint32_t* index) {
     h.cells = (uint32_t)cells;
     b->scenes.push_back(h);
     b->n_total += h.n;
-    b->cells_total += h.cells;
+    b->cells_total += padded_cells(h.cells);
     b->layout_dirty = true;
     b->counts_valid = false;
     if (index) *index = (uint32_t)(b->scenes.size() - 1u);
@@ -199,6 +216,7 @@ cudaError_t sync_tables(mb_batch* b, const std::vector<uint32_t>& modes) {
         d.agent_end = h.agent_base + h.n;
         d.cell_base = h.cell_base;
         d.mode = modes[i];
+        d.parity = h.parity;
     }
     if ((e = cudaMemcpyAsync(b->d_scenes, b->h_scenes, sizeof(mb::SceneDev) * S, cudaMemcpyHostToDevice,
                              b->stream)))
@@ -213,6 +231,16 @@ cudaError_t sync_tables(mb_batch* b, const std::vector<uint32_t>& modes) {
         if ((e = cudaMemcpyAsync(b->d_tile_scene, b->h_tile_scene, sizeof(uint32_t) * std::max(tiles, 1u),
                                  cudaMemcpyHostToDevice, b->stream)))
             return e;
+        const uint32_t ctiles = b->cells_total / mb::kScanTile;
+        sc = 0;
+        for (uint32_t t = 0; t < ctiles; ++t) {
+            while (sc + 1u < S && t * mb::kScanTile >= b->scenes[sc].cell_base + padded_cells(b->scenes[sc].cells))
+                ++sc;
+            b->h_cell_tile_scene[t] = sc;
+        }
+        if ((e = cudaMemcpyAsync(b->d_cell_tile_scene, b->h_cell_tile_scene, sizeof(uint32_t) * std::max(ctiles, 1u),
+                                 cudaMemcpyHostToDevice, b->stream)))
+            return e;
         drop_graphs(b);
         b->layout_dirty = false;
     }
@@ -220,21 +248,27 @@ cudaError_t sync_tables(mb_batch* b, const std::vector<uint32_t>& modes) {
     return cudaEventRecord(b->table_ev, b->stream);
 }
 
-cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st, int cur) {
+cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st) {
     cudaError_t e;
-    if ((e = mb::count_scan(b->cnt, b->ctl, b->cells_total, b->offs, st))) return e;
-    if ((e = mb::count_scatter(b->cnt, b->keys, b->n_total, b->cells_total, b->offs, b->perm, b->pos[cur],
-                               b->vfme[cur], b->spos, b->svfme, st)))
+    if ((e = mb::count_scan_scenes(b->cnt, b->d_scenes, b->d_cell_tile_scene, b->cells_total, b->offs, st)))
         return e;
-    return mb::launch_physics_batch(b->d_scenes, b->d_tile_scene, b->n_total, b->offs, b->spos, b->svfme,
-                                    b->pos[cur], b->vfme[cur], b->pos[cur ^ 1], b->vfme[cur ^ 1], b->keys,
-                                    b->cnt.hist, b->cnt.coarse, b->ctl + mb::kCtlError, st);
+    if ((e = mb::count_scatter_scenes(b->cnt, b->d_scenes, b->d_tile_scene, b->d_cell_tile_scene, b->keys, b->n_total,
+                                      b->cells_total, b->offs, b->perm, b->pos[0], b->pos[1], b->vfme[0],
+                                      b->vfme[1], b->spos, b->svfme, st)))
+        return e;
+    if ((e = mb::launch_physics_batch(b->d_scenes, b->d_tile_scene, b->n_total, b->offs, b->spos, b->svfme,
+                                      b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->keys, b->cnt.hist,
+                                      b->cnt.coarse, b->ctl + mb::kCtlError, st)))
+        return e;
+    const uint32_t S = (uint32_t)b->scenes.size();
+    k_flip_parity<<<(S + 127u) / 128u, 128, 0, st>>>(b->d_scenes, S);
+    return cudaGetLastError();
 }
 
-cudaError_t build_graph(mb_batch* b, int cur) {
+cudaError_t build_graph(mb_batch* b) {
     cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e) return e;
-    cudaError_t fe = enqueue_frame(b, b->cap_stream, cur);
+    cudaError_t fe = enqueue_frame(b, b->cap_stream);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(b->cap_stream, &g);
     if (fe) {
@@ -242,7 +276,7 @@ cudaError_t build_graph(mb_batch* b, int cur) {
         return fe;
     }
     if (e) return e;
-    e = cudaGraphInstantiate(&b->graph[cur], g, 0);
+    e = cudaGraphInstantiate(&b->graph[0], g, 0);
     cudaGraphDestroy(g);
     return e;
 }
@@ -259,17 +293,17 @@ mb_status run_frame(mb_batch* b, const std::vector<uint32_t>& modes) {
     cudaError_t e;
     if (!b->counts_valid && (e = recount(b))) return bcuda(b, "batch recount", e);
     if ((e = sync_tables(b, modes))) return bcuda(b, "batch tables", e);
-    if (!b->graph[b->cur] && (e = build_graph(b, b->cur))) return bcuda(b, "batch capture", e);
-    if ((e = cudaGraphLaunch(b->graph[b->cur], b->stream))) return bcuda(b, "batch frame", e);
+    if (!b->graph[0] && (e = build_graph(b))) return bcuda(b, "batch capture", e);
+    if ((e = cudaGraphLaunch(b->graph[0], b->stream))) return bcuda(b, "batch frame", e);
     for (size_t i = 0; i < b->scenes.size(); ++i) {
         SceneHost& h = b->scenes[i];
         if (modes[i] != mb::kModeHold) {
             h.time += 1;
             h.frame_done = true;
+            h.parity ^= 1u;  // mirrors k_flip_parity
         }
         if (modes[i] == mb::kModeInit) h.init_pending = false;
     }
-    b->cur ^= 1;
     return MB_OK;
 }
 
@@ -281,9 +315,9 @@ mb_status set_scene_state(mb_batch* b, uint32_t si, const float* pos, const uint
     SceneHost& h = b->scenes[si];
     cudaMemcpyKind kind = where == MB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(b->pos[b->cur] + h.agent_base, pos, sizeof(float4) * h.n, kind, b->stream)))
+    if ((e = cudaMemcpyAsync(b->pos[h.parity] + h.agent_base, pos, sizeof(float4) * h.n, kind, b->stream)))
         return bcuda(b, "batch set_state", e);
-    if ((e = cudaMemcpyAsync(b->vfme[b->cur] + h.agent_base, vfme, sizeof(uint4) * h.n, kind, b->stream)))
+    if ((e = cudaMemcpyAsync(b->vfme[h.parity] + h.agent_base, vfme, sizeof(uint4) * h.n, kind, b->stream)))
         return bcuda(b, "batch set_state", e);
     k_fill_keys<<<(h.n + 255u) / 256u, 256, 0, b->stream>>>(b->keys + h.agent_base, h.n,
                                                              h.cell_base | mb::kInitKeyBit);
@@ -311,10 +345,12 @@ mb_status mb_batch_create(const mb_settings* scenes, uint32_t num_scenes, uint32
     for (uint32_t i = 0; i < num_scenes; ++i) {
         if (!mb::settings_valid(&scenes[i], why)) return bfail(nullptr, MB_ERR_INVALID_ARG, why);
         agents += scenes[i].max_number_of_agents;
-        cells += (uint64_t)scenes[i].number_of_grids_one_dimension * scenes[i].number_of_grids_one_dimension;
+        cells += padded_cells((uint64_t)scenes[i].number_of_grids_one_dimension * scenes[i].number_of_grids_one_dimension);
     }
     agents = std::max<uint64_t>(agents, capacity_agents);
-    cells = std::max<uint64_t>(cells, capacity_cells);
+    // capacity_cells counts N*N cells; each scene may add up to one scan tile of padding
+    const uint64_t scenes_cap = std::max(num_scenes, capacity_scenes);
+    if (capacity_cells) cells = std::max<uint64_t>(cells, capacity_cells + scenes_cap * (mb::kScanTile - 1u));
     if (agents > mb::kMaxAgents || cells > mb::kMaxCells)
         return bfail(nullptr, MB_ERR_INVALID_ARG, "batch exceeds 2^28 spheres or cells");
     mb_batch* b = new (std::nothrow) mb_batch();
@@ -370,9 +406,9 @@ mb_status mb_batch_get_state(mb_batch* b, uint32_t scene, float* pos_scale, uint
     cudaMemcpyKind kind = where == MB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     cudaError_t e;
     if (pos_scale &&
-        (e = cudaMemcpyAsync(pos_scale, b->pos[b->cur] + h.agent_base, sizeof(float4) * h.n, kind, b->stream)))
+        (e = cudaMemcpyAsync(pos_scale, b->pos[h.parity] + h.agent_base, sizeof(float4) * h.n, kind, b->stream)))
         return bcuda(b, "batch get_state", e);
-    if (vfme && (e = cudaMemcpyAsync(vfme, b->vfme[b->cur] + h.agent_base, sizeof(uint4) * h.n, kind, b->stream)))
+    if (vfme && (e = cudaMemcpyAsync(vfme, b->vfme[h.parity] + h.agent_base, sizeof(uint4) * h.n, kind, b->stream)))
         return bcuda(b, "batch get_state", e);
     if (where == MB_HOST && (e = cudaStreamSynchronize(b->stream))) return bcuda(b, "batch get_state", e);
     return MB_OK;

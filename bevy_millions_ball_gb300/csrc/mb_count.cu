@@ -33,9 +33,15 @@ namespace {
 // Tile t of the scan covers cells [4096 t, 4096 t + 4096).  coarse[t] holds the
 // number of spheres in those cells (emitted with the per-cell counts), so a tile
 // finds its base by summing coarse[0..t) - no look-back, no waiting on other tiles.
+//
+// kScenes (a batch): every scene's cell range is padded to whole tiles, so a tile
+// belongs to one scene; its base is that scene's first slot plus the coarse
+// counts of the scene's earlier tiles, and tiles of HOLD scenes are left alone.
+template <bool kScenes>
 __global__ void __launch_bounds__(kScanThreads)
     k_cell_scan(uint32_t* __restrict__ hist, const uint32_t* __restrict__ coarse, uint32_t cells,
-                uint32_t* __restrict__ offs, uint32_t* __restrict__ cursor, uint32_t* big_ctl) {
+                uint32_t* __restrict__ offs, uint32_t* __restrict__ cursor, uint32_t* big_ctl,
+                const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ cell_tile_scene) {
     constexpr int W = kScanThreads / 32;
     __shared__ uint32_t s_warp[W], s_base[W];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -43,9 +49,16 @@ __global__ void __launch_bounds__(kScanThreads)
     if (tile == 0 && tid < 2) big_ctl[tid] = 0u;  // big-cell list of this frame starts empty
     const uint32_t base = tile * kScanTile + tid * kScanItems;
 
-    // exclusive base of this tile: sum of the coarse counts of all earlier tiles
+    uint32_t first_tile = 0, base_slot = 0;
+    if (kScenes) {
+        const uint32_t sc = __ldg(cell_tile_scene + tile);
+        if (__ldg(&scenes[sc].mode) == kModeHold) return;
+        first_tile = __ldg(&scenes[sc].cell_base) / kScanTile;
+        base_slot = __ldg(&scenes[sc].agent_base);
+    }
+    // exclusive base of this tile: sum of the coarse counts of the earlier tiles
     uint32_t bsum = 0;
-    for (uint32_t t = tid; t < tile; t += kScanThreads) bsum += __ldg(coarse + t);
+    for (uint32_t t = first_tile + tid; t < tile; t += kScanThreads) bsum += __ldg(coarse + t);
 
     uint32_t v[kScanItems];
     if (base + kScanItems <= cells) {
@@ -76,7 +89,7 @@ __global__ void __launch_bounds__(kScanThreads)
     if (lane == 31u) s_warp[warp] = incl;
     if (lane == 0u) s_base[warp] = bsum;
     __syncthreads();
-    uint32_t run = incl - sum;
+    uint32_t run = base_slot + incl - sum;
 #pragma unroll
     for (int w = 0; w < W; ++w) {
         if ((uint32_t)w < warp) run += s_warp[w];
@@ -97,7 +110,8 @@ __global__ void __launch_bounds__(kScanThreads)
             c4[q] = x;
             h4[q] = make_uint4(0u, 0u, 0u, 0u);
         }
-        if (base + kScanItems == cells) offs[cells] = run;
+        // end of the tile: the next tile's first offset, or the scene's / table's end
+        if (base + kScanItems == cells || (kScenes && tid == kScanThreads - 1)) offs[base + kScanItems] = run;
     } else {
         for (int q = 0; q < kScanItems; ++q) {
             uint32_t c = base + q;
@@ -148,20 +162,96 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// The same for a batch: slot i's scene (from the tile table) gives the buffer
+// holding its state; spheres of HOLD scenes are left alone.
+__global__ void __launch_bounds__(256)
+    k_cell_scatter_scenes(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
+                          const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ cursor,
+                          uint32_t* __restrict__ perm, const float4* __restrict__ pos0,
+                          const float4* __restrict__ pos1, const uint4* __restrict__ vfme0,
+                          const uint4* __restrict__ vfme1, float4* __restrict__ spos, uint4* __restrict__ svfme) {
+    const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        uint32_t i = i0 + threadIdx.x;
+        bool valid = i < n;
+        uint32_t mode = kModeHold, parity = 0;
+        if (valid) {
+            uint32_t s = __ldg(tile_scene + i / kPhysicsTile);
+            while (i >= __ldg(&scenes[s].agent_end)) ++s;
+            mode = __ldg(&scenes[s].mode);
+            parity = __ldg(&scenes[s].parity);
+        }
+        valid = valid && mode != kModeHold;
+        uint32_t k = valid ? __ldg(keys + i) : 0xFFFFFFFFu;
+        float4 p;
+        uint4 q;
+        if (valid) {
+            p = __ldg((parity ? pos1 : pos0) + i);
+            q = __ldg((parity ? vfme1 : vfme0) + i);
+        }
+        const bool ident = valid && (k & kInitKeyBit);
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k);
+        uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+        uint32_t b = 0;
+        if (valid && !ident && lane == leader) b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
+        b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
+        if (valid) {
+            const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
+            perm[dst] = i;
+            spos[dst] = p;
+            svfme[dst] = q;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- fixup
 // Cells of up to kSmallCell slots are re-sorted by their own thread (insertion
 // sort, after a sortedness check); larger ones go to a list for k_cell_fixup_big.
+// A cell whose order changes re-gathers its sorted state copy from the state
+// source: one buffer (a world), or each scene's current buffer (a batch, where
+// cells and coarse tiles of HOLD scenes are left alone).
 constexpr uint32_t kSmallCell = 32;
 constexpr uint32_t kBlockSortMax = 8192;
 
+struct OneBuffer {
+    const float4* p;
+    const uint4* q;
+    __device__ __forceinline__ bool tile_active(uint32_t) const { return true; }
+    __device__ __forceinline__ float4 pos(uint32_t o) const { return __ldg(p + o); }
+    __device__ __forceinline__ uint4 vfme(uint32_t o) const { return __ldg(q + o); }
+};
+
+struct SceneBuffers {
+    const SceneDev* scenes;
+    const uint32_t* slot_tile_scene;  // scene of slot t * kPhysicsTile
+    const uint32_t* cell_tile_scene;  // scene of scan tile t
+    const float4* p0;
+    const float4* p1;
+    const uint4* q0;
+    const uint4* q1;
+    __device__ __forceinline__ bool tile_active(uint32_t t) const {
+        return __ldg(&scenes[__ldg(cell_tile_scene + t)].mode) != kModeHold;
+    }
+    __device__ __forceinline__ uint32_t parity(uint32_t o) const {
+        uint32_t s = __ldg(slot_tile_scene + o / kPhysicsTile);
+        while (o >= __ldg(&scenes[s].agent_end)) ++s;
+        return __ldg(&scenes[s].parity);
+    }
+    __device__ __forceinline__ float4 pos(uint32_t o) const { return __ldg((parity(o) ? p1 : p0) + o); }
+    __device__ __forceinline__ uint4 vfme(uint32_t o) const { return __ldg((parity(o) ? q1 : q0) + o); }
+};
+
+template <class Src>
 __global__ void __launch_bounds__(256)
     k_cell_fixup(const uint32_t* __restrict__ offs, uint32_t cells, uint32_t* perm, uint32_t* coarse,
-                 uint32_t tiles, uint32_t* big_ctl, uint32_t* big, const float4* __restrict__ pos_in,
-                 const uint4* __restrict__ vfme_in, float4* __restrict__ spos, uint4* __restrict__ svfme) {
+                 uint32_t tiles, uint32_t* big_ctl, uint32_t* big, Src src, float4* __restrict__ spos,
+                 uint4* __restrict__ svfme) {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (blockIdx.x == 0)  // the scan of this frame is over: clear the tile counts for the next one
-        for (uint32_t t = threadIdx.x; t < tiles; t += blockDim.x) coarse[t] = 0u;
-    if (c >= cells) return;
+        for (uint32_t t = threadIdx.x; t < tiles; t += blockDim.x)
+            if (src.tile_active(t)) coarse[t] = 0u;
+    if (c >= cells || !src.tile_active(c / kScanTile)) return;
     const uint32_t lo = offs[c], hi = offs[c + 1u];
     if (hi - lo < 2u) return;
     if (hi - lo > kSmallCell) {
@@ -189,8 +279,8 @@ __global__ void __launch_bounds__(256)
     }
     for (uint32_t j = lo; j < hi; ++j) {  // the sorted state copy follows the new order
         const uint32_t o = perm[j];
-        spos[j] = __ldg(pos_in + o);
-        svfme[j] = __ldg(vfme_in + o);
+        spos[j] = src.pos(o);
+        svfme[j] = src.vfme(o);
     }
 }
 
@@ -210,10 +300,10 @@ __device__ void heap_sift(uint32_t* a, uint32_t root, uint32_t end) {
 // One block per listed cell: bitonic sort in shared memory (up to kBlockSortMax
 // slots), else an O(m log m) heapsort in place by one thread (only degenerate
 // scenes with thousands of spheres in one cell get there).
+template <class Src>
 __global__ void __launch_bounds__(256)
     k_cell_fixup_big(const uint32_t* __restrict__ offs, uint32_t* perm, uint32_t* big_ctl,
-                     const uint32_t* __restrict__ big, const float4* __restrict__ pos_in,
-                     const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
+                     const uint32_t* __restrict__ big, Src src, float4* __restrict__ spos,
                      uint4* __restrict__ svfme) {
     __shared__ uint32_t s_v[kBlockSortMax];
     __shared__ uint32_t s_idx, s_unsorted;
@@ -267,8 +357,8 @@ __global__ void __launch_bounds__(256)
             __syncthreads();
             for (uint32_t j = tid; j < m; j += blockDim.x) {  // sorted state copy follows
                 const uint32_t o = perm[lo + j];
-                spos[lo + j] = __ldg(pos_in + o);
-                svfme[lo + j] = __ldg(vfme_in + o);
+                spos[lo + j] = src.pos(o);
+                svfme[lo + j] = src.vfme(o);
             }
         }
         __syncthreads();
@@ -364,7 +454,8 @@ cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, c
 cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st) {
     (void)ctl;
     uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
-    k_cell_scan<<<tiles, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.big_ctl);
+    k_cell_scan<false><<<tiles, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.big_ctl,
+                                                       nullptr, nullptr);
     return cudaGetLastError();
 }
 
@@ -378,11 +469,42 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
         if ((e = cudaGetLastError())) return e;
     }
     uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
-    k_cell_fixup<<<(cells + 255u) / 256u, 256, 0, st>>>(offs, cells, perm, s.coarse, tiles, s.big_ctl, s.big,
-                                                        pos_in, vfme_in, spos, svfme);
+    OneBuffer src{pos_in, vfme_in};
+    k_cell_fixup<OneBuffer><<<(cells + 255u) / 256u, 256, 0, st>>>(offs, cells, perm, s.coarse, tiles, s.big_ctl,
+                                                                   s.big, src, spos, svfme);
     if ((e = cudaGetLastError())) return e;
-    k_cell_fixup_big<<<(uint32_t)device_sm_count(), 256, 0, st>>>(offs, perm, s.big_ctl, s.big, pos_in,
-                                                                  vfme_in, spos, svfme);
+    k_cell_fixup_big<OneBuffer><<<(uint32_t)device_sm_count(), 256, 0, st>>>(offs, perm, s.big_ctl, s.big, src,
+                                                                             spos, svfme);
+    return cudaGetLastError();
+}
+
+cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
+                              uint32_t cells, uint32_t* offs, cudaStream_t st) {
+    uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
+    k_cell_scan<true><<<tiles, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.big_ctl, scenes,
+                                                      cell_tile_scene);
+    return cudaGetLastError();
+}
+
+cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* tile_scene,
+                                 const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
+                                 const uint32_t* offs, uint32_t* perm, const float4* pos_buf0,
+                                 const float4* pos_buf1, const uint4* vfme_buf0, const uint4* vfme_buf1,
+                                 float4* spos, uint4* svfme, cudaStream_t st) {
+    cudaError_t e;
+    if (n) {
+        uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
+        k_cell_scatter_scenes<<<blocks, 256, 0, st>>>(scenes, tile_scene, keys, n, s.cursor, perm, pos_buf0,
+                                                      pos_buf1, vfme_buf0, vfme_buf1, spos, svfme);
+        if ((e = cudaGetLastError())) return e;
+    }
+    uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
+    SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
+    k_cell_fixup<SceneBuffers><<<(cells + 255u) / 256u, 256, 0, st>>>(offs, cells, perm, s.coarse, tiles,
+                                                                      s.big_ctl, s.big, src, spos, svfme);
+    if ((e = cudaGetLastError())) return e;
+    k_cell_fixup_big<SceneBuffers><<<(uint32_t)device_sm_count(), 256, 0, st>>>(offs, perm, s.big_ctl, s.big,
+                                                                                src, spos, svfme);
     return cudaGetLastError();
 }
 

@@ -108,6 +108,8 @@ struct SceneDev {
     uint32_t agent_base, agent_end;  // sorted slots [agent_base, agent_end)
     uint32_t cell_base;              // cells [cell_base, cell_base + N*N)
     uint32_t mode;                   // kModeHold / kModeInit / kModeLoop
+    uint32_t parity;                 // which state buffer holds the scene's current state
+    uint32_t pad[3];
 };
 constexpr uint32_t kPhysicsTile = 128;  // slots per block of the physics pass
 
@@ -127,11 +129,13 @@ cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uin
                          uint32_t* hist, uint32_t* coarse, cudaStream_t st);
 
 // Batched LOOP/INIT/HOLD pass: tile_scene[t] = scene of slot t*kPhysicsTile.
-// pos_in/vfme_in: the frame's input state in input order (HOLD scenes copy it).
+// Batched physics: scene s reads the sorted copy and writes buffer 1 - parity
+// (pos_buf[2] / vfme_buf[2]); a HOLD scene only re-emits the counts of its keys.
 cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
-                                 const uint32_t* offs, const float4* spos, const uint4* svfme, const float4* pos_in,
-                                 const uint4* vfme_in, float4* pos_out, uint4* vfme_out, uint32_t* keys_out,
+                                 const uint32_t* offs, const float4* spos, const uint4* svfme, float4* pos_buf0,
+                                 float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1, uint32_t* keys,
                                  uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st);
+
 
 // Counting sort of cell keys (mb_count.cu).
 constexpr int kScanThreads = 256;
@@ -166,6 +170,17 @@ cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
                           float4* spos, uint4* svfme, cudaStream_t st);
+// Batched count scan: scene cell ranges are padded to whole scan tiles
+// (cell_tile_scene[t] = scene of tile t); tiles of HOLD scenes are skipped.
+cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
+                              uint32_t cells, uint32_t* offs, cudaStream_t st);
+// Batched scatter + fixup: like count_scatter, reading each scene's state from its
+// parity buffer; spheres and cells of HOLD scenes are left alone.
+cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* tile_scene,
+                                 const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
+                                 const uint32_t* offs, uint32_t* perm, const float4* pos_buf0,
+                                 const float4* pos_buf1, const uint4* vfme_buf0, const uint4* vfme_buf1,
+                                 float4* spos, uint4* svfme, cudaStream_t st);
 // spos/svfme := pos_in/vfme_in gathered through perm (after the onesweep sort).
 cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in, const uint4* vfme_in,
                          float4* spos, uint4* svfme, cudaStream_t st);

@@ -386,10 +386,9 @@ template <bool kBatched>
 __global__ void __launch_bounds__(kTileThreads)
     k_physics_frame(PhysParams P1, const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
                     uint32_t n, const uint32_t* __restrict__ offs, const float4* __restrict__ spos,
-                    const uint4* __restrict__ svfme, const float4* __restrict__ pos_in,
-                    const uint4* __restrict__ vfme_in, float4* __restrict__ pos_out, uint4* __restrict__ vfme_out,
-                    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
-                    uint32_t* __restrict__ err) {
+                    const uint4* __restrict__ svfme, float4* __restrict__ pos_out0, float4* __restrict__ pos_out1,
+                    uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1, uint32_t* __restrict__ keys_out,
+                    uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse, uint32_t* __restrict__ err) {
     __shared__ __align__(16) float4 s_pos[3][kBandCap];
     __shared__ __align__(16) uint4 s_vfme[3][kBandCap];
     __shared__ __align__(8) uint64_t s_bar;
@@ -401,9 +400,11 @@ __global__ void __launch_bounds__(kTileThreads)
     const uint32_t ilast = min(i0 + kTileThreads, n) - 1u;
     const bool valid = i < n;
 
-    // this slot's scene
+    // this slot's scene; its output buffer is the one its current state is not in
     uint32_t sc = 0, base_a = 0, base_c = 0, mode = kModeLoop;
     PhysParams P = P1;
+    float4* __restrict__ pos_out = pos_out0;
+    uint4* __restrict__ vfme_out = vfme_out0;
     if (kBatched) {
         const uint32_t first = __ldg(tile_scene + blockIdx.x);
         sc = scene_of(scenes, first, valid ? i : ilast);
@@ -411,6 +412,10 @@ __global__ void __launch_bounds__(kTileThreads)
         base_a = scenes[sc].agent_base;
         base_c = scenes[sc].cell_base;
         mode = scenes[sc].mode;
+        if (scenes[sc].parity == 0u) {
+            pos_out = pos_out1;
+            vfme_out = vfme_out1;
+        }
     }
 
     if (tid == 0) mbar_init(&s_bar, 1u);
@@ -516,15 +521,7 @@ __global__ void __launch_bounds__(kTileThreads)
         emit_count(hist, coarse, base_c + key);
         return;
     }
-    if (kBatched && mode == kModeHold) {
-        // a scene without a pending step keeps its state in its own slot order
-        // (input order, not this frame's sorted copy) and its key, which is
-        // counted again for the next frame's sort
-        pos_out[i] = __ldg(pos_in + i);
-        vfme_out[i] = __ldg(vfme_in + i);
-        emit_count(hist, coarse, keys_out[i] & ~kInitKeyBit);
-        return;
-    }
+    if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
 
     // candidate rows in the reference's order: own row (band 1), below (0), above (2)
     Row rows[3];
@@ -649,18 +646,18 @@ cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t*
                                 cudaStream_t st) {
     if (!n) return cudaSuccess;
     k_physics_frame<false><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
-        p, nullptr, nullptr, n, offs, spos, svfme, nullptr, nullptr, pos_out, vfme_out, keys_out, hist, coarse, err);
+        p, nullptr, nullptr, n, offs, spos, svfme, pos_out, nullptr, vfme_out, nullptr, keys_out, hist, coarse, err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
-                                 const uint32_t* offs, const float4* spos, const uint4* svfme, const float4* pos_in,
-                                 const uint4* vfme_in, float4* pos_out, uint4* vfme_out, uint32_t* keys_out,
+                                 const uint32_t* offs, const float4* spos, const uint4* svfme, float4* pos_buf0,
+                                 float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1, uint32_t* keys,
                                  uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st) {
     if (!n) return cudaSuccess;
     PhysParams unused{};
     k_physics_frame<true><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
-        unused, scenes, tile_scene, n, offs, spos, svfme, pos_in, vfme_in, pos_out, vfme_out, keys_out, hist,
+        unused, scenes, tile_scene, n, offs, spos, svfme, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, keys, hist,
         coarse, err);
     return cudaGetLastError();
 }

@@ -262,13 +262,12 @@ uint32_t mb_kernels_per_frame(const mb_world* w);
  * after mb_batch_set_state) or HOLD (inactive: state kept, nothing advances).
  *
  *   mb_batch_create    scenes[0..num_scenes) plus room for later
- *                      mb_batch_add_scene calls (capacity_* >= the initial sum;
- *                      0 = just the initial scenes)
+ *                      mb_batch_add_scene calls (capacity_* >= the initial sum,
+ *                      capacity_cells counted as N*N per scene; 0 = just the
+ *                      initial scenes)
  *   mb_batch_step      k frames for every active scene with a state
- *   mb_batch_get_debug slot-local keys / perm / start / close of one scene; the
- *                      pool sorts every frame, so for a scene that was held in
- *                      the last frame perm / start / close are the ones its next
- *                      frame will use (its state and keys are unchanged)
+ *   mb_batch_get_debug slot-local keys / perm / start / close of one scene (as of
+ *                      its last frame; a held scene is not touched at all)
  */
 typedef struct mb_batch mb_batch;
 mb_status mb_batch_create(const mb_settings* scenes, uint32_t num_scenes, uint32_t capacity_agents,
