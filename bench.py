@@ -217,7 +217,6 @@ def run_ours(args, rank, world_size, local_rank):
     cells = p.number_of_grids_one_dimension ** 2
     stream = torch.cuda.current_stream()
     w = World(p, stream=stream.cuda_stream)
-    w.set_profiling(True)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     w.set_state(sc.pos_scale, sc.vfme)
@@ -227,7 +226,6 @@ def run_ours(args, rank, world_size, local_rank):
     w.sync()
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    stage = np.zeros((args.steps, 3))
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -239,7 +237,6 @@ def run_ours(args, rank, world_size, local_rank):
             ev[k][0].record(stream)
             w.step(1)
             ev[k][1].record(stream)
-            stage[k] = w.last_frame_times()  # waits for this frame; stage events are inside the graph
         torch.cuda.synchronize()
     w.sync()
     if dist:
@@ -250,6 +247,23 @@ def run_ours(args, rank, world_size, local_rank):
         t = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
+
+    # stage split (sort / cell offsets / physics kernel durations): event nodes inside
+    # the frame graph cost a few microseconds each, so they run in a second pass of
+    # the same frames right after the timed region, not inside it
+    prof_frames = min(args.steps, 200)
+    stage = np.zeros((prof_frames, 3))
+    prof_ms = 0.0
+    w.set_profiling(True)
+    for k in range(prof_frames):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        w.step(1)
+        b.record(stream)
+        stage[k] = w.last_frame_times()  # waits for this frame
+        prof_ms += a.elapsed_time(b)
+    w.set_profiling(False)
     value = world_size * n * args.steps / (total_ms * 1e-3)
     kernels = w.kernels_per_frame
 
@@ -268,7 +282,6 @@ def run_ours(args, rank, world_size, local_rank):
             w.step(1 + F)
             w._check(lib.mb_get_state(w._h, out_p.data_ptr(), out_q.data_ptr(), 0))
 
-        w.set_profiling(False)
         job()
         reps = max(3, args.e2e_reps)
         torch.cuda.synchronize()
@@ -318,7 +331,10 @@ def run_ours(args, rank, world_size, local_rank):
                    "l2": "flushed before every timed frame (256 MB write, outside the events)",
                    "digit_bits_max": w.tuning.digit_bits_max, "collide_block": w.tuning.collide_block},
         "stages_ms": {"sort": float(stage[:, 0].mean()), "cells": float(stage[:, 1].mean()),
-                      "physics": phys_ms},
+                      "physics": phys_ms, "frames": prof_frames,
+                      "ms_per_step_with_stage_events": prof_ms / prof_frames,
+                      "how": "CUDA events inside the frame graph, on the world's stream, in a second pass of "
+                             f"{prof_frames} frames right after the timed region"},
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,

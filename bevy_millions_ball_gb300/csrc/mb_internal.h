@@ -94,8 +94,6 @@ struct PhysParams {
     float neg_c_over_dt;      // -C_AGENT / T_DELTA
     float neg_1pe_over_dt;    // -(1 + E_ENVIR) / T_DELTA
     uint32_t spring;
-    float filter_margin;      // contact-loop pre-filter margin (0 = exact loop only)
-    float pos_slack;          // rounding slack added per applied contact shift
     uint32_t div_m, div_s1, div_s2;  // exact n / grid_size by multiply-shift
 };
 

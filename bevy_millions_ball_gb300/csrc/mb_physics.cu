@@ -98,13 +98,11 @@ __device__ __forceinline__ void cell_of(const PhysParams& P, float x, float z, u
     cz = min(cz, P.N - 1u);
 }
 
-// solve_sphere_constraint (physics.wgsl:300-331).  Returns the length factor of
-// the position change it applied (0 if none): |dp| <= returned value * |norm|.
-__device__ __forceinline__ float sphere(const PhysParams& P, Agent& a, const Agent& b) {
+// solve_sphere_constraint (physics.wgsl:300-331)
+__device__ __forceinline__ void sphere(const PhysParams& P, Agent& a, const Agent& b) {
     float edge = b.scale + a.scale;
     V3 tpos = a.position - b.position;
     float dist = len3(tpos);
-    float moved = 0.0f;
     if (dist <= edge) {
         V3 norm = normalize3(tpos);
         if (!P.spring) {
@@ -121,7 +119,6 @@ __device__ __forceinline__ float sphere(const PhysParams& P, Agent& a, const Age
             }
             float h = 0.5f * (edge - dist);
             a.position = a.position + h * norm;
-            moved = h;
         } else {
             float makeup = edge - dist;
             V3 kforce = (P.k_agent * makeup) * norm;
@@ -130,11 +127,9 @@ __device__ __forceinline__ float sphere(const PhysParams& P, Agent& a, const Age
             float limit = makeup - P.r_agent * a.scale;
             if (limit > 0.0f) {
                 a.position = a.position + limit * norm;
-                moved = limit;
             }
         }
     }
-    return moved;
 }
 
 // solve_cube_constraint (physics.wgsl:269-298)
@@ -169,18 +164,6 @@ __device__ __forceinline__ void cube(const PhysParams& P, Agent& a) {
             a.force = a.force + a.massv * acc;
         }
     }
-}
-
-// solve_sphere_constraint against a packed neighbour (raw float4 + uint4).  The
-// distance test first rejects pairs whose squared distance exceeds the squared
-// edge by a 0.3% margin: sqrt is monotone and correctly rounded, so such pairs
-// can never pass `length(tpos) <= edge`, and all others take the exact path.
-__device__ __forceinline__ float sphere_raw(const PhysParams& P, Agent& a, float4 bp, uint4 bq) {
-    float edge = bp.w + a.scale;
-    V3 tpos = a.position - V3{bp.x, bp.y, bp.z};
-    float d2 = dot3(tpos, tpos);
-    if (d2 > (edge * edge) * 1.003f) return 0.0f;
-    return sphere(P, a, unpack(bp, bq));
 }
 
 // Counts of the emitted key for the next frame's counting sort: the cell, and the
@@ -256,106 +239,30 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
         : "memory");
 }
 
-// One row of one sphere's candidates: sorted slots [lo, lo + cnt), read from
-// shared memory when the whole range was staged (sp/sq indexed by slot - slo).
-struct Row {
-    uint32_t lo, cnt;
-    const float4* sp;
-    const uint4* sq;
-    uint32_t slo;
-    bool smem;
-};
-
-__device__ __forceinline__ float4 row_pos(const Row& R, uint32_t j, const float4* __restrict__ spos) {
-    return R.smem ? R.sp[j - R.slo] : __ldg(spos + j);
-}
-__device__ __forceinline__ uint4 row_vfme(const Row& R, uint32_t j, const uint4* __restrict__ svfme) {
-    return R.smem ? R.sq[j - R.slo] : __ldg(svfme + j);
-}
-
-// Phase-1 classification of one row (see collide_rows): bit q of the result is
-// set when candidate lo+q (q < 32) lies within edge + margin of p0.
-template <bool kOwnRow>
-__device__ __forceinline__ uint32_t classify_row(const Row& R, const V3& p0, float scale_m, uint32_t self,
-                                                 const float4* __restrict__ spos) {
-    const uint32_t lim = min(R.cnt, 32u);
-    const float4* src = R.smem ? R.sp + (R.lo - R.slo) : spos + R.lo;
-    uint32_t m = 0;
-    for (uint32_t q = 0; q < lim; ++q) {
-        if (kOwnRow && R.lo + q == self) continue;
-        const float4 bp = src[q];
-        const float em = bp.w + scale_m;
-        const float dx = p0.x - bp.x, dy = p0.y - bp.y, dz = p0.z - bp.z;
-        const float d2 = (dx * dx + dy * dy) + dz * dz;
-        if (!(d2 > (em * em) * 1.0001f)) m |= 1u << q;
+// handle_collisions' contact loop (physics.wgsl:122-160): the candidates of the
+// three rows in the reference's order (own row without the sphere itself, row
+// below, row above) as one flat sequence t in [0, T), so that a warp runs
+// max(T) iterations rather than the sum of per-row maxima.  Row r holds t in
+// [start_r, start_r + c_r) and candidate t sits at base[t + o_r] (o_r folds in
+// the row's first slot, its band and start_r; unsigned wrap-around is intended).
+// A squared-distance test rejects pairs that cannot touch before the exact
+// solve: sqrt is monotone and correctly rounded, so a pair whose squared
+// distance exceeds edge^2 by 0.3% can never pass `length(tpos) <= edge` (the
+// fused d2 differs from the unfused one by a few ulps, far inside the margin).
+template <bool kShared>
+__device__ __forceinline__ void contact_loop(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
+                                             const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
+                                             uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself) {
+    for (uint32_t t = 0; t < T; ++t) {
+        if (t == tself) continue;
+        const uint32_t j = t + (t < c0 ? o[0] : (t < c01 ? o[1] : o[2]));
+        const float4 bp = kShared ? bpos[j] : __ldg(bpos + j);
+        const float edge = bp.w + a.scale;
+        const float dx = a.position.x - bp.x, dy = a.position.y - bp.y, dz = a.position.z - bp.z;
+        const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+        if (d2 > (edge * edge) * 1.003f) continue;
+        sphere(P, a, unpack(bp, kShared ? bvfme[j] : __ldg(bvfme + j)));
     }
-    return m;
-}
-
-// Phase 2 of one row: near candidates in order while the displacement bound
-// holds, then the exact loop from wherever the bound broke (or from q = 32).
-template <bool kOwnRow>
-__device__ __forceinline__ void contact_row(const PhysParams& P, Agent& a, const Row& R, uint32_t near,
-                                            bool& exact, float& disp, float limit, uint32_t self,
-                                            const float4* __restrict__ spos, const uint4* __restrict__ svfme) {
-    uint32_t q0 = 0;
-    if (!exact) {
-        q0 = min(R.cnt, 32u);
-        while (near) {
-            const uint32_t q = (uint32_t)(__ffs(near) - 1);
-            near &= near - 1u;
-            const uint32_t j = R.lo + q;
-            float mv = sphere_raw(P, a, row_pos(R, j, spos), row_vfme(R, j, svfme));
-            if (mv != 0.0f) {
-                disp = disp + (mv * 1.001f + P.pos_slack);
-                if (!(disp <= limit)) {  // moved too far: later skips would not be safe
-                    exact = true;
-                    q0 = q + 1u;
-                    break;
-                }
-            }
-        }
-    }
-    for (uint32_t q = q0; q < R.cnt; ++q) {
-        const uint32_t j = R.lo + q;
-        if (kOwnRow && j == self) continue;
-        float mv = sphere_raw(P, a, row_pos(R, j, spos), row_vfme(R, j, svfme));
-        // shifts applied here count too: later rows still skip by the bound
-        if (mv != 0.0f && !exact) {
-            disp = disp + (mv * 1.001f + P.pos_slack);
-            if (!(disp <= limit)) exact = true;
-        }
-    }
-}
-
-// handle_collisions' contact loop (physics.wgsl:122-160) over the rows in the
-// reference's order (own row without itself, row below, row above), in two
-// phases that give exactly the result of the plain sequential loop:
-//  1. the first 32 candidates of each row are classified against the position
-//     p0 at loop entry: "near" if within edge + margin (squared test, slack);
-//  2. contacts run in candidate order over the near ones only while a bound on
-//     |p - p0| (sum of applied shifts plus rounding slack) stays below the
-//     margin minus 0.02: every skipped candidate is then farther than edge from
-//     p and would have been a no-op.  Once the bound is exceeded, and beyond the
-//     32nd candidate of a row, candidates run through the exact loop.
-__device__ __forceinline__ void collide_rows(const PhysParams& P, Agent& a, const Row (&rows)[3],
-                                             uint32_t self, const float4* __restrict__ spos,
-                                             const uint4* __restrict__ svfme) {
-    // the rounding slack assumes |coordinate| <= 8192 (ulp <= 2^-10)
-    bool exact = !(P.filter_margin > 0.0f && fabsf(a.position.x) <= 8192.0f &&
-                   fabsf(a.position.y) <= 8192.0f && fabsf(a.position.z) <= 8192.0f);
-    uint32_t n0 = 0, n1 = 0, n2 = 0;
-    if (!exact) {
-        const float scale_m = a.scale + P.filter_margin;
-        n0 = classify_row<true>(rows[0], a.position, scale_m, self, spos);
-        n1 = classify_row<false>(rows[1], a.position, scale_m, self, spos);
-        n2 = classify_row<false>(rows[2], a.position, scale_m, self, spos);
-    }
-    float disp = 0.0f;
-    const float limit = P.filter_margin - 0.02f;
-    contact_row<true>(P, a, rows[0], n0, exact, disp, limit, self, spos, svfme);
-    contact_row<false>(P, a, rows[1], n1, exact, disp, limit, self, spos, svfme);
-    contact_row<false>(P, a, rows[2], n2, exact, disp, limit, self, spos, svfme);
 }
 
 // Key of a position (physics.wgsl:115-117).
@@ -524,23 +431,25 @@ __global__ void __launch_bounds__(kTileThreads)
     if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
 
     // candidate rows in the reference's order: own row (band 1), below (0), above (2)
-    Row rows[3];
+    uint32_t c[3], o_s[3], o_g[3];
+    bool shared = true;
     {
-        const int band[3] = {1, 0, 2};
+        const uint32_t band[3] = {1u, 0u, 2u};
+        uint32_t start = 0;
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-            const int b = band[r];
+            const uint32_t b = band[r];
             const uint32_t h = min(hi[r], n);
-            rows[r].lo = lo[r];
-            rows[r].cnt = h > lo[r] ? h - lo[r] : 0u;
-            rows[r].sp = s_pos[b];
-            rows[r].sq = s_vfme[b];
-            rows[r].slo = s_lo[b];
-            rows[r].smem = lo[r] >= s_lo[b] && h <= s_lo[b] + s_cnt[b];
+            c[r] = h > lo[r] ? h - lo[r] : 0u;
+            if (r == 0 && !(i >= lo[0] && i < lo[0] + c[0])) c[0] = 0u;  // inconsistent input: drop
+            shared = shared && (c[r] == 0u || (lo[r] >= s_lo[b] && h <= s_lo[b] + s_cnt[b]));
+            o_s[r] = b * kBandCap + lo[r] - s_lo[b] - start;
+            o_g[r] = lo[r] - start;
+            start += c[r];
         }
-        // own cell holds i; a range that does not (inconsistent input) is dropped
-        if (!(i >= rows[0].lo && i < rows[0].lo + rows[0].cnt)) rows[0].cnt = 0;
     }
+    const uint32_t c01 = c[0] + c[1], T = c01 + c[2];
+    const uint32_t tself = c[0] ? i - lo[0] : 0xFFFFFFFFu;
 
     // verlet_integration (physics.wgsl:262-266)
     {
@@ -552,7 +461,10 @@ __global__ void __launch_bounds__(kTileThreads)
 
     // handle_collisions (physics.wgsl:119-169)
     V3 old_pos = a.position;
-    collide_rows(P, a, rows, i, spos, svfme);
+    if (shared)
+        contact_loop<true>(P, a, &s_pos[0][0], &s_vfme[0][0], o_s, c[0], c01, T, tself);
+    else
+        contact_loop<false>(P, a, spos, svfme, o_g, c[0], c01, T, tself);
     V3 diff = a.position - old_pos;
     if (len3(diff) > a.scale) {
         // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337); the
@@ -617,16 +529,12 @@ PhysParams make_params(const mb_consts& c) {
     p.neg_c_over_dt = nc / c.time_delta;
     p.neg_1pe_over_dt = n1pe / c.time_delta;
     p.spring = c.enable_spring;
-    // contact-loop filter margin (collide_all): disabled on maps so large that
-    // f32 rounding of positions approaches the margin
-    p.filter_margin = c.half_map_size <= 4096.0f ? 0.25f : 0.0f;
     // magic numbers of n / grid_size (Hacker's Delight 10-8, 33-bit multiplier)
     uint32_t d = c.grid_size ? c.grid_size : 1u, lg = 0;
     while (lg < 32u && (1ull << lg) < d) ++lg;
     p.div_m = (uint32_t)(((1ull << 32) * ((1ull << lg) - d)) / d + 1ull);
     p.div_s1 = lg > 0u ? 1u : 0u;
     p.div_s2 = lg > 0u ? lg - 1u : 0u;
-    p.pos_slack = 1e-3f;
     return p;
 }
 
