@@ -60,6 +60,7 @@ struct mb_world {
     uint4* svfme = nullptr;
     uint32_t* keys = nullptr;          // unsorted keys emitted by the last physics pass
     uint32_t* sorted_keys = nullptr;
+    uint4* bands = nullptr;            // band table of the sorted order (written by the sort)
     uint32_t* perm = nullptr;
     mb::SortScratch scratch;      // onesweep sort scratch + the cell offsets (offs)
     mb::CountScratch cnt;         // counting-sort scratch (per-cell counts, cursors)
@@ -156,7 +157,7 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         if ((e = mb::count_scan(w->cnt, w->scratch.ctl, w->cells, w->scratch.offs, st))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
         if ((e = mb::count_scatter(w->cnt, w->keys, w->n, w->cells, w->scratch.offs, w->perm, w->pos[cur],
-                                   w->vfme[cur], w->spos, w->svfme, st)))
+                                   w->vfme[cur], w->spos, w->svfme, w->bands, w->P.N, st)))
             return e;
         hist = w->cnt.hist;
         coarse = w->cnt.coarse;
@@ -164,7 +165,8 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         if ((e = mb::sort_pairs(w->scratch, w->sched, w->keys, nullptr, w->sorted_keys, w->perm, st))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
         if ((e = mb::cell_offsets(w->scratch, w->sched, w->sorted_keys, st))) return e;
-        if (!init && (e = mb::gather_state(w->perm, w->n, w->pos[cur], w->vfme[cur], w->spos, w->svfme, st)))
+        if (!init && (e = mb::gather_state(w->perm, w->n, w->pos[cur], w->vfme[cur], w->spos, w->svfme,
+                                           w->sorted_keys, w->scratch.offs, w->bands, w->P.N, st)))
             return e;
     }
     if ((e = mark(w, 2, st, capturing))) return e;
@@ -173,7 +175,7 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         e = mb::launch_physics_init(w->P, w->n, w->perm, w->pos[cur], w->vfme[cur], w->pos[nxt],
                                     w->vfme[nxt], w->keys, hist, coarse, st);
     else
-        e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->spos, w->svfme, w->pos[nxt], w->vfme[nxt],
+        e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->spos, w->svfme, w->pos[nxt], w->vfme[nxt],
                                     w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError, st);
     if (e) return e;
     return mark(w, 3, st, capturing);
@@ -282,6 +284,7 @@ mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out) {
         if ((e = cudaMalloc(&w->svfme, sizeof(uint4) * n))) return e;
         if ((e = cudaMalloc(&w->keys, sizeof(uint32_t) * n))) return e;
         if ((e = cudaMalloc(&w->sorted_keys, sizeof(uint32_t) * n))) return e;
+        if ((e = cudaMalloc(&w->bands, sizeof(uint4) * mb::band_table_entries(n)))) return e;
         if ((e = cudaMalloc(&w->perm, sizeof(uint32_t) * n))) return e;
         if ((e = mb::scratch_alloc(w->scratch, w->n, w->cells))) return e;
         return mb::count_scratch_alloc(w->cnt, w->cells);
@@ -308,6 +311,7 @@ mb_status mb_destroy(mb_world* w) {
     cudaFree(w->svfme);
     cudaFree(w->keys);
     cudaFree(w->sorted_keys);
+    cudaFree(w->bands);
     cudaFree(w->perm);
     mb::scratch_free(w->scratch);
     mb::count_scratch_free(w->cnt);

@@ -127,12 +127,16 @@ __global__ void __launch_bounds__(kScanThreads)
 }
 
 // ---------------------------------------------------------------- scatter
-// Also moves each sphere's state to its slot (sorted copy for the physics pass).
+// Also moves each sphere's state to its slot (sorted copy for the physics pass)
+// and, where a slot begins or ends a physics tile, writes that side of the
+// tile's band table entry (the cell of a slot is final here; the fixup only
+// reorders slots inside a cell).
 __global__ void __launch_bounds__(256)
     k_cell_scatter(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ cursor,
                    uint32_t* __restrict__ perm, const float4* __restrict__ pos_in,
                    const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
-                   uint4* __restrict__ svfme) {
+                   uint4* __restrict__ svfme, const uint32_t* __restrict__ offs, uint4* __restrict__ bands,
+                   uint32_t N) {
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
@@ -158,6 +162,7 @@ __global__ void __launch_bounds__(256)
             perm[dst] = i;
             spos[dst] = p;
             svfme[dst] = q;
+            if (bands && !ident) write_band_bounds(bands, offs, N, n, dst, k);
         }
     }
 }
@@ -461,11 +466,12 @@ cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t*
 
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
-                          float4* spos, uint4* svfme, cudaStream_t st) {
+                          float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st) {
     cudaError_t e;
     if (n) {
         uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
-        k_cell_scatter<<<blocks, 256, 0, st>>>(keys, n, s.cursor, perm, pos_in, vfme_in, spos, svfme);
+        k_cell_scatter<<<blocks, 256, 0, st>>>(keys, n, s.cursor, perm, pos_in, vfme_in, spos, svfme, offs, bands,
+                                               N);
         if ((e = cudaGetLastError())) return e;
     }
     uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;

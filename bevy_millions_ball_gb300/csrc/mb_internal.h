@@ -111,6 +111,38 @@ struct SceneDev {
 };
 constexpr uint32_t kPhysicsTile = 128;  // slots per block of the physics pass
 
+// Band table of the physics pass: for physics tile t (sorted slots
+// [t*kPhysicsTile, t*kPhysicsTile + kPhysicsTile)), bands[2t] = lower and
+// bands[2t+1] = upper slot bounds of its three candidate bands (x: row below,
+// y: own row, z: row above), each covering the tile's cells one column to either
+// side.  The sort writes it while it places the slots: the thread that places
+// a tile's first slot writes the lower bounds (from that slot's cell kf), the
+// one that places its last slot the upper bounds (from its cell kl).  A band
+// whose upper bound is not above its lower bound is empty.
+inline uint32_t band_table_entries(uint32_t n) { return 2u * ((n + kPhysicsTile - 1u) / kPhysicsTile); }
+#ifdef __CUDACC__
+__device__ __forceinline__ void write_band_bounds(uint4* __restrict__ bands, const uint32_t* __restrict__ offs,
+                                                  uint32_t N, uint32_t n, uint32_t slot, uint32_t key) {
+    const uint32_t r = slot % kPhysicsTile;
+    const bool first = r == 0u, last = r == kPhysicsTile - 1u || slot + 1u == n;
+    if (!first && !last) return;
+    const uint32_t t = slot / kPhysicsTile;
+    const uint32_t cx = key % N, top = N * (N - 1u);
+    if (first) {
+        const uint32_t l = cx > 0u ? 1u : 0u;
+        const uint32_t f = max(key, N), lf = f % N > 0u ? 1u : 0u;  // row below: from column cx-1 of row cz-1
+        bands[2u * t] = make_uint4(__ldg(offs + f - N - lf), __ldg(offs + key - l),
+                                   key < top ? __ldg(offs + key + N - l) : n, 0u);
+    }
+    if (last) {
+        const uint32_t rr = cx < N - 1u ? 2u : 1u;
+        const uint32_t a = min(key, top - 1u), ra = a % N < N - 1u ? 2u : 1u;  // row above: to column cx+1
+        bands[2u * t + 1u] = make_uint4(key >= N ? __ldg(offs + key - N + rr) : 0u, __ldg(offs + key + rr),
+                                        top ? __ldg(offs + a + N + ra) : 0u, 0u);
+    }
+}
+#endif
+
 // Physics passes.  `hist` / `coarse` (nullable together) accumulate the per-cell
 // and per-4096-cell-tile counts of the keys they emit, for the next frame's
 // counting sort.
@@ -119,7 +151,8 @@ cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t*
                                 uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse,
                                 cudaStream_t st);
 // LOOP pass over the state in sorted order (spos/svfme, slot j = sorted slot j).
-cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs,
+// `bands` is the band table the sort wrote for this order.
+cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                 const float4* spos, const uint4* svfme, float4* pos_out, uint4* vfme_out,
                                 uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
                                 cudaStream_t st);
@@ -164,10 +197,11 @@ cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t*
 cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32_t* offs, uint32_t* perm,
                              cudaStream_t st);
 // perm := stable permutation sorting keys by cell, from the cursors of count_scan;
-// spos/svfme := the state in that order (spos[j] = pos_in[perm[j]]).
+// spos/svfme := the state in that order (spos[j] = pos_in[perm[j]]); bands
+// (nullable) := the band table of that order for an N x N grid.
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
-                          float4* spos, uint4* svfme, cudaStream_t st);
+                          float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st);
 // Batched count scan: scene cell ranges are padded to whole scan tiles
 // (cell_tile_scene[t] = scene of tile t); tiles of HOLD scenes are skipped.
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
@@ -179,9 +213,11 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
                                  const uint32_t* offs, uint32_t* perm, const float4* pos_buf0,
                                  const float4* pos_buf1, const uint4* vfme_buf0, const uint4* vfme_buf1,
                                  float4* spos, uint4* svfme, cudaStream_t st);
-// spos/svfme := pos_in/vfme_in gathered through perm (after the onesweep sort).
+// spos/svfme := pos_in/vfme_in gathered through perm (after the onesweep sort);
+// bands (nullable) := the band table of the sorted keys for an N x N grid.
 cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in, const uint4* vfme_in,
-                         float4* spos, uint4* svfme, cudaStream_t st);
+                         float4* spos, uint4* svfme, const uint32_t* sorted_keys, const uint32_t* offs,
+                         uint4* bands, uint32_t N, cudaStream_t st);
 
 int device_sm_count();
 

@@ -211,9 +211,14 @@ constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier wait (error flag 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
+// The barrier is initialised through the generic proxy and completed by bulk
+// copies through the async proxy: the proxy fence, and a CTA barrier before the
+// first copy is issued, order the two (a copy issued straight after the init by
+// the initialising thread is not ordered with it).
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
@@ -292,7 +297,8 @@ __device__ __forceinline__ uint32_t scene_of(const SceneDev* __restrict__ scenes
 template <bool kBatched>
 __global__ void __launch_bounds__(kTileThreads)
     k_physics_frame(PhysParams P1, const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
-                    uint32_t n, const uint32_t* __restrict__ offs, const float4* __restrict__ spos,
+                    uint32_t n, const uint32_t* __restrict__ offs, const uint4* __restrict__ bands,
+                    const float4* __restrict__ spos,
                     const uint4* __restrict__ svfme, float4* __restrict__ pos_out0, float4* __restrict__ pos_out1,
                     uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1, uint32_t* __restrict__ keys_out,
                     uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse, uint32_t* __restrict__ err) {
@@ -326,7 +332,19 @@ __global__ void __launch_bounds__(kTileThreads)
     }
 
     if (tid == 0) mbar_init(&s_bar, 1u);
-    if (tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
+    const bool table = !kBatched && bands != nullptr;
+    if (table) {  // bounds from the band table: one load
+        if (tid == 0) {
+            const uint4 l = __ldg(bands + 2u * blockIdx.x), h = __ldg(bands + 2u * blockIdx.x + 1u);
+            const uint32_t lo3[3] = {l.x, l.y, l.z}, hi3[3] = {h.x, h.y, h.z};
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                const uint32_t hb = min(hi3[b], n);
+                s_lo[b] = lo3[b];
+                s_cnt[b] = (hb > lo3[b] && hb - lo3[b] <= kBandCap) ? hb - lo3[b] : 0u;
+            }
+        }
+    } else if (tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
         uint32_t lo = 0, hi = 0;
         bool stage = true;
         PhysParams Q = P;
@@ -368,16 +386,35 @@ __global__ void __launch_bounds__(kTileThreads)
         s_cnt[tid] = (hi > lo && hi - lo <= kBandCap) ? hi - lo : 0u;
     }
 
-    // own sphere and its candidate rows (overlaps the band set-up above)
-    const uint32_t N = P.N;
-    Agent a;
-    float4 own_p;
-    uint4 own_q;
-    uint32_t cx = 0, cz = 0, key = 0;
-    uint32_t lo[3] = {0u, 0u, 0u}, hi[3] = {0u, 0u, 0u};
+    // own sphere: loads issued here overlap the band set-up; the copies start
+    // after the barrier (mbarrier initialised and bounds published by then)
+    float4 own_p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint4 own_q = make_uint4(0u, 0u, 0u, 0u);
     if (valid) {
         own_p = __ldg(spos + i);
         own_q = __ldg(svfme + i);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t bytes = 0;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) bytes += s_cnt[b] * 32u;
+        mbar_arrive_expect_tx(&s_bar, bytes);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            if (s_cnt[b]) {
+                bulk_g2s(s_pos[b], spos + s_lo[b], s_cnt[b] * 16u, &s_bar);
+                bulk_g2s(s_vfme[b], svfme + s_lo[b], s_cnt[b] * 16u, &s_bar);
+            }
+        }
+    }
+
+    // candidate rows of the own sphere (overlaps the copies)
+    const uint32_t N = P.N;
+    Agent a;
+    uint32_t cx = 0, cz = 0, key = 0;
+    uint32_t lo[3] = {0u, 0u, 0u}, hi[3] = {0u, 0u, 0u};
+    if (valid) {
         a = unpack(own_p, own_q);
         cell_of(P, a.position.x, a.position.z, cx, cz);
         key = cz * N + cx;
@@ -393,20 +430,6 @@ __global__ void __launch_bounds__(kTileThreads)
             if (cz < N - 1u) {
                 lo[2] = __ldg(of + key + N - l);
                 hi[2] = __ldg(of + key + N + rr);
-            }
-        }
-    }
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t bytes = 0;
-#pragma unroll
-        for (int b = 0; b < 3; ++b) bytes += s_cnt[b] * 32u;
-        mbar_arrive_expect_tx(&s_bar, bytes);
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            if (s_cnt[b]) {
-                bulk_g2s(s_pos[b], spos + s_lo[b], s_cnt[b] * 16u, &s_bar);
-                bulk_g2s(s_vfme[b], svfme + s_lo[b], s_cnt[b] * 16u, &s_bar);
             }
         }
     }
@@ -548,13 +571,14 @@ cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t*
     return cudaGetLastError();
 }
 
-cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs,
+cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                 const float4* spos, const uint4* svfme, float4* pos_out, uint4* vfme_out,
                                 uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
                                 cudaStream_t st) {
     if (!n) return cudaSuccess;
     k_physics_frame<false><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
-        p, nullptr, nullptr, n, offs, spos, svfme, pos_out, nullptr, vfme_out, nullptr, keys_out, hist, coarse, err);
+        p, nullptr, nullptr, n, offs, bands, spos, svfme, pos_out, nullptr, vfme_out, nullptr, keys_out, hist, coarse,
+        err);
     return cudaGetLastError();
 }
 
@@ -565,7 +589,7 @@ cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_sc
     if (!n) return cudaSuccess;
     PhysParams unused{};
     k_physics_frame<true><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
-        unused, scenes, tile_scene, n, offs, spos, svfme, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, keys, hist,
+        unused, scenes, tile_scene, n, offs, nullptr, spos, svfme, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, keys, hist,
         coarse, err);
     return cudaGetLastError();
 }

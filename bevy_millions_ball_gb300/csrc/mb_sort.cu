@@ -351,12 +351,15 @@ __global__ void k_offs_to_start_close(const uint32_t* __restrict__ offs, uint32_
 
 __global__ void __launch_bounds__(256)
     k_gather_state(const uint32_t* __restrict__ perm, uint32_t n, const float4* __restrict__ pos_in,
-                   const uint4* __restrict__ vfme_in, float4* __restrict__ spos, uint4* __restrict__ svfme) {
+                   const uint4* __restrict__ vfme_in, float4* __restrict__ spos, uint4* __restrict__ svfme,
+                   const uint32_t* __restrict__ sorted_keys, const uint32_t* __restrict__ offs,
+                   uint4* __restrict__ bands, uint32_t N) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t o = min(__ldg(perm + i), n - 1u);
     spos[i] = __ldg(pos_in + o);
     svfme[i] = __ldg(vfme_in + o);
+    if (bands) write_band_bounds(bands, offs, N, n, i, __ldg(sorted_keys + i));
 }
 
 size_t onesweep_smem(uint32_t R) {
@@ -509,9 +512,11 @@ cudaError_t sort_and_offsets(SortScratch& s, const SortSchedule& sch, const uint
 }
 
 cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in, const uint4* vfme_in,
-                         float4* spos, uint4* svfme, cudaStream_t st) {
+                         float4* spos, uint4* svfme, const uint32_t* sorted_keys, const uint32_t* offs,
+                         uint4* bands, uint32_t N, cudaStream_t st) {
     if (!n) return cudaSuccess;
-    k_gather_state<<<(n + 255u) / 256u, 256, 0, st>>>(perm, n, pos_in, vfme_in, spos, svfme);
+    k_gather_state<<<(n + 255u) / 256u, 256, 0, st>>>(perm, n, pos_in, vfme_in, spos, svfme, sorted_keys, offs,
+                                                      bands, N);
     return cudaGetLastError();
 }
 
