@@ -287,7 +287,7 @@ mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out) {
         if ((e = cudaMalloc(&w->bands, sizeof(uint4) * mb::band_table_entries(n)))) return e;
         if ((e = cudaMalloc(&w->perm, sizeof(uint32_t) * n))) return e;
         if ((e = mb::scratch_alloc(w->scratch, w->n, w->cells))) return e;
-        return mb::count_scratch_alloc(w->cnt, w->cells);
+        return mb::count_scratch_alloc(w->cnt, w->cells, w->n);
     };
     cudaError_t e = alloc_all();
     if (e) {
@@ -338,7 +338,7 @@ mb_status mb_set_settings(mb_world* w, const mb_settings* s) {
         if ((e = cudaMalloc(&offs, sizeof(uint32_t) * ((size_t)new_cells + 1u))))
             return cuda_fail(w, "mb_set_settings", e);
         mb::CountScratch cnt;
-        if ((e = mb::count_scratch_alloc(cnt, new_cells))) {
+        if ((e = mb::count_scratch_alloc(cnt, new_cells, w->n))) {
             cudaFree(offs);
             mb::count_scratch_free(cnt);
             return cuda_fail(w, "mb_set_settings", e);
@@ -596,9 +596,9 @@ mb_status mb_last_frame_times(mb_world* w, float* ms) {
 
 uint32_t mb_kernels_per_frame(const mb_world* w) {
     if (!w) return 0u;
-    // counting: scan + scatter + fixup + big-cell fixup + physics;
+    // counting: scan + scatter + in-cell fixup + physics;
     // onesweep: histogram + one kernel per digit pass + cell offsets + gather + physics
-    return counting(w) ? 5u : (uint32_t)w->sched.passes + 4u;
+    return counting(w) ? 4u : (uint32_t)w->sched.passes + 4u;
 }
 
 const char* mb_version(void) { return "millionsball-gb300 " __DATE__ " sm_103a"; }

@@ -123,9 +123,9 @@ void drop_graphs(mb_batch* b) {
 }
 
 uint64_t bytes_for(uint64_t agents, uint64_t cells, uint64_t scenes) {
-    // state x2, sorted copy, keys, perm; offs, counts, cursors, big list; tables
-    return agents * (32u * 3u + 8u) + cells * 16u + scenes * sizeof(mb::SceneDev) + (agents / kTile + 1u) * 4u +
-           (cells / mb::kScanTile + 2u) * 4u + 64u * 1024u;
+    // state x2, sorted copy, keys, perm; offs; counts, cursors, fixup lists; tables
+    return agents * (32u * 3u + 8u) + cells * 4u + mb::count_scratch_bytes((uint32_t)cells, (uint32_t)agents) +
+           scenes * sizeof(mb::SceneDev) + (agents / kTile + 1u) * 4u + 64u * 1024u;
 }
 
 cudaError_t alloc_pool(mb_batch* b) {
@@ -151,7 +151,7 @@ cudaError_t alloc_pool(mb_batch* b) {
     if ((e = cudaMallocHost(&b->h_tile_scene, sizeof(uint32_t) * (A / kTile + 1u)))) return e;
     if ((e = cudaEventCreateWithFlags(&b->table_ev, cudaEventDisableTiming))) return e;
     if ((e = cudaMemset(b->keys, 0, sizeof(uint32_t) * A))) return e;
-    return mb::count_scratch_alloc(b->cnt, (uint32_t)Cc);
+    return mb::count_scratch_alloc(b->cnt, (uint32_t)Cc, (uint32_t)A);
 }
 
 void free_pool(mb_batch* b) {

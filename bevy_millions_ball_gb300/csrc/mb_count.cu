@@ -13,10 +13,11 @@
 //      with the per-cell ones, so tiles never wait on each other;
 //   3. k_cell_scatter: each sphere claims a slot of its cell with one atomic per
 //      run of equal keys in its warp (match.any), so spheres of one warp keep
-//      their order, and its 32-byte state is copied to that slot;
-//   4. k_cell_fixup: every cell's slots are put back in ascending input order
-//      (what a stable sort yields; only cells filled by several warps need it),
-//      re-gathering the state copy of the cells it reorders.
+//      their order, and its 32-byte state is copied to that slot; the run that
+//      fills a cell last lists the cell if earlier runs of other warps got there
+//      first (only such cells can be out of order);
+//   4. k_cell_fix: the listed cells' slots are put back in ascending input order
+//      (what a stable sort yields), re-gathering their state copy.
 //
 // The result is bit-identical to a stable sort; offs[] replaces start/close.
 
@@ -40,13 +41,13 @@ namespace {
 template <bool kScenes>
 __global__ void __launch_bounds__(kScanThreads)
     k_cell_scan(uint32_t* __restrict__ hist, const uint32_t* __restrict__ coarse, uint32_t cells,
-                uint32_t* __restrict__ offs, uint32_t* __restrict__ cursor, uint32_t* big_ctl,
+                uint32_t* __restrict__ offs, uint32_t* __restrict__ cursor, uint32_t* fix_ctl,
                 const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ cell_tile_scene) {
     constexpr int W = kScanThreads / 32;
     __shared__ uint32_t s_warp[W], s_base[W];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t tile = blockIdx.x;
-    if (tile == 0 && tid < 2) big_ctl[tid] = 0u;  // big-cell list of this frame starts empty
+    if (tile == 0 && tid < (uint32_t)kFixLists) fix_ctl[tid] = 0u;  // fixup lists of this frame start empty
     const uint32_t base = tile * kScanTile + tid * kScanItems;
 
     uint32_t first_tile = 0, base_slot = 0;
@@ -127,6 +128,40 @@ __global__ void __launch_bounds__(kScanThreads)
 }
 
 // ---------------------------------------------------------------- scatter
+// Fixup lists, filled with one global atomic per list per block iteration.
+struct FixLists {
+    uint32_t* ctl;
+    uint32_t* list[kFixLists];
+    uint32_t cap[kFixLists];
+};
+
+// Called by every thread of the block (block-uniform loop): `cls` is the list the
+// thread appends `cell` to, or -1.
+__device__ __forceinline__ void push_fix(const FixLists& L, int cls, uint32_t cell) {
+    __shared__ uint32_t s_n[kFixLists], s_base[kFixLists];
+    if (threadIdx.x < (uint32_t)kFixLists) s_n[threadIdx.x] = 0u;
+    __syncthreads();
+    uint32_t at = 0;
+    if (cls >= 0) at = atomicAdd(&s_n[cls], 1u);
+    __syncthreads();
+    if (threadIdx.x < (uint32_t)kFixLists && s_n[threadIdx.x])
+        s_base[threadIdx.x] = atomicAdd(L.ctl + threadIdx.x, s_n[threadIdx.x]);
+    __syncthreads();
+    if (cls >= 0) {  // lists hold every cell that can qualify; the bound only guards bad counts
+        uint32_t* list = cls == kFixListSmall ? L.list[0] : (cls == kFixListWarp ? L.list[1] : L.list[2]);
+        const uint32_t cap = cls == kFixListSmall ? L.cap[0] : (cls == kFixListWarp ? L.cap[1] : L.cap[2]);
+        if (s_base[cls] + at < cap) list[s_base[cls] + at] = cell;
+    }
+}
+
+// The run [b, b + g) of cell k ends the cell and did not start it: other warps'
+// runs came first, so the cell is listed for the fixup (once: one run ends it).
+__device__ __forceinline__ int fix_class(const uint32_t* __restrict__ offs, uint32_t k, uint32_t b, uint32_t g) {
+    const uint32_t lo = __ldg(offs + k), hi = __ldg(offs + k + 1u);
+    if (b + g != hi || b == lo) return -1;
+    const uint32_t m = hi - lo;
+    return m <= kFixSmall ? kFixListSmall : (m <= kFixWarp ? kFixListWarp : kFixListHuge);
+}
 // Also moves each sphere's state to its slot (sorted copy for the physics pass)
 // and, where a slot begins or ends a physics tile, writes that side of the
 // tile's band table entry (the cell of a slot is final here; the fixup only
@@ -136,7 +171,7 @@ __global__ void __launch_bounds__(256)
                    uint32_t* __restrict__ perm, const float4* __restrict__ pos_in,
                    const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
                    uint4* __restrict__ svfme, const uint32_t* __restrict__ offs, uint4* __restrict__ bands,
-                   uint32_t N) {
+                   uint32_t N, FixLists fix) {
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
@@ -155,8 +190,13 @@ __global__ void __launch_bounds__(256)
         uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k);
         uint32_t leader = (uint32_t)(__ffs(peers) - 1);
         uint32_t b = 0;
-        if (valid && !ident && lane == leader) b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
+        int cls = -1;
+        if (valid && !ident && lane == leader) {
+            b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
+            cls = fix_class(offs, k, b, (uint32_t)__popc(peers));
+        }
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
+        push_fix(fix, cls, k);
         if (valid) {
             const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
             perm[dst] = i;
@@ -174,7 +214,8 @@ __global__ void __launch_bounds__(256)
                           const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ cursor,
                           uint32_t* __restrict__ perm, const float4* __restrict__ pos0,
                           const float4* __restrict__ pos1, const uint4* __restrict__ vfme0,
-                          const uint4* __restrict__ vfme1, float4* __restrict__ spos, uint4* __restrict__ svfme) {
+                          const uint4* __restrict__ vfme1, float4* __restrict__ spos, uint4* __restrict__ svfme,
+                          const uint32_t* __restrict__ offs, FixLists fix) {
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
@@ -199,8 +240,13 @@ __global__ void __launch_bounds__(256)
         uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k);
         uint32_t leader = (uint32_t)(__ffs(peers) - 1);
         uint32_t b = 0;
-        if (valid && !ident && lane == leader) b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
+        int cls = -1;
+        if (valid && !ident && lane == leader) {
+            b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
+            cls = fix_class(offs, k, b, (uint32_t)__popc(peers));
+        }
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
+        push_fix(fix, cls, k);
         if (valid) {
             const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
             perm[dst] = i;
@@ -211,13 +257,51 @@ __global__ void __launch_bounds__(256)
 }
 
 // ---------------------------------------------------------------- fixup
-// Cells of up to kSmallCell slots are re-sorted by their own thread (insertion
-// sort, after a sortedness check); larger ones go to a list for k_cell_fixup_big.
-// A cell whose order changes re-gathers its sorted state copy from the state
-// source: one buffer (a world), or each scene's current buffer (a batch, where
-// cells and coarse tiles of HOLD scenes are left alone).
-constexpr uint32_t kSmallCell = 32;
-constexpr uint32_t kBlockSortMax = 8192;
+// The listed cells (see fix_class) get their slots back in ascending input order
+// and re-gather their sorted state copy from the state source: one buffer (a
+// world), or each scene's current buffer (a batch, where cells and coarse tiles
+// of HOLD scenes are left alone).  Cells of up to kFixSmall slots: a thread
+// each (insertion sort); up to kFixWarp: a warp each (rank of every slot among
+// the cell's input indices, held in registers); larger: a block each (bitmap of
+// the input indices, chunk by chunk of their range, read back in order).
+constexpr uint32_t kFixThreads = 256;
+constexpr uint32_t kBitmapWords = 8192;                 // 32 KB of shared memory
+constexpr uint32_t kBitmapValues = kBitmapWords * 32u;  // input indices per bitmap chunk
+
+// Block-wide min (is_min) or max of v; every thread gets the result.
+__device__ __forceinline__ uint32_t block_reduce(uint32_t v, uint32_t* s_red, bool is_min) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint32_t u = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        v = is_min ? min(v, u) : max(v, u);
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31u) == 0u) s_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    v = s_red[0];
+    for (uint32_t w = 1; w < blockDim.x / 32u; ++w) v = is_min ? min(v, s_red[w]) : max(v, s_red[w]);
+    __syncthreads();
+    return v;
+}
+
+// Block-wide exclusive prefix sum of v; `total` receives the sum over the block.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_red, uint32_t& total) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31u) s_red[warp] = incl;
+    __syncthreads();
+    uint32_t base = 0, sum = 0;
+    for (uint32_t w = 0; w < blockDim.x / 32u; ++w) {
+        if (w < warp) base += s_red[w];
+        sum += s_red[w];
+    }
+    __syncthreads();
+    total = sum;
+    return base + incl - v;
+}
 
 struct OneBuffer {
     const float4* p;
@@ -248,125 +332,159 @@ struct SceneBuffers {
 };
 
 template <class Src>
-__global__ void __launch_bounds__(256)
-    k_cell_fixup(const uint32_t* __restrict__ offs, uint32_t cells, uint32_t* perm, uint32_t* coarse,
-                 uint32_t tiles, uint32_t* big_ctl, uint32_t* big, Src src, float4* __restrict__ spos,
-                 uint4* __restrict__ svfme) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (blockIdx.x == 0)  // the scan of this frame is over: clear the tile counts for the next one
-        for (uint32_t t = threadIdx.x; t < tiles; t += blockDim.x)
-            if (src.tile_active(t)) coarse[t] = 0u;
-    if (c >= cells || !src.tile_active(c / kScanTile)) return;
-    const uint32_t lo = offs[c], hi = offs[c + 1u];
-    if (hi - lo < 2u) return;
-    if (hi - lo > kSmallCell) {
-        big[atomicAdd(big_ctl, 1u)] = c;
-        return;
-    }
-    bool sorted = true;
-    uint32_t prev = perm[lo];
-    for (uint32_t j = lo + 1u; j < hi; ++j) {
-        uint32_t x = perm[j];
-        if (x < prev) { sorted = false; break; }
-        prev = x;
-    }
-    if (sorted) return;
-    for (uint32_t a = lo + 1u; a < hi; ++a) {  // insertion sort of this cell's slots
-        uint32_t x = perm[a];
-        uint32_t b = a;
-        while (b > lo) {
-            uint32_t y = perm[b - 1u];
-            if (y <= x) break;
-            perm[b] = y;
-            --b;
-        }
-        perm[b] = x;
-    }
-    for (uint32_t j = lo; j < hi; ++j) {  // the sorted state copy follows the new order
-        const uint32_t o = perm[j];
-        spos[j] = src.pos(o);
-        svfme[j] = src.vfme(o);
-    }
+__device__ __forceinline__ void regather(const Src& src, const uint32_t* perm, uint32_t lo, uint32_t j,
+                                         float4* __restrict__ spos, uint4* __restrict__ svfme) {
+    const uint32_t o = perm[lo + j];
+    spos[lo + j] = src.pos(o);
+    svfme[lo + j] = src.vfme(o);
 }
 
-__device__ void heap_sift(uint32_t* a, uint32_t root, uint32_t end) {
-    while (true) {
-        uint32_t child = 2u * root + 1u;
-        if (child >= end) return;
-        if (child + 1u < end && a[child + 1u] > a[child]) ++child;
-        if (a[root] >= a[child]) return;
-        uint32_t t = a[root];
-        a[root] = a[child];
-        a[child] = t;
-        root = child;
-    }
-}
-
-// One block per listed cell: bitonic sort in shared memory (up to kBlockSortMax
-// slots), else an O(m log m) heapsort in place by one thread (only degenerate
-// scenes with thousands of spheres in one cell get there).
 template <class Src>
-__global__ void __launch_bounds__(256)
-    k_cell_fixup_big(const uint32_t* __restrict__ offs, uint32_t* perm, uint32_t* big_ctl,
-                     const uint32_t* __restrict__ big, Src src, float4* __restrict__ spos,
-                     uint4* __restrict__ svfme) {
-    __shared__ uint32_t s_v[kBlockSortMax];
-    __shared__ uint32_t s_idx, s_unsorted;
-    const uint32_t tid = threadIdx.x;
-    while (true) {
-        if (tid == 0) {
-            s_idx = atomicAdd(big_ctl + 1, 1u);
-            s_unsorted = 0u;
-        }
-        __syncthreads();
-        const uint32_t idx = s_idx;
-        if (idx >= __ldcg(big_ctl)) return;
-        const uint32_t c = __ldg(big + idx);
+__global__ void __launch_bounds__(kFixThreads)
+    k_cell_fix(const uint32_t* __restrict__ offs, uint32_t* perm, uint32_t* __restrict__ coarse, uint32_t tiles,
+               FixLists lists, uint32_t* __restrict__ tmp, Src src,
+               float4* __restrict__ spos, uint4* __restrict__ svfme) {
+    __shared__ uint32_t s_v[kBitmapWords];
+    __shared__ uint32_t s_red[kFixThreads / 32 + 1];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    if (blockIdx.x == 0)  // the scan of this frame is over: clear the tile counts for the next one
+        for (uint32_t t = tid; t < tiles; t += blockDim.x)
+            if (src.tile_active(t)) coarse[t] = 0u;
+
+    const uint32_t* __restrict__ small = lists.list[0];
+    const uint32_t* __restrict__ mid = lists.list[1];
+    const uint32_t* __restrict__ huge = lists.list[2];
+
+    // small cells: one thread each, the cell held in registers (a sorting
+    // network over kFixSmall slots; empty slots hold 0xFFFFFFFF and stay last)
+    const uint32_t n_small = min(lists.ctl[kFixListSmall], lists.cap[0]);
+    for (uint32_t x = blockIdx.x * blockDim.x + tid; x < n_small; x += gridDim.x * blockDim.x) {
+        const uint32_t c = small[x];
         const uint32_t lo = offs[c], m = offs[c + 1u] - lo;
-        for (uint32_t j = tid + 1u; j < m; j += blockDim.x)
-            if (perm[lo + j] < perm[lo + j - 1u]) s_unsorted = 1u;
-        __syncthreads();
-        if (s_unsorted) {
-            if (m <= kBlockSortMax) {
-                uint32_t P = 2u;
-                while (P < m) P <<= 1;
-                for (uint32_t j = tid; j < P; j += blockDim.x) s_v[j] = j < m ? perm[lo + j] : 0xFFFFFFFFu;
-                __syncthreads();
-                for (uint32_t k = 2u; k <= P; k <<= 1) {
-                    for (uint32_t jj = k >> 1; jj > 0u; jj >>= 1) {
-                        for (uint32_t i = tid; i < P; i += blockDim.x) {
-                            uint32_t ixj = i ^ jj;
-                            if (ixj > i) {
-                                uint32_t a = s_v[i], b = s_v[ixj];
-                                bool up = (i & k) == 0u;
-                                if ((a > b) == up) {
-                                    s_v[i] = b;
-                                    s_v[ixj] = a;
-                                }
-                            }
-                        }
-                        __syncthreads();
-                    }
-                }
-                for (uint32_t j = tid; j < m; j += blockDim.x) perm[lo + j] = s_v[j];
-            } else if (tid == 0) {
-                uint32_t* a = perm + lo;
-                for (uint32_t r = m / 2u; r-- > 0u;) heap_sift(a, r, m);
-                for (uint32_t end = m - 1u; end > 0u; --end) {
-                    uint32_t t = a[0];
-                    a[0] = a[end];
-                    a[end] = t;
-                    heap_sift(a, 0u, end);
-                }
+        uint32_t v[kFixSmall];
+        bool sorted = true;
+#pragma unroll
+        for (uint32_t k = 0; k < kFixSmall; ++k) v[k] = k < m ? perm[lo + k] : 0xFFFFFFFFu;
+#pragma unroll
+        for (uint32_t k = 1; k < kFixSmall; ++k) sorted = sorted && v[k - 1u] <= v[k];
+        if (sorted) continue;
+        // Batcher's odd-even merge sort of 8 keys (19 compare-exchanges)
+        constexpr uint8_t kNet[19][2] = {{0, 1}, {2, 3}, {4, 5}, {6, 7}, {0, 2}, {1, 3}, {4, 6}, {5, 7}, {1, 2},
+                                         {5, 6}, {0, 4}, {1, 5}, {2, 6}, {3, 7}, {2, 4}, {3, 5}, {1, 2}, {3, 4},
+                                         {5, 6}};
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const uint32_t a = v[kNet[q][0]], b = v[kNet[q][1]];
+            v[kNet[q][0]] = min(a, b);
+            v[kNet[q][1]] = max(a, b);
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kFixSmall; ++k) {
+            if (k < m) {
+                perm[lo + k] = v[k];
+                spos[lo + k] = src.pos(v[k]);
+                svfme[lo + k] = src.vfme(v[k]);
+            }
+        }
+    }
+
+    // mid cells: one warp each; slot e = lane + 32 s of the cell is v[s]
+    const uint32_t n_mid = min(lists.ctl[kFixListWarp], lists.cap[1]);
+    const uint32_t warps = gridDim.x * (blockDim.x / 32u);
+    for (uint32_t x = blockIdx.x * (blockDim.x / 32u) + tid / 32u; x < n_mid; x += warps) {
+        const uint32_t c = mid[x];
+        const uint32_t lo = offs[c], m = offs[c + 1u] - lo;
+        const uint32_t S = (m + 31u) / 32u;  // <= kFixWarp / 32
+        uint32_t v[kFixWarp / 32], r[kFixWarp / 32];
+#pragma unroll
+        for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
+            const uint32_t e = lane + 32u * s;
+            v[s] = e < m ? perm[lo + e] : 0xFFFFFFFFu;
+            r[s] = 0u;
+        }
+        for (uint32_t s2 = 0; s2 < S; ++s2) {
+#pragma unroll 4
+            for (uint32_t l = 0; l < 32u; ++l) {
+                uint32_t u = 0;
+#pragma unroll
+                for (uint32_t q = 0; q < kFixWarp / 32; ++q)
+                    if (q == s2) u = __shfl_sync(0xFFFFFFFFu, v[q], (int)l);
+#pragma unroll
+                for (uint32_t s = 0; s < kFixWarp / 32; ++s) r[s] += u < v[s] ? 1u : 0u;
+            }
+        }
+        __syncwarp();  // every lane has read the cell before any slot is rewritten
+#pragma unroll
+        for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
+            const uint32_t e = lane + 32u * s;
+            if (e < m && r[s] != e) {
+                perm[lo + r[s]] = v[s];
+                spos[lo + r[s]] = src.pos(v[s]);
+                svfme[lo + r[s]] = src.vfme(v[s]);
+            }
+        }
+    }
+
+    // huge cells: one block each.  The cell's input indices are copied aside,
+    // then each chunk of their value range becomes a bitmap in shared memory: the
+    // set bits, read in order, are the chunk's indices in ascending order, and a
+    // block scan of per-thread bit counts gives every thread its output position.
+    const uint32_t n_huge = min(lists.ctl[kFixListHuge], lists.cap[2]);
+    for (uint32_t x = blockIdx.x; x < n_huge; x += gridDim.x) {
+        const uint32_t c = huge[x];
+        const uint32_t lo = offs[c], m = offs[c + 1u] - lo;
+        uint32_t vmin = 0xFFFFFFFFu, vmax = 0u;
+        for (uint32_t j = tid; j < m; j += blockDim.x) {
+            const uint32_t v = perm[lo + j];
+            tmp[lo + j] = v;
+            vmin = min(vmin, v);
+            vmax = max(vmax, v);
+        }
+        vmin = block_reduce(vmin, s_red, true);
+        vmax = block_reduce(vmax, s_red, false);  // ends with a barrier: tmp is complete
+        uint32_t done = 0;
+        for (uint32_t c0 = vmin;; c0 += kBitmapValues) {
+            for (uint32_t w = tid; w < kBitmapWords; w += blockDim.x) s_v[w] = 0u;
+            __syncthreads();
+            for (uint32_t j = tid; j < m; j += blockDim.x) {
+                const uint32_t d = tmp[lo + j] - c0;
+                if (d < kBitmapValues) atomicOr(&s_v[d >> 5], 1u << (d & 31u));
             }
             __syncthreads();
-            for (uint32_t j = tid; j < m; j += blockDim.x) {  // sorted state copy follows
-                const uint32_t o = perm[lo + j];
-                spos[lo + j] = src.pos(o);
-                svfme[lo + j] = src.vfme(o);
+            constexpr uint32_t kWordsPer = kBitmapWords / kFixThreads;
+            uint32_t mine = 0;
+#pragma unroll 8
+            for (uint32_t w = 0; w < kWordsPer; ++w) mine += (uint32_t)__popc(s_v[tid * kWordsPer + w]);
+            uint32_t total;
+            const uint32_t before = block_exclusive_scan(mine, s_red, total);
+            uint32_t at = lo + done + before;
+            for (uint32_t w = 0; w < kWordsPer; ++w) {
+                uint32_t bits = s_v[tid * kWordsPer + w];
+                const uint32_t vb = c0 + (tid * kWordsPer + w) * 32u;
+                while (bits) {  // four at a time, so the state loads overlap
+                    uint32_t vv[4];
+                    uint32_t got = 0;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        vv[q] = bits ? vb + (uint32_t)(__ffs(bits) - 1) : 0u;
+                        got += bits ? 1u : 0u;
+                        bits &= bits - 1u;
+                    }
+#pragma unroll
+                    for (uint32_t q = 0; q < 4; ++q) {
+                        if (q < got) {
+                            perm[at + q] = vv[q];
+                            spos[at + q] = src.pos(vv[q]);
+                            svfme[at + q] = src.vfme(vv[q]);
+                        }
+                    }
+                    at += got;
+                }
             }
+            done += total;
+            __syncthreads();  // bitmap free for the next chunk
+            if (vmax - c0 < kBitmapValues) break;
         }
-        __syncthreads();
     }
 }
 
@@ -409,7 +527,26 @@ __global__ void k_set_word(uint32_t* p, uint32_t v, uint32_t* q) {
 
 }  // namespace
 
-cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells) {
+namespace {
+FixLists fix_lists(const CountScratch& s) {
+    return FixLists{s.fix_ctl, {s.fix[0], s.fix[1], s.fix[2]}, {s.fix_cap[0], s.fix_cap[1], s.fix_cap[2]}};
+}
+uint32_t fix_blocks() { return (uint32_t)device_sm_count() * 4u; }
+uint32_t scan_tiles(uint32_t cells) { return (cells + kScanTile - 1u) / kScanTile; }
+uint32_t fix_capacity(int cls, uint32_t max_cells, uint32_t max_keys) {
+    const uint32_t per = cls == kFixListSmall ? 2u : (cls == kFixListWarp ? kFixSmall + 1u : kFixWarp + 1u);
+    return std::min(max_cells, max_keys / per) + 1u;
+}
+}  // namespace
+
+uint64_t count_scratch_bytes(uint32_t max_cells, uint32_t max_keys) {
+    const uint64_t padded = ((uint64_t)max_cells + kScanTile) & ~(uint64_t)15;
+    uint64_t b = 4u * (2u * padded + (max_cells + kScanTile - 1u) / kScanTile + 1u + kFixLists);
+    for (int c = 0; c < kFixLists; ++c) b += 4u * fix_capacity(c, max_cells, max_keys);
+    return b + 4u * ((uint64_t)max_keys + 1u);
+}
+
+cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells, uint32_t max_keys) {
     s.max_cells = max_cells;
     size_t padded = ((size_t)max_cells + kScanTile) & ~(size_t)15;  // uint4-aligned, room for offs[C]
     s.tiles = (max_cells + kScanTile - 1u) / kScanTile;
@@ -417,11 +554,15 @@ cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells) {
     if ((e = cudaMalloc(&s.hist, sizeof(uint32_t) * padded))) return e;
     if ((e = cudaMalloc(&s.cursor, sizeof(uint32_t) * padded))) return e;
     if ((e = cudaMalloc(&s.coarse, sizeof(uint32_t) * (s.tiles + 1u)))) return e;
-    if ((e = cudaMalloc(&s.big_ctl, sizeof(uint32_t) * 2u))) return e;
-    if ((e = cudaMalloc(&s.big, sizeof(uint32_t) * ((size_t)max_cells + 1u)))) return e;
+    if ((e = cudaMalloc(&s.fix_ctl, sizeof(uint32_t) * kFixLists))) return e;
+    if ((e = cudaMalloc(&s.fix_tmp, sizeof(uint32_t) * ((size_t)max_keys + 1u)))) return e;
+    for (int c = 0; c < kFixLists; ++c) {
+        s.fix_cap[c] = fix_capacity(c, max_cells, max_keys);
+        if ((e = cudaMalloc(&s.fix[c], sizeof(uint32_t) * s.fix_cap[c]))) return e;
+    }
     if ((e = cudaMemset(s.hist, 0, sizeof(uint32_t) * padded))) return e;
     if ((e = cudaMemset(s.coarse, 0, sizeof(uint32_t) * (s.tiles + 1u)))) return e;
-    if ((e = cudaMemset(s.big_ctl, 0, sizeof(uint32_t) * 2u))) return e;
+    if ((e = cudaMemset(s.fix_ctl, 0, sizeof(uint32_t) * kFixLists))) return e;
     return cudaSuccess;
 }
 
@@ -429,8 +570,9 @@ void count_scratch_free(CountScratch& s) {
     cudaFree(s.hist);
     cudaFree(s.cursor);
     cudaFree(s.coarse);
-    cudaFree(s.big_ctl);
-    cudaFree(s.big);
+    cudaFree(s.fix_ctl);
+    cudaFree(s.fix_tmp);
+    for (auto* l : s.fix) cudaFree(l);
     s = CountScratch();
 }
 
@@ -459,7 +601,7 @@ cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, c
 cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st) {
     (void)ctl;
     uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
-    k_cell_scan<false><<<tiles, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.big_ctl,
+    k_cell_scan<false><<<tiles, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.fix_ctl,
                                                        nullptr, nullptr);
     return cudaGetLastError();
 }
@@ -471,23 +613,19 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
     if (n) {
         uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
         k_cell_scatter<<<blocks, 256, 0, st>>>(keys, n, s.cursor, perm, pos_in, vfme_in, spos, svfme, offs, bands,
-                                               N);
+                                               N, fix_lists(s));
         if ((e = cudaGetLastError())) return e;
     }
-    uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
     OneBuffer src{pos_in, vfme_in};
-    k_cell_fixup<OneBuffer><<<(cells + 255u) / 256u, 256, 0, st>>>(offs, cells, perm, s.coarse, tiles, s.big_ctl,
-                                                                   s.big, src, spos, svfme);
-    if ((e = cudaGetLastError())) return e;
-    k_cell_fixup_big<OneBuffer><<<(uint32_t)device_sm_count(), 256, 0, st>>>(offs, perm, s.big_ctl, s.big, src,
-                                                                             spos, svfme);
+    k_cell_fix<OneBuffer><<<fix_blocks(), kFixThreads, 0, st>>>(offs, perm, s.coarse, scan_tiles(cells),
+                                                                fix_lists(s), s.fix_tmp, src, spos, svfme);
     return cudaGetLastError();
 }
 
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
                               uint32_t cells, uint32_t* offs, cudaStream_t st) {
     uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
-    k_cell_scan<true><<<tiles, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.big_ctl, scenes,
+    k_cell_scan<true><<<tiles, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.fix_ctl, scenes,
                                                       cell_tile_scene);
     return cudaGetLastError();
 }
@@ -501,16 +639,13 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
     if (n) {
         uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
         k_cell_scatter_scenes<<<blocks, 256, 0, st>>>(scenes, tile_scene, keys, n, s.cursor, perm, pos_buf0,
-                                                      pos_buf1, vfme_buf0, vfme_buf1, spos, svfme);
+                                                      pos_buf1, vfme_buf0, vfme_buf1, spos, svfme, offs,
+                                                      fix_lists(s));
         if ((e = cudaGetLastError())) return e;
     }
-    uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
     SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
-    k_cell_fixup<SceneBuffers><<<(cells + 255u) / 256u, 256, 0, st>>>(offs, cells, perm, s.coarse, tiles,
-                                                                      s.big_ctl, s.big, src, spos, svfme);
-    if ((e = cudaGetLastError())) return e;
-    k_cell_fixup_big<SceneBuffers><<<(uint32_t)device_sm_count(), 256, 0, st>>>(offs, perm, s.big_ctl, s.big,
-                                                                                src, spos, svfme);
+    k_cell_fix<SceneBuffers><<<fix_blocks(), kFixThreads, 0, st>>>(offs, perm, s.coarse, scan_tiles(cells),
+                                                                   fix_lists(s), s.fix_tmp, src, spos, svfme);
     return cudaGetLastError();
 }
 

@@ -173,16 +173,27 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr uint32_t kScanTile = kScanThreads * kScanItems;
 
+// Cells the scatter filled from several warp runs are listed for the in-cell
+// fixup by size: up to kFixSmall slots (a thread each), up to kFixWarp (a warp
+// each), larger (a block each).
+constexpr uint32_t kFixSmall = 8;
+constexpr uint32_t kFixWarp = 256;
+enum : int { kFixListSmall = 0, kFixListWarp = 1, kFixListHuge = 2, kFixLists = 3 };
+
 struct CountScratch {
     uint32_t max_cells = 0;
     uint32_t* hist = nullptr;     // [max_cells] counts of the keys of the next sort
     uint32_t* cursor = nullptr;   // [max_cells] scatter cursors
     uint32_t* coarse = nullptr;   // [tiles] counts per 4096-cell scan tile
-    uint32_t* big_ctl = nullptr;  // [2] big-cell list count and cursor
-    uint32_t* big = nullptr;      // cells with more than 32 spheres this frame
+    uint32_t* fix_ctl = nullptr;  // [kFixLists] lengths of the fixup lists
+    uint32_t* fix[kFixLists] = {nullptr, nullptr, nullptr};  // listed cells, by size class
+    uint32_t fix_cap[kFixLists] = {0u, 0u, 0u};                // their capacities
+    uint32_t* fix_tmp = nullptr;  // [max_keys] copy of a large cell's input indices
     uint32_t tiles = 0;
 };
-cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells);
+// Lists are sized from max_keys: a listed cell holds >= 2, > kFixSmall or > kFixWarp keys.
+cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells, uint32_t max_keys);
+uint64_t count_scratch_bytes(uint32_t max_cells, uint32_t max_keys);
 void count_scratch_free(CountScratch& s);
 // hist := 0, coarse := 0 for `cells` cells.
 cudaError_t count_clear(CountScratch& s, uint32_t cells, cudaStream_t st);

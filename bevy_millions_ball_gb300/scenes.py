@@ -82,7 +82,8 @@ def plain_clustered(n: int, grids: int, *, clusters: int = 16, sigma_xz: float =
                     grid_size: int = 1, half_map_height: int = 8, radius: float = 0.5, seed: int = 0,
                     k: float = 1000.0, c: float = 5.0, e: float = 0.8, dt: float = 1.0 / 60.0,
                     gravity=(0.0, -9.81, 0.0)) -> Scene:
-    """Gaussian clusters (sigma in cells), centres uniform in the box, spring response."""
+    """Gaussian clusters (sigma in cells), centres uniform in the box, truncated to
+    the box, spring response."""
     plugin = PhysicsPlugin(
         max_number_of_agents=n, number_of_grids_one_dimension=grids, grid_size=grid_size,
         half_map_height=half_map_height, gravity=tuple(gravity), e_envir=e, e_agent=e,
@@ -95,12 +96,22 @@ def plain_clustered(n: int, grids: int, *, clusters: int = 16, sigma_xz: float =
     cz = rng.uniform(-hs, hs, clusters)
     cy = rng.uniform(0.0, h2, clusters)
     which = rng.integers(0, clusters, n)
-    x = cx[which] + rng.standard_normal(n) * sigma_xz * grid_size
-    z = cz[which] + rng.standard_normal(n) * sigma_xz * grid_size
-    y = cy[which] + rng.standard_normal(n) * sigma_y * grid_size
-    x = _below(np.clip(x, -hs, hs).astype(np.float32), hs)
-    z = _below(np.clip(z, -hs, hs).astype(np.float32), hs)
-    y = _below(np.clip(y, 0.0, h2).astype(np.float32), h2)
+    # Gaussian clusters truncated to the domain: samples that fall outside are
+    # drawn again (clipping them would pile them onto the border cells)
+    x = np.empty(n)
+    y = np.empty(n)
+    z = np.empty(n)
+    todo = np.arange(n)
+    while todo.size:
+        w = which[todo]
+        x[todo] = cx[w] + rng.standard_normal(todo.size) * sigma_xz * grid_size
+        z[todo] = cz[w] + rng.standard_normal(todo.size) * sigma_xz * grid_size
+        y[todo] = cy[w] + rng.standard_normal(todo.size) * sigma_y * grid_size
+        out = (x[todo] < -hs) | (x[todo] >= hs) | (z[todo] < -hs) | (z[todo] >= hs) | (y[todo] < 0.0) | (y[todo] > h2)
+        todo = todo[out]
+    x = _below(x.astype(np.float32), hs)
+    z = _below(z.astype(np.float32), hs)
+    y = _below(y.astype(np.float32), h2)
     v0 = rng.standard_normal((n, 3)).astype(np.float32)
     pos, vfme = _state(np.stack([x, y, z], 1), radius, v0, plugin)
     return Scene(plugin, pos, vfme, f"clustered n={n} N={grids} k={clusters}")
