@@ -143,6 +143,9 @@ bool counting(const mb_world* w) { return w->tuning.sort_algorithm == MB_SORT_CO
 // first ordering stage, [2] after the second, [3] after physics.
 cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool capturing = false) {
     cudaError_t e;
+    // kernels after the first start while their predecessor drains (programmatic
+    // dependent launch) in captured LOOP frames without profiling marks between them
+    const bool pdl = capturing && !init && !w->profiling;
     uint32_t* hist = nullptr;
     uint32_t* coarse = nullptr;
     if ((e = mark(w, 0, st, capturing))) return e;
@@ -157,7 +160,7 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         if ((e = mb::count_scan(w->cnt, w->scratch.ctl, w->cells, w->scratch.offs, st))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
         if ((e = mb::count_scatter(w->cnt, w->keys, w->n, w->cells, w->scratch.offs, w->perm, w->pos[cur],
-                                   w->vfme[cur], w->spos, w->svfme, w->bands, w->P.N, st)))
+                                   w->vfme[cur], w->spos, w->svfme, w->bands, w->P.N, st, pdl)))
             return e;
         hist = w->cnt.hist;
         coarse = w->cnt.coarse;
@@ -175,8 +178,9 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         e = mb::launch_physics_init(w->P, w->n, w->perm, w->pos[cur], w->vfme[cur], w->pos[nxt],
                                     w->vfme[nxt], w->keys, hist, coarse, st);
     else
-        e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->spos, w->svfme, w->pos[nxt], w->vfme[nxt],
-                                    w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError, st);
+        e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->spos, w->svfme, w->pos[nxt],
+                                    w->vfme[nxt], w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError, st,
+                                    pdl && counting(w));
     if (e) return e;
     return mark(w, 3, st, capturing);
 }

@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(kScanThreads)
     __shared__ uint32_t s_warp[W], s_base[W];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t tile = blockIdx.x;
+    griddep_launch();
     if (tile == 0 && tid < (uint32_t)kFixLists) fix_ctl[tid] = 0u;  // fixup lists of this frame start empty
     const uint32_t base = tile * kScanTile + tid * kScanItems;
 
@@ -172,6 +173,8 @@ __global__ void __launch_bounds__(256)
                    const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
                    uint4* __restrict__ svfme, const uint32_t* __restrict__ offs, uint4* __restrict__ bands,
                    uint32_t N, FixLists fix) {
+    griddep_wait();
+    griddep_launch();
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
@@ -346,6 +349,8 @@ __global__ void __launch_bounds__(kFixThreads)
                float4* __restrict__ spos, uint4* __restrict__ svfme) {
     __shared__ uint32_t s_v[kBitmapWords];
     __shared__ uint32_t s_red[kFixThreads / 32 + 1];
+    griddep_wait();
+    griddep_launch();
     const uint32_t tid = threadIdx.x, lane = tid & 31u;
     if (blockIdx.x == 0)  // the scan of this frame is over: clear the tile counts for the next one
         for (uint32_t t = tid; t < tiles; t += blockDim.x)
@@ -608,18 +613,17 @@ cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t*
 
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
-                          float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st) {
+                          float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st, bool pdl) {
     cudaError_t e;
     if (n) {
         uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
-        k_cell_scatter<<<blocks, 256, 0, st>>>(keys, n, s.cursor, perm, pos_in, vfme_in, spos, svfme, offs, bands,
-                                               N, fix_lists(s));
-        if ((e = cudaGetLastError())) return e;
+        if ((e = launch_pdl(pdl, k_cell_scatter, dim3(blocks), dim3(256), 0, st, keys, n, s.cursor, perm, pos_in,
+                            vfme_in, spos, svfme, offs, bands, N, fix_lists(s))))
+            return e;
     }
     OneBuffer src{pos_in, vfme_in};
-    k_cell_fix<OneBuffer><<<fix_blocks(), kFixThreads, 0, st>>>(offs, perm, s.coarse, scan_tiles(cells),
-                                                                fix_lists(s), s.fix_tmp, src, spos, svfme);
-    return cudaGetLastError();
+    return launch_pdl(pdl && n, k_cell_fix<OneBuffer>, dim3(fix_blocks()), dim3(kFixThreads), 0, st, offs, perm,
+                      s.coarse, scan_tiles(cells), fix_lists(s), s.fix_tmp, src, spos, svfme);
 }
 
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,

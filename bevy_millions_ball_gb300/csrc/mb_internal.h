@@ -121,6 +121,31 @@ constexpr uint32_t kPhysicsTile = 128;  // slots per block of the physics pass
 // whose upper bound is not above its lower bound is empty.
 inline uint32_t band_table_entries(uint32_t n) { return 2u * ((n + kPhysicsTile - 1u) / kPhysicsTile); }
 #ifdef __CUDACC__
+// Programmatic dependent launch.  A kernel launched with launch_pdl may start
+// while the kernel before it on the stream is still finishing; it calls
+// griddep_wait() before it touches memory that kernel writes (the wait returns
+// once that kernel has completed and its writes are visible; without a
+// programmatic predecessor it returns at once).  griddep_launch() lets the next
+// kernel start launching.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1u : 0u;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 __device__ __forceinline__ void write_band_bounds(uint4* __restrict__ bands, const uint32_t* __restrict__ offs,
                                                   uint32_t N, uint32_t n, uint32_t slot, uint32_t key) {
     const uint32_t r = slot % kPhysicsTile;
@@ -152,10 +177,11 @@ cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t*
                                 cudaStream_t st);
 // LOOP pass over the state in sorted order (spos/svfme, slot j = sorted slot j).
 // `bands` is the band table the sort wrote for this order.
+// `pdl`: launched as a programmatic dependent of the kernel before it.
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                 const float4* spos, const uint4* svfme, float4* pos_out, uint4* vfme_out,
                                 uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
-                                cudaStream_t st);
+                                cudaStream_t st, bool pdl = false);
 cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,
                          uint32_t* hist, uint32_t* coarse, cudaStream_t st);
 
@@ -212,7 +238,8 @@ cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32
 // (nullable) := the band table of that order for an N x N grid.
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
-                          float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st);
+                          float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,
+                          bool pdl = false);
 // Batched count scan: scene cell ranges are padded to whole scan tiles
 // (cell_tile_scene[t] = scene of tile t); tiles of HOLD scenes are skipped.
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,

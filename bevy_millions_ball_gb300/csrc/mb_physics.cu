@@ -270,6 +270,102 @@ __device__ __forceinline__ void contact_loop(const PhysParams& P, Agent& a, cons
     }
 }
 
+// Slot ranges of the three candidate rows of a sphere in cell (cx, cz), key =
+// cz*N + cx (get_collision_grid_id's neighbourhood, physics.wgsl:122-160): own
+// row [0], row below [1], row above [2]; rows off the map stay empty.
+__device__ __forceinline__ void row_bounds(uint32_t N, const uint32_t* __restrict__ of, uint32_t key, uint32_t cx,
+                                           uint32_t cz, uint32_t (&lo)[3], uint32_t (&hi)[3]) {
+    const uint32_t l = cx > 0u ? 1u : 0u, rr = cx < N - 1u ? 2u : 1u;
+    lo[0] = __ldg(of + key - l);
+    hi[0] = __ldg(of + key + rr);
+    lo[1] = hi[1] = lo[2] = hi[2] = 0u;
+    if (cz > 0u) {
+        lo[1] = __ldg(of + key - N - l);
+        hi[1] = __ldg(of + key - N + rr);
+    }
+    if (cz < N - 1u) {
+        lo[2] = __ldg(of + key + N - l);
+        hi[2] = __ldg(of + key + N + rr);
+    }
+}
+
+// One sphere's LOOP step (physics.wgsl:57-90) at sorted slot i, state `a`
+// unpacked from it: Verlet, contacts against its candidate rows, jitter, walls,
+// clamp, pack, store, new key and its counts.  The bands of its tile are staged
+// in b_pos/b_vfme ([3][kBandCap]: band 0 row below, 1 own row, 2 row above; band
+// b holds slots [b_lo[b], b_lo[b] + b_cnt[b])); rows outside them are read from
+// spos/svfme.  base_a / base_c: the scene's first slot and cell (0 for a world).
+__device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32_t i, uint32_t n, uint32_t base_a,
+                                            uint32_t base_c, const uint32_t (&lo)[3], const uint32_t (&hi)[3],
+                                            const float4* b_pos, const uint4* b_vfme, const uint32_t* b_lo,
+                                            const uint32_t* b_cnt, const float4* __restrict__ spos,
+                                            const uint4* __restrict__ svfme, float4* __restrict__ pos_out,
+                                            uint4* __restrict__ vfme_out, uint32_t* __restrict__ keys_out,
+                                            uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse) {
+    // candidate rows in the reference's order: own row (band 1), below (0), above (2)
+    uint32_t c[3], o_s[3], o_g[3];
+    bool shared = true;
+    {
+        const uint32_t band[3] = {1u, 0u, 2u};
+        uint32_t start = 0;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const uint32_t b = band[r];
+            const uint32_t h = min(hi[r], n);
+            c[r] = h > lo[r] ? h - lo[r] : 0u;
+            if (r == 0 && !(i >= lo[0] && i < lo[0] + c[0])) c[0] = 0u;  // inconsistent input: drop
+            shared = shared && (c[r] == 0u || (lo[r] >= b_lo[b] && h <= b_lo[b] + b_cnt[b]));
+            o_s[r] = b * kBandCap + lo[r] - b_lo[b] - start;
+            o_g[r] = lo[r] - start;
+            start += c[r];
+        }
+    }
+    const uint32_t c01 = c[0] + c[1], T = c01 + c[2];
+    const uint32_t tself = c[0] ? i - lo[0] : 0xFFFFFFFFu;
+
+    // verlet_integration (physics.wgsl:262-266)
+    {
+        V3 acc = a.force / a.massv;
+        a.velocity = a.velocity + ((V3{P.gx, P.gy, P.gz} + acc) * P.dt) * P.dt;
+        a.position = a.position + a.velocity;
+    }
+    a.force = splat(0.0f);
+
+    // handle_collisions (physics.wgsl:119-169)
+    V3 old_pos = a.position;
+    if (shared)
+        contact_loop<true>(P, a, b_pos, b_vfme, o_s, c[0], c01, T, tself);
+    else
+        contact_loop<false>(P, a, spos, svfme, o_g, c[0], c01, T, tself);
+    V3 diff = a.position - old_pos;
+    if (len3(diff) > a.scale) {
+        // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337); the
+        // index is the slot inside the sphere's own scene
+        const uint32_t li = i - base_a;
+        uint32_t v = li * (li ^ (li >> 15));
+        const float d = 4294967296.0f;
+        V3 h = {__uint2float_rn(v * 0x1u) / d, __uint2float_rn(v * 0x1FFu) / d,
+                __uint2float_rn(v * 0x3FFFFu) / d};
+        V3 jitter = {h.x * 2.0f - 1.0f, h.y * 2.0f - 1.0f, h.z * 2.0f - 1.0f};
+        a.position = a.position + normalize3(jitter);
+    }
+
+    cube(P, a);
+
+    const float lim = 65504.0f;  // CLAMP_F16
+    a.velocity = {wclamp(a.velocity.x, -lim, lim), wclamp(a.velocity.y, -lim, lim),
+                  wclamp(a.velocity.z, -lim, lim)};
+    a.force = {wclamp(a.force.x, -lim, lim), wclamp(a.force.y, -lim, lim), wclamp(a.force.z, -lim, lim)};
+
+    pos_out[i] = make_float4(a.position.x, a.position.y, a.position.z, a.scale);
+    vfme_out[i] = pack(a);
+    uint32_t nx, nz;
+    cell_of(P, a.position.x, a.position.z, nx, nz);
+    const uint32_t nk = base_c + nz * P.N + nx;
+    keys_out[i] = nk;
+    emit_count(hist, coarse, nk);
+}
+
 // Key of a position (physics.wgsl:115-117).
 __device__ __forceinline__ uint32_t key_of(const PhysParams& P, float4 p) {
     uint32_t cx, cz;
@@ -307,6 +403,7 @@ __global__ void __launch_bounds__(kTileThreads)
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ uint32_t s_lo[3], s_cnt[3];
 
+    griddep_wait();  // the sort's outputs are complete and visible
     const uint32_t tid = threadIdx.x;
     const uint32_t i0 = blockIdx.x * kTileThreads;
     const uint32_t i = i0 + tid;
@@ -418,20 +515,7 @@ __global__ void __launch_bounds__(kTileThreads)
         a = unpack(own_p, own_q);
         cell_of(P, a.position.x, a.position.z, cx, cz);
         key = cz * N + cx;
-        if (mode == kModeLoop) {
-            const uint32_t l = cx > 0u ? 1u : 0u, rr = cx < N - 1u ? 2u : 1u;
-            const uint32_t* of = offs + base_c;
-            lo[0] = __ldg(of + key - l);
-            hi[0] = __ldg(of + key + rr);
-            if (cz > 0u) {
-                lo[1] = __ldg(of + key - N - l);
-                hi[1] = __ldg(of + key - N + rr);
-            }
-            if (cz < N - 1u) {
-                lo[2] = __ldg(of + key + N - l);
-                hi[2] = __ldg(of + key + N + rr);
-            }
-        }
+        if (mode == kModeLoop) row_bounds(N, offs + base_c, key, cx, cz, lo, hi);
     }
     {  // bounded wait for the bands (every thread, so all copies land before exit)
         uint32_t spins = 0;
@@ -453,68 +537,8 @@ __global__ void __launch_bounds__(kTileThreads)
     }
     if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
 
-    // candidate rows in the reference's order: own row (band 1), below (0), above (2)
-    uint32_t c[3], o_s[3], o_g[3];
-    bool shared = true;
-    {
-        const uint32_t band[3] = {1u, 0u, 2u};
-        uint32_t start = 0;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            const uint32_t b = band[r];
-            const uint32_t h = min(hi[r], n);
-            c[r] = h > lo[r] ? h - lo[r] : 0u;
-            if (r == 0 && !(i >= lo[0] && i < lo[0] + c[0])) c[0] = 0u;  // inconsistent input: drop
-            shared = shared && (c[r] == 0u || (lo[r] >= s_lo[b] && h <= s_lo[b] + s_cnt[b]));
-            o_s[r] = b * kBandCap + lo[r] - s_lo[b] - start;
-            o_g[r] = lo[r] - start;
-            start += c[r];
-        }
-    }
-    const uint32_t c01 = c[0] + c[1], T = c01 + c[2];
-    const uint32_t tself = c[0] ? i - lo[0] : 0xFFFFFFFFu;
-
-    // verlet_integration (physics.wgsl:262-266)
-    {
-        V3 acc = a.force / a.massv;
-        a.velocity = a.velocity + ((V3{P.gx, P.gy, P.gz} + acc) * P.dt) * P.dt;
-        a.position = a.position + a.velocity;
-    }
-    a.force = splat(0.0f);
-
-    // handle_collisions (physics.wgsl:119-169)
-    V3 old_pos = a.position;
-    if (shared)
-        contact_loop<true>(P, a, &s_pos[0][0], &s_vfme[0][0], o_s, c[0], c01, T, tself);
-    else
-        contact_loop<false>(P, a, spos, svfme, o_g, c[0], c01, T, tself);
-    V3 diff = a.position - old_pos;
-    if (len3(diff) > a.scale) {
-        // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337); the
-        // index is the slot inside the sphere's own scene
-        const uint32_t li = i - base_a;
-        uint32_t v = li * (li ^ (li >> 15));
-        const float d = 4294967296.0f;
-        V3 h = {__uint2float_rn(v * 0x1u) / d, __uint2float_rn(v * 0x1FFu) / d,
-                __uint2float_rn(v * 0x3FFFFu) / d};
-        V3 jitter = {h.x * 2.0f - 1.0f, h.y * 2.0f - 1.0f, h.z * 2.0f - 1.0f};
-        a.position = a.position + normalize3(jitter);
-    }
-
-    cube(P, a);
-
-    const float lim = 65504.0f;  // CLAMP_F16
-    a.velocity = {wclamp(a.velocity.x, -lim, lim), wclamp(a.velocity.y, -lim, lim),
-                  wclamp(a.velocity.z, -lim, lim)};
-    a.force = {wclamp(a.force.x, -lim, lim), wclamp(a.force.y, -lim, lim), wclamp(a.force.z, -lim, lim)};
-
-    pos_out[i] = make_float4(a.position.x, a.position.y, a.position.z, a.scale);
-    vfme_out[i] = pack(a);
-    uint32_t nx, nz;
-    cell_of(P, a.position.x, a.position.z, nx, nz);
-    const uint32_t nk = base_c + nz * N + nx;
-    keys_out[i] = nk;
-    emit_count(hist, coarse, nk);
+    step_sphere(P, a, i, n, base_a, base_c, lo, hi, &s_pos[0][0], &s_vfme[0][0], s_lo, s_cnt, spos, svfme, pos_out,
+                vfme_out, keys_out, hist, coarse);
 }
 
 __global__ void k_rekey(PhysParams P, uint32_t n, const float4* __restrict__ pos,
@@ -574,12 +598,11 @@ cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t*
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                 const float4* spos, const uint4* svfme, float4* pos_out, uint4* vfme_out,
                                 uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
-                                cudaStream_t st) {
+                                cudaStream_t st, bool pdl) {
     if (!n) return cudaSuccess;
-    k_physics_frame<false><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
-        p, nullptr, nullptr, n, offs, bands, spos, svfme, pos_out, nullptr, vfme_out, nullptr, keys_out, hist, coarse,
-        err);
-    return cudaGetLastError();
+    return launch_pdl(pdl, k_physics_frame<false>, dim3((n + kTileThreads - 1u) / kTileThreads), dim3(kTileThreads),
+                      0, st, p, (const SceneDev*)nullptr, (const uint32_t*)nullptr, n, offs, bands, spos, svfme,
+                      pos_out, (float4*)nullptr, vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
 }
 
 cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
