@@ -8,16 +8,18 @@
 //   1. per-cell counts, accumulated by the physics pass of the previous frame as
 //      it emits the keys (one red.add per sphere);
 //   2. k_cell_scan: one exclusive scan turns the counts into the cell offsets
-//      offs[c] (= start of cell c; offs[C] = n) and a cursor copy, and zeroes the
-//      counts; each 4096-cell tile takes its base from per-tile counts emitted
-//      with the per-cell ones, so tiles never wait on each other;
+//      offs[c] (= start of cell c; offs[C] = n) and a cursor copy; each
+//      1024-cell chunk takes its base from per-4096-cell-tile counts emitted with
+//      the per-cell ones (plus the counts of its tile's earlier chunks), so
+//      chunks never wait on each other;
 //   3. k_cell_scatter: each sphere claims a slot of its cell with one atomic per
 //      run of equal keys in its warp (match.any), so spheres of one warp keep
 //      their order, and its 32-byte state is copied to that slot; the run that
 //      fills a cell last lists the cell if earlier runs of other warps got there
 //      first (only such cells can be out of order);
 //   4. k_cell_fix: the listed cells' slots are put back in ascending input order
-//      (what a stable sort yields), re-gathering their state copy.
+//      (what a stable sort yields), re-gathering their state copy; it also
+//      clears the counts for the next frame.
 //
 // The result is bit-identical to a stable sort; offs[] replaces start/close.
 
@@ -31,25 +33,28 @@ namespace mb {
 namespace {
 
 // ---------------------------------------------------------------- scan
-// Tile t of the scan covers cells [4096 t, 4096 t + 4096).  coarse[t] holds the
-// number of spheres in those cells (emitted with the per-cell counts), so a tile
-// finds its base by summing coarse[0..t) - no look-back, no waiting on other tiles.
+// Block b of the scan covers the chunk of cells [1024 b, 1024 b + 1024) inside
+// tile t = b / 4 (cells [4096 t, 4096 t + 4096)).  coarse[t] holds the number of
+// spheres in tile t (emitted with the per-cell counts), so a chunk finds its base
+// by summing coarse[0..t) and the counts of the tile's cells before it - no
+// look-back, no waiting on other blocks.  The counts are left in place (other
+// chunks read them); the fixup kernel clears them.
 //
 // kScenes (a batch): every scene's cell range is padded to whole tiles, so a tile
 // belongs to one scene; its base is that scene's first slot plus the coarse
 // counts of the scene's earlier tiles, and tiles of HOLD scenes are left alone.
 template <bool kScenes>
 __global__ void __launch_bounds__(kScanThreads)
-    k_cell_scan(uint32_t* __restrict__ hist, const uint32_t* __restrict__ coarse, uint32_t cells,
+    k_cell_scan(const uint32_t* __restrict__ hist, const uint32_t* __restrict__ coarse, uint32_t cells,
                 uint32_t* __restrict__ offs, uint32_t* __restrict__ cursor, uint32_t* fix_ctl,
                 const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ cell_tile_scene) {
     constexpr int W = kScanThreads / 32;
     __shared__ uint32_t s_warp[W], s_base[W];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t tile = blockIdx.x;
+    const uint32_t chunk = blockIdx.x, c0 = chunk * kScanChunk, tile = c0 / kScanTile;
     griddep_launch();
-    if (tile == 0 && tid < (uint32_t)kFixLists) fix_ctl[tid] = 0u;  // fixup lists of this frame start empty
-    const uint32_t base = tile * kScanTile + tid * kScanItems;
+    if (chunk == 0 && tid < (uint32_t)kFixLists) fix_ctl[tid] = 0u;  // fixup lists of this frame start empty
+    const uint32_t base = c0 + tid * kScanItems;
 
     uint32_t first_tile = 0, base_slot = 0;
     if (kScenes) {
@@ -58,9 +63,14 @@ __global__ void __launch_bounds__(kScanThreads)
         first_tile = __ldg(&scenes[sc].cell_base) / kScanTile;
         base_slot = __ldg(&scenes[sc].agent_base);
     }
-    // exclusive base of this tile: sum of the coarse counts of the earlier tiles
+    // exclusive base of this chunk: the coarse counts of the earlier tiles, plus
+    // the counts of the tile's cells before the chunk
     uint32_t bsum = 0;
     for (uint32_t t = first_tile + tid; t < tile; t += kScanThreads) bsum += __ldg(coarse + t);
+    for (uint32_t c = tile * kScanTile + tid * 4u; c < c0; c += kScanThreads * 4u) {
+        const uint4 x = __ldcg(reinterpret_cast<const uint4*>(hist + c));
+        bsum += (x.x + x.y) + (x.z + x.w);
+    }
 
     uint32_t v[kScanItems];
     if (base + kScanItems <= cells) {
@@ -100,7 +110,6 @@ __global__ void __launch_bounds__(kScanThreads)
     if (base + kScanItems <= cells) {
         uint4* o4 = reinterpret_cast<uint4*>(offs + base);
         uint4* c4 = reinterpret_cast<uint4*>(cursor + base);
-        uint4* h4 = reinterpret_cast<uint4*>(hist + base);
 #pragma unroll
         for (int q = 0; q < kScanItems / 4; ++q) {
             uint4 x;
@@ -110,7 +119,6 @@ __global__ void __launch_bounds__(kScanThreads)
             x.w = run; run += v[4 * q + 3];
             o4[q] = x;
             c4[q] = x;
-            h4[q] = make_uint4(0u, 0u, 0u, 0u);
         }
         // end of the tile: the next tile's first offset, or the scene's / table's end
         if (base + kScanItems == cells || (kScenes && tid == kScanThreads - 1)) offs[base + kScanItems] = run;
@@ -120,7 +128,6 @@ __global__ void __launch_bounds__(kScanThreads)
             if (c < cells) {
                 offs[c] = run;
                 cursor[c] = run;
-                hist[c] = 0u;
                 run += v[q];
                 if (c + 1u == cells) offs[cells] = run;
             }
@@ -136,22 +143,28 @@ struct FixLists {
     uint32_t cap[kFixLists];
 };
 
-// Called by every thread of the block (block-uniform loop): `cls` is the list the
-// thread appends `cell` to, or -1.
-__device__ __forceinline__ void push_fix(const FixLists& L, int cls, uint32_t cell) {
+// Called by every thread of the block (block-uniform loop): cls[u] is the list
+// the thread appends cell[u] to, or -1.
+template <int kItems>
+__device__ __forceinline__ void push_fix(const FixLists& L, const int (&cls)[kItems], const uint32_t (&cell)[kItems]) {
     __shared__ uint32_t s_n[kFixLists], s_base[kFixLists];
     if (threadIdx.x < (uint32_t)kFixLists) s_n[threadIdx.x] = 0u;
     __syncthreads();
-    uint32_t at = 0;
-    if (cls >= 0) at = atomicAdd(&s_n[cls], 1u);
+    uint32_t at[kItems];
+#pragma unroll
+    for (int u = 0; u < kItems; ++u) at[u] = cls[u] >= 0 ? atomicAdd(&s_n[cls[u]], 1u) : 0u;
     __syncthreads();
     if (threadIdx.x < (uint32_t)kFixLists && s_n[threadIdx.x])
         s_base[threadIdx.x] = atomicAdd(L.ctl + threadIdx.x, s_n[threadIdx.x]);
     __syncthreads();
-    if (cls >= 0) {  // lists hold every cell that can qualify; the bound only guards bad counts
-        uint32_t* list = cls == kFixListSmall ? L.list[0] : (cls == kFixListWarp ? L.list[1] : L.list[2]);
-        const uint32_t cap = cls == kFixListSmall ? L.cap[0] : (cls == kFixListWarp ? L.cap[1] : L.cap[2]);
-        if (s_base[cls] + at < cap) list[s_base[cls] + at] = cell;
+#pragma unroll
+    for (int u = 0; u < kItems; ++u) {
+        const int c = cls[u];
+        if (c >= 0) {  // lists hold every cell that can qualify; the bound only guards bad counts
+            uint32_t* list = c == kFixListSmall ? L.list[0] : (c == kFixListWarp ? L.list[1] : L.list[2]);
+            const uint32_t cap = c == kFixListSmall ? L.cap[0] : (c == kFixListWarp ? L.cap[1] : L.cap[2]);
+            if (s_base[c] + at[u] < cap) list[s_base[c] + at[u]] = cell[u];
+        }
     }
 }
 
@@ -199,7 +212,11 @@ __global__ void __launch_bounds__(256)
             cls = fix_class(offs, k, b, (uint32_t)__popc(peers));
         }
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
-        push_fix(fix, cls, k);
+        {
+            const int c1[1] = {cls};
+            const uint32_t k1[1] = {k};
+            push_fix<1>(fix, c1, k1);
+        }
         if (valid) {
             const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
             perm[dst] = i;
@@ -249,7 +266,11 @@ __global__ void __launch_bounds__(256)
             cls = fix_class(offs, k, b, (uint32_t)__popc(peers));
         }
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
-        push_fix(fix, cls, k);
+        {
+            const int c1[1] = {cls};
+            const uint32_t k1[1] = {k};
+            push_fix<1>(fix, c1, k1);
+        }
         if (valid) {
             const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
             perm[dst] = i;
@@ -344,7 +365,8 @@ __device__ __forceinline__ void regather(const Src& src, const uint32_t* perm, u
 
 template <class Src>
 __global__ void __launch_bounds__(kFixThreads)
-    k_cell_fix(const uint32_t* __restrict__ offs, uint32_t* perm, uint32_t* __restrict__ coarse, uint32_t tiles,
+    k_cell_fix(const uint32_t* __restrict__ offs, uint32_t* perm, uint32_t* __restrict__ hist, uint32_t cells,
+               uint32_t* __restrict__ coarse, uint32_t tiles,
                FixLists lists, uint32_t* __restrict__ tmp, Src src,
                float4* __restrict__ spos, uint4* __restrict__ svfme) {
     __shared__ uint32_t s_v[kBitmapWords];
@@ -352,9 +374,12 @@ __global__ void __launch_bounds__(kFixThreads)
     griddep_wait();
     griddep_launch();
     const uint32_t tid = threadIdx.x, lane = tid & 31u;
-    if (blockIdx.x == 0)  // the scan of this frame is over: clear the tile counts for the next one
+    // the scan of this frame is over: clear the cell and tile counts for the next one
+    if (blockIdx.x == 0)
         for (uint32_t t = tid; t < tiles; t += blockDim.x)
             if (src.tile_active(t)) coarse[t] = 0u;
+    for (uint32_t c = (blockIdx.x * blockDim.x + tid) * 4u; c < cells; c += gridDim.x * blockDim.x * 4u)
+        if (src.tile_active(c / kScanTile)) *reinterpret_cast<uint4*>(hist + c) = make_uint4(0u, 0u, 0u, 0u);
 
     const uint32_t* __restrict__ small = lists.list[0];
     const uint32_t* __restrict__ mid = lists.list[1];
@@ -605,8 +630,8 @@ cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, c
 
 cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st) {
     (void)ctl;
-    uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
-    k_cell_scan<false><<<tiles, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.fix_ctl,
+    const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
+    k_cell_scan<false><<<chunks, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.fix_ctl,
                                                        nullptr, nullptr);
     return cudaGetLastError();
 }
@@ -623,13 +648,13 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
     }
     OneBuffer src{pos_in, vfme_in};
     return launch_pdl(pdl && n, k_cell_fix<OneBuffer>, dim3(fix_blocks()), dim3(kFixThreads), 0, st, offs, perm,
-                      s.coarse, scan_tiles(cells), fix_lists(s), s.fix_tmp, src, spos, svfme);
+                      s.hist, cells, s.coarse, scan_tiles(cells), fix_lists(s), s.fix_tmp, src, spos, svfme);
 }
 
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
                               uint32_t cells, uint32_t* offs, cudaStream_t st) {
-    uint32_t tiles = (cells + kScanTile - 1u) / kScanTile;
-    k_cell_scan<true><<<tiles, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.fix_ctl, scenes,
+    const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
+    k_cell_scan<true><<<chunks, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.fix_ctl, scenes,
                                                       cell_tile_scene);
     return cudaGetLastError();
 }
@@ -648,7 +673,8 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
         if ((e = cudaGetLastError())) return e;
     }
     SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
-    k_cell_fix<SceneBuffers><<<fix_blocks(), kFixThreads, 0, st>>>(offs, perm, s.coarse, scan_tiles(cells),
+    k_cell_fix<SceneBuffers><<<fix_blocks(), kFixThreads, 0, st>>>(offs, perm, s.hist, cells, s.coarse,
+                                                                   scan_tiles(cells),
                                                                    fix_lists(s), s.fix_tmp, src, spos, svfme);
     return cudaGetLastError();
 }

@@ -196,8 +196,10 @@ cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_sc
 
 // Counting sort of cell keys (mb_count.cu).
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 16;
-constexpr uint32_t kScanTile = kScanThreads * kScanItems;
+constexpr int kScanItems = 4;
+constexpr uint32_t kScanChunk = kScanThreads * kScanItems;  // cells per block of the scan
+constexpr uint32_t kScanTile = 4096;                        // cells per coarse count (tile base)
+static_assert(kScanTile % kScanChunk == 0, "scan chunks tile the coarse tiles");
 
 // Cells the scatter filled from several warp runs are listed for the in-cell
 // fixup by size: up to kFixSmall slots (a thread each), up to kFixWarp (a warp
@@ -228,14 +230,15 @@ cudaError_t count_keys(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
                        cudaStream_t st);
 // hist := counts of n all-zero keys (a fresh upload).
 cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, cudaStream_t st);
-// offs[0..cells] := exclusive scan of hist (offs[cells] = n), cursors := offs, hist := 0.
+// offs[0..cells] := exclusive scan of hist (offs[cells] = n), cursors := offs; the
+// counts are cleared later in the frame by the fixup of count_scatter.
 cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st);
 // INIT frame after an upload (all keys 0): perm := identity, offs := [0, n, .., n], hist := 0.
 cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32_t* offs, uint32_t* perm,
                              cudaStream_t st);
 // perm := stable permutation sorting keys by cell, from the cursors of count_scan;
 // spos/svfme := the state in that order (spos[j] = pos_in[perm[j]]); bands
-// (nullable) := the band table of that order for an N x N grid.
+// (nullable) := the band table of that order for an N x N grid; hist, coarse := 0.
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
                           float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,
