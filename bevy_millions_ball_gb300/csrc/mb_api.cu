@@ -174,10 +174,11 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
     }
     if ((e = mark(w, 2, st, capturing))) return e;
     int nxt = cur ^ 1;
-    if (init)
+    if (init) {
         e = mb::launch_physics_init(w->P, w->n, w->perm, w->pos[cur], w->vfme[cur], w->pos[nxt],
                                     w->vfme[nxt], w->keys, hist, coarse, st);
-    else
+        if (!e && hist) e = mb::count_tile_counts(w->cnt, w->cells, st);
+    } else
         e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->spos, w->svfme, w->pos[nxt],
                                     w->vfme[nxt], w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError, st,
                                     pdl && counting(w));
@@ -365,6 +366,7 @@ mb_status mb_set_settings(mb_world* w, const mb_settings* s) {
             uint32_t* coarse = counting(w) ? w->cnt.coarse : nullptr;
             if (hist) e = mb::count_clear(w->cnt, w->cells, w->stream);
             if (!e) e = mb::launch_rekey(w->P, w->n, w->pos[w->cur], w->keys, hist, coarse, w->stream);
+            if (!e && hist) e = mb::count_tile_counts(w->cnt, w->cells, w->stream);
         }
         if (e) return cuda_fail(w, "mb_set_settings", e);
     }

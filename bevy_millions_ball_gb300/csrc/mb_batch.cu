@@ -260,6 +260,8 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st) {
                                       b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->keys, b->cnt.hist,
                                       b->cnt.coarse, b->ctl + mb::kCtlError, st)))
         return e;
+    // INIT scenes emitted cell counts only: their tile counts from the cell counts
+    if ((e = mb::count_tile_counts_scenes(b->cnt, b->d_scenes, b->d_cell_tile_scene, b->cells_total, st))) return e;
     const uint32_t S = (uint32_t)b->scenes.size();
     k_flip_parity<<<(S + 127u) / 128u, 128, 0, st>>>(b->d_scenes, S);
     return cudaGetLastError();
@@ -673,7 +675,9 @@ mb_status mb_server_create(const mb_server_config* cfg, void* cuda_stream, mb_se
         const uint64_t fixed = bytes_for(0, 0, cfg->max_scenes);
         const uint64_t per = 104u + 2u * 16u + 1u;  // a sphere and two cells, plus tile tables
         agents = budget > fixed ? std::min<uint64_t>((budget - fixed) / per, mb::kMaxAgents) : 0u;
-        cells = std::min<uint64_t>(2u * agents, mb::kMaxCells);
+        // room for each scene's padding to whole scan tiles inside the 2^28-cell key space
+        const uint64_t pad = (uint64_t)std::max<uint32_t>(cfg->max_scenes, 1u) * (mb::kScanTile - 1u);
+        cells = std::min<uint64_t>(2u * agents, mb::kMaxCells > pad ? mb::kMaxCells - pad : 0u);
     }
     if (bytes_for(agents, cells, cfg->max_scenes) > budget)
         return bfail(nullptr, MB_ERR_BUDGET_EXCEEDED, "configured capacity exceeds the memory budget");

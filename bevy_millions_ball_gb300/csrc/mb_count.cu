@@ -531,6 +531,36 @@ __global__ void k_init_order(uint32_t n, uint32_t cells, uint32_t* perm, uint32_
     }
 }
 
+// ---------------------------------------------------------------- tile counts
+// coarse[t] := sum of hist over tile t's 4096 cells, one block per tile; for a
+// batch only the tiles of scenes in their INIT frame (the others' tile counts
+// are emitted by their LOOP pass or kept while they are held).
+template <bool kScenes>
+__global__ void __launch_bounds__(256)
+    k_tile_counts(const uint32_t* __restrict__ hist, uint32_t cells, uint32_t* __restrict__ coarse,
+                  const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ cell_tile_scene) {
+    __shared__ uint32_t s_red[8];
+    const uint32_t t = blockIdx.x, tid = threadIdx.x;
+    if (kScenes && __ldg(&scenes[__ldg(cell_tile_scene + t)].mode) != kModeInit) return;
+    uint32_t sum = 0;
+    for (uint32_t c = t * kScanTile + tid * 4u; c < min((t + 1u) * kScanTile, cells); c += 1024u) {
+        if (c + 4u <= cells) {
+            const uint4 x = __ldcg(reinterpret_cast<const uint4*>(hist + c));
+            sum += (x.x + x.y) + (x.z + x.w);
+        } else {
+            for (uint32_t q = c; q < cells; ++q) sum += __ldcg(hist + q);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, o);
+    if ((tid & 31u) == 0u) s_red[tid >> 5] = sum;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t total = 0;
+        for (int w = 0; w < 8; ++w) total += s_red[w];
+        coarse[t] = total;
+    }
+}
+
 // ---------------------------------------------------------------- counting
 // hist[keys[i]] += 1 for every sphere, one atomic per run of equal keys in a warp.
 __global__ void __launch_bounds__(256)
@@ -676,6 +706,19 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
     k_cell_fix<SceneBuffers><<<fix_blocks(), kFixThreads, 0, st>>>(offs, perm, s.hist, cells, s.coarse,
                                                                    scan_tiles(cells),
                                                                    fix_lists(s), s.fix_tmp, src, spos, svfme);
+    return cudaGetLastError();
+}
+
+cudaError_t count_tile_counts(CountScratch& s, uint32_t cells, cudaStream_t st) {
+    if (!cells) return cudaSuccess;
+    k_tile_counts<false><<<scan_tiles(cells), 256, 0, st>>>(s.hist, cells, s.coarse, nullptr, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t count_tile_counts_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
+                                     uint32_t cells, cudaStream_t st) {
+    if (!cells) return cudaSuccess;
+    k_tile_counts<true><<<scan_tiles(cells), 256, 0, st>>>(s.hist, cells, s.coarse, scenes, cell_tile_scene);
     return cudaGetLastError();
 }
 

@@ -170,7 +170,8 @@ __device__ __forceinline__ void write_band_bounds(uint4* __restrict__ bands, con
 
 // Physics passes.  `hist` / `coarse` (nullable together) accumulate the per-cell
 // and per-4096-cell-tile counts of the keys they emit, for the next frame's
-// counting sort.
+// counting sort; the INIT pass and re-keying emit cell counts only (their tile
+// counts come from count_tile_counts).
 cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t* perm,
                                 const float4* pos_in, const uint4* vfme_in, float4* pos_out,
                                 uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse,
@@ -233,6 +234,11 @@ cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, c
 // offs[0..cells] := exclusive scan of hist (offs[cells] = n), cursors := offs; the
 // counts are cleared later in the frame by the fixup of count_scatter.
 cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st);
+// coarse[t] := sum of hist over scan tile t (after a pass that emitted cell counts
+// only: INIT frames, re-keying); the batched form touches only INIT scenes' tiles.
+cudaError_t count_tile_counts(CountScratch& s, uint32_t cells, cudaStream_t st);
+cudaError_t count_tile_counts_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
+                                     uint32_t cells, cudaStream_t st);
 // INIT frame after an upload (all keys 0): perm := identity, offs := [0, n, .., n], hist := 0.
 cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32_t* offs, uint32_t* perm,
                              cudaStream_t st);

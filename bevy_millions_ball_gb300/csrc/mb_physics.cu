@@ -166,8 +166,17 @@ __device__ __forceinline__ void cube(const PhysParams& P, Agent& a) {
     }
 }
 
+// Count of the emitted key's cell only: for keys in no particular order (INIT
+// frames, re-keying), whose per-tile counts are summed from the cell counts
+// afterwards (count_tile_counts) instead of thousands of lanes contending for a
+// few tile counters.
+__device__ __forceinline__ void emit_cell(uint32_t* hist, uint32_t key) {
+    if (hist) atomicAdd(hist + key, 1u);
+}
+
 // Counts of the emitted key for the next frame's counting sort: the cell, and the
-// 4096-cell scan tile (one atomic per run of equal tiles among the active lanes).
+// 4096-cell scan tile (one atomic per run of equal tiles among the active lanes;
+// the keys of a LOOP pass follow the sorted order, so a warp's keys share tiles).
 __device__ __forceinline__ void emit_count(uint32_t* hist, uint32_t* coarse, uint32_t key) {
     if (!hist) return;
     atomicAdd(hist + key, 1u);
@@ -195,7 +204,7 @@ __global__ void __launch_bounds__(256)
     vfme_out[i] = pack(a);
     uint32_t key = cz * P.N + cx;
     keys_out[i] = key;
-    emit_count(hist, coarse, key);
+    emit_cell(hist, key);
 }
 
 // Neighbour row-bands of a tile of sorted slots.  Band b (row offset b-1 = -1, 0,
@@ -532,7 +541,7 @@ __global__ void __launch_bounds__(kTileThreads)
         pos_out[i] = own_p;
         vfme_out[i] = pack(a);
         keys_out[i] = base_c + key;
-        emit_count(hist, coarse, base_c + key);
+        emit_cell(hist, base_c + key);  // tile counts of INIT scenes: count_tile_counts
         return;
     }
     if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
@@ -550,7 +559,7 @@ __global__ void k_rekey(PhysParams P, uint32_t n, const float4* __restrict__ pos
     uint32_t cx, cz;
     cell_of(P, p.x, p.z, cx, cz);
     keys[i] = cz * P.N + cx;
-    emit_count(hist, coarse, keys[i]);
+    emit_cell(hist, keys[i]);
 }
 
 }  // namespace

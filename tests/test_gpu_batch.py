@@ -151,3 +151,16 @@ def test_server_rejects_over_budget(built_lib, cuda):
         p, _ = srv.get_state(h_small)
         rp, _, _ = alone(small, 5)
         np.testing.assert_array_equal(p.view(np.uint32), rp.view(np.uint32))
+
+
+def test_server_with_budget_beyond_the_key_space(built_lib, cuda):
+    """A budget large enough for more than 2^28 spheres is capped to the key space
+    (spheres and cells, with each scene's tile padding) instead of failing."""
+    sc = scenes.plain_uniform(3000, 64, seed=21)
+    with Server(budget_bytes=40 << 30, max_scenes=64) as srv:
+        h, r = srv.create(sc.plugin, sc.pos_scale, sc.vfme)
+        srv.wait(r)
+        srv.wait(srv.advance(h, 5))
+        p, _ = srv.get_state(h)
+        rp, _, _ = alone(sc, 6)
+        np.testing.assert_array_equal(p.view(np.uint32), rp.view(np.uint32))
