@@ -493,6 +493,8 @@ def run_serving(args):
                                "[4096, 1048576], advances k ~ U{1..64}, 120 GB budget",
                    "scenes": n_scenes},
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "busy": {"value": st.agent_steps / max(st.busy_seconds, 1e-9), "seconds": st.busy_seconds,
+                 "what": "agent-steps over the time the server's worker had frames on the GPU"},
         "plain_loop": {"value": steps_done / t_plain,
                        "latency_s": {"p50": float(np.percentile(plain_lat, 50)),
                                      "p99": float(np.percentile(plain_lat, 99))},

@@ -609,19 +609,13 @@ void worker_loop(mb_server* s) {
             }
         }
         s->cv_done.notify_all();
-        // frames while the active set is unchanged (up to 16, INIT frames alone)
+        // a round of up to 16 frames; each frame runs the scenes that still have
+        // frames owed (INIT first after an upload), the others are held
         const size_t S = b->scenes.size();
         int64_t frames = 0;
-        {
-            int64_t m = 16;
-            bool any = false;
-            for (size_t i = 0; i < S; ++i) {
-                const ServerScene& sc = s->sscenes[s->pool_handle[i]];
-                if (!sc.admitted || sc.pending <= 0) continue;
-                any = true;
-                m = std::min<int64_t>(m, b->scenes[i].init_pending ? 1 : sc.pending);
-            }
-            frames = any ? m : 0;
+        for (size_t i = 0; i < S; ++i) {
+            const ServerScene& sc = s->sscenes[s->pool_handle[i]];
+            if (sc.admitted && sc.pending > 0) frames = std::max<int64_t>(frames, std::min<int64_t>(sc.pending, 16));
         }
         if (frames == 0) continue;
         const auto t0 = Clock::now();
