@@ -71,6 +71,7 @@ struct mb_world {
     bool has_state = false;
     bool frame_done = false;           // a frame ran since the last upload
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t chain[2] = {nullptr, nullptr};  // kChainFrames LOOP frames from each parity
     bool profiling = false;
     cudaEvent_t prof_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::string err;
@@ -114,11 +115,16 @@ bool mb::settings_valid(const mb_settings* s, std::string& why) {
 namespace {
 using mb::settings_valid;
 
+// LOOP frames captured back to back in one graph for multi-frame steps (even, so
+// a chain ends in the parity it started from).
+constexpr uint32_t kChainFrames = 8;
+
 void drop_graphs(mb_world* w) {
-    for (auto& g : w->graph) {
-        if (g) cudaGraphExecDestroy(g);
-        g = nullptr;
-    }
+    for (auto* set : {w->graph, w->chain})
+        for (int i = 0; i < 2; ++i) {
+            if (set[i]) cudaGraphExecDestroy(set[i]);
+            set[i] = nullptr;
+        }
 }
 
 void apply_settings(mb_world* w, const mb_settings& s) {
@@ -140,8 +146,10 @@ cudaError_t mark(mb_world* w, int i, cudaStream_t st, bool capturing) {
 bool counting(const mb_world* w) { return w->tuning.sort_algorithm == MB_SORT_COUNTING; }
 
 // Enqueue one frame on `st`.  Profiling marks: [0] frame start, [1] after the
-// first ordering stage, [2] after the second, [3] after physics.
-cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool capturing = false) {
+// first ordering stage, [2] after the second, [3] after physics.  `chained`: the
+// frame follows another frame in the same capture.
+cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool capturing = false,
+                          bool chained = false) {
     cudaError_t e;
     // kernels after the first start while their predecessor drains (programmatic
     // dependent launch) in captured LOOP frames without profiling marks between them
@@ -157,7 +165,7 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         coarse = w->cnt.coarse;
     } else if (counting(w)) {
         // cell offsets first (scan of the counts), then the permutation
-        if ((e = mb::count_scan(w->cnt, w->scratch.ctl, w->cells, w->scratch.offs, st))) return e;
+        if ((e = mb::count_scan(w->cnt, w->scratch.ctl, w->cells, w->scratch.offs, st, pdl && chained))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
         if ((e = mb::count_scatter(w->cnt, w->keys, w->n, w->cells, w->scratch.offs, w->perm, w->pos[cur],
                                    w->vfme[cur], w->spos, w->svfme, w->bands, w->P.N, st, pdl)))
@@ -193,10 +201,13 @@ cudaError_t recount(mb_world* w) {
     return mb::count_keys(w->cnt, w->keys, w->n, w->cells, w->stream);
 }
 
-cudaError_t build_graph(mb_world* w, int cur) {
+// One LOOP frame (frames = 1, into graph[cur]) or a chain of kChainFrames LOOP
+// frames (into chain[cur]) captured from parity `cur`.
+cudaError_t build_graph(mb_world* w, int cur, uint32_t frames = 1) {
     cudaError_t e = cudaStreamBeginCapture(w->cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e) return e;
-    cudaError_t fe = enqueue_frame(w, w->cap_stream, cur, false, true);
+    cudaError_t fe = cudaSuccess;
+    for (uint32_t f = 0; f < frames && !fe; ++f) fe = enqueue_frame(w, w->cap_stream, cur ^ (int)(f & 1u), false, true, f > 0);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(w->cap_stream, &g);
     if (fe) {
@@ -204,7 +215,7 @@ cudaError_t build_graph(mb_world* w, int cur) {
         return fe;
     }
     if (e) return e;
-    e = cudaGraphInstantiate(&w->graph[cur], g, 0);
+    e = cudaGraphInstantiate(frames == 1 ? &w->graph[cur] : &w->chain[cur], g, 0);
     cudaGraphDestroy(g);
     return e;
 }
@@ -418,9 +429,17 @@ mb_status mb_step(mb_world* w, uint32_t k) {
     if (!w->has_state) return fail(w, MB_ERR_NOT_READY, "no state uploaded");
     if (!w->s.enable_simulation) return MB_OK;
     cudaError_t e;
-    for (uint32_t f = 0; f < k; ++f) {
+    for (uint32_t f = 0; f < k;) {
         if (w->time == 0) {
             if ((e = enqueue_frame(w, w->stream, w->cur, true))) return cuda_fail(w, "mb_step(init)", e);
+        } else if (k - f >= kChainFrames && !w->profiling) {  // a chain of LOOP frames, one launch
+            if (!w->chain[w->cur] && (e = build_graph(w, w->cur, kChainFrames)))
+                return cuda_fail(w, "mb_step(capture)", e);
+            if ((e = cudaGraphLaunch(w->chain[w->cur], w->stream))) return cuda_fail(w, "mb_step", e);
+            f += kChainFrames;
+            w->time += kChainFrames;
+            w->frame_done = true;
+            continue;
         } else {
             if (!w->graph[w->cur] && (e = build_graph(w, w->cur)))
                 return cuda_fail(w, "mb_step(capture)", e);
@@ -429,6 +448,7 @@ mb_status mb_step(mb_world* w, uint32_t k) {
         w->cur ^= 1;
         w->time += 1;
         w->frame_done = true;
+        ++f;
     }
     return MB_OK;
 }

@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
+#include <cstdint>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -86,6 +88,7 @@ struct mb_batch {
     uint4* vfme[2] = {nullptr, nullptr};
     float4* spos = nullptr;
     uint4* svfme = nullptr;
+    uint4* bands = nullptr;  // band table of the sorted order (written by the batched scatter)
     uint32_t *keys = nullptr, *perm = nullptr, *offs = nullptr, *ctl = nullptr, *d_tile_scene = nullptr;
     uint32_t* d_cell_tile_scene = nullptr;  // scene of each 4096-cell scan tile
     uint32_t* h_cell_tile_scene = nullptr;  // pinned
@@ -123,9 +126,9 @@ void drop_graphs(mb_batch* b) {
 }
 
 uint64_t bytes_for(uint64_t agents, uint64_t cells, uint64_t scenes) {
-    // state x2, sorted copy, keys, perm; offs; counts, cursors, fixup lists; tables
+    // state x2, sorted copy, keys, perm; offs; counts, cursors, fixup lists; tile and band tables
     return agents * (32u * 3u + 8u) + cells * 4u + mb::count_scratch_bytes((uint32_t)cells, (uint32_t)agents) +
-           scenes * sizeof(mb::SceneDev) + (agents / kTile + 1u) * 4u + 64u * 1024u;
+           scenes * sizeof(mb::SceneDev) + (agents / kTile + 1u) * (4u + 32u) + 64u * 1024u;
 }
 
 cudaError_t alloc_pool(mb_batch* b) {
@@ -138,6 +141,7 @@ cudaError_t alloc_pool(mb_batch* b) {
     }
     if ((e = cudaMalloc(&b->spos, sizeof(float4) * A))) return e;
     if ((e = cudaMalloc(&b->svfme, sizeof(uint4) * A))) return e;
+    if ((e = cudaMalloc(&b->bands, sizeof(uint4) * mb::band_table_entries((uint32_t)A)))) return e;
     if ((e = cudaMalloc(&b->keys, sizeof(uint32_t) * A))) return e;
     if ((e = cudaMalloc(&b->perm, sizeof(uint32_t) * A))) return e;
     if ((e = cudaMalloc(&b->offs, sizeof(uint32_t) * (Cc + 1u)))) return e;
@@ -162,6 +166,7 @@ void free_pool(mb_batch* b) {
     }
     cudaFree(b->spos);
     cudaFree(b->svfme);
+    cudaFree(b->bands);
     cudaFree(b->keys);
     cudaFree(b->perm);
     cudaFree(b->offs);
@@ -254,9 +259,9 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st) {
         return e;
     if ((e = mb::count_scatter_scenes(b->cnt, b->d_scenes, b->d_tile_scene, b->d_cell_tile_scene, b->keys, b->n_total,
                                       b->cells_total, b->offs, b->perm, b->pos[0], b->pos[1], b->vfme[0],
-                                      b->vfme[1], b->spos, b->svfme, st)))
+                                      b->vfme[1], b->spos, b->svfme, b->bands, st)))
         return e;
-    if ((e = mb::launch_physics_batch(b->d_scenes, b->d_tile_scene, b->n_total, b->offs, b->spos, b->svfme,
+    if ((e = mb::launch_physics_batch(b->d_scenes, b->d_tile_scene, b->n_total, b->offs, b->bands, b->spos, b->svfme,
                                       b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->keys, b->cnt.hist,
                                       b->cnt.coarse, b->ctl + mb::kCtlError, st)))
         return e;
@@ -267,10 +272,15 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t build_graph(mb_batch* b) {
+// graph[0]: one frame; graph[1]: kChainFrames frames back to back (used while no
+// scene changes mode; even, so every scene ends in the buffer it started from).
+constexpr uint32_t kChainFrames = 8;
+
+cudaError_t build_graph(mb_batch* b, int which = 0) {
     cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e) return e;
-    cudaError_t fe = enqueue_frame(b, b->cap_stream);
+    cudaError_t fe = cudaSuccess;
+    for (uint32_t f = 0; f < (which ? kChainFrames : 1u) && !fe; ++f) fe = enqueue_frame(b, b->cap_stream);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(b->cap_stream, &g);
     if (fe) {
@@ -278,7 +288,7 @@ cudaError_t build_graph(mb_batch* b) {
         return fe;
     }
     if (e) return e;
-    e = cudaGraphInstantiate(&b->graph[0], g, 0);
+    e = cudaGraphInstantiate(&b->graph[which], g, 0);
     cudaGraphDestroy(g);
     return e;
 }
@@ -290,19 +300,21 @@ cudaError_t recount(mb_batch* b) {
     return e;
 }
 
-// One frame over every scene; modes[i] is scene i's mode for this frame.
-mb_status run_frame(mb_batch* b, const std::vector<uint32_t>& modes) {
+// One frame over every scene (frames = 1), or kChainFrames frames with the same
+// modes and no INIT among them (frames = kChainFrames); modes[i] is scene i's mode.
+mb_status run_frame(mb_batch* b, const std::vector<uint32_t>& modes, uint32_t frames = 1) {
     cudaError_t e;
+    const int which = frames == 1 ? 0 : 1;
     if (!b->counts_valid && (e = recount(b))) return bcuda(b, "batch recount", e);
     if ((e = sync_tables(b, modes))) return bcuda(b, "batch tables", e);
-    if (!b->graph[0] && (e = build_graph(b))) return bcuda(b, "batch capture", e);
-    if ((e = cudaGraphLaunch(b->graph[0], b->stream))) return bcuda(b, "batch frame", e);
+    if (!b->graph[which] && (e = build_graph(b, which))) return bcuda(b, "batch capture", e);
+    if ((e = cudaGraphLaunch(b->graph[which], b->stream))) return bcuda(b, "batch frame", e);
     for (size_t i = 0; i < b->scenes.size(); ++i) {
         SceneHost& h = b->scenes[i];
         if (modes[i] != mb::kModeHold) {
-            h.time += 1;
+            h.time += frames;
             h.frame_done = true;
-            h.parity ^= 1u;  // mirrors k_flip_parity
+            h.parity ^= frames & 1u;  // mirrors k_flip_parity
         }
         if (modes[i] == mb::kModeInit) h.init_pending = false;
     }
@@ -428,14 +440,18 @@ mb_status mb_batch_step(mb_batch* b, uint32_t k) {
     for (const SceneHost& h : b->scenes)
         if (!h.has_state) return bfail(b, MB_ERR_NOT_READY, "every scene needs a state before stepping");
     std::vector<uint32_t> modes(b->scenes.size());
-    for (uint32_t f = 0; f < k; ++f) {
+    for (uint32_t f = 0; f < k;) {
+        bool init = false;
         for (size_t i = 0; i < b->scenes.size(); ++i) {
             const SceneHost& h = b->scenes[i];
             const bool run = h.active && h.s.enable_simulation;
             modes[i] = !run ? mb::kModeHold : (h.init_pending ? mb::kModeInit : mb::kModeLoop);
+            init = init || modes[i] == mb::kModeInit;
         }
-        mb_status st = run_frame(b, modes);
+        const uint32_t frames = (!init && k - f >= kChainFrames) ? kChainFrames : 1u;
+        mb_status st = run_frame(b, modes, frames);
         if (st != MB_OK) return st;
+        f += frames;
     }
     return MB_OK;
 }
@@ -621,19 +637,29 @@ void worker_loop(mb_server* s) {
         const auto t0 = Clock::now();
         uint64_t agent_steps = 0;
         modes.assign(S, mb::kModeHold);
-        for (int64_t f = 0; f < frames; ++f) {
+        for (int64_t f = 0; f < frames;) {
+            bool init = false;
+            int64_t least = INT64_MAX;  // fewest frames owed by a scene that runs
             for (size_t i = 0; i < S; ++i) {
                 const ServerScene& sc = s->sscenes[s->pool_handle[i]];
                 const bool run = sc.admitted && sc.pending > 0 && b->scenes[i].s.enable_simulation;
                 modes[i] = !run ? mb::kModeHold : (b->scenes[i].init_pending ? mb::kModeInit : mb::kModeLoop);
-                if (modes[i] == mb::kModeLoop) agent_steps += b->scenes[i].n;
+                init = init || modes[i] == mb::kModeInit;
+                if (run) least = std::min<int64_t>(least, sc.pending);
             }
-            if (run_frame(b, modes) != MB_OK) {
+            // a chain of frames while every running scene owes that many and none is new
+            const uint32_t chain = (!init && least >= (int64_t)kChainFrames && frames - f >= (int64_t)kChainFrames)
+                                       ? kChainFrames
+                                       : 1u;
+            for (size_t i = 0; i < S; ++i)
+                if (modes[i] == mb::kModeLoop) agent_steps += (uint64_t)b->scenes[i].n * chain;
+            if (run_frame(b, modes, chain) != MB_OK) {
                 s->err = b->err;
                 break;
             }
             for (size_t i = 0; i < S; ++i)
-                if (modes[i] != mb::kModeHold) s->sscenes[s->pool_handle[i]].pending -= 1;
+                if (modes[i] != mb::kModeHold) s->sscenes[s->pool_handle[i]].pending -= chain;
+            f += chain;
         }
         lk.unlock();  // submitters keep queueing while the GPU works
         cudaStreamSynchronize(b->stream);

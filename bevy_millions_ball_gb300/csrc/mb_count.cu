@@ -52,6 +52,7 @@ __global__ void __launch_bounds__(kScanThreads)
     __shared__ uint32_t s_warp[W], s_base[W];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t chunk = blockIdx.x, c0 = chunk * kScanChunk, tile = c0 / kScanTile;
+    griddep_wait();  // after the previous frame's physics pass, when chained to it
     griddep_launch();
     if (chunk == 0 && tid < (uint32_t)kFixLists) fix_ctl[tid] = 0u;  // fixup lists of this frame start empty
     const uint32_t base = c0 + tid * kScanItems;
@@ -235,18 +236,19 @@ __global__ void __launch_bounds__(256)
                           uint32_t* __restrict__ perm, const float4* __restrict__ pos0,
                           const float4* __restrict__ pos1, const uint4* __restrict__ vfme0,
                           const uint4* __restrict__ vfme1, float4* __restrict__ spos, uint4* __restrict__ svfme,
-                          const uint32_t* __restrict__ offs, FixLists fix) {
+                          const uint32_t* __restrict__ offs, FixLists fix, uint4* __restrict__ bands) {
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
         uint32_t i = i0 + threadIdx.x;
         bool valid = i < n;
-        uint32_t mode = kModeHold, parity = 0;
+        uint32_t mode = kModeHold, parity = 0, sc = 0;
         if (valid) {
             uint32_t s = __ldg(tile_scene + i / kPhysicsTile);
             while (i >= __ldg(&scenes[s].agent_end)) ++s;
             mode = __ldg(&scenes[s].mode);
             parity = __ldg(&scenes[s].parity);
+            sc = s;
         }
         valid = valid && mode != kModeHold;
         uint32_t k = valid ? __ldg(keys + i) : 0xFFFFFFFFu;
@@ -276,6 +278,10 @@ __global__ void __launch_bounds__(256)
             perm[dst] = i;
             spos[dst] = p;
             svfme[dst] = q;
+            if (bands && !ident) {  // the scene's band table entries, in its own cell coordinates
+                const uint32_t cb = __ldg(&scenes[sc].cell_base);
+                write_band_bounds(bands, offs + cb, __ldg(&scenes[sc].P.N), n, dst, k - cb);
+            }
         }
     }
 }
@@ -658,12 +664,12 @@ cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, c
     return cudaGetLastError();
 }
 
-cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st) {
+cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st, bool pdl) {
     (void)ctl;
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
-    k_cell_scan<false><<<chunks, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.fix_ctl,
-                                                       nullptr, nullptr);
-    return cudaGetLastError();
+    return launch_pdl(pdl, k_cell_scan<false>, dim3(chunks), dim3(kScanThreads), 0, st, (const uint32_t*)s.hist,
+                      (const uint32_t*)s.coarse, cells, offs, s.cursor, s.fix_ctl, (const SceneDev*)nullptr,
+                      (const uint32_t*)nullptr);
 }
 
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
@@ -693,13 +699,13 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
                                  const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
                                  const uint32_t* offs, uint32_t* perm, const float4* pos_buf0,
                                  const float4* pos_buf1, const uint4* vfme_buf0, const uint4* vfme_buf1,
-                                 float4* spos, uint4* svfme, cudaStream_t st) {
+                                 float4* spos, uint4* svfme, uint4* bands, cudaStream_t st) {
     cudaError_t e;
     if (n) {
         uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
         k_cell_scatter_scenes<<<blocks, 256, 0, st>>>(scenes, tile_scene, keys, n, s.cursor, perm, pos_buf0,
                                                       pos_buf1, vfme_buf0, vfme_buf1, spos, svfme, offs,
-                                                      fix_lists(s));
+                                                      fix_lists(s), bands);
         if ((e = cudaGetLastError())) return e;
     }
     SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};

@@ -186,11 +186,14 @@ cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t*
 cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,
                          uint32_t* hist, uint32_t* coarse, cudaStream_t st);
 
-// Batched LOOP/INIT/HOLD pass: tile_scene[t] = scene of slot t*kPhysicsTile.
+// Batched LOOP/INIT/HOLD pass: tile_scene[t] = scene of slot t*kPhysicsTile;
+// `bands` is the band table the batched scatter wrote (used for tiles inside one
+// LOOP scene).
 // Batched physics: scene s reads the sorted copy and writes buffer 1 - parity
 // (pos_buf[2] / vfme_buf[2]); a HOLD scene only re-emits the counts of its keys.
 cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
-                                 const uint32_t* offs, const float4* spos, const uint4* svfme, float4* pos_buf0,
+                                 const uint32_t* offs, const uint4* bands, const float4* spos, const uint4* svfme,
+                                 float4* pos_buf0,
                                  float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1, uint32_t* keys,
                                  uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st);
 
@@ -233,7 +236,8 @@ cudaError_t count_keys(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
 cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, cudaStream_t st);
 // offs[0..cells] := exclusive scan of hist (offs[cells] = n), cursors := offs; the
 // counts are cleared later in the frame by the fixup of count_scatter.
-cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st);
+cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st,
+                       bool pdl = false);
 // coarse[t] := sum of hist over scan tile t (after a pass that emitted cell counts
 // only: INIT frames, re-keying); the batched form touches only INIT scenes' tiles.
 cudaError_t count_tile_counts(CountScratch& s, uint32_t cells, cudaStream_t st);
@@ -259,7 +263,7 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
                                  const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
                                  const uint32_t* offs, uint32_t* perm, const float4* pos_buf0,
                                  const float4* pos_buf1, const uint4* vfme_buf0, const uint4* vfme_buf1,
-                                 float4* spos, uint4* svfme, cudaStream_t st);
+                                 float4* spos, uint4* svfme, uint4* bands, cudaStream_t st);
 // spos/svfme := pos_in/vfme_in gathered through perm (after the onesweep sort);
 // bands (nullable) := the band table of the sorted keys for an N x N grid.
 cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in, const uint4* vfme_in,

@@ -401,7 +401,7 @@ __device__ __forceinline__ uint32_t scene_of(const SceneDev* __restrict__ scenes
 // are local, so every scene evolves exactly as it would alone.
 template <bool kBatched>
 __global__ void __launch_bounds__(kTileThreads)
-    k_physics_frame(PhysParams P1, const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
+    k_physics_frame(const __grid_constant__ PhysParams P1, const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
                     uint32_t n, const uint32_t* __restrict__ offs, const uint4* __restrict__ bands,
                     const float4* __restrict__ spos,
                     const uint4* __restrict__ svfme, float4* __restrict__ pos_out0, float4* __restrict__ pos_out1,
@@ -421,13 +421,11 @@ __global__ void __launch_bounds__(kTileThreads)
 
     // this slot's scene; its output buffer is the one its current state is not in
     uint32_t sc = 0, base_a = 0, base_c = 0, mode = kModeLoop;
-    PhysParams P = P1;
     float4* __restrict__ pos_out = pos_out0;
     uint4* __restrict__ vfme_out = vfme_out0;
     if (kBatched) {
         const uint32_t first = __ldg(tile_scene + blockIdx.x);
         sc = scene_of(scenes, first, valid ? i : ilast);
-        P = scenes[sc].P;
         base_a = scenes[sc].agent_base;
         base_c = scenes[sc].cell_base;
         mode = scenes[sc].mode;
@@ -437,11 +435,19 @@ __global__ void __launch_bounds__(kTileThreads)
         }
     }
 
+    const PhysParams& P = kBatched ? scenes[sc].P : P1;  // read where it lives, not copied
     if (tid == 0) mbar_init(&s_bar, 1u);
-    const bool table = !kBatched && bands != nullptr;
-    if (table) {  // bounds from the band table: one load
+    if (bands) {  // bounds from the band table: one load (a batch: tiles inside one LOOP scene)
         if (tid == 0) {
-            const uint4 l = __ldg(bands + 2u * blockIdx.x), h = __ldg(bands + 2u * blockIdx.x + 1u);
+            bool stage = true;
+            if (kBatched) {
+                const uint32_t first = __ldg(tile_scene + blockIdx.x);
+                const uint32_t sf = scene_of(scenes, first, i0), sl = scene_of(scenes, first, ilast);
+                stage = sf == sl && __ldg(&scenes[sf].mode) == kModeLoop;
+            }
+            const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+            const uint4 l = stage ? __ldg(bands + 2u * blockIdx.x) : z;
+            const uint4 h = stage ? __ldg(bands + 2u * blockIdx.x + 1u) : z;
             const uint32_t lo3[3] = {l.x, l.y, l.z}, hi3[3] = {h.x, h.y, h.z};
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
@@ -615,13 +621,13 @@ cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t*
 }
 
 cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
-                                 const uint32_t* offs, const float4* spos, const uint4* svfme, float4* pos_buf0,
-                                 float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1, uint32_t* keys,
-                                 uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st) {
+                                 const uint32_t* offs, const uint4* bands, const float4* spos, const uint4* svfme,
+                                 float4* pos_buf0, float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1,
+                                 uint32_t* keys, uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st) {
     if (!n) return cudaSuccess;
     PhysParams unused{};
     k_physics_frame<true><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
-        unused, scenes, tile_scene, n, offs, nullptr, spos, svfme, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, keys, hist,
+        unused, scenes, tile_scene, n, offs, bands, spos, svfme, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, keys, hist,
         coarse, err);
     return cudaGetLastError();
 }

@@ -164,3 +164,22 @@ def test_server_with_budget_beyond_the_key_space(built_lib, cuda):
         p, _ = srv.get_state(h)
         rp, _, _ = alone(sc, 6)
         np.testing.assert_array_equal(p.view(np.uint32), rp.view(np.uint32))
+
+
+def test_batch_long_steps_chain_frames(built_lib, cuda):
+    """Multi-frame steps run as chains of frames in one launch while no scene
+    changes mode; a held scene stays put through them."""
+    scs = mixed_scenes(4, seed=31)
+    with Batch([s.plugin for s in scs]) as b:
+        for i, s in enumerate(scs):
+            b.set_state(i, s.pos_scale, s.vfme)
+        b.step(2)
+        b.set_active(2, False)
+        b.step(19)  # 8 + 8 + 1 + 1 + 1 frames
+        b.set_active(2, True)
+        b.step(9)
+        b.sync()
+        frames = {0: 30, 1: 30, 2: 11, 3: 30}
+        for i, s in enumerate(scs):
+            assert b.time(i) == frames[i]
+            assert_same(b, i, alone(s, frames[i]), f"scene {i}")
