@@ -205,6 +205,56 @@ def test_full_size_1m_properties(built_lib, cuda):
         assert not np.isnan(p).any()
 
 
+def check_frame_properties(w, plugin, n):
+    """Size-independent properties of a world after a LOOP frame: the order is a
+    stable permutation, the cell ranges tile [0, n) in cell order, and every
+    emitted key is the cell of the sphere's position."""
+    p, _ = w.get_state()
+    d = w.debug()
+    perm = d["perm"].astype(np.int64)
+    assert np.array_equal(np.sort(perm), np.arange(n))  # a permutation
+    full = d["start"] != INV
+    cells = np.nonzero(full)[0]
+    st = d["start"][full].astype(np.int64)
+    sizes = d["close"][full].astype(np.int64) - st + 1
+    assert sizes.sum() == n and np.all(sizes >= 1)
+    assert st[0] == 0 and np.all(st[1:] == st[:-1] + sizes[:-1])  # ranges in cell order, back to back
+    cell_of_slot = np.repeat(cells, sizes)
+    # stable: inside a cell the old slots ascend
+    same = cell_of_slot[1:] == cell_of_slot[:-1]
+    assert np.all(perm[1:][same] > perm[:-1][same])
+    # keys emitted for the next frame are the cells of the new positions
+    N, g = plugin.number_of_grids_one_dimension, plugin.grid_size
+    H = np.float32(N * g // 2)
+    def cell(v):
+        u = np.clip(np.trunc((v + H).astype(np.float32)), 0, 2.0**32 - 1).astype(np.uint64)
+        return np.minimum(u // g, N - 1)
+    keys = cell(p[:, 2]) * N + cell(p[:, 0])
+    np.testing.assert_array_equal(d["keys"].astype(np.uint64), keys)
+    assert not np.isnan(p).any()
+
+
+def test_clustered_4m_properties(built_lib, cuda):
+    """The 4,194,304-sphere clustered spring workload: stable order, cell ranges
+    and keys after 20 frames (cells near the cluster centres hold ~100 spheres)."""
+    sc = scenes.workload("P-4M")
+    with World(sc.plugin) as w:
+        w.set_state(sc.pos_scale, sc.vfme)
+        w.step(20)
+        w.sync()
+        check_frame_properties(w, sc.plugin, sc.n)
+
+
+def test_16m_uniform_properties(built_lib, cuda):
+    """16,777,216 spheres on a 4096 x 4096 grid (16x the benchmark scene)."""
+    sc = scenes.plain_uniform(1 << 24, 4096, seed=77)
+    with World(sc.plugin) as w:
+        w.set_state(sc.pos_scale, sc.vfme)
+        w.step(3)
+        w.sync()
+        check_frame_properties(w, sc.plugin, sc.n)
+
+
 def test_disabled_simulation_is_noop(built_lib, cuda):
     sc = scenes.plain_uniform(4096, 64, seed=1)
     with World(sc.plugin.replace(enable_simulation=False)) as w:
