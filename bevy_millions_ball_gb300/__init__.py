@@ -210,7 +210,7 @@ class World:
         return t
 
     def set_tuning(self, digit_bits_max: int | None = None, collide_block: int | None = None,
-                   sort_algorithm: int | None = None) -> None:
+                   sort_algorithm: int | None = None, frames_per_launch: int | None = None) -> None:
         t = self.tuning
         if digit_bits_max is not None:
             t.digit_bits_max = digit_bits_max
@@ -218,7 +218,20 @@ class World:
             t.collide_block = collide_block
         if sort_algorithm is not None:
             t.sort_algorithm = sort_algorithm
+        if frames_per_launch is not None:
+            t.frames_per_launch = frames_per_launch
         self._check(self._lib.mb_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self, frames: int = 16) -> dict:
+        """mb_autotune: time every candidate tuning on this scene, keep the state,
+        apply the fastest.  Returns the chosen tuning and each candidate's ms/frame."""
+        best = MbTuning()
+        ms = (C.c_float * _abi.MB_TUNE_CANDIDATES)()
+        tried = (MbTuning * _abi.MB_TUNE_CANDIDATES)()
+        self._check(self._lib.mb_autotune(self._h, frames, C.byref(best), ms, tried))
+        desc = lambda t: {"sort_algorithm": t.sort_algorithm, "digit_bits_max": t.digit_bits_max,
+                          "frames_per_launch": t.frames_per_launch}
+        return {"best": desc(best), "candidates": [dict(desc(t), ms_per_frame=float(m)) for t, m in zip(tried, ms)]}
 
     # -- state
     def set_state(self, pos_scale: np.ndarray, vfme: np.ndarray) -> None:

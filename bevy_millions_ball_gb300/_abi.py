@@ -59,10 +59,11 @@ class MbConsts(C.Structure):
 
 class MbTuning(C.Structure):
     _fields_ = [("digit_bits_max", u32), ("collide_block", u32), ("sort_algorithm", u32),
-                ("reserved", u32 * 5)]
+                ("frames_per_launch", u32), ("reserved", u32 * 4)]
 
 
 MB_SORT_COUNTING, MB_SORT_ONESWEEP = 0, 1
+MB_TUNE_CANDIDATES = 12
 
 
 class MbServerConfig(C.Structure):
@@ -109,6 +110,7 @@ SIGNATURES = {
     "mb_sort_and_hash_static": (C.c_int, [vp, vp, u32, u32, vp, vp, vp, vp, vp]),
     "mb_get_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),
     "mb_set_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),
+    "mb_autotune": (C.c_int, [vp, u32, C.POINTER(MbTuning), C.POINTER(C.c_float), C.POINTER(MbTuning)]),
     "mb_set_profiling": (C.c_int, [vp, C.c_int]),
     "mb_last_frame_times": (C.c_int, [vp, C.POINTER(C.c_float)]),
     "mb_kernels_per_frame": (u32, [vp]),

@@ -10,6 +10,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -115,9 +116,12 @@ bool mb::settings_valid(const mb_settings* s, std::string& why) {
 namespace {
 using mb::settings_valid;
 
-// LOOP frames captured back to back in one graph for multi-frame steps (even, so
-// a chain ends in the parity it started from).
-constexpr uint32_t kChainFrames = 8;
+// LOOP frames captured back to back in one graph for multi-frame steps: the
+// tuning's frames_per_launch (even, or 1; so a chain ends in the parity it
+// started from), 8 by default.
+uint32_t chain_frames(const mb_world* w) {
+    return w->tuning.frames_per_launch ? w->tuning.frames_per_launch : 8u;
+}
 
 void drop_graphs(mb_world* w) {
     for (auto* set : {w->graph, w->chain})
@@ -432,12 +436,13 @@ mb_status mb_step(mb_world* w, uint32_t k) {
     for (uint32_t f = 0; f < k;) {
         if (w->time == 0) {
             if ((e = enqueue_frame(w, w->stream, w->cur, true))) return cuda_fail(w, "mb_step(init)", e);
-        } else if (k - f >= kChainFrames && !w->profiling) {  // a chain of LOOP frames, one launch
-            if (!w->chain[w->cur] && (e = build_graph(w, w->cur, kChainFrames)))
-                return cuda_fail(w, "mb_step(capture)", e);
+        } else if (chain_frames(w) > 1u && k - f >= chain_frames(w) && !w->profiling) {
+            // a chain of LOOP frames, one launch
+            const uint32_t cf = chain_frames(w);
+            if (!w->chain[w->cur] && (e = build_graph(w, w->cur, cf))) return cuda_fail(w, "mb_step(capture)", e);
             if ((e = cudaGraphLaunch(w->chain[w->cur], w->stream))) return cuda_fail(w, "mb_step", e);
-            f += kChainFrames;
-            w->time += kChainFrames;
+            f += cf;
+            w->time += cf;
             w->frame_done = true;
             continue;
         } else {
@@ -530,6 +535,9 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
         return fail(w, MB_ERR_INVALID_ARG, "collide_block must be a multiple of 32 in [32, 256]");
     if (t->sort_algorithm != MB_SORT_COUNTING && t->sort_algorithm != MB_SORT_ONESWEEP)
         return fail(w, MB_ERR_INVALID_ARG, "sort_algorithm must be MB_SORT_COUNTING or MB_SORT_ONESWEEP");
+    const uint32_t fpl = t->frames_per_launch;
+    if (!(fpl == 0 || fpl == 1 || fpl == 2 || fpl == 4 || fpl == 8 || fpl == 16))
+        return fail(w, MB_ERR_INVALID_ARG, "frames_per_launch must be 0, 1, 2, 4, 8 or 16");
     drop_graphs(w);
     bool to_counting = t->sort_algorithm == MB_SORT_COUNTING && !counting(w);
     w->tuning = *t;
@@ -538,6 +546,104 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
         cudaError_t e = recount(w);
         if (e) return cuda_fail(w, "mb_set_tuning", e);
     }
+    return MB_OK;
+}
+
+mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* frame_ms, mb_tuning* tried) {
+    if (!w || !best) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
+    if (frames == 0) return fail(w, MB_ERR_INVALID_ARG, "frames must be positive");
+    if (!w->frame_done || w->time == 0) return fail(w, MB_ERR_NOT_READY, "run a frame before autotuning");
+    if (w->profiling) return fail(w, MB_ERR_INVALID_ARG, "turn profiling off before autotuning");
+    const mb_tuning start = w->tuning;
+    mb_tuning cand[MB_TUNE_CANDIDATES];
+    {
+        const uint32_t sorts[4][2] = {{MB_SORT_COUNTING, 8u}, {MB_SORT_ONESWEEP, 6u}, {MB_SORT_ONESWEEP, 8u},
+                                      {MB_SORT_ONESWEEP, 11u}};
+        const uint32_t fpl[3] = {1u, 8u, 16u};
+        uint32_t c = 0;
+        for (const auto& so : sorts)
+            for (uint32_t f : fpl) {
+                cand[c] = start;
+                cand[c].sort_algorithm = so[0];
+                cand[c].digit_bits_max = so[1];
+                cand[c].frames_per_launch = f;
+                ++c;
+            }
+    }
+    // save what the frames overwrite
+    const size_t n = w->n, C = w->cells;
+    float4* pos = nullptr;
+    uint4* vfme = nullptr;
+    uint32_t *keys = nullptr, *perm = nullptr, *offs = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    auto release = [&]() {
+        cudaFree(pos);
+        cudaFree(vfme);
+        cudaFree(keys);
+        cudaFree(perm);
+        cudaFree(offs);
+        for (auto& x : ev)
+            if (x) cudaEventDestroy(x);
+    };
+    const int cur0 = w->cur;
+    const int64_t time0 = w->time;
+    cudaError_t e = cudaSuccess;
+    auto snap = [&](bool save) -> cudaError_t {
+        cudaError_t r;
+        auto cp = [&](void* a, void* b, size_t bytes) {
+            return cudaMemcpyAsync(save ? a : b, save ? b : a, bytes, cudaMemcpyDeviceToDevice, w->stream);
+        };
+        if ((r = cp(pos, w->pos[cur0], sizeof(float4) * n))) return r;
+        if ((r = cp(vfme, w->vfme[cur0], sizeof(uint4) * n))) return r;
+        if ((r = cp(keys, w->keys, sizeof(uint32_t) * n))) return r;
+        if ((r = cp(perm, w->perm, sizeof(uint32_t) * n))) return r;
+        return cp(offs, w->scratch.offs, sizeof(uint32_t) * (C + 1u));
+    };
+    if ((e = cudaMalloc(&pos, sizeof(float4) * std::max<size_t>(n, 1))) ||
+        (e = cudaMalloc(&vfme, sizeof(uint4) * std::max<size_t>(n, 1))) ||
+        (e = cudaMalloc(&keys, sizeof(uint32_t) * std::max<size_t>(n, 1))) ||
+        (e = cudaMalloc(&perm, sizeof(uint32_t) * std::max<size_t>(n, 1))) ||
+        (e = cudaMalloc(&offs, sizeof(uint32_t) * (C + 1u))) || (e = cudaEventCreate(&ev[0])) ||
+        (e = cudaEventCreate(&ev[1])) || (e = snap(true))) {
+        release();
+        return cuda_fail(w, "mb_autotune", e);
+    }
+    float best_ms = 0.0f;
+    uint32_t best_i = 0;
+    mb_status st = MB_OK;
+    for (uint32_t c = 0; c < MB_TUNE_CANDIDATES && st == MB_OK; ++c) {
+        if ((e = snap(false))) break;  // every candidate starts from the saved frame
+        w->cur = cur0;
+        w->time = time0;
+        if ((st = mb_set_tuning(w, &cand[c])) != MB_OK) break;
+        if ((e = recount(w))) break;  // counts of the restored keys
+        if ((st = mb_step(w, 1)) != MB_OK) break;  // warm-up: graphs built, caches touched
+        if ((e = cudaEventRecord(ev[0], w->stream))) break;
+        if ((st = mb_step(w, frames)) != MB_OK) break;
+        if ((e = cudaEventRecord(ev[1], w->stream)) || (e = cudaEventSynchronize(ev[1]))) break;
+        float ms = 0.0f;
+        if ((e = cudaEventElapsedTime(&ms, ev[0], ev[1]))) break;
+        ms /= (float)frames;
+        if (frame_ms) frame_ms[c] = ms;
+        if (tried) tried[c] = cand[c];
+        if (c == 0 || ms < best_ms) {
+            best_ms = ms;
+            best_i = c;
+        }
+    }
+    // restore the saved frame under the winning tuning
+    cudaError_t e2 = snap(false);
+    w->cur = cur0;
+    w->time = time0;
+    mb_status st2 = mb_set_tuning(w, (e || st != MB_OK) ? &start : &cand[best_i]);
+    if (!e2) e2 = recount(w);
+    if (!e2) e2 = cudaStreamSynchronize(w->stream);
+    release();
+    if (e) return cuda_fail(w, "mb_autotune", e);
+    if (st != MB_OK) return st;
+    if (e2) return cuda_fail(w, "mb_autotune", e2);
+    if (st2 != MB_OK) return st2;
+    *best = cand[best_i];
     return MB_OK;
 }
 

@@ -224,7 +224,9 @@ typedef struct mb_tuning {
     uint32_t digit_bits_max;   /* widest radix digit of the onesweep sort, 4..11 */
     uint32_t collide_block;    /* reserved: the physics kernel's tile is fixed at 128 slots */
     uint32_t sort_algorithm;   /* MB_SORT_COUNTING (default) or MB_SORT_ONESWEEP */
-    uint32_t reserved[5];
+    uint32_t frames_per_launch; /* LOOP frames captured per graph launch in multi-frame steps:
+                                   1, 2, 4, 8 (default; 0 reads as 8) or 16 */
+    uint32_t reserved[4];
 } mb_tuning;
 
 /* Frame sort: both produce the identical stable permutation and cell ranges.
@@ -235,6 +237,22 @@ typedef struct mb_tuning {
 #define MB_SORT_ONESWEEP 1u
 mb_status mb_get_tuning(const mb_world* w, mb_tuning* out);
 mb_status mb_set_tuning(mb_world* w, const mb_tuning* t);
+
+/*
+ * Autotuner (no counterpart in the reference, whose sort and passes have fixed
+ * workgroup shapes).  Times every candidate tuning on the world's own scene for
+ * `frames` LOOP frames each (CUDA events on the world's stream, one warm-up
+ * frame per candidate): the counting sort and the onesweep sort with 6-, 8- and
+ * 11-bit digits, each with 1, 8 and 16 frames per graph launch.  The world's
+ * state, keys, permutation, cell ranges and time are saved first and restored
+ * afterwards, so the simulation continues exactly as if the tuner had not run.
+ * The fastest candidate is applied and written to *best; frame_ms (nullable,
+ * MB_TUNE_CANDIDATES entries) receives each candidate's mean frame time, in the
+ * order of tried[] (nullable, same length).  Needs a frame to have run since the
+ * last upload (MB_ERR_NOT_READY otherwise).  Allocates temporary device memory.
+ */
+#define MB_TUNE_CANDIDATES 12u
+mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* frame_ms, mb_tuning* tried);
 
 /*
  * Per-stage device timing (no counterpart in the reference, which only labels

@@ -328,3 +328,41 @@ def test_single_agent_and_tiny_grid(built_lib, cuda):
         w.step(30)
         ow.step(30)
         compare(w, ow, 30)
+
+
+def test_autotune_keeps_the_frame_sequence(built_lib, cuda):
+    """mb_autotune times its candidates on the scene and restores the saved frame:
+    the world then continues exactly like the oracle that never paused."""
+    sc = scenes.workload("P-small")
+    with World(sc.plugin) as w:
+        ow = oracle.OracleWorld(sc.plugin.to_c())
+        w.set_state(sc.pos_scale, sc.vfme)
+        ow.set_state(sc.pos_scale, sc.vfme)
+        w.step(5)
+        ow.step(5)
+        res = w.autotune(frames=8)
+        assert len(res["candidates"]) == 12 and all(c["ms_per_frame"] > 0 for c in res["candidates"])
+        fastest = min(res["candidates"], key=lambda c: c["ms_per_frame"])
+        assert res["best"] == {k: fastest[k] for k in res["best"]}
+        t = w.tuning
+        assert (t.sort_algorithm, t.digit_bits_max, t.frames_per_launch) == tuple(res["best"].values())
+        assert w.time == 5
+        compare(w, ow, 5)
+        w.step(21)
+        ow.step(21)
+        compare(w, ow, 26)
+
+
+@pytest.mark.parametrize("fpl", [1, 2, 16])
+def test_frames_per_launch(built_lib, cuda, fpl):
+    sc = scenes.plain_uniform(30_000, 256, seed=50 + fpl)
+    with World(sc.plugin) as w:
+        w.set_tuning(frames_per_launch=fpl)
+        ow = oracle.OracleWorld(sc.plugin.to_c())
+        w.set_state(sc.pos_scale, sc.vfme)
+        ow.set_state(sc.pos_scale, sc.vfme)
+        w.step(37)
+        ow.step(37)
+        compare(w, ow, 37)
+        with pytest.raises(MbError):
+            w.set_tuning(frames_per_launch=3)
