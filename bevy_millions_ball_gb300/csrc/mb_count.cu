@@ -291,9 +291,9 @@ __global__ void __launch_bounds__(256)
 // and re-gather their sorted state copy from the state source: one buffer (a
 // world), or each scene's current buffer (a batch, where cells and coarse tiles
 // of HOLD scenes are left alone).  Cells of up to kFixSmall slots: a thread
-// each (insertion sort); up to kFixWarp: a warp each (rank of every slot among
-// the cell's input indices, held in registers); larger: a block each (bitmap of
-// the input indices, chunk by chunk of their range, read back in order).
+// each (sorting network in registers); up to kFixWarp: a warp each (bitonic sort
+// in registers and shuffles); larger: a block each (bitmap of the input indices,
+// chunk by chunk of their range, read back in order).
 constexpr uint32_t kFixThreads = 256;
 constexpr uint32_t kBitmapWords = 8192;                 // 32 KB of shared memory
 constexpr uint32_t kBitmapValues = kBitmapWords * 32u;  // input indices per bitmap chunk
@@ -361,6 +361,39 @@ struct SceneBuffers {
     __device__ __forceinline__ uint4 vfme(uint32_t o) const { return __ldg((parity(o) ? q1 : q0) + o); }
 };
 
+// Ascending bitonic sort of the warp's 32 S keys, key e = 32 s + lane in v[s]
+// (S a power of two, at most kFixWarp / 32): partners e ^ j in other lanes are
+// exchanged with shuffles, partners in other registers of the same lane in place.
+template <uint32_t S>
+__device__ __forceinline__ void warp_bitonic(uint32_t (&v)[kFixWarp / 32], uint32_t lane) {
+#pragma unroll
+    for (uint32_t k = 2u; k <= 32u * S; k <<= 1) {
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0u; j >>= 1) {
+            if (j < 32u) {
+#pragma unroll
+                for (uint32_t s = 0; s < S; ++s) {
+                    const uint32_t e = 32u * s + lane;
+                    const uint32_t o = __shfl_xor_sync(0xFFFFFFFFu, v[s], (int)j);
+                    const bool up = (e & k) == 0u, low = (e & j) == 0u;
+                    v[s] = (low == up) ? min(v[s], o) : max(v[s], o);
+                }
+            } else {
+                const uint32_t js = j / 32u;
+#pragma unroll
+                for (uint32_t s = 0; s < S; ++s) {
+                    if (s & js) continue;
+                    const uint32_t e = 32u * s + lane;
+                    const uint32_t a = v[s], b = v[s | js];
+                    const bool up = (e & k) == 0u;
+                    v[s] = up ? min(a, b) : max(a, b);
+                    v[s | js] = up ? max(a, b) : min(a, b);
+                }
+            }
+        }
+    }
+}
+
 template <class Src>
 __device__ __forceinline__ void regather(const Src& src, const uint32_t* perm, uint32_t lo, uint32_t j,
                                          float4* __restrict__ spos, uint4* __restrict__ svfme) {
@@ -424,39 +457,32 @@ __global__ void __launch_bounds__(kFixThreads)
         }
     }
 
-    // mid cells: one warp each; slot e = lane + 32 s of the cell is v[s]
+    // mid cells: one warp each, a bitonic sort of the cell's input indices held
+    // in registers (slot e = 32 s + lane is v[s]; padded with 0xFFFFFFFF to 32 S
+    // slots, S a power of two)
     const uint32_t n_mid = min(lists.ctl[kFixListWarp], lists.cap[1]);
     const uint32_t warps = gridDim.x * (blockDim.x / 32u);
     for (uint32_t x = blockIdx.x * (blockDim.x / 32u) + tid / 32u; x < n_mid; x += warps) {
         const uint32_t c = mid[x];
-        const uint32_t lo = offs[c], m = offs[c + 1u] - lo;
-        const uint32_t S = (m + 31u) / 32u;  // <= kFixWarp / 32
-        uint32_t v[kFixWarp / 32], r[kFixWarp / 32];
+        const uint32_t lo = offs[c], m = offs[c + 1u] - lo;  // 9 <= m <= kFixWarp
+        uint32_t v[kFixWarp / 32];
 #pragma unroll
         for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
-            const uint32_t e = lane + 32u * s;
+            const uint32_t e = 32u * s + lane;
             v[s] = e < m ? perm[lo + e] : 0xFFFFFFFFu;
-            r[s] = 0u;
         }
-        for (uint32_t s2 = 0; s2 < S; ++s2) {
-#pragma unroll 4
-            for (uint32_t l = 0; l < 32u; ++l) {
-                uint32_t u = 0;
-#pragma unroll
-                for (uint32_t q = 0; q < kFixWarp / 32; ++q)
-                    if (q == s2) u = __shfl_sync(0xFFFFFFFFu, v[q], (int)l);
-#pragma unroll
-                for (uint32_t s = 0; s < kFixWarp / 32; ++s) r[s] += u < v[s] ? 1u : 0u;
-            }
-        }
+        if (m <= 32u) warp_bitonic<1>(v, lane);
+        else if (m <= 64u) warp_bitonic<2>(v, lane);
+        else if (m <= 128u) warp_bitonic<4>(v, lane);
+        else warp_bitonic<8>(v, lane);
         __syncwarp();  // every lane has read the cell before any slot is rewritten
 #pragma unroll
         for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
-            const uint32_t e = lane + 32u * s;
-            if (e < m && r[s] != e) {
-                perm[lo + r[s]] = v[s];
-                spos[lo + r[s]] = src.pos(v[s]);
-                svfme[lo + r[s]] = src.vfme(v[s]);
+            const uint32_t e = 32u * s + lane;
+            if (e < m) {
+                perm[lo + e] = v[s];
+                spos[lo + e] = src.pos(v[s]);
+                svfme[lo + e] = src.vfme(v[s]);
             }
         }
     }
