@@ -163,6 +163,18 @@ def _stream_handle(stream) -> int:
     return int(getattr(stream, "cuda_stream", stream))
 
 
+class _DeviceArray:
+    """A view of library-owned device memory (CUDA array interface v3).  It is
+    exported writable because torch rejects read-only device arrays; a write
+    changes the world's current state in place (no INIT frame follows, unlike
+    set_state)."""
+
+    def __init__(self, ptr: int, shape, typestr: str, owner):
+        self._owner = owner  # keeps the world alive while the view exists
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3, "strides": None, "stream": None}
+
+
 class World:
     """One scene resident on the GPU (the reference plugin's buffers + per-frame node)."""
 
@@ -257,6 +269,16 @@ class World:
         a, b = C.c_void_p(), C.c_void_p()
         self._check(self._lib.mb_device_buffers(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def device_state(self):
+        """The current state as zero-copy device arrays (the renderer's input,
+        physics_ball/mod.rs:709-740): positions+radius (n, 4) float32 and packed
+        velocity/force/mass (n, 4) uint32, exposed through
+        __cuda_array_interface__ (e.g. torch.as_tensor(pos, device="cuda")).
+        Valid until the next step, upload or close; in the order of the last
+        frame's sorted slots."""
+        a, b = self.device_buffers()
+        return _DeviceArray(a, (self.n, 4), "<f4", self), _DeviceArray(b, (self.n, 4), "<u4", self)
 
     # -- stepping
     def step(self, k: int = 1) -> None:

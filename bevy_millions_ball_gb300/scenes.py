@@ -117,6 +117,36 @@ def plain_clustered(n: int, grids: int, *, clusters: int = 16, sigma_xz: float =
     return Scene(plugin, pos, vfme, f"clustered n={n} N={grids} k={clusters}")
 
 
+def reference_default(plugin: PhysicsPlugin | None = None, seed: int = 0) -> Scene:
+    """The reference plugin's own start-up scene (src/physics/mod.rs:172-212) for
+    its default settings (16,384 spheres, N = 128, grid_size 8): a lattice of
+    2^(L//2) x 2^(L - L//2) spheres (L = log2 n), x-major, 4 units apart, centred
+    on the origin, at height 4, radius 1, mass 1, horizontal velocities (stored
+    as displacement per step, as the reference packs them) uniform in
+    [-0.8, 0.8) per axis, vertical 0.  The reference draws the velocities from
+    ChaCha8 (rand 0.8), which is not reproduced here: numpy's PCG64 draws the
+    same distribution, so the lattice is identical and the velocity stream is not."""
+    plugin = plugin or PhysicsPlugin()
+    n = int(plugin.max_number_of_agents)
+    if n <= 0 or n & (n - 1):
+        raise ValueError("the reference lattice needs a power-of-two sphere count")
+    L = n.bit_length() - 1
+    cx, cz = 1 << (L // 2), 1 << (L - L // 2)
+    xs = (np.arange(cx, dtype=np.float32) - np.float32(0.5) * np.float32(cx - 1)) * np.float32(4.0)
+    zs = (np.arange(cz, dtype=np.float32) - np.float32(0.5) * np.float32(cz - 1)) * np.float32(4.0)
+    pos = np.empty((n, 4), np.float32)
+    pos[:, 0] = np.repeat(xs, cz)
+    pos[:, 1] = 4.0
+    pos[:, 2] = np.tile(zs, cx)
+    pos[:, 3] = 1.0
+    rng = np.random.default_rng(seed)
+    v = np.zeros((n, 3), np.float32)
+    v[:, 0] = rng.uniform(-0.8, 0.8, n).astype(np.float32)
+    v[:, 2] = rng.uniform(-0.8, 0.8, n).astype(np.float32)
+    vfme = pack_vfme(v, np.zeros_like(v), 1.0)
+    return Scene(plugin, pos, vfme, f"reference default lattice n={n}")
+
+
 def next_pow2(x: int) -> int:
     return 1 << max(0, (int(x) - 1).bit_length())
 

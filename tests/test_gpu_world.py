@@ -366,3 +366,32 @@ def test_frames_per_launch(built_lib, cuda, fpl):
         compare(w, ow, 37)
         with pytest.raises(MbError):
             w.set_tuning(frames_per_launch=3)
+
+
+def test_reference_default_scene(built_lib, cuda):
+    """The reference plugin's default settings and its start-up lattice (16,384
+    spheres of radius 1 at spacing 4, N = 128, grid_size 8, dt = 1/120)."""
+    sc = scenes.reference_default()
+    run_pair(sc, 60, [1, 2, 11, 60])
+
+
+def test_device_state_views(built_lib, cuda):
+    """Zero-copy device views of the state buffers (torch reads them in place)."""
+    torch = cuda
+    sc = scenes.plain_uniform(5000, 64, seed=3)
+    with World(sc.plugin) as w:
+        w.set_state(sc.pos_scale, sc.vfme)
+        w.step(4)
+        w.sync()
+        pv, qv = w.device_state()
+        tp = torch.as_tensor(pv, device="cuda")
+        assert tp.shape == (5000, 4) and tp.dtype == torch.float32
+        assert tp.data_ptr() == w.device_buffers()[0]  # a view, not a copy
+        p, q = w.get_state()
+        np.testing.assert_array_equal(tp.cpu().numpy(), p)
+        assert qv.__cuda_array_interface__["typestr"] == "<u4" and qv.__cuda_array_interface__["shape"] == (5000, 4)
+        tq = torch.empty((5000, 4), dtype=torch.int32, device="cuda")
+        scratch = torch.empty_like(tp)
+        w.get_state_device(scratch.data_ptr(), tq.data_ptr())
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(tq.cpu().numpy().view(np.uint32), q)

@@ -210,3 +210,20 @@ def test_spring_wall_force_sign():
 
     f = unpack_vfme(q)[1]
     assert f[0, 1] > 0  # floor at y=0 pushes up
+
+
+def test_reference_default_lattice():
+    """src/physics/mod.rs:172-212: 2^(L//2) x 2^(L - L//2) lattice, x-major, spacing 4."""
+    from bevy_millions_ball_gb300 import PhysicsPlugin, scenes, unpack_vfme
+    sc = scenes.reference_default(PhysicsPlugin(max_number_of_agents=1 << 13))
+    p = sc.pos_scale
+    assert p.shape == (8192, 4)
+    # count_x = 2^6 = 64 rows of count_z = 2^7 = 128
+    assert p[0, 0] == -0.5 * 63 * 4 and p[0, 2] == -0.5 * 127 * 4
+    assert p[127, 0] == p[0, 0] and p[127, 2] == 0.5 * 127 * 4
+    assert p[128, 0] == p[0, 0] + 4 and p[128, 2] == p[0, 2]
+    assert np.all(p[:, 1] == 4.0) and np.all(p[:, 3] == 1.0)
+    v, f, m = unpack_vfme(sc.vfme)
+    assert np.all(np.abs(v[:, [0, 2]]) <= 0.8) and np.all(v[:, 1] == 0) and np.all(f == 0) and np.all(m == 1)
+    with pytest.raises(ValueError):
+        scenes.reference_default(PhysicsPlugin(max_number_of_agents=1000))
