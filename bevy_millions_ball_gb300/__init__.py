@@ -330,6 +330,12 @@ class SortPlan:
                                                          sorted_keys_ptr, sorted_vals_ptr, start_ptr,
                                                          close_ptr, _stream_handle(stream)))
 
+    def assemble_segments(self, sorted_keys_ptr: int, n: int, segs_ptr: int, key_seg_map_ptr: int,
+                          num_segs_ptr: int, stream=None) -> None:
+        """mb_assemble_segments: one segment per run of equal sorted keys (device pointers)."""
+        _abi.check(self._lib, self._lib.mb_assemble_segments(self._h, sorted_keys_ptr, int(n), segs_ptr,
+                                                             key_seg_map_ptr, num_segs_ptr, _stream_handle(stream)))
+
     def close(self) -> None:
         if self._h:
             self._lib.mb_sort_plan_destroy(self._h)

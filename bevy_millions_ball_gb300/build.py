@@ -32,6 +32,7 @@ UNITS = {
     "mb_sort.cu": [],
     "mb_count.cu": [],
     "mb_static.cu": [],
+    "mb_segs.cu": [],
     "mb_batch.cu": [],
     "mb_physics.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
 }

@@ -651,6 +651,7 @@ mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* fram
 struct mb_sort_plan {
     mb::SortScratch scratch;
     uint32_t digit_bits_max = 8;
+    uint32_t* seg_blocks = nullptr;  // per-block segment counts of mb_assemble_segments
 };
 
 mb_status mb_sort_plan_create(uint32_t max_keys, uint32_t max_cells, mb_sort_plan** out) {
@@ -661,7 +662,9 @@ mb_status mb_sort_plan_create(uint32_t max_keys, uint32_t max_cells, mb_sort_pla
     mb_sort_plan* p = new (std::nothrow) mb_sort_plan();
     if (!p) return fail(nullptr, MB_ERR_OOM, "host allocation failed");
     cudaError_t e = mb::scratch_alloc(p->scratch, max_keys, max_cells);
+    if (!e) e = cudaMalloc(&p->seg_blocks, sizeof(uint32_t) * (mb::segment_blocks(max_keys) + 1u));
     if (e) {
+        cudaFree(p->seg_blocks);
         mb::scratch_free(p->scratch);
         delete p;
         return cuda_fail(nullptr, "mb_sort_plan_create", e);
@@ -673,6 +676,7 @@ mb_status mb_sort_plan_create(uint32_t max_keys, uint32_t max_cells, mb_sort_pla
 mb_status mb_sort_plan_destroy(mb_sort_plan* p) {
     if (!p) return MB_OK;
     cudaDeviceSynchronize();
+    cudaFree(p->seg_blocks);
     mb::scratch_free(p->scratch);
     delete p;
     return MB_OK;
@@ -692,6 +696,18 @@ mb_status mb_sort_and_hash(mb_sort_plan* p, const uint32_t* keys, const uint32_t
     if (e) return cuda_fail(nullptr, "mb_sort_and_hash", e);
     if ((start || close) && (e = mb::offsets_to_start_close(p->scratch.offs, number_of_cells, start, close, st)))
         return cuda_fail(nullptr, "mb_sort_and_hash", e);
+    return MB_OK;
+}
+
+mb_status mb_assemble_segments(mb_sort_plan* p, const uint32_t* sorted_keys, uint32_t n, uint32_t* segs,
+                               uint32_t* key_seg_map, uint32_t* num_segs, void* cuda_stream) {
+    if (!p) return fail(nullptr, MB_ERR_INVALID_ARG, "plan is NULL");
+    if (n > p->scratch.max_keys) return fail(nullptr, MB_ERR_INVALID_ARG, "n exceeds the plan");
+    if (!num_segs || (n && (!sorted_keys || !segs || !key_seg_map)))
+        return fail(nullptr, MB_ERR_INVALID_ARG, "NULL buffer");
+    cudaError_t e = mb::assemble_segments(sorted_keys, n, p->seg_blocks, segs, key_seg_map, num_segs,
+                              static_cast<cudaStream_t>(cuda_stream));
+    if (e) return cuda_fail(nullptr, "mb_assemble_segments", e);
     return MB_OK;
 }
 

@@ -270,6 +270,13 @@ cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in,
                          float4* spos, uint4* svfme, const uint32_t* sorted_keys, const uint32_t* offs,
                          uint4* bands, uint32_t N, cudaStream_t st);
 
+// Compacted segment table of sorted keys (mb_segs.cu): segs[s] = first slot of
+// run s, key_seg_map[key] = s, *num_segs = runs (device pointers); block_scratch
+// holds segment_blocks(n) words.
+uint32_t segment_blocks(uint32_t n);
+cudaError_t assemble_segments(const uint32_t* sorted_keys, uint32_t n, uint32_t* block_scratch, uint32_t* segs,
+                              uint32_t* key_seg_map, uint32_t* num_segs, cudaStream_t st);
+
 int device_sm_count();
 
 // Settings checks shared by worlds and batches ("" = valid).

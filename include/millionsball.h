@@ -197,6 +197,20 @@ mb_status mb_sort_and_hash(mb_sort_plan* p, const uint32_t* keys, const uint32_t
                            uint32_t* start, uint32_t* close, void* cuda_stream);
 
 /*
+ * Compacted segment table of sorted keys, the reference's segment assembly
+ * (src/physics/assemble_segs.rs:314-430, assemble_segs.wgsl): each run of equal
+ * keys in sorted_keys[0..n) is one segment, in slot order.  Device pointers:
+ *   segs        : receives the first slot of every segment (at most n entries)
+ *   key_seg_map : key_seg_map[key] = its segment, for every key that occurs
+ *                 (entries of absent keys are left as they were; the map must
+ *                 hold max key + 1 entries)
+ *   num_segs    : one u32, receives the number of segments (0 for n = 0)
+ * Scratch comes from the plan (n <= its max_keys).
+ */
+mb_status mb_assemble_segments(mb_sort_plan* p, const uint32_t* sorted_keys, uint32_t n, uint32_t* segs,
+                               uint32_t* key_seg_map, uint32_t* num_segs, void* cuda_stream);
+
+/*
  * mb_sort_and_hash without any device allocation (no counterpart in the
  * reference).  For callers that may not allocate device memory where they issue
  * GPU work: a frame loop that forbids allocation after start-up (allocator
