@@ -36,6 +36,7 @@ __all__ = [
     "unpack_vfme",
     "quantize",
     "library",
+    "save_png",
 ]
 
 
@@ -127,6 +128,22 @@ class PhysicsSettings(PhysicsPlugin):
 
     def map_height(self) -> float:
         return 2.0 * float(self.half_map_height)
+
+
+def save_png(path, rgba: np.ndarray) -> None:
+    """Write an (H, W, 4) uint8 image as a PNG file (zlib, no other dependency)."""
+    import struct
+    import zlib
+
+    h, w = rgba.shape[:2]
+    raw = b"".join(b"\x00" + np.ascontiguousarray(rgba[y]).tobytes() for y in range(h))
+
+    def chunk(tag: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)) +
+                chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
 
 
 def quantize(plugin: PhysicsPlugin) -> MbConsts:
@@ -279,6 +296,21 @@ class World:
         frame's sorted slots."""
         a, b = self.device_buffers()
         return _DeviceArray(a, (self.n, 4), "<f4", self), _DeviceArray(b, (self.n, 4), "<u4", self)
+
+    def render_topdown(self, width: int, height: int, window=None):
+        """mb_render_topdown: a width x height RGBA8 image (H, W, 4) uint8 and the
+        surface height map (H, W) float32 of the current state, seen straight down
+        onto the x/z window (x0, z0, x1, z1) (default: the whole map)."""
+        if window is None:
+            s = self.settings
+            hs = s.number_of_grids_one_dimension * s.grid_size / 2.0
+            window = (-hs, -hs, hs, hs)
+        x0, z0, x1, z1 = (float(v) for v in window)
+        img = np.empty((height, width), np.uint32)
+        hmap = np.empty((height, width), np.float32)
+        self._check(self._lib.mb_render_topdown(self._h, width, height, x0, z0, x1, z1, img.ctypes.data,
+                                                hmap.ctypes.data, MB_HOST))
+        return img.view(np.uint8).reshape(height, width, 4), hmap
 
     # -- stepping
     def step(self, k: int = 1) -> None:

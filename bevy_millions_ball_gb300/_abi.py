@@ -109,6 +109,7 @@ SIGNATURES = {
     "mb_sort_and_hash": (C.c_int, [vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]),
     "mb_sort_and_hash_static": (C.c_int, [vp, vp, u32, u32, vp, vp, vp, vp, vp]),
     "mb_assemble_segments": (C.c_int, [vp, vp, u32, vp, vp, vp, vp]),
+    "mb_render_topdown": (C.c_int, [vp, u32, u32, C.c_float, C.c_float, C.c_float, C.c_float, vp, vp, C.c_int]),
     "mb_get_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),
     "mb_set_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),
     "mb_autotune": (C.c_int, [vp, u32, C.POINTER(MbTuning), C.POINTER(C.c_float), C.POINTER(MbTuning)]),

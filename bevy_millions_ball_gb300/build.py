@@ -33,6 +33,7 @@ UNITS = {
     "mb_count.cu": [],
     "mb_static.cu": [],
     "mb_segs.cu": [],
+    "mb_render.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
     "mb_batch.cu": [],
     "mb_physics.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
 }

@@ -72,7 +72,11 @@ struct mb_world {
     bool has_state = false;
     bool frame_done = false;           // a frame ran since the last upload
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    cudaGraphExec_t chain[2] = {nullptr, nullptr};  // kChainFrames LOOP frames from each parity
+    cudaGraphExec_t chain[2] = {nullptr, nullptr};  // chained LOOP frames from each parity
+    unsigned long long* zbuf = nullptr;             // render depth buffer (grown on demand)
+    size_t zbuf_pixels = 0;
+    uint32_t* img = nullptr;                        // render outputs for MB_HOST
+    float* img_h = nullptr;
     bool profiling = false;
     cudaEvent_t prof_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::string err;
@@ -332,6 +336,9 @@ mb_status mb_destroy(mb_world* w) {
     cudaFree(w->keys);
     cudaFree(w->sorted_keys);
     cudaFree(w->bands);
+    cudaFree(w->zbuf);
+    cudaFree(w->img);
+    cudaFree(w->img_h);
     cudaFree(w->perm);
     mb::scratch_free(w->scratch);
     mb::count_scratch_free(w->cnt);
@@ -545,6 +552,47 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
     if (to_counting && w->has_state) {  // counts were not kept while the radix sort ran
         cudaError_t e = recount(w);
         if (e) return cuda_fail(w, "mb_set_tuning", e);
+    }
+    return MB_OK;
+}
+
+mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float x0, float z0, float x1, float z1,
+                            uint32_t* rgba, float* height_map, mb_memory where) {
+    if (!w || !rgba) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
+    if (!w->has_state) return fail(w, MB_ERR_NOT_READY, "no state uploaded");
+    if (width == 0 || height == 0 || (uint64_t)width * height > (1ull << 28))
+        return fail(w, MB_ERR_INVALID_ARG, "image must have 1 .. 2^28 pixels");
+    if (!(x1 > x0) || !(z1 > z0) || !std::isfinite(x0) || !std::isfinite(x1) || !std::isfinite(z0) ||
+        !std::isfinite(z1))
+        return fail(w, MB_ERR_INVALID_ARG, "window must satisfy x0 < x1, z0 < z1 (finite)");
+    const size_t px = (size_t)width * height;
+    cudaError_t e;
+    if (px > w->zbuf_pixels) {
+        cudaFree(w->zbuf);
+        cudaFree(w->img);
+        cudaFree(w->img_h);
+        w->zbuf = nullptr;
+        w->img = nullptr;
+        w->img_h = nullptr;
+        w->zbuf_pixels = 0;
+        if ((e = cudaMalloc(&w->zbuf, sizeof(unsigned long long) * px)) ||
+            (e = cudaMalloc(&w->img, sizeof(uint32_t) * px)) || (e = cudaMalloc(&w->img_h, sizeof(float) * px)))
+            return cuda_fail(w, "mb_render_topdown", e);
+        w->zbuf_pixels = px;
+    }
+    const bool host = where == MB_HOST;
+    uint32_t* out = host ? w->img : rgba;
+    float* out_h = host ? w->img_h : (height_map ? height_map : w->img_h);
+    if ((e = mb::render_topdown(w->pos[w->cur], w->n, width, height, x0, z0, x1, z1, w->zbuf, out, out_h,
+                                w->stream)))
+        return cuda_fail(w, "mb_render_topdown", e);
+    if (host) {
+        if ((e = cudaMemcpyAsync(rgba, out, sizeof(uint32_t) * px, cudaMemcpyDeviceToHost, w->stream)))
+            return cuda_fail(w, "mb_render_topdown", e);
+        if (height_map &&
+            (e = cudaMemcpyAsync(height_map, out_h, sizeof(float) * px, cudaMemcpyDeviceToHost, w->stream)))
+            return cuda_fail(w, "mb_render_topdown", e);
+        if ((e = cudaStreamSynchronize(w->stream))) return cuda_fail(w, "mb_render_topdown", e);
     }
     return MB_OK;
 }

@@ -277,6 +277,12 @@ uint32_t segment_blocks(uint32_t n);
 cudaError_t assemble_segments(const uint32_t* sorted_keys, uint32_t n, uint32_t* block_scratch, uint32_t* segs,
                               uint32_t* key_seg_map, uint32_t* num_segs, cudaStream_t st);
 
+// Headless top-down impostor render of n spheres (mb_render.cu): w x h pixels
+// over the x/z window [x0, x1) x [z0, z1); zbuf: w*h 64-bit scratch; rgba and
+// height: w*h outputs on the device.
+cudaError_t render_topdown(const float4* pos, uint32_t n, uint32_t w, uint32_t h, float x0, float z0, float x1,
+                           float z1, unsigned long long* zbuf, uint32_t* rgba, float* height, cudaStream_t st);
+
 int device_sm_count();
 
 // Settings checks shared by worlds and batches ("" = valid).

@@ -253,6 +253,23 @@ mb_status mb_get_tuning(const mb_world* w, mb_tuning* out);
 mb_status mb_set_tuning(mb_world* w, const mb_tuning* t);
 
 /*
+ * Headless sphere-impostor render of the current state (the reference draws the
+ * spheres with src/custom_materials/physics_ball/deferred_physics_ball.wgsl and
+ * src/custom_materials/sdf.wgsl through Bevy's renderer): an orthographic view
+ * straight down onto the x/z window [x0, x1) x [z0, z1), width x height pixels,
+ * row v covering z = z0 + (v + 0.5)(z1 - z0)/height.  Per pixel the highest
+ * sphere surface (radius grown near the floor as the shader does) is marched 16
+ * steps on the smooth maximum (k = 0.08) of the sphere's and the floor's signed
+ * distances and lit by one directional light.  rgba: width*height u32 (R in the
+ * low byte, A = 255); height_map (nullable): width*height f32 surface heights
+ * (0 for the floor).  where: MB_DEVICE (device pointers, asynchronous on the
+ * world's stream) or MB_HOST (copied back, synchronous).  Keeps a per-world
+ * 8-byte-per-pixel depth buffer, grown on demand (allocates).
+ */
+mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float x0, float z0, float x1, float z1,
+                            uint32_t* rgba, float* height_map, mb_memory where);
+
+/*
  * Autotuner (no counterpart in the reference, whose sort and passes have fixed
  * workgroup shapes).  Times every candidate tuning on the world's own scene for
  * `frames` LOOP frames each (CUDA events on the world's stream, one warm-up

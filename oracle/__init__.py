@@ -38,6 +38,7 @@ _SIG = {
     "mbo_get_debug": (C.c_int, [vp, vp, vp, vp, vp]),
     "mbo_time": (i64, [vp]),
     "mbo_hardware_threads": (C.c_int, []),
+    "mbo_render_topdown": (None, [vp, u32, u32, u32, C.c_float, C.c_float, C.c_float, C.c_float, vp, vp, vp]),
 }
 
 _lib = None
@@ -133,6 +134,16 @@ class OracleWorld:
             self.close()
         except Exception:
             pass
+
+
+def render_topdown(pos: np.ndarray, width: int, height: int, x0: float, z0: float, x1: float, z1: float):
+    """Top-down impostor render: (rgba u32 (h, w), height f32 (h, w), winner u32 (h, w): sphere index + 1)."""
+    p = np.ascontiguousarray(pos, np.float32)
+    rgba = np.empty((height, width), np.uint32)
+    hmap = np.empty((height, width), np.float32)
+    win = np.empty((height, width), np.uint32)
+    lib().mbo_render_topdown(_p(p), p.shape[0], width, height, x0, z0, x1, z1, _p(rgba), _p(hmap), _p(win))
+    return rgba, hmap, win
 
 
 def hardware_threads() -> int:

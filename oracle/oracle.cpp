@@ -642,3 +642,110 @@ extern "C" int mbo_get_debug(const mbo_world* w, uint32_t* keys, uint32_t* perm,
 extern "C" int64_t mbo_time(const mbo_world* w) { return w ? w->time : -1; }
 
 extern "C" int mbo_hardware_threads(void) { return resolve_threads(0); }
+
+// ---------------------------------------------------------------- impostor render
+// Test infrastructure: CPU restatement of the headless top-down impostor render
+// (the per-fragment arithmetic of src/custom_materials/physics_ball/
+// deferred_physics_ball.wgsl:26-107 and src/custom_materials/sdf.wgsl:11-27,
+// 93-109 for an orthographic view straight down), in the same operation order
+// as the library's renderer so that results agree up to exp2/log2 rounding.
+namespace {
+struct RSphere {
+    float x, y, z, r;
+};
+RSphere grown(const float* p) {  // temporary_solution (deferred_physics_ball.wgsl:28-33)
+    float x = std::fmin(std::fmax(p[1] / p[3], 0.0f), 1.0f);
+    float y = 0.26f * (x - 1.0f) * (x - 1.0f) + 1.0f;
+    return {p[0], p[1], p[2], p[3] * y};
+}
+float len3r(float x, float y, float z) { return std::sqrt(x * x + y * y + z * z); }
+float smooth_max_r(float a, float b, float k) {
+    const float ki = 1.0f / k;
+    return k * std::log2(std::exp2(a * ki) + std::exp2(b * ki));
+}
+}  // namespace
+
+extern "C" void mbo_render_topdown(const float* pos4, uint32_t n, uint32_t w, uint32_t h, float x0, float z0,
+                                   float x1, float z1, uint32_t* rgba, float* height, uint32_t* winner) {
+    const float sx = (x1 - x0) / (float)w, sz = (z1 - z0) / (float)h;
+    std::vector<uint64_t> zb((size_t)w * h, 0ull);
+    for (uint32_t i = 0; i < n; ++i) {
+        const RSphere s = grown(pos4 + 4 * (size_t)i);
+        if (!(s.r > 0.0f)) continue;
+        const float u0 = std::ceil((s.x - s.r - x0) / sx - 0.5f), u1 = std::floor((s.x + s.r - x0) / sx - 0.5f);
+        const float v0 = std::ceil((s.z - s.r - z0) / sz - 0.5f), v1 = std::floor((s.z + s.r - z0) / sz - 0.5f);
+        if (!(u1 >= 0.0f && v1 >= 0.0f && u0 < (float)w && v0 < (float)h)) continue;
+        const int ua = (int)std::fmax(u0, 0.0f), ub = (int)std::fmin(u1, (float)w - 1.0f);
+        const int va = (int)std::fmax(v0, 0.0f), vb = (int)std::fmin(v1, (float)h - 1.0f);
+        const float r2 = s.r * s.r;
+        for (int v = va; v <= vb; ++v) {
+            const float dz = z0 + ((float)v + 0.5f) * sz - s.z;
+            for (int u = ua; u <= ub; ++u) {
+                const float dx = x0 + ((float)u + 0.5f) * sx - s.x;
+                const float c2 = r2 - (dx * dx + dz * dz);
+                if (c2 < 0.0f) continue;
+                float top = s.y + std::sqrt(c2);
+                top = top > 0.0f ? top : 0.0f;
+                uint32_t bits;
+                std::memcpy(&bits, &top, 4);
+                const uint64_t key = ((uint64_t)bits << 32) | (uint64_t)(i + 1u);
+                uint64_t& z = zb[(size_t)v * w + u];
+                if (key > z) z = key;
+            }
+        }
+    }
+    const float K = 0.08f;
+    for (size_t p = 0; p < (size_t)w * h; ++p) {
+        const uint32_t u = (uint32_t)(p % w), v = (uint32_t)(p / w);
+        const uint64_t key = zb[p];
+        const uint32_t floor_rgba = 0xFF4D4D4Du;
+        if (winner) winner[p] = (uint32_t)(key & 0xFFFFFFFFull);  // sphere index + 1, 0 = none
+        if (key == 0ull) {
+            rgba[p] = floor_rgba;
+            height[p] = 0.0f;
+            continue;
+        }
+        const RSphere s = grown(pos4 + 4 * (size_t)((uint32_t)(key & 0xFFFFFFFFull) - 1u));
+        float hx = x0 + ((float)u + 0.5f) * sx, hz = z0 + ((float)v + 0.5f) * sz;
+        const uint32_t hb = (uint32_t)(key >> 32);
+        float hy;
+        std::memcpy(&hy, &hb, 4);
+        float nx = hx - s.x, ny = hy - s.y, nz = hz - s.z;
+        const float nl = len3r(nx, ny, nz);
+        nx /= nl;
+        ny /= nl;
+        nz /= nl;
+        float sd_sphere = 0.0f, sd_plane = -hy;
+        bool hit = false;
+        for (int it = 0; it < 16; ++it) {
+            const float d = smooth_max_r(sd_sphere, sd_plane, K);
+            hy -= d;
+            if (d < 0.001f) {
+                hit = true;
+                break;
+            }
+            sd_sphere = len3r(hx - s.x, hy - s.y, hz - s.z) - s.r;
+            sd_plane = -hy;
+        }
+        if (!hit) {
+            rgba[p] = floor_rgba;
+            height[p] = 0.0f;
+            continue;
+        }
+        const float hh = (sd_plane - sd_sphere) / K;
+        const float pa = 1.0f / (1.0f + std::exp2(hh)), pb = 1.0f / (1.0f + std::exp2(-hh));
+        float gx = pa * nx, gy = pa * ny - pb, gz = pa * nz;
+        const float gl = len3r(gx, gy, gz);
+        if (gl > 0.0f) {
+            gx /= gl;
+            gy /= gl;
+            gz /= gl;
+        }
+        const float lx = 0.3713907f, ly = 0.9284767f, lz = 0.0f;
+        const float lit = 0.25f + 0.75f * std::fmax(gx * lx + gy * ly + gz * lz, 0.0f);
+        const uint32_t r = (uint32_t)std::fmin(255.0f * lit + 0.5f, 255.0f);
+        const uint32_t g = (uint32_t)std::fmin(191.0f * lit + 0.5f, 255.0f);
+        rgba[p] = 0xFF000000u | r | (g << 8);
+        height[p] = hy;
+    }
+}

@@ -80,6 +80,12 @@ int mbo_get_debug(const mbo_world* w, uint32_t* keys, uint32_t* perm, uint32_t* 
 int64_t mbo_time(const mbo_world* w);
 int mbo_hardware_threads(void);
 
+/* Top-down impostor render (deferred_physics_ball.wgsl + sdf.wgsl per-pixel
+ * math, orthographic view down -y onto [x0, x1) x [z0, z1)): rgba u32 and
+ * surface height per pixel; winner (nullable) = sphere index + 1, 0 = floor. */
+void mbo_render_topdown(const float* pos4, uint32_t n, uint32_t w, uint32_t h, float x0, float z0, float x1,
+                        float z1, uint32_t* rgba, float* height, uint32_t* winner);
+
 #ifdef __cplusplus
 }
 #endif
