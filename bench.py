@@ -357,16 +357,26 @@ def run_ours(args, rank, world_size, local_rank):
     return 0
 
 
-def run_batch(args):
-    """Batching workload: independent scenes (log-uniform sizes) stepped together vs one at a time."""
+def run_batch(args, rank=0, world_size=1, local_rank=0):
+    """Batching workload: independent scenes (log-uniform sizes) stepped together vs one at a time.
+    Under N ranks every rank steps its own share of the scenes (sharding.partition_by_size) on its
+    own GPU; nothing is exchanged but the timing (max over ranks)."""
     import numpy as np
     import torch
 
     from bevy_millions_ball_gb300 import Batch, World, scenes
+    from bevy_millions_ball_gb300.sharding import my_scenes
 
-    torch.cuda.set_device(0)
-    scs = scenes.batch(count=args.batch_scenes, seed=0)
-    total = sum(s.n for s in scs)
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    all_scs = scenes.batch(count=args.batch_scenes, seed=0)
+    mine = my_scenes([s.n for s in all_scs], rank, world_size)
+    scs = [all_scs[i] for i in mine]
+    total = sum(s.n for s in all_scs)
     stream = torch.cuda.current_stream()
     K = args.steps
     b = Batch([s.plugin for s in scs], stream=stream.cuda_stream)
@@ -375,11 +385,18 @@ def run_batch(args):
     b.step(1 + max(args.warmup, 3))
     b.sync()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
     e0.record(stream)
     b.step(K)
     e1.record(stream)
     b.sync()
     t_batch = e0.elapsed_time(e1) * 1e-3
+    if dist:
+        t = torch.tensor([t_batch], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_batch = float(t.item())
     mem = b.memory()
     b.close()
     # the plain loop: each scene in its own world, one after the other
@@ -398,15 +415,24 @@ def run_batch(args):
     t_plain = e0.elapsed_time(e1) * 1e-3
     for w in worlds:
         w.close()
-    sizes = np.array([s.n for s in scs])
+    if dist:
+        t = torch.tensor([t_plain], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_plain = float(t.item())
+        dist.destroy_process_group()
+    if rank != 0:
+        return 0
+    sizes = np.array([s.n for s in all_scs])
     line = {
         "metric": "agent-steps/s (batched scenes)", "value": total * K / t_batch, "unit": "agent-steps/s",
-        "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": 1e3 * t_batch / K,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "n_gpus": world_size, "steps": K, "warmup": args.warmup, "ms_per_step": 1e3 * t_batch / K,
+        "higher_is_better": True, "scaling": "strong" if world_size > 1 else "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"batch: {len(scs)} scenes, n log-uniform [1024, 262144], total {total:,} spheres, "
                                "N = next_pow2(sqrt n), H in {4,8,16}, e in [0.5,0.95], half spring",
                    "spheres_total": int(total), "median_scene": int(np.median(sizes)), "pool_bytes": int(mem),
-                   "l2": "pool larger than L2"},
+                   "l2": "pool larger than L2",
+                   "parallelism": f"scene shards x{world_size} (no collective)" if world_size > 1 else "single"},
         "plain_loop": {"value": total * K / t_plain, "ms_per_step": 1e3 * t_plain / K,
                        "what": "same scenes, each in its own world, stepped one after the other"},
         "speedup_vs_plain_loop": t_plain / t_batch,
@@ -532,7 +558,7 @@ def main():
 
     build()
     if args.workload == "batch":
-        return run_batch(args)
+        return run_batch(args, rank, world_size, local_rank)
     if args.workload == "serving":
         return run_serving(args)
     return run_ours(args, rank, world_size, local_rank)
