@@ -131,12 +131,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_oracle_run(scene, frames_budget_s: float, max_frames: int | None = None):
+def cpu_oracle_run(scene, frames_budget_s: float, max_frames: int | None = None, threads: int | None = None):
     """Time the oracle (CPU restatement) on the scene: INIT untimed, then LOOP frames
     until the time budget is spent.  Returns (agent-steps/s, frames, seconds, threads)."""
     import oracle
 
-    threads = oracle.hardware_threads()
+    threads = threads or oracle.hardware_threads()
     ow = oracle.OracleWorld(scene.plugin.to_c(), threads=threads)
     ow.set_state(scene.pos_scale, scene.vfme)
     ow.step(1)  # INIT frame
@@ -328,8 +328,10 @@ def run_ours(args, rank, world_size, local_rank):
     cpu = None
     if world_size == 1 and not args.no_cpu_baseline:
         v, frames, el, thr = cpu_oracle_run(sc, args.cpu_seconds)
+        v1, frames1, el1, _ = cpu_oracle_run(sc, max(args.cpu_seconds / 4.0, 1.0), threads=1)
         cpu = {"value": v, "unit": "agent-steps/s", "cores": thr, "kind": "port",
-               "sample": f"{frames} LOOP frames of the same {n:,}-sphere scene ({el:.1f} s wall), oracle, {thr} threads"}
+               "sample": f"{frames} LOOP frames of the same {n:,}-sphere scene ({el:.1f} s wall), oracle, {thr} threads",
+               "one_thread": {"value": v1, "sample": f"{frames1} LOOP frames ({el1:.1f} s wall), 1 thread"}}
     line = {
         "metric": "agent-steps/s", "value": value, "unit": "agent-steps/s", "n_gpus": world_size,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,

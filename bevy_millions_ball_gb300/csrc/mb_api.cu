@@ -64,7 +64,7 @@ struct mb_world {
     uint4* bands = nullptr;            // band table of the sorted order (written by the sort)
     uint32_t* perm = nullptr;
     mb::SortScratch scratch;      // onesweep sort scratch + the cell offsets (offs)
-    mb::CountScratch cnt;         // counting-sort scratch (per-cell counts, cursors)
+    mb::CountScratch cnt;         // counting-sort scratch (per-cell and per-tile counts, fixup lists)
     mb::SortSchedule sched;
     mb_tuning tuning{};
     int cur = 0;

@@ -126,7 +126,7 @@ void drop_graphs(mb_batch* b) {
 }
 
 uint64_t bytes_for(uint64_t agents, uint64_t cells, uint64_t scenes) {
-    // state x2, sorted copy, keys, perm; offs; counts, cursors, fixup lists; tile and band tables
+    // state x2, sorted copy, keys, perm; offs; counts, fixup lists; tile and band tables
     return agents * (32u * 3u + 8u) + cells * 4u + mb::count_scratch_bytes((uint32_t)cells, (uint32_t)agents) +
            scenes * sizeof(mb::SceneDev) + (agents / kTile + 1u) * (4u + 32u) + 64u * 1024u;
 }

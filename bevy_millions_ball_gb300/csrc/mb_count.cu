@@ -8,18 +8,20 @@
 //   1. per-cell counts, accumulated by the physics pass of the previous frame as
 //      it emits the keys (one red.add per sphere);
 //   2. k_cell_scan: one exclusive scan turns the counts into the cell offsets
-//      offs[c] (= start of cell c; offs[C] = n) and a cursor copy; each
+//      offs[c] (= start of cell c; offs[C] = n); each
 //      1024-cell chunk takes its base from per-4096-cell-tile counts emitted with
 //      the per-cell ones (plus the counts of its tile's earlier chunks), so
 //      chunks never wait on each other;
 //   3. k_cell_scatter: each sphere claims a slot of its cell with one atomic per
-//      run of equal keys in its warp (match.any), so spheres of one warp keep
-//      their order, and its 32-byte state is copied to that slot; the run that
+//      run of equal keys in its warp (match.any) - it subtracts the run's length
+//      from the cell's count, and the count left before it says where the run
+//      starts (offs[c+1] - left), so the counts are back to zero when the
+//      scatter ends - spheres of one warp keep their order, and its 32-byte
+//      state is copied to that slot; the run that
 //      fills a cell last lists the cell if earlier runs of other warps got there
 //      first (only such cells can be out of order);
 //   4. k_cell_fix: the listed cells' slots are put back in ascending input order
-//      (what a stable sort yields), re-gathering their state copy; it also
-//      clears the counts for the next frame.
+//      (what a stable sort yields), re-gathering their state copy.
 //
 // The result is bit-identical to a stable sort; offs[] replaces start/close.
 
@@ -46,7 +48,7 @@ namespace {
 template <bool kScenes>
 __global__ void __launch_bounds__(kScanThreads)
     k_cell_scan(const uint32_t* __restrict__ hist, const uint32_t* __restrict__ coarse, uint32_t cells,
-                uint32_t* __restrict__ offs, uint32_t* __restrict__ cursor, uint32_t* fix_ctl,
+                uint32_t* __restrict__ offs, uint32_t* fix_ctl,
                 const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ cell_tile_scene) {
     constexpr int W = kScanThreads / 32;
     __shared__ uint32_t s_warp[W], s_base[W];
@@ -110,7 +112,6 @@ __global__ void __launch_bounds__(kScanThreads)
     }
     if (base + kScanItems <= cells) {
         uint4* o4 = reinterpret_cast<uint4*>(offs + base);
-        uint4* c4 = reinterpret_cast<uint4*>(cursor + base);
 #pragma unroll
         for (int q = 0; q < kScanItems / 4; ++q) {
             uint4 x;
@@ -119,7 +120,6 @@ __global__ void __launch_bounds__(kScanThreads)
             x.z = run; run += v[4 * q + 2];
             x.w = run; run += v[4 * q + 3];
             o4[q] = x;
-            c4[q] = x;
         }
         // end of the tile: the next tile's first offset, or the scene's / table's end
         if (base + kScanItems == cells || (kScenes && tid == kScanThreads - 1)) offs[base + kScanItems] = run;
@@ -128,7 +128,6 @@ __global__ void __launch_bounds__(kScanThreads)
             uint32_t c = base + q;
             if (c < cells) {
                 offs[c] = run;
-                cursor[c] = run;
                 run += v[q];
                 if (c + 1u == cells) offs[cells] = run;
             }
@@ -182,7 +181,7 @@ __device__ __forceinline__ int fix_class(const uint32_t* __restrict__ offs, uint
 // tile's band table entry (the cell of a slot is final here; the fixup only
 // reorders slots inside a cell).
 __global__ void __launch_bounds__(256)
-    k_cell_scatter(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ cursor,
+    k_cell_scatter(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
                    uint32_t* __restrict__ perm, const float4* __restrict__ pos_in,
                    const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
                    uint4* __restrict__ svfme, const uint32_t* __restrict__ offs, uint4* __restrict__ bands,
@@ -209,8 +208,9 @@ __global__ void __launch_bounds__(256)
         uint32_t b = 0;
         int cls = -1;
         if (valid && !ident && lane == leader) {
-            b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
-            cls = fix_class(offs, k, b, (uint32_t)__popc(peers));
+            const uint32_t g = (uint32_t)__popc(peers);
+            b = __ldg(offs + k + 1u) - atomicSub(hist + k, g);  // the run's first slot
+            cls = fix_class(offs, k, b, g);
         }
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
         {
@@ -220,6 +220,7 @@ __global__ void __launch_bounds__(256)
         }
         if (valid) {
             const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
+            if (dst >= n) continue;  // only counts that disagree with the keys get here
             perm[dst] = i;
             spos[dst] = p;
             svfme[dst] = q;
@@ -232,7 +233,7 @@ __global__ void __launch_bounds__(256)
 // holding its state; spheres of HOLD scenes are left alone.
 __global__ void __launch_bounds__(256)
     k_cell_scatter_scenes(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
-                          const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ cursor,
+                          const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
                           uint32_t* __restrict__ perm, const float4* __restrict__ pos0,
                           const float4* __restrict__ pos1, const uint4* __restrict__ vfme0,
                           const uint4* __restrict__ vfme1, float4* __restrict__ spos, uint4* __restrict__ svfme,
@@ -264,8 +265,9 @@ __global__ void __launch_bounds__(256)
         uint32_t b = 0;
         int cls = -1;
         if (valid && !ident && lane == leader) {
-            b = atomicAdd(cursor + k, (uint32_t)__popc(peers));
-            cls = fix_class(offs, k, b, (uint32_t)__popc(peers));
+            const uint32_t g = (uint32_t)__popc(peers);
+            b = __ldg(offs + k + 1u) - atomicSub(hist + k, g);  // the run's first slot
+            cls = fix_class(offs, k, b, g);
         }
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
         {
@@ -275,6 +277,7 @@ __global__ void __launch_bounds__(256)
         }
         if (valid) {
             const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
+            if (dst >= n) continue;  // only counts that disagree with the keys get here
             perm[dst] = i;
             spos[dst] = p;
             svfme[dst] = q;
@@ -337,6 +340,8 @@ struct OneBuffer {
     const float4* p;
     const uint4* q;
     __device__ __forceinline__ bool tile_active(uint32_t) const { return true; }
+    __device__ __forceinline__ bool any_init() const { return false; }
+    __device__ __forceinline__ bool tile_init(uint32_t) const { return false; }
     __device__ __forceinline__ float4 pos(uint32_t o) const { return __ldg(p + o); }
     __device__ __forceinline__ uint4 vfme(uint32_t o) const { return __ldg(q + o); }
 };
@@ -351,6 +356,10 @@ struct SceneBuffers {
     const uint4* q1;
     __device__ __forceinline__ bool tile_active(uint32_t t) const {
         return __ldg(&scenes[__ldg(cell_tile_scene + t)].mode) != kModeHold;
+    }
+    __device__ __forceinline__ bool any_init() const { return true; }
+    __device__ __forceinline__ bool tile_init(uint32_t t) const {
+        return __ldg(&scenes[__ldg(cell_tile_scene + t)].mode) == kModeInit;
     }
     __device__ __forceinline__ uint32_t parity(uint32_t o) const {
         uint32_t s = __ldg(slot_tile_scene + o / kPhysicsTile);
@@ -413,12 +422,15 @@ __global__ void __launch_bounds__(kFixThreads)
     griddep_wait();
     griddep_launch();
     const uint32_t tid = threadIdx.x, lane = tid & 31u;
-    // the scan of this frame is over: clear the cell and tile counts for the next one
+    // the scan of this frame is over: clear the tile counts for the next one; the
+    // cell counts went back to zero in the scatter, except those of scenes in
+    // their INIT frame (placed in identity order, nothing subtracted)
     if (blockIdx.x == 0)
         for (uint32_t t = tid; t < tiles; t += blockDim.x)
             if (src.tile_active(t)) coarse[t] = 0u;
-    for (uint32_t c = (blockIdx.x * blockDim.x + tid) * 4u; c < cells; c += gridDim.x * blockDim.x * 4u)
-        if (src.tile_active(c / kScanTile)) *reinterpret_cast<uint4*>(hist + c) = make_uint4(0u, 0u, 0u, 0u);
+    if (src.any_init())
+        for (uint32_t c = (blockIdx.x * blockDim.x + tid) * 4u; c < cells; c += gridDim.x * blockDim.x * 4u)
+            if (src.tile_init(c / kScanTile)) *reinterpret_cast<uint4*>(hist + c) = make_uint4(0u, 0u, 0u, 0u);
 
     const uint32_t* __restrict__ small = lists.list[0];
     const uint32_t* __restrict__ mid = lists.list[1];
@@ -633,7 +645,7 @@ uint32_t fix_capacity(int cls, uint32_t max_cells, uint32_t max_keys) {
 
 uint64_t count_scratch_bytes(uint32_t max_cells, uint32_t max_keys) {
     const uint64_t padded = ((uint64_t)max_cells + kScanTile) & ~(uint64_t)15;
-    uint64_t b = 4u * (2u * padded + (max_cells + kScanTile - 1u) / kScanTile + 1u + kFixLists);
+    uint64_t b = 4u * (padded + (max_cells + kScanTile - 1u) / kScanTile + 1u + kFixLists);
     for (int c = 0; c < kFixLists; ++c) b += 4u * fix_capacity(c, max_cells, max_keys);
     return b + 4u * ((uint64_t)max_keys + 1u);
 }
@@ -644,7 +656,6 @@ cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells, uint32_t ma
     s.tiles = (max_cells + kScanTile - 1u) / kScanTile;
     cudaError_t e;
     if ((e = cudaMalloc(&s.hist, sizeof(uint32_t) * padded))) return e;
-    if ((e = cudaMalloc(&s.cursor, sizeof(uint32_t) * padded))) return e;
     if ((e = cudaMalloc(&s.coarse, sizeof(uint32_t) * (s.tiles + 1u)))) return e;
     if ((e = cudaMalloc(&s.fix_ctl, sizeof(uint32_t) * kFixLists))) return e;
     if ((e = cudaMalloc(&s.fix_tmp, sizeof(uint32_t) * ((size_t)max_keys + 1u)))) return e;
@@ -660,7 +671,6 @@ cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells, uint32_t ma
 
 void count_scratch_free(CountScratch& s) {
     cudaFree(s.hist);
-    cudaFree(s.cursor);
     cudaFree(s.coarse);
     cudaFree(s.fix_ctl);
     cudaFree(s.fix_tmp);
@@ -694,7 +704,7 @@ cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t*
     (void)ctl;
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
     return launch_pdl(pdl, k_cell_scan<false>, dim3(chunks), dim3(kScanThreads), 0, st, (const uint32_t*)s.hist,
-                      (const uint32_t*)s.coarse, cells, offs, s.cursor, s.fix_ctl, (const SceneDev*)nullptr,
+                      (const uint32_t*)s.coarse, cells, offs, s.fix_ctl, (const SceneDev*)nullptr,
                       (const uint32_t*)nullptr);
 }
 
@@ -704,7 +714,7 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
     cudaError_t e;
     if (n) {
         uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
-        if ((e = launch_pdl(pdl, k_cell_scatter, dim3(blocks), dim3(256), 0, st, keys, n, s.cursor, perm, pos_in,
+        if ((e = launch_pdl(pdl, k_cell_scatter, dim3(blocks), dim3(256), 0, st, keys, n, s.hist, perm, pos_in,
                             vfme_in, spos, svfme, offs, bands, N, fix_lists(s))))
             return e;
     }
@@ -716,7 +726,7 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
                               uint32_t cells, uint32_t* offs, cudaStream_t st) {
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
-    k_cell_scan<true><<<chunks, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.cursor, s.fix_ctl, scenes,
+    k_cell_scan<true><<<chunks, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.fix_ctl, scenes,
                                                       cell_tile_scene);
     return cudaGetLastError();
 }
@@ -729,7 +739,7 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
     cudaError_t e;
     if (n) {
         uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
-        k_cell_scatter_scenes<<<blocks, 256, 0, st>>>(scenes, tile_scene, keys, n, s.cursor, perm, pos_buf0,
+        k_cell_scatter_scenes<<<blocks, 256, 0, st>>>(scenes, tile_scene, keys, n, s.hist, perm, pos_buf0,
                                                       pos_buf1, vfme_buf0, vfme_buf1, spos, svfme, offs,
                                                       fix_lists(s), bands);
         if ((e = cudaGetLastError())) return e;

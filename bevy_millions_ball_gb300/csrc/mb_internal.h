@@ -215,7 +215,6 @@ enum : int { kFixListSmall = 0, kFixListWarp = 1, kFixListHuge = 2, kFixLists = 
 struct CountScratch {
     uint32_t max_cells = 0;
     uint32_t* hist = nullptr;     // [max_cells] counts of the keys of the next sort
-    uint32_t* cursor = nullptr;   // [max_cells] scatter cursors
     uint32_t* coarse = nullptr;   // [tiles] counts per 4096-cell scan tile
     uint32_t* fix_ctl = nullptr;  // [kFixLists] lengths of the fixup lists
     uint32_t* fix[kFixLists] = {nullptr, nullptr, nullptr};  // listed cells, by size class
@@ -234,8 +233,8 @@ cudaError_t count_keys(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
                        cudaStream_t st);
 // hist := counts of n all-zero keys (a fresh upload).
 cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, cudaStream_t st);
-// offs[0..cells] := exclusive scan of hist (offs[cells] = n), cursors := offs; the
-// counts are cleared later in the frame by the fixup of count_scatter.
+// offs[0..cells] := exclusive scan of hist (offs[cells] = n); the scatter of
+// count_scatter then counts hist back down to zero.
 cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st,
                        bool pdl = false);
 // coarse[t] := sum of hist over scan tile t (after a pass that emitted cell counts
@@ -246,9 +245,10 @@ cudaError_t count_tile_counts_scenes(CountScratch& s, const SceneDev* scenes, co
 // INIT frame after an upload (all keys 0): perm := identity, offs := [0, n, .., n], hist := 0.
 cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32_t* offs, uint32_t* perm,
                              cudaStream_t st);
-// perm := stable permutation sorting keys by cell, from the cursors of count_scan;
-// spos/svfme := the state in that order (spos[j] = pos_in[perm[j]]); bands
-// (nullable) := the band table of that order for an N x N grid; hist, coarse := 0.
+// perm := stable permutation sorting keys by cell, from the offsets of count_scan
+// and the counts in hist (counted back down to 0); spos/svfme := the state in that
+// order (spos[j] = pos_in[perm[j]]); bands (nullable) := the band table of that
+// order for an N x N grid; coarse := 0.
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
                           float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,

@@ -35,7 +35,7 @@ typedef enum mb_status {
     MB_ERR_INVALID_ARG = 1,     /* bad pointer, size or setting                         */
     MB_ERR_OOM = 2,             /* device or host allocation failed                     */
     MB_ERR_CUDA = 3,            /* a CUDA runtime call failed (see mb_last_error)       */
-    MB_ERR_TIMEOUT = 4,         /* a bounded device-side wait gave up (sort look-back)  */
+    MB_ERR_TIMEOUT = 4,         /* a bounded device-side wait gave up (sort look-back or band copy) */
     MB_ERR_BUDGET_EXCEEDED = 5, /* the request does not fit the device-memory budget    */
     MB_ERR_NOT_READY = 6        /* state was never uploaded / request still running     */
 } mb_status;
@@ -245,7 +245,7 @@ typedef struct mb_tuning {
 
 /* Frame sort: both produce the identical stable permutation and cell ranges.
  *   MB_SORT_COUNTING: per-cell counts (emitted by the previous physics pass) ->
- *                     look-back scan = cell offsets -> scatter -> in-cell fixup
+ *                     scan = cell offsets -> scatter -> in-cell fixup
  *   MB_SORT_ONESWEEP: onesweep LSD radix sort of the keys, then the cell-offset build */
 #define MB_SORT_COUNTING 0u
 #define MB_SORT_ONESWEEP 1u
