@@ -30,6 +30,7 @@ enum : int {
     kCtlDone = kMaxPasses,        // histogram blocks finished
     kCtlError = kMaxPasses + 1,   // nonzero: a bounded wait gave up
     kCtlEpoch = kMaxPasses + 2,   // look-back epoch of the running sort (1..3)
+    kCtlGaps = kMaxPasses + 3,    // long cell gaps listed by the cell-offset build
     kCtlWords = 8
 };
 
@@ -58,11 +59,16 @@ struct SortScratch {
     uint32_t* lookback = nullptr;   // [kMaxPasses][tiles_max * kMaxRadix]
     uint32_t* ctl = nullptr;        // [kCtlWords]
     uint32_t* offs = nullptr;       // [max_cells + 1] cell offsets (CSR)
+    uint32_t* gaps = nullptr;       // [3 * gap_capacity(max_cells)] long runs of cells to fill
     size_t lookback_words_per_pass = 0;
     uint32_t last_tiles = 0;        // tiles of the previous sort (look-back reuse check)
     int last_passes = 0;
 };
 
+// Runs of more than kGapCells cells between consecutive sorted keys are written
+// by a fill kernel from a list instead of by one thread each.
+constexpr uint32_t kGapCells = 64;
+inline uint32_t gap_capacity(uint32_t max_cells) { return max_cells / kGapCells + 2u; }
 cudaError_t scratch_alloc(SortScratch& s, uint32_t max_keys, uint32_t max_cells);
 void scratch_free(SortScratch& s);
 

@@ -12,12 +12,12 @@
 // digit offsets by decoupled look-back over predecessor tiles, stages the tile in
 // shared memory in digit order and writes it out in contiguous runs.
 //
-// Cell offsets: offs[c] = number of keys < c, c in [0, cells].  One block per value
-// of the most significant digit: that digit's keys occupy the contiguous slot
-// range [base[d], base[d+1]) and cover a contiguous block of cells, so every
-// cell's offset is a lower_bound into at most one chunk, done in shared memory.
-// start[c] / close[c] of the reference are offs[c] / offs[c+1]-1 for non-empty
-// cells.
+// Cell offsets: offs[c] = number of keys < c, c in [0, cells].  Sorted slot i
+// (and one extra thread for the end) writes offs[c] = i for the cells c in
+// (key[i-1], key[i]]: every cell is written once, coalesced where keys are
+// dense; a run longer than kGapCells cells is listed and filled by a second
+// kernel across many threads.  start[c] / close[c] of the reference are offs[c]
+// / offs[c+1]-1 for non-empty cells.
 
 #include <cuda_runtime.h>
 
@@ -56,8 +56,23 @@ struct HistParams {
 };
 
 // ---------------------------------------------------------------- histogram
-// Digit counts of every pass in one read of the keys; the block that finishes
-// last turns the counts into exclusive bases and zeroes them for the next sort.
+// Digit counts of every pass in one read of the keys (shared-memory atomics; a
+// warp whose lanes share a digit adds once); the block that finishes last turns
+// the counts into exclusive bases and zeroes them for the next sort.
+__device__ __forceinline__ void hist_key(uint32_t* s_hist, const HistParams& hp, uint32_t key, bool full_warp) {
+    for (int p = 0; p < hp.passes; ++p) {
+        const uint32_t d = (key >> hp.shift[p]) & ((1u << hp.bits[p]) - 1u);
+        if (full_warp) {
+            const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
+            if (__all_sync(0xFFFFFFFFu, d == d0)) {
+                if ((threadIdx.x & 31u) == 0u) atomicAdd(&s_hist[hp.hist_off[p] + d], 32u);
+                continue;
+            }
+        }
+        atomicAdd(&s_hist[hp.hist_off[p] + d], 1u);
+    }
+}
+
 __global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n,
                                                    HistParams hp, uint32_t* counts,
                                                    uint32_t* bases, uint32_t* ctl) {
@@ -67,20 +82,25 @@ __global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ 
     const uint32_t tid = threadIdx.x, lane = tid & 31u;
     for (uint32_t b = tid; b < hp.total_bins; b += blockDim.x) s_hist[b] = 0;
     if (blockIdx.x == 0 && tid < (uint32_t)kMaxPasses) ctl[kCtlTile0 + tid] = 0;
+    if (blockIdx.x == 0 && tid == 0) ctl[kCtlGaps] = 0;  // the cell-offset build of this sort lists anew
     __syncthreads();
 
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
-        uint32_t i = i0 + tid;
-        bool valid = i < n;
-        uint32_t key = valid ? __ldg(keys + i) : 0u;
-        for (int p = 0; p < hp.passes; ++p) {
-            uint32_t d = valid ? ((key >> hp.shift[p]) & ((1u << hp.bits[p]) - 1u)) : 0xFFFFFFFFu;
-            uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-            if (valid && lane == (uint32_t)(__ffs(peers) - 1))
-                atomicAdd(&s_hist[hp.hist_off[p] + d], (uint32_t)__popc(peers));
+    const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0u;
+    const uint32_t n4 = vec ? n / 4u : 0u;  // whole uint4 groups, read four keys at a time
+    for (uint32_t g0 = blockIdx.x * blockDim.x; g0 < n4; g0 += stride) {
+        const uint32_t g = g0 + tid;
+        const bool full = g0 + blockDim.x <= n4;  // every lane of the block has a group
+        if (g < n4) {
+            const uint4 k4 = __ldg(reinterpret_cast<const uint4*>(keys) + g);
+            hist_key(s_hist, hp, k4.x, full);
+            hist_key(s_hist, hp, k4.y, full);
+            hist_key(s_hist, hp, k4.z, full);
+            hist_key(s_hist, hp, k4.w, full);
         }
     }
+    for (uint32_t i = 4u * n4 + blockIdx.x * blockDim.x + tid; i < n; i += stride)
+        hist_key(s_hist, hp, __ldg(keys + i), false);
     __syncthreads();
     for (int p = 0; p < hp.passes; ++p) {
         uint32_t R = 1u << hp.bits[p];
@@ -304,39 +324,37 @@ __global__ void __launch_bounds__(THREADS)
 }
 
 // ---------------------------------------------------------------- cell offsets
-constexpr int kOffsThreads = 256;
-constexpr uint32_t kOffsBatch = 1024;
-
-__global__ void __launch_bounds__(kOffsThreads)
-    k_cell_offsets(const uint32_t* __restrict__ sorted_keys, uint32_t cells, uint32_t chunk_shift,
-                   uint32_t chunks, const uint32_t* __restrict__ top_bases, uint32_t* offs) {
-    __shared__ uint32_t s_k[kOffsBatch];
-    const uint32_t d = blockIdx.x;
-    const uint64_t cell_lo64 = (uint64_t)d << chunk_shift;
-    if (cell_lo64 > cells) return;
-    const uint32_t cell_lo = (uint32_t)cell_lo64;
-    uint64_t hi64 = (uint64_t)(d + 1u) << chunk_shift;
-    uint32_t cell_hi = (d == chunks - 1u || hi64 > (uint64_t)cells + 1u) ? cells + 1u : (uint32_t)hi64;
-    const uint32_t slot_lo = __ldg(top_bases + d), slot_hi = __ldg(top_bases + d + 1u);
-    uint32_t next_cell = cell_lo;
-    for (uint32_t p0 = slot_lo; p0 < slot_hi; p0 += kOffsBatch) {
-        uint32_t cnt = min(kOffsBatch, slot_hi - p0);
-        for (uint32_t i = threadIdx.x; i < cnt; i += kOffsThreads) s_k[i] = __ldg(sorted_keys + p0 + i);
-        __syncthreads();
-        uint32_t last = min(s_k[cnt - 1u], cells);  // keys >= cells are a caller error; stay in bounds
-        for (uint32_t c = next_cell + threadIdx.x; c <= last; c += kOffsThreads) {
-            uint32_t lo = 0, hi = cnt;  // first index with s_k[idx] >= c
-            while (lo < hi) {
-                uint32_t mid = (lo + hi) >> 1;
-                if (s_k[mid] < c) lo = mid + 1u;
-                else hi = mid;
-            }
-            offs[c] = p0 + lo;
-        }
-        next_cell = last + 1u;
-        __syncthreads();
+// Thread i in [0, n] writes offs[c] = i for c in (key[i-1], key[i]] (key[-1] =
+// -1, key[n] = cells; keys clamped to cells).
+__global__ void __launch_bounds__(256)
+    k_cell_offsets(const uint32_t* __restrict__ sorted_keys, uint32_t n, uint32_t cells, uint32_t* offs,
+                   uint32_t* gaps, uint32_t gap_cap, uint32_t* gap_count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    const uint32_t k = i < n ? min(__ldg(sorted_keys + i), cells) : cells;
+    const uint32_t from = i > 0u ? min(__ldg(sorted_keys + i - 1u), cells) + 1u : 0u;
+    if (from > k) return;  // same cell as the previous key (or a caller's unsorted input)
+    if (k - from < kGapCells) {
+        for (uint32_t c = from; c <= k; ++c) offs[c] = i;
+        return;
     }
-    for (uint32_t c = next_cell + threadIdx.x; c < cell_hi; c += kOffsThreads) offs[c] = slot_hi;
+    const uint32_t g = atomicAdd(gap_count, 1u);
+    if (g < gap_cap) {
+        gaps[3u * g] = from;
+        gaps[3u * g + 1u] = k;
+        gaps[3u * g + 2u] = i;
+    }
+}
+
+// Each block fills listed runs (run e = blockIdx.x, + gridDim.x, ...).
+__global__ void __launch_bounds__(256)
+    k_fill_gaps(const uint32_t* __restrict__ gaps, uint32_t gap_cap, const uint32_t* __restrict__ gap_count,
+                uint32_t* offs) {
+    const uint32_t m = min(*gap_count, gap_cap);
+    for (uint32_t e = blockIdx.x; e < m; e += gridDim.x) {
+        const uint32_t from = gaps[3u * e], to = gaps[3u * e + 1u], v = gaps[3u * e + 2u];
+        for (uint32_t c = from + threadIdx.x; c <= to; c += blockDim.x) offs[c] = v;
+    }
 }
 
 __global__ void k_offs_to_start_close(const uint32_t* __restrict__ offs, uint32_t cells,
@@ -418,6 +436,7 @@ cudaError_t scratch_alloc(SortScratch& s, uint32_t max_keys, uint32_t max_cells)
     if ((e = cudaMalloc(&s.lookback, sizeof(uint32_t) * kMaxPasses * s.lookback_words_per_pass))) return e;
     if ((e = cudaMalloc(&s.ctl, sizeof(uint32_t) * kCtlWords))) return e;
     if ((e = cudaMalloc(&s.offs, sizeof(uint32_t) * ((size_t)max_cells + 1u)))) return e;
+    if ((e = cudaMalloc(&s.gaps, sizeof(uint32_t) * 3u * gap_capacity(max_cells)))) return e;
     if ((e = cudaMemset(s.counts, 0, sizeof(uint32_t) * kMaxPasses * kMaxRadix))) return e;
     if ((e = cudaMemset(s.lookback, 0, sizeof(uint32_t) * kMaxPasses * s.lookback_words_per_pass))) return e;
     if ((e = cudaMemset(s.ctl, 0, sizeof(uint32_t) * kCtlWords))) return e;
@@ -438,6 +457,7 @@ void scratch_free(SortScratch& s) {
     cudaFree(s.lookback);
     cudaFree(s.ctl);
     cudaFree(s.offs);
+    cudaFree(s.gaps);
     s = SortScratch();
 }
 
@@ -467,7 +487,7 @@ cudaError_t sort_pairs(SortScratch& s, const SortSchedule& sch, const uint32_t* 
         if (p < sch.passes) hp.total_bins += 1u << sch.bits[p];
     }
     int sms = device_sm_count();
-    uint32_t hist_blocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + 511u) / 512u, (uint32_t)sms * 2u));
+    uint32_t hist_blocks = std::max<uint32_t>(1u, std::min<uint32_t>((n + 2047u) / 2048u, (uint32_t)sms * 4u));
     k_sort_hist<<<hist_blocks, 512, sizeof(uint32_t) * hp.total_bins, st>>>(keys, n, hp, s.counts,
                                                                              s.bases, s.ctl);
     cudaError_t e = cudaGetLastError();
@@ -496,10 +516,12 @@ cudaError_t cell_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t
                          cudaStream_t st) {
     if (sch.n == 0)  // every cell offset is 0
         return cudaMemsetAsync(s.offs, 0, sizeof(uint32_t) * ((size_t)sch.cells + 1u), st);
-    const int last = sch.passes - 1;
-    uint32_t chunks = 1u << sch.bits[last];
-    k_cell_offsets<<<chunks, kOffsThreads, 0, st>>>(sorted_keys, sch.cells, sch.shift[last], chunks,
-                                                    s.bases + last * (kMaxRadix + 1), s.offs);
+    const uint32_t cap = gap_capacity(s.max_cells);
+    k_cell_offsets<<<(sch.n + 256u) / 256u, 256, 0, st>>>(sorted_keys, sch.n, sch.cells, s.offs, s.gaps, cap,
+                                                          s.ctl + kCtlGaps);
+    cudaError_t e = cudaGetLastError();
+    if (e) return e;
+    k_fill_gaps<<<(uint32_t)device_sm_count() * 4u, 256, 0, st>>>(s.gaps, cap, s.ctl + kCtlGaps, s.offs);
     return cudaGetLastError();
 }
 

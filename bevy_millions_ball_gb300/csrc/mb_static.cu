@@ -43,7 +43,8 @@ constexpr size_t kOffBases = kOffCounts + align4((size_t)mb::kMaxPasses * mb::kM
 constexpr size_t kOffLookback = kOffBases + align4((size_t)mb::kMaxPasses * (mb::kMaxRadix + 1u));
 constexpr size_t kOffCtl = kOffLookback + align4((size_t)mb::kMaxPasses * kLookbackPerPass);
 constexpr size_t kOffOffs = kOffCtl + align4(mb::kCtlWords);
-constexpr size_t kScratchWords = kOffOffs + align4((size_t)kStaticMaxCells + 1u);
+constexpr size_t kOffGaps = kOffOffs + align4((size_t)kStaticMaxCells + 1u);
+constexpr size_t kScratchWords = kOffGaps + align4((size_t)3u * ((size_t)kStaticMaxCells / mb::kGapCells + 2u));
 
 // The shared scratch: about 3.5 MB, resident on every GPU that loads the library.
 static __device__ __align__(256) uint32_t g_static_scratch[kScratchWords];
@@ -97,6 +98,7 @@ extern "C" mb_status mb_sort_and_hash_static(const uint32_t* keys, const uint32_
         v.lookback = base + kOffLookback;
         v.ctl = base + kOffCtl;
         v.offs = base + kOffOffs;
+        v.gaps = base + kOffGaps;
         v.lookback_words_per_pass = kLookbackPerPass;
         v.last_tiles = 0;
         v.last_passes = 0;
