@@ -20,8 +20,11 @@ constexpr uint32_t kMaxCells = 1u << 28;
 constexpr uint32_t kInitKeyBit = 0x80000000u;
 
 // Onesweep tile shape: 256 threads x 16 keys.
+#ifndef MB_SORT_ITEMS
+#define MB_SORT_ITEMS 16
+#endif
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
+constexpr int kSortItems = MB_SORT_ITEMS;
 constexpr uint32_t kSortTile = kSortThreads * kSortItems;
 
 // Control words of a sort plan (device u32 array).

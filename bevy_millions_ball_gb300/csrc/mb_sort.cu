@@ -7,7 +7,8 @@
 // Sort: one histogram kernel computes the digit counts of every pass in a single
 // read of the keys and the exclusive digit bases (last-block-done scan).  Each
 // pass is one onesweep kernel: a block takes the next tile (atomic ticket), ranks
-// its keys per warp with match.any (stable: warp-striped order, warps in order),
+// its keys per warp with one ballot per digit bit (stable: warp-striped order,
+// warps in order),
 // publishes per-digit tile counts into a look-back table, resolves its global
 // digit offsets by decoupled look-back over predecessor tiles, stages the tile in
 // shared memory in digit order and writes it out in contiguous runs.
@@ -32,7 +33,7 @@ constexpr uint32_t kFlagAggregate = 1u;
 constexpr uint32_t kFlagPrefix = 2u;
 constexpr uint32_t kValueMask = (1u << 28) - 1u;
 constexpr uint32_t kSpinLimit = 1u << 21;
-constexpr int kWindow = 16;  // look-back words loaded per step
+constexpr int kWindow = 8;  // look-back words loaded per step
 
 __device__ __forceinline__ uint32_t lb_pack(uint32_t flag, uint32_t epoch, uint32_t value) {
     return (flag << 30) | ((epoch & 3u) << 28) | (value & kValueMask);
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ 
 
 // ---------------------------------------------------------------- onesweep pass
 template <int THREADS, int ITEMS>
-__global__ void __launch_bounds__(THREADS)
+__global__ void __launch_bounds__(THREADS, 3)
     k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
                uint32_t shift, uint32_t bits, const uint32_t* __restrict__ bases,
@@ -184,16 +185,16 @@ __global__ void __launch_bounds__(THREADS)
     const uint32_t epoch = s_epoch;
     const uint32_t wbase = tile * TILE + warp * 32u * ITEMS;
 
-    uint32_t k[ITEMS], v[ITEMS], rank[ITEMS];
+    uint32_t k[ITEMS], rank[ITEMS];  // values are fetched when the tile is staged
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
         uint32_t idx = wbase + (uint32_t)j * 32u + lane;
         bool valid = idx < n;
         k[j] = valid ? __ldg(keys_in + idx) : 0u;
-        v[j] = vals_in ? (valid ? __ldg(vals_in + idx) : 0u) : idx;
     }
 
-    // per-warp stable ranking
+    // per-warp stable ranking; the lanes holding the same digit are found with one
+    // ballot per digit bit (warp-level multi-split)
     uint16_t* wh = s_whist + warp * R;
     const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
@@ -201,7 +202,13 @@ __global__ void __launch_bounds__(THREADS)
         uint32_t idx = wbase + (uint32_t)j * 32u + lane;
         bool valid = idx < n;
         uint32_t d = valid ? ((k[j] >> shift) & mask) : 0xFFFFFFFFu;
-        uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        uint32_t peers = __ballot_sync(0xFFFFFFFFu, valid);
+        for (uint32_t bit = 0; bit < bits; ++bit) {
+            const bool on = (d >> bit) & 1u;
+            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, on);
+            peers &= on ? bal : ~bal;
+        }
+        if (!valid) peers = 1u << lane;
         uint32_t b = valid ? (uint32_t)wh[d] : 0u;
         rank[j] = b + (uint32_t)__popc(peers & lt);
         __syncwarp();
@@ -304,7 +311,7 @@ __global__ void __launch_bounds__(THREADS)
             uint32_t d = (k[j] >> shift) & mask;
             uint32_t lpos = s_cnt[d] + (uint32_t)s_whist[warp * R + d] + rank[j];
             s_keys[lpos] = k[j];
-            s_vals[lpos] = v[j];
+            s_vals[lpos] = vals_in ? __ldg(vals_in + idx) : idx;
         }
     }
     __syncthreads();
