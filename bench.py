@@ -443,6 +443,62 @@ def run_batch(args, rank=0, world_size=1, local_rank=0):
     return 0
 
 
+def run_sort(args):
+    """Stage workload: mb_sort_and_hash (stable sort of u32 cell keys with iota values, then the
+    start/close cell tables) on 2^24 random keys over 2^24 cells, the reference's largest
+    hashing known-answer size (src/physics/spatial_hashing.rs:536-632)."""
+    import numpy as np
+    import torch
+
+    from bevy_millions_ball_gb300 import SortPlan
+
+    torch.cuda.set_device(0)
+    n = cells = 1 << 24
+    plan = SortPlan(max_keys=n, max_cells=cells)
+    keys_np = np.random.default_rng(0).integers(0, cells, n).astype(np.uint32)
+    keys = torch.from_numpy(keys_np.view(np.int32)).cuda()
+    sk = torch.empty(n, dtype=torch.int32, device="cuda")
+    sv = torch.empty_like(sk)
+    st = torch.empty(cells, dtype=torch.int32, device="cuda")
+    cl = torch.empty_like(st)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    run = lambda: plan.run(keys.data_ptr(), None, n, cells, sk.data_ptr(), sv.data_ptr(), st.data_ptr(),
+                           cl.data_ptr(), stream.cuda_stream)
+    for _ in range(max(args.warmup, 3)):
+        run()
+    torch.cuda.synchronize()
+    assert np.array_equal(sk.cpu().numpy().view(np.uint32), np.sort(keys_np))
+    K = min(args.steps, 50)
+    total = 0.0
+    for _ in range(K):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        run()
+        b.record(stream)
+        torch.cuda.synchronize()
+        total += a.elapsed_time(b)
+    plan.close()
+    ms = total / K
+    hbm, peak_kind = peaks()
+    # byte model: histogram read 4, 3 passes x (8 read + 8 write), sorted keys read 4, start/close
+    # write 8 per key, offsets write 4 per cell
+    model = 4 * n + 3 * 16 * n + 4 * n + 8 * cells + 4 * cells
+    achieved = model / (ms * 1e-3) / 1e9
+    line = {
+        "metric": "keys/s (stable sort + cell ranges)", "value": n / (ms * 1e-3), "unit": "keys/s", "n_gpus": 1,
+        "steps": K, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "stage: 16,777,216 uniform random keys < 2^24, iota values, 2^24 cells, 3 x 8-bit passes",
+                   "l2": "flushed before every timed call (256 MB write, outside the events)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": peak_kind, "model_bytes": model},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_serving(args):
     """Serving workload: Poisson arrivals of create / advance(k) requests; latency p50/p99."""
     import math
@@ -539,7 +595,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="P-1M", choices=["P-small", "P-1M", "P-4M", "batch", "serving"])
+    ap.add_argument("--workload", default="P-1M", choices=["P-small", "P-1M", "P-4M", "batch", "serving", "sort"])
     ap.add_argument("--batch-scenes", type=int, default=512)
     ap.add_argument("--serve-requests", type=int, default=300)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
@@ -551,9 +607,11 @@ def main():
     args = ap.parse_args()
     rank, world_size, local_rank = env_rank()
     if args.impl == "reference":
-        if args.workload in ("batch", "serving"):
-            print(json.dumps({"impl": "reference", "unavailable": "the reference runs one scene per app; "
-                              "batching/serving have no reference implementation"}))
+        if args.workload in ("batch", "serving", "sort"):
+            why = ("the reference's sort runs only as wgpu compute passes (no graphics stack on this box)"
+                   if args.workload == "sort" else
+                   "the reference runs one scene per app; batching/serving have no reference implementation")
+            print(json.dumps({"impl": "reference", "unavailable": why}))
             return 0
         return run_reference(args, rank, world_size)
     from __graft_entry__ import build
@@ -563,6 +621,8 @@ def main():
         return run_batch(args, rank, world_size, local_rank)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "sort":
+        return run_sort(args)
     return run_ours(args, rank, world_size, local_rank)
 
 
