@@ -255,28 +255,69 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 
 // handle_collisions' contact loop (physics.wgsl:122-160): the candidates of the
 // three rows in the reference's order (own row without the sphere itself, row
-// below, row above) as one flat sequence t in [0, T), so that a warp runs
-// max(T) iterations rather than the sum of per-row maxima.  Row r holds t in
+// below, row above) as one flat sequence t in [0, T).  Row r holds t in
 // [start_r, start_r + c_r) and candidate t sits at base[t + o_r] (o_r folds in
 // the row's first slot, its band and start_r; unsigned wrap-around is intended).
-// A squared-distance test rejects pairs that cannot touch before the exact
-// solve: sqrt is monotone and correctly rounded, so a pair whose squared
-// distance exceeds edge^2 by 0.3% can never pass `length(tpos) <= edge` (the
-// fused d2 differs from the unfused one by a few ulps, far inside the margin).
+//
+// The walk tests kLook candidates at a time at the sphere's current position
+// (their loads are independent, so they are in flight together) and stops at
+// the first that may touch: that one gets the exact solve, which moves the
+// sphere, and the walk resumes right after it.  Every candidate is therefore
+// decided at the position the sphere has when the reference's sequential loop
+// reaches it.  The test is a squared-distance bound: sqrt is monotone and
+// correctly rounded, so a pair whose squared distance exceeds edge^2 by 0.3% can
+// never pass `length(tpos) <= edge` in the solve (the fused d2 differs from the
+// unfused one by a few ulps, far inside the margin).
+__device__ __forceinline__ uint32_t cand_slot(uint32_t t, const uint32_t (&o)[3], uint32_t c0, uint32_t c01) {
+    return t + (t < c0 ? o[0] : (t < c01 ? o[1] : o[2]));
+}
+
+template <bool kShared, uint32_t kLook>
+__device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
+                                             const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
+                                             uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself) {
+    uint32_t t = 0;
+    while (t < T) {
+        float4 bp[kLook];
+#pragma unroll
+        for (uint32_t q = 0; q < kLook; ++q) {
+            const uint32_t j = cand_slot(min(t + q, T - 1u), o, c0, c01);
+            bp[q] = kShared ? bpos[j] : __ldg(bpos + j);
+        }
+        uint32_t m = 0;
+#pragma unroll
+        for (uint32_t q = 0; q < kLook; ++q) {
+            const float edge = bp[q].w + a.scale;
+            const float dx = a.position.x - bp[q].x, dy = a.position.y - bp[q].y, dz = a.position.z - bp[q].z;
+            const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+            const bool near = d2 <= (edge * edge) * 1.003f && t + q < T && t + q != tself;
+            m |= near ? 1u << q : 0u;
+        }
+        if (m) {
+            t += (uint32_t)(__ffs(m) - 1);
+            const uint32_t j = cand_slot(t, o, c0, c01);
+            const float4 bq = kShared ? bpos[j] : __ldg(bpos + j);
+            sphere(P, a, unpack(bq, kShared ? bvfme[j] : __ldg(bvfme + j)));
+            ++t;
+        } else {
+            t += kLook;
+        }
+    }
+}
+
+// Four candidates per step suit sparse neighbourhoods (about nine candidates);
+// six hide more latency where cells are crowded.  The warp agrees on one width
+// so its lanes run one loop.
+constexpr uint32_t kCrowdedT = 48;
+
 template <bool kShared>
 __device__ __forceinline__ void contact_loop(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
                                              uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself) {
-    for (uint32_t t = 0; t < T; ++t) {
-        if (t == tself) continue;
-        const uint32_t j = t + (t < c0 ? o[0] : (t < c01 ? o[1] : o[2]));
-        const float4 bp = kShared ? bpos[j] : __ldg(bpos + j);
-        const float edge = bp.w + a.scale;
-        const float dx = a.position.x - bp.x, dy = a.position.y - bp.y, dz = a.position.z - bp.z;
-        const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-        if (d2 > (edge * edge) * 1.003f) continue;
-        sphere(P, a, unpack(bp, kShared ? bvfme[j] : __ldg(bvfme + j)));
-    }
+    if (__any_sync(__activemask(), T >= kCrowdedT))
+        contact_walk<kShared, 6>(P, a, bpos, bvfme, o, c0, c01, T, tself);
+    else
+        contact_walk<kShared, 4>(P, a, bpos, bvfme, o, c0, c01, T, tself);
 }
 
 // Slot ranges of the three candidate rows of a sphere in cell (cx, cz), key =
