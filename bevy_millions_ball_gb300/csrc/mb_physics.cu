@@ -98,6 +98,18 @@ __device__ __forceinline__ void cell_of(const PhysParams& P, float x, float z, u
     cz = min(cz, P.N - 1u);
 }
 
+// v / d.  When d is a power of two whose reciprocal is a normal float (equal
+// masses make den = 2m), v * (1/d) is the same real number v / d, so it rounds
+// to the same float: three multiplies replace three IEEE divisions.
+__device__ __forceinline__ V3 div_exact(V3 v, float d) {
+    const uint32_t bits = __float_as_uint(d), e = (bits >> 23) & 0xFFu;
+    if ((bits & 0x007FFFFFu) == 0u && e >= 1u && e <= 253u) {
+        const float r = __uint_as_float((bits & 0x80000000u) | ((254u - e) << 23));
+        return {v.x * r, v.y * r, v.z * r};
+    }
+    return v / d;
+}
+
 // solve_sphere_constraint (physics.wgsl:300-331)
 __device__ __forceinline__ void sphere(const PhysParams& P, Agent& a, const Agent& b) {
     float edge = b.scale + a.scale;
@@ -114,7 +126,7 @@ __device__ __forceinline__ void sphere(const PhysParams& P, Agent& a, const Agen
                 float e_m2 = P.e_agent * m2;
                 float num = m1 - e_m2;
                 float den = m1 + m2;
-                V3 rvel_c = (num * rvel_n) / den;
+                V3 rvel_c = div_exact(num * rvel_n, den);
                 a.velocity = (b.velocity + (rvel - rvel_n)) + rvel_c;
             }
             float h = 0.5f * (edge - dist);
@@ -215,6 +227,7 @@ __global__ void __launch_bounds__(256)
 // spanning a row boundary) are read from global memory instead.
 constexpr int kTileThreads = kPhysicsTile;
 constexpr uint32_t kBandCap = 2 * kTileThreads;
+constexpr uint32_t kBandPad = 8;  // >= the widest look-ahead of the contact walk, minus one
 constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier wait (error flag on expiry)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -259,48 +272,55 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 // [start_r, start_r + c_r) and candidate t sits at base[t + o_r] (o_r folds in
 // the row's first slot, its band and start_r; unsigned wrap-around is intended).
 //
-// The walk tests kLook candidates at a time at the sphere's current position
-// (their loads are independent, so they are in flight together) and stops at
-// the first that may touch: that one gets the exact solve, which moves the
-// sphere, and the walk resumes right after it.  Every candidate is therefore
-// decided at the position the sphere has when the reference's sequential loop
-// reaches it.  The test is a squared-distance bound: sqrt is monotone and
-// correctly rounded, so a pair whose squared distance exceeds edge^2 by 0.3% can
-// never pass `length(tpos) <= edge` in the solve (the fused d2 differs from the
-// unfused one by a few ulps, far inside the margin).
+// The walk tests up to kLook candidates of the current row at a time, at the
+// sphere's current position (consecutive slots: their loads are independent and
+// in flight together), and stops at the first that may touch: that one gets the
+// exact solve, which moves the sphere, and the walk resumes right after it.
+// Every candidate is therefore decided at the position the sphere has when the
+// reference's sequential loop reaches it.  The test is a squared-distance bound
+// with a 0.3% margin, d2 - (edge * sqrt(1.003))^2 > 0 in one fused step: sqrt is
+// monotone and correctly rounded, so a pair it rejects can never pass
+// `length(tpos) <= edge` in the solve (the fused d2 differs from the unfused one
+// by a few ulps, far inside the margin); a NaN result counts as "may touch" and
+// is left to the exact test.  Slots past the row's end inside a step are read
+// but masked out: `bpos` must stay readable kLook - 1 slots past every row
+// (the shared bands are padded; global reads are clamped).
 __device__ __forceinline__ uint32_t cand_slot(uint32_t t, const uint32_t (&o)[3], uint32_t c0, uint32_t c01) {
     return t + (t < c0 ? o[0] : (t < c01 ? o[1] : o[2]));
 }
+
+constexpr float kNearScale = 1.0014989f;  // about sqrt(1.003): squared, a 0.3% margin on edge^2
 
 template <bool kShared, uint32_t kLook>
 __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
                                              uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself) {
+    const float sk = a.scale * kNearScale;
     uint32_t t = 0;
     while (t < T) {
+        const bool r0 = t < c0, r01 = t < c01;
+        const uint32_t j0 = t + (r0 ? o[0] : (r01 ? o[1] : o[2]));
+        const uint32_t rem = (r0 ? c0 : (r01 ? c01 : T)) - t;  // candidates left in this row, >= 1
         float4 bp[kLook];
 #pragma unroll
-        for (uint32_t q = 0; q < kLook; ++q) {
-            const uint32_t j = cand_slot(min(t + q, T - 1u), o, c0, c01);
-            bp[q] = kShared ? bpos[j] : __ldg(bpos + j);
-        }
+        for (uint32_t q = 0; q < kLook; ++q) bp[q] = kShared ? bpos[j0 + q] : __ldg(bpos + j0 + min(q, rem - 1u));
         uint32_t m = 0;
 #pragma unroll
         for (uint32_t q = 0; q < kLook; ++q) {
-            const float edge = bp[q].w + a.scale;
+            const float e = __fmaf_rn(bp[q].w, kNearScale, sk);
             const float dx = a.position.x - bp[q].x, dy = a.position.y - bp[q].y, dz = a.position.z - bp[q].z;
             const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-            const bool near = d2 <= (edge * edge) * 1.003f && t + q < T && t + q != tself;
-            m |= near ? 1u << q : 0u;
+            m |= !(__fmaf_rn(-e, e, d2) > 0.0f) ? 1u << q : 0u;
         }
+        if (rem < kLook) m &= (1u << rem) - 1u;
+        if (tself - t < kLook) m &= ~(1u << (tself - t));
         if (m) {
-            t += (uint32_t)(__ffs(m) - 1);
-            const uint32_t j = cand_slot(t, o, c0, c01);
-            const float4 bq = kShared ? bpos[j] : __ldg(bpos + j);
-            sphere(P, a, unpack(bq, kShared ? bvfme[j] : __ldg(bvfme + j)));
-            ++t;
+            const uint32_t q = (uint32_t)(__ffs(m) - 1);
+            t += q + 1u;
+            const uint32_t j = j0 + q;
+            sphere(P, a, unpack(kShared ? bpos[j] : __ldg(bpos + j), kShared ? bvfme[j] : __ldg(bvfme + j)));
         } else {
-            t += kLook;
+            t += min(rem, kLook);
         }
     }
 }
@@ -309,15 +329,21 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
 // six hide more latency where cells are crowded.  The warp agrees on one width
 // so its lanes run one loop.
 constexpr uint32_t kCrowdedT = 48;
+#ifndef MB_LOOK
+#define MB_LOOK 4
+#endif
+#ifndef MB_LOOK_CROWDED
+#define MB_LOOK_CROWDED 6
+#endif
 
 template <bool kShared>
 __device__ __forceinline__ void contact_loop(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
                                              uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself) {
     if (__any_sync(__activemask(), T >= kCrowdedT))
-        contact_walk<kShared, 6>(P, a, bpos, bvfme, o, c0, c01, T, tself);
+        contact_walk<kShared, MB_LOOK_CROWDED>(P, a, bpos, bvfme, o, c0, c01, T, tself);
     else
-        contact_walk<kShared, 4>(P, a, bpos, bvfme, o, c0, c01, T, tself);
+        contact_walk<kShared, MB_LOOK>(P, a, bpos, bvfme, o, c0, c01, T, tself);
 }
 
 // Slot ranges of the three candidate rows of a sphere in cell (cx, cz), key =
@@ -448,7 +474,7 @@ __global__ void __launch_bounds__(kTileThreads)
                     const uint4* __restrict__ svfme, float4* __restrict__ pos_out0, float4* __restrict__ pos_out1,
                     uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1, uint32_t* __restrict__ keys_out,
                     uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse, uint32_t* __restrict__ err) {
-    __shared__ __align__(16) float4 s_pos[3][kBandCap];
+    __shared__ __align__(16) float4 s_pos[3 * kBandCap + kBandPad];  // padded: the walk reads past rows
     __shared__ __align__(16) uint4 s_vfme[3][kBandCap];
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ uint32_t s_lo[3], s_cnt[3];
@@ -556,7 +582,7 @@ __global__ void __launch_bounds__(kTileThreads)
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
             if (s_cnt[b]) {
-                bulk_g2s(s_pos[b], spos + s_lo[b], s_cnt[b] * 16u, &s_bar);
+                bulk_g2s(s_pos + b * kBandCap, spos + s_lo[b], s_cnt[b] * 16u, &s_bar);
                 bulk_g2s(s_vfme[b], svfme + s_lo[b], s_cnt[b] * 16u, &s_bar);
             }
         }
@@ -593,7 +619,7 @@ __global__ void __launch_bounds__(kTileThreads)
     }
     if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
 
-    step_sphere(P, a, i, n, base_a, base_c, lo, hi, &s_pos[0][0], &s_vfme[0][0], s_lo, s_cnt, spos, svfme, pos_out,
+    step_sphere(P, a, i, n, base_a, base_c, lo, hi, s_pos, &s_vfme[0][0], s_lo, s_cnt, spos, svfme, pos_out,
                 vfme_out, keys_out, hist, coarse);
 }
 

@@ -89,6 +89,20 @@ def test_clustered_spring(built_lib, cuda):
     run_pair(sc, 40, [1, 2, 11, 40])
 
 
+@pytest.mark.parametrize("spring", [False, True])
+def test_mixed_masses_and_radii(built_lib, cuda, spring):
+    """Masses whose sums are powers of two (den = m1 + m2 in 2, 4, ...) and ones
+    that are not, radii 0.3-0.6: both ways the contact solve divides stay exact."""
+    sc = scenes.plain_uniform(40_000, 128, half_map_height=4, seed=31, spring=spring)
+    rng = np.random.default_rng(32)
+    from bevy_millions_ball_gb300 import unpack_vfme
+    v, f, _ = unpack_vfme(sc.vfme)
+    mass = rng.choice(np.array([0.5, 1.0, 1.5, 2.0, 3.0, 0.7, 1.25], np.float32), sc.n)
+    sc.vfme = pack_vfme(v, f, mass)
+    sc.pos_scale[:, 3] = rng.choice(np.array([0.3, 0.45, 0.5, 0.6], np.float32), sc.n)
+    run_pair(sc, 40, [1, 2, 11, 40])
+
+
 def test_nonpow2_grid_and_grid_size(built_lib, cuda):
     sc = scenes.plain_uniform(30_000, 300, grid_size=2, half_map_height=4, seed=12)
     run_pair(sc, 30, [1, 2, 11, 30])
