@@ -170,8 +170,8 @@ __device__ __forceinline__ void push_fix(const FixLists& L, const int (&cls)[kIt
 
 // The run [b, b + g) of cell k ends the cell and did not start it: other warps'
 // runs came first, so the cell is listed for the fixup (once: one run ends it).
-__device__ __forceinline__ int fix_class(const uint32_t* __restrict__ offs, uint32_t k, uint32_t b, uint32_t g) {
-    const uint32_t lo = __ldg(offs + k), hi = __ldg(offs + k + 1u);
+// lo, hi: the cell's slot range offs[k], offs[k + 1].
+__device__ __forceinline__ int fix_class(uint32_t lo, uint32_t hi, uint32_t b, uint32_t g) {
     if (b + g != hi || b == lo) return -1;
     const uint32_t m = hi - lo;
     return m <= kFixSmall ? kFixListSmall : (m <= kFixWarp ? kFixListWarp : kFixListHuge);
@@ -209,8 +209,9 @@ __global__ void __launch_bounds__(256)
         int cls = -1;
         if (valid && !ident && lane == leader) {
             const uint32_t g = (uint32_t)__popc(peers);
-            b = __ldg(offs + k + 1u) - atomicSub(hist + k, g);  // the run's first slot
-            cls = fix_class(offs, k, b, g);
+            const uint32_t lo = __ldg(offs + k), hi = __ldg(offs + k + 1u);
+            b = hi - atomicSub(hist + k, g);  // the run's first slot
+            cls = fix_class(lo, hi, b, g);
         }
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
         {
@@ -266,8 +267,9 @@ __global__ void __launch_bounds__(256)
         int cls = -1;
         if (valid && !ident && lane == leader) {
             const uint32_t g = (uint32_t)__popc(peers);
-            b = __ldg(offs + k + 1u) - atomicSub(hist + k, g);  // the run's first slot
-            cls = fix_class(offs, k, b, g);
+            const uint32_t lo = __ldg(offs + k), hi = __ldg(offs + k + 1u);
+            b = hi - atomicSub(hist + k, g);  // the run's first slot
+            cls = fix_class(lo, hi, b, g);
         }
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
         {
@@ -482,6 +484,17 @@ __global__ void __launch_bounds__(kFixThreads)
         for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
             const uint32_t e = 32u * s + lane;
             v[s] = e < m ? perm[lo + e] : 0xFFFFFFFFu;
+        }
+        {  // the runs may have claimed their slots in input order already
+            bool ok = true;
+#pragma unroll
+            for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
+                const uint32_t down = __shfl_down_sync(0xFFFFFFFFu, v[s], 1);
+                const uint32_t wrap = s + 1u < kFixWarp / 32 ? __shfl_sync(0xFFFFFFFFu, v[s + 1u < kFixWarp / 32 ? s + 1u : s], 0)
+                                                              : 0xFFFFFFFFu;
+                ok = ok && v[s] <= (lane == 31u ? wrap : down);
+            }
+            if (__all_sync(0xFFFFFFFFu, ok)) continue;
         }
         if (m <= 32u) warp_bitonic<1>(v, lane);
         else if (m <= 64u) warp_bitonic<2>(v, lane);
