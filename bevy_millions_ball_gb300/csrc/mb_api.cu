@@ -792,9 +792,9 @@ mb_status mb_last_frame_times(mb_world* w, float* ms) {
 
 uint32_t mb_kernels_per_frame(const mb_world* w) {
     if (!w) return 0u;
-    // counting: scan + scatter + in-cell fixup + physics;
-    // onesweep: histogram + one kernel per digit pass + cell offsets + gather + physics
-    return counting(w) ? 4u : (uint32_t)w->sched.passes + 4u;
+    // counting: scan + scatter + fixup listing + in-cell fixup + physics;
+    // onesweep: histogram + one kernel per digit pass + cell offsets + gap fill + gather + physics
+    return counting(w) ? 5u : (uint32_t)w->sched.passes + 5u;
 }
 
 const char* mb_version(void) { return "millionsball-gb300 " __DATE__ " sm_103a"; }

@@ -143,38 +143,19 @@ struct FixLists {
     uint32_t cap[kFixLists];
 };
 
-// Called by every thread of the block (block-uniform loop): cls[u] is the list
-// the thread appends cell[u] to, or -1.
-template <int kItems>
-__device__ __forceinline__ void push_fix(const FixLists& L, const int (&cls)[kItems], const uint32_t (&cell)[kItems]) {
-    __shared__ uint32_t s_n[kFixLists], s_base[kFixLists];
-    if (threadIdx.x < (uint32_t)kFixLists) s_n[threadIdx.x] = 0u;
-    __syncthreads();
-    uint32_t at[kItems];
-#pragma unroll
-    for (int u = 0; u < kItems; ++u) at[u] = cls[u] >= 0 ? atomicAdd(&s_n[cls[u]], 1u) : 0u;
-    __syncthreads();
-    if (threadIdx.x < (uint32_t)kFixLists && s_n[threadIdx.x])
-        s_base[threadIdx.x] = atomicAdd(L.ctl + threadIdx.x, s_n[threadIdx.x]);
-    __syncthreads();
-#pragma unroll
-    for (int u = 0; u < kItems; ++u) {
-        const int c = cls[u];
-        if (c >= 0) {  // lists hold every cell that can qualify; the bound only guards bad counts
-            uint32_t* list = c == kFixListSmall ? L.list[0] : (c == kFixListWarp ? L.list[1] : L.list[2]);
-            const uint32_t cap = c == kFixListSmall ? L.cap[0] : (c == kFixListWarp ? L.cap[1] : L.cap[2]);
-            if (s_base[c] + at[u] < cap) list[s_base[c] + at[u]] = cell[u];
-        }
-    }
+// The run [b, b + g) of a cell with slots [lo, hi) ends the cell and did not
+// start it: other warps' runs came first, so the cell may be out of input order.
+// The run's leader marks its input slot in the fixup bitmap (once per cell: one
+// run ends it); k_fix_collect lists the marked cells.
+__device__ __forceinline__ bool listed(uint32_t lo, uint32_t hi, uint32_t b, uint32_t g) {
+    return b + g == hi && b != lo;
 }
-
-// The run [b, b + g) of cell k ends the cell and did not start it: other warps'
-// runs came first, so the cell is listed for the fixup (once: one run ends it).
-// lo, hi: the cell's slot range offs[k], offs[k + 1].
-__device__ __forceinline__ int fix_class(uint32_t lo, uint32_t hi, uint32_t b, uint32_t g) {
-    if (b + g != hi || b == lo) return -1;
-    const uint32_t m = hi - lo;
-    return m <= kFixSmall ? kFixListSmall : (m <= kFixWarp ? kFixListWarp : kFixListHuge);
+// One word of the bitmap per 32 input slots, written whole by the warp that
+// scatters them (every word below ceil(n / 32) is rewritten each frame, so
+// nothing is cleared and the scatter needs no atomics or barriers for it).
+__device__ __forceinline__ void mark_fix(uint32_t* __restrict__ fix_bits, uint32_t i, uint32_t n, bool mark) {
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, mark);
+    if ((threadIdx.x & 31u) == 0u && i < n) fix_bits[i >> 5] = m;
 }
 // Also moves each sphere's state to its slot (sorted copy for the physics pass)
 // and, where a slot begins or ends a physics tile, writes that side of the
@@ -185,7 +166,7 @@ __global__ void __launch_bounds__(256)
                    uint32_t* __restrict__ perm, const float4* __restrict__ pos_in,
                    const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
                    uint4* __restrict__ svfme, const uint32_t* __restrict__ offs, uint4* __restrict__ bands,
-                   uint32_t N, FixLists fix) {
+                   uint32_t N, uint32_t* __restrict__ fix_bits) {
     griddep_wait();
     griddep_launch();
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
@@ -206,19 +187,15 @@ __global__ void __launch_bounds__(256)
         uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k);
         uint32_t leader = (uint32_t)(__ffs(peers) - 1);
         uint32_t b = 0;
-        int cls = -1;
+        bool mark = false;
         if (valid && !ident && lane == leader) {
             const uint32_t g = (uint32_t)__popc(peers);
             const uint32_t lo = __ldg(offs + k), hi = __ldg(offs + k + 1u);
             b = hi - atomicSub(hist + k, g);  // the run's first slot
-            cls = fix_class(lo, hi, b, g);
+            mark = listed(lo, hi, b, g);
         }
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
-        {
-            const int c1[1] = {cls};
-            const uint32_t k1[1] = {k};
-            push_fix<1>(fix, c1, k1);
-        }
+        mark_fix(fix_bits, i, n, mark);
         if (valid) {
             const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
             if (dst >= n) continue;  // only counts that disagree with the keys get here
@@ -238,7 +215,8 @@ __global__ void __launch_bounds__(256)
                           uint32_t* __restrict__ perm, const float4* __restrict__ pos0,
                           const float4* __restrict__ pos1, const uint4* __restrict__ vfme0,
                           const uint4* __restrict__ vfme1, float4* __restrict__ spos, uint4* __restrict__ svfme,
-                          const uint32_t* __restrict__ offs, FixLists fix, uint4* __restrict__ bands) {
+                          const uint32_t* __restrict__ offs, uint32_t* __restrict__ fix_bits,
+                          uint4* __restrict__ bands) {
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
@@ -264,19 +242,15 @@ __global__ void __launch_bounds__(256)
         uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k);
         uint32_t leader = (uint32_t)(__ffs(peers) - 1);
         uint32_t b = 0;
-        int cls = -1;
+        bool mark = false;
         if (valid && !ident && lane == leader) {
             const uint32_t g = (uint32_t)__popc(peers);
             const uint32_t lo = __ldg(offs + k), hi = __ldg(offs + k + 1u);
             b = hi - atomicSub(hist + k, g);  // the run's first slot
-            cls = fix_class(lo, hi, b, g);
+            mark = listed(lo, hi, b, g);
         }
         b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
-        {
-            const int c1[1] = {cls};
-            const uint32_t k1[1] = {k};
-            push_fix<1>(fix, c1, k1);
-        }
+        mark_fix(fix_bits, i, n, mark);
         if (valid) {
             const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
             if (dst >= n) continue;  // only counts that disagree with the keys get here
@@ -291,8 +265,47 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// ---------------------------------------------------------------- collect
+// Lists the cells marked in the fixup bitmap by size class (a marked input
+// slot's key is its cell).  A block reads kCollectWords words, a byte per
+// thread, stages the cells in shared memory and appends them to the global
+// lists with one atomic per list.
+constexpr uint32_t kCollectThreads = 256, kCollectWords = kCollectThreads / 4u;
+
+__global__ void __launch_bounds__(kCollectThreads)
+    k_fix_collect(const uint32_t* __restrict__ fix_bits, const uint32_t* __restrict__ keys, uint32_t n,
+                  const uint32_t* __restrict__ offs, FixLists lists) {
+    __shared__ uint32_t s_cell[kFixLists][kCollectWords * 32u];
+    __shared__ uint32_t s_n[kFixLists], s_base[kFixLists];
+    griddep_wait();  // the scatter's bitmap is complete
+    griddep_launch();
+    const uint32_t tid = threadIdx.x;
+    if (tid < (uint32_t)kFixLists) s_n[tid] = 0u;
+    __syncthreads();
+    const uint32_t words = (n + 31u) / 32u;
+    const uint32_t w = blockIdx.x * kCollectWords + tid / 4u, sh = 8u * (tid & 3u);
+    uint32_t bits = w < words ? (__ldcg(fix_bits + w) >> sh) & 0xFFu : 0u;
+    while (bits) {
+        const uint32_t c = __ldg(keys + 32u * w + sh + (uint32_t)(__ffs(bits) - 1));
+        bits &= bits - 1u;
+        const uint32_t m = __ldg(offs + c + 1u) - __ldg(offs + c);
+        const int cls = m <= kFixSmall ? kFixListSmall : (m <= kFixWarp ? kFixListWarp : kFixListHuge);
+        s_cell[cls][atomicAdd(&s_n[cls], 1u)] = c;  // at most 32 * kCollectWords marks per block
+    }
+    __syncthreads();
+    if (tid < (uint32_t)kFixLists && s_n[tid]) s_base[tid] = atomicAdd(lists.ctl + tid, s_n[tid]);
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < kFixLists; ++c) {
+        for (uint32_t j = tid; j < s_n[c]; j += kCollectThreads) {
+            const uint32_t at = s_base[c] + j;  // lists hold every cell that can qualify; the bound guards bad counts
+            if (at < lists.cap[c]) lists.list[c][at] = s_cell[c][j];
+        }
+    }
+}
+
 // ---------------------------------------------------------------- fixup
-// The listed cells (see fix_class) get their slots back in ascending input order
+// The listed cells (see k_fix_collect) get their slots back in ascending input order
 // and re-gather their sorted state copy from the state source: one buffer (a
 // world), or each scene's current buffer (a batch, where cells and coarse tiles
 // of HOLD scenes are left alone).  Cells of up to kFixSmall slots: a thread
@@ -649,6 +662,8 @@ FixLists fix_lists(const CountScratch& s) {
     return FixLists{s.fix_ctl, {s.fix[0], s.fix[1], s.fix[2]}, {s.fix_cap[0], s.fix_cap[1], s.fix_cap[2]}};
 }
 uint32_t fix_blocks() { return (uint32_t)device_sm_count() * 4u; }
+uint32_t fix_words(uint32_t max_keys) { return max_keys / 32u + 1u; }
+uint32_t collect_grid(uint32_t n) { return ((n + 31u) / 32u + kCollectWords - 1u) / kCollectWords; }
 uint32_t scan_tiles(uint32_t cells) { return (cells + kScanTile - 1u) / kScanTile; }
 uint32_t fix_capacity(int cls, uint32_t max_cells, uint32_t max_keys) {
     const uint32_t per = cls == kFixListSmall ? 2u : (cls == kFixListWarp ? kFixSmall + 1u : kFixWarp + 1u);
@@ -660,7 +675,7 @@ uint64_t count_scratch_bytes(uint32_t max_cells, uint32_t max_keys) {
     const uint64_t padded = ((uint64_t)max_cells + kScanTile) & ~(uint64_t)15;
     uint64_t b = 4u * (padded + (max_cells + kScanTile - 1u) / kScanTile + 1u + kFixLists);
     for (int c = 0; c < kFixLists; ++c) b += 4u * fix_capacity(c, max_cells, max_keys);
-    return b + 4u * ((uint64_t)max_keys + 1u);
+    return b + 4u * ((uint64_t)max_keys + 1u) + 4u * (uint64_t)fix_words(max_keys);
 }
 
 cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells, uint32_t max_keys) {
@@ -672,6 +687,7 @@ cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells, uint32_t ma
     if ((e = cudaMalloc(&s.coarse, sizeof(uint32_t) * (s.tiles + 1u)))) return e;
     if ((e = cudaMalloc(&s.fix_ctl, sizeof(uint32_t) * kFixLists))) return e;
     if ((e = cudaMalloc(&s.fix_tmp, sizeof(uint32_t) * ((size_t)max_keys + 1u)))) return e;
+    if ((e = cudaMalloc(&s.fix_bits, sizeof(uint32_t) * fix_words(max_keys)))) return e;
     for (int c = 0; c < kFixLists; ++c) {
         s.fix_cap[c] = fix_capacity(c, max_cells, max_keys);
         if ((e = cudaMalloc(&s.fix[c], sizeof(uint32_t) * s.fix_cap[c]))) return e;
@@ -687,6 +703,7 @@ void count_scratch_free(CountScratch& s) {
     cudaFree(s.coarse);
     cudaFree(s.fix_ctl);
     cudaFree(s.fix_tmp);
+    cudaFree(s.fix_bits);
     for (auto* l : s.fix) cudaFree(l);
     s = CountScratch();
 }
@@ -728,7 +745,10 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
     if (n) {
         uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
         if ((e = launch_pdl(pdl, k_cell_scatter, dim3(blocks), dim3(256), 0, st, keys, n, s.hist, perm, pos_in,
-                            vfme_in, spos, svfme, offs, bands, N, fix_lists(s))))
+                            vfme_in, spos, svfme, offs, bands, N, s.fix_bits)))
+            return e;
+        if ((e = launch_pdl(pdl, k_fix_collect, dim3(collect_grid(n)), dim3(kCollectThreads), 0, st,
+                            (const uint32_t*)s.fix_bits, keys, n, offs, fix_lists(s))))
             return e;
     }
     OneBuffer src{pos_in, vfme_in};
@@ -754,7 +774,9 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
         uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
         k_cell_scatter_scenes<<<blocks, 256, 0, st>>>(scenes, tile_scene, keys, n, s.hist, perm, pos_buf0,
                                                       pos_buf1, vfme_buf0, vfme_buf1, spos, svfme, offs,
-                                                      fix_lists(s), bands);
+                                                      s.fix_bits, bands);
+        if ((e = cudaGetLastError())) return e;
+        k_fix_collect<<<collect_grid(n), kCollectThreads, 0, st>>>(s.fix_bits, keys, n, offs, fix_lists(s));
         if ((e = cudaGetLastError())) return e;
     }
     SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};

@@ -214,9 +214,9 @@ constexpr uint32_t kScanChunk = kScanThreads * kScanItems;  // cells per block o
 constexpr uint32_t kScanTile = 4096;                        // cells per coarse count (tile base)
 static_assert(kScanTile % kScanChunk == 0, "scan chunks tile the coarse tiles");
 
-// Cells the scatter filled from several warp runs are listed for the in-cell
-// fixup by size: up to kFixSmall slots (a thread each), up to kFixWarp (a warp
-// each), larger (a block each).
+// Cells the scatter filled from several warp runs are marked (one bit per input
+// slot), then listed for the in-cell fixup by size: up to kFixSmall slots (a
+// thread each), up to kFixWarp (a warp each), larger (a block each).
 constexpr uint32_t kFixSmall = 8;
 constexpr uint32_t kFixWarp = 256;
 enum : int { kFixListSmall = 0, kFixListWarp = 1, kFixListHuge = 2, kFixLists = 3 };
@@ -229,6 +229,7 @@ struct CountScratch {
     uint32_t* fix[kFixLists] = {nullptr, nullptr, nullptr};  // listed cells, by size class
     uint32_t fix_cap[kFixLists] = {0u, 0u, 0u};                // their capacities
     uint32_t* fix_tmp = nullptr;  // [max_keys] copy of a large cell's input indices
+    uint32_t* fix_bits = nullptr; // [max_keys / 32 + 1] input slots whose run listed its cell
     uint32_t tiles = 0;
 };
 // Lists are sized from max_keys: a listed cell holds >= 2, > kFixSmall or > kFixWarp keys.
