@@ -18,9 +18,10 @@
 //      starts (offs[c+1] - left), so the counts are back to zero when the
 //      scatter ends - spheres of one warp keep their order, and its 32-byte
 //      state is copied to that slot; the run that
-//      fills a cell last lists the cell if earlier runs of other warps got there
-//      first (only such cells can be out of order);
-//   4. k_cell_fix: the listed cells' slots are put back in ascending input order
+//      fills a cell last marks the cell (a bit per input slot) if earlier runs
+//      of other warps got there first (only such cells can be out of order);
+//   4. k_fix_collect: the marked cells are listed by size;
+//   5. k_cell_fix: the listed cells' slots are put back in ascending input order
 //      (what a stable sort yields), re-gathering their state copy.
 //
 // The result is bit-identical to a stable sort; offs[] replaces start/close.
