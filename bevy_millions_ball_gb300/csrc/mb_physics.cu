@@ -98,9 +98,9 @@ __device__ __forceinline__ void cell_of(const PhysParams& P, float x, float z, u
     cz = min(cz, P.N - 1u);
 }
 
-// v / d.  When d is a power of two whose reciprocal is a normal float (equal
-// masses make den = 2m), v * (1/d) is the same real number v / d, so it rounds
-// to the same float: three multiplies replace three IEEE divisions.
+// v / d.  When d is a power of two whose reciprocal is a normal float (unit
+// masses, or equal masses in den = 2m), v * (1/d) is the same real number v / d,
+// so it rounds to the same float: three multiplies replace three IEEE divisions.
 __device__ __forceinline__ V3 div_exact(V3 v, float d) {
     const uint32_t bits = __float_as_uint(d), e = (bits >> 23) & 0xFFu;
     if ((bits & 0x007FFFFFu) == 0u && e >= 1u && e <= 253u) {
@@ -401,7 +401,7 @@ __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32
 
     // verlet_integration (physics.wgsl:262-266)
     {
-        V3 acc = a.force / a.massv;
+        V3 acc = div_exact(a.force, a.massv);  // unit masses: three multiplies
         a.velocity = a.velocity + ((V3{P.gx, P.gy, P.gz} + acc) * P.dt) * P.dt;
         a.position = a.position + a.velocity;
     }
@@ -479,7 +479,6 @@ __global__ void __launch_bounds__(kTileThreads)
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ uint32_t s_lo[3], s_cnt[3];
 
-    griddep_wait();  // the sort's outputs are complete and visible
     const uint32_t tid = threadIdx.x;
     const uint32_t i0 = blockIdx.x * kTileThreads;
     const uint32_t i = i0 + tid;
@@ -513,8 +512,12 @@ __global__ void __launch_bounds__(kTileThreads)
                 stage = sf == sl && __ldg(&scenes[sf].mode) == kModeLoop;
             }
             const uint4 z = make_uint4(0u, 0u, 0u, 0u);
-            const uint4 l = stage ? __ldg(bands + 2u * blockIdx.x) : z;
-            const uint4 h = stage ? __ldg(bands + 2u * blockIdx.x + 1u) : z;
+            // read before the wait below: the scatter wrote the table and had
+            // completed before the kernel this one follows could start (the
+            // fixups in between reorder slots inside cells, never tile bounds);
+            // read through L2
+            const uint4 l = stage ? __ldcg(bands + 2u * blockIdx.x) : z;
+            const uint4 h = stage ? __ldcg(bands + 2u * blockIdx.x + 1u) : z;
             const uint32_t lo3[3] = {l.x, l.y, l.z}, hi3[3] = {h.x, h.y, h.z};
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
@@ -523,7 +526,9 @@ __global__ void __launch_bounds__(kTileThreads)
                 s_cnt[b] = (hb > lo3[b] && hb - lo3[b] <= kBandCap) ? hb - lo3[b] : 0u;
             }
         }
-    } else if (tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
+    }
+    griddep_wait();  // the sort's outputs (the sorted state copy) are complete and visible
+    if (!bands && tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
         uint32_t lo = 0, hi = 0;
         bool stage = true;
         PhysParams Q = P;
