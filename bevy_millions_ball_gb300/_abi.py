@@ -135,6 +135,7 @@ SIGNATURES = {
     "mb_server_wait": (C.c_int, [vp, C.c_uint64, C.c_double, C.POINTER(C.c_double)]),
     "mb_server_get_state": (C.c_int, [vp, u32, vp, vp]),
     "mb_server_get_stats": (C.c_int, [vp, C.POINTER(MbServerStats)]),
+    "mb_selftest_divide": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]),
     "mb_version": (C.c_char_p, []),
 }
 

@@ -797,6 +797,13 @@ uint32_t mb_kernels_per_frame(const mb_world* w) {
     return counting(w) ? 5u : (uint32_t)w->sched.passes + 5u;
 }
 
+mb_status mb_selftest_divide(uint64_t seed, uint64_t count, uint64_t* mismatches, uint32_t* first_bad) {
+    if (!mismatches) return MB_ERR_INVALID_ARG;
+    const cudaError_t e = mb::selftest_divide(seed, count, mismatches, first_bad);
+    if (e == cudaErrorMemoryAllocation) return MB_ERR_OOM;
+    return e ? MB_ERR_CUDA : MB_OK;
+}
+
 const char* mb_version(void) { return "millionsball-gb300 " __DATE__ " sm_103a"; }
 
 }  // extern "C"

@@ -192,6 +192,9 @@ cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t*
                                 const float4* spos, const uint4* svfme, float4* pos_out, uint4* vfme_out,
                                 uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
                                 cudaStream_t st, bool pdl = false);
+// Compares the physics pass's division (div_exact) with IEEE division over
+// `count` generated cases on the current device (synchronous).
+cudaError_t selftest_divide(uint64_t seed, uint64_t count, uint64_t* mismatches, uint32_t* bad4);
 cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,
                          uint32_t* hist, uint32_t* coarse, cudaStream_t st);
 

@@ -99,8 +99,12 @@ __device__ __forceinline__ void cell_of(const PhysParams& P, float x, float z, u
 }
 
 // v / d.  When d is a power of two whose reciprocal is a normal float (unit
-// masses, or equal masses in den = 2m), v * (1/d) is the same real number v / d,
-// so it rounds to the same float: three multiplies replace three IEEE divisions.
+// masses, or equal masses in den = 2m), v * (1/d) is the same real number as
+// v / d, so it rounds to the same float: three multiplies replace three IEEE
+// divisions.  Otherwise IEEE division.  (A reciprocal with one checked
+// correction step per numerator was exact too, but slower than IEEE division
+// here: 74 vs 58 us per late 1M frame.)  mb_selftest_divide compares this with
+// IEEE division on the GPU.
 __device__ __forceinline__ V3 div_exact(V3 v, float d) {
     const uint32_t bits = __float_as_uint(d), e = (bits >> 23) & 0xFFu;
     if ((bits & 0x007FFFFFu) == 0u && e >= 1u && e <= 253u) {
@@ -628,6 +632,56 @@ __global__ void __launch_bounds__(kTileThreads)
                 vfme_out, keys_out, hist, coarse);
 }
 
+// Self-test of div_exact against IEEE division over count generated cases:
+// operands from all float bit patterns, normal-range operands, power-of-two
+// divisors and exact multiples.  Mismatching bit patterns are counted;
+// the first one is kept in bad[0..3] = a, d, div_exact, IEEE.
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {  // splitmix64 finaliser
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+__global__ void k_selftest_divide(uint64_t seed, uint64_t count, unsigned long long* mismatches, uint32_t* bad) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
+        const uint64_t h = mix64(seed ^ mix64(k));
+        uint32_t ua = (uint32_t)h, ud = (uint32_t)(h >> 32);
+        switch (k & 3u) {
+            case 0: break;  // any bit patterns
+            case 1:  // any numerator, a power-of-two divisor of either sign
+                ud &= 0xFF800000u;
+                break;
+            case 2: {  // a = d * m for a small integer or a power of two: exact and power-of-two quotients
+                ud = (ud & 0x807FFFFFu) | ((100u + (ud >> 23) % 40u) << 23);
+                const float m = (ua & 1u) ? (float)((ua >> 1) & 0xFFFu) : __uint_as_float((120u + ((ua >> 1) & 15u)) << 23);
+                ua = __float_as_uint(__fmul_rn(__uint_as_float(ud), m));
+                break;
+            }
+            default: {  // normalised vectors: |a| <= d, d near 1
+                ud = 0x3F000000u + (ud & 0x00FFFFFFu);
+                ua = (ua & 0x80000000u) | (__float_as_uint(__uint_as_float(ud) * ((ua & 0x7FFFFFu) * 0x1p-23f)));
+                break;
+            }
+        }
+        const float a = __uint_as_float(ua), d = __uint_as_float(ud);
+        const V3 got = div_exact(V3{a, -a, __fmul_rn(a, 0.75f)}, d);
+        const float want[3] = {__fdiv_rn(a, d), __fdiv_rn(-a, d), __fdiv_rn(__fmul_rn(a, 0.75f), d)};
+        const float g[3] = {got.x, got.y, got.z};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (__float_as_uint(g[c]) != __float_as_uint(want[c])) {
+                if (atomicAdd(mismatches, 1ull) == 0ull) {
+                    bad[0] = ua;
+                    bad[1] = ud;
+                    bad[2] = __float_as_uint(g[c]);
+                    bad[3] = __float_as_uint(want[c]);
+                }
+            }
+        }
+    }
+}
+
 __global__ void k_rekey(PhysParams P, uint32_t n, const float4* __restrict__ pos,
                         uint32_t* __restrict__ keys, uint32_t* __restrict__ hist,
                         uint32_t* __restrict__ coarse) {
@@ -709,6 +763,26 @@ cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uin
     if (!n) return cudaSuccess;
     k_rekey<<<(n + 255u) / 256u, 256, 0, st>>>(p, n, pos, keys, hist, coarse);
     return cudaGetLastError();
+}
+
+cudaError_t selftest_divide(uint64_t seed, uint64_t count, uint64_t* mismatches, uint32_t* bad4) {
+    unsigned long long* d_mis = nullptr;
+    uint32_t* d_bad = nullptr;
+    cudaError_t e = cudaMalloc(&d_mis, sizeof(unsigned long long));
+    if (!e) e = cudaMalloc(&d_bad, 4 * sizeof(uint32_t));
+    if (!e) e = cudaMemset(d_mis, 0, sizeof(unsigned long long));
+    if (!e) e = cudaMemset(d_bad, 0, 4 * sizeof(uint32_t));
+    if (!e) {
+        k_selftest_divide<<<(uint32_t)device_sm_count() * 8u, 256>>>(seed, count, d_mis, d_bad);
+        e = cudaGetLastError();
+    }
+    unsigned long long mis = 0;
+    if (!e) e = cudaMemcpy(&mis, d_mis, sizeof(mis), cudaMemcpyDeviceToHost);
+    if (!e && bad4) e = cudaMemcpy(bad4, d_bad, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d_mis);
+    cudaFree(d_bad);
+    if (!e && mismatches) *mismatches = (uint64_t)mis;
+    return e;
 }
 
 }  // namespace mb

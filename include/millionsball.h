@@ -380,6 +380,14 @@ mb_status mb_server_wait(mb_server* s, uint64_t request, double timeout_s, doubl
 mb_status mb_server_get_state(mb_server* s, uint32_t scene, float* pos_scale, uint32_t* vfme);
 mb_status mb_server_get_stats(mb_server* s, mb_server_stats* out);
 
+/* Diagnostic: compares the physics pass's division (an exact reciprocal
+ * multiply for power-of-two divisors, IEEE division otherwise) with IEEE
+ * division on `count` generated operand pairs on the current device; *mismatches = the
+ * number of differing results (0 expected), first_bad (nullable, 4 words) =
+ * the first mismatch's a, d, result, IEEE result as float bit patterns.
+ * Synchronous. */
+mb_status mb_selftest_divide(uint64_t seed, uint64_t count, uint64_t* mismatches, uint32_t* first_bad);
+
 /* Library version string (build id). */
 const char* mb_version(void);
 
