@@ -114,6 +114,23 @@ __device__ __forceinline__ V3 div_exact(V3 v, float d) {
     return v / d;
 }
 
+// length(v) > s (the jitter test, physics.wgsl:162-168).  sqrt is correctly
+// rounded and monotone, so where dot(v, v) is below s^2 * (1 - 1e-5) or above
+// s^2 * (1 + 1e-5) (products rounded once each, far inside the margin) the
+// rounded length is certainly <= s, resp. > s; in between, and for s outside
+// [2^-63, 2^63] or not positive, the length is computed.  The usual case, a
+// sphere moved by less than its radius, needs no square root.
+__device__ __forceinline__ bool longer_than(V3 v, float s) {
+    const float d = dot3(v, v);  // the dot length() rounds
+    const uint32_t es = (__float_as_uint(s) >> 23) & 0xFFu;
+    if (s > 0.0f && es >= 64u && es <= 190u) {
+        const float s2 = s * s;
+        if (d < s2 * 0.99999f) return false;
+        if (d > s2 * 1.00001f) return true;
+    }
+    return sqrtf(d) > s;
+}
+
 // solve_sphere_constraint (physics.wgsl:300-331)
 __device__ __forceinline__ void sphere(const PhysParams& P, Agent& a, const Agent& b) {
     float edge = b.scale + a.scale;
@@ -418,7 +435,7 @@ __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32
     else
         contact_loop<false>(P, a, spos, svfme, o_g, c[0], c01, T, tself);
     V3 diff = a.position - old_pos;
-    if (len3(diff) > a.scale) {
+    if (longer_than(diff, a.scale)) {
         // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337); the
         // index is the slot inside the sphere's own scene
         const uint32_t li = i - base_a;
