@@ -349,22 +349,16 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
 // Four candidates per step suit sparse neighbourhoods (about nine candidates);
 // six hide more latency where cells are crowded.  The warp agrees on one width
 // so its lanes run one loop.
-constexpr uint32_t kCrowdedT = 48;
-#ifndef MB_LOOK
-#define MB_LOOK 4
-#endif
-#ifndef MB_LOOK_CROWDED
-#define MB_LOOK_CROWDED 6
-#endif
+constexpr uint32_t kCrowdedT = 48, kLookSparse = 4, kLookCrowded = 6;
 
 template <bool kShared>
 __device__ __forceinline__ void contact_loop(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
                                              uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself) {
     if (__any_sync(__activemask(), T >= kCrowdedT))
-        contact_walk<kShared, MB_LOOK_CROWDED>(P, a, bpos, bvfme, o, c0, c01, T, tself);
+        contact_walk<kShared, kLookCrowded>(P, a, bpos, bvfme, o, c0, c01, T, tself);
     else
-        contact_walk<kShared, MB_LOOK>(P, a, bpos, bvfme, o, c0, c01, T, tself);
+        contact_walk<kShared, kLookSparse>(P, a, bpos, bvfme, o, c0, c01, T, tself);
 }
 
 // Slot ranges of the three candidate rows of a sphere in cell (cx, cz), key =
