@@ -253,7 +253,9 @@ cudaError_t sync_tables(mb_batch* b, const std::vector<uint32_t>& modes) {
     return cudaEventRecord(b->table_ev, b->stream);
 }
 
-cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st) {
+// may_init: a scene can be in its INIT frame (false for chained frames, which
+// never hold one), so the tile counts of INIT scenes are summed afterwards.
+cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st, bool may_init) {
     cudaError_t e;
     if ((e = mb::count_scan_scenes(b->cnt, b->d_scenes, b->d_cell_tile_scene, b->cells_total, b->offs, st)))
         return e;
@@ -266,7 +268,9 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st) {
                                       b->cnt.coarse, b->ctl + mb::kCtlError, st)))
         return e;
     // INIT scenes emitted cell counts only: their tile counts from the cell counts
-    if ((e = mb::count_tile_counts_scenes(b->cnt, b->d_scenes, b->d_cell_tile_scene, b->cells_total, st))) return e;
+    if (may_init &&
+        (e = mb::count_tile_counts_scenes(b->cnt, b->d_scenes, b->d_cell_tile_scene, b->cells_total, st)))
+        return e;
     const uint32_t S = (uint32_t)b->scenes.size();
     k_flip_parity<<<(S + 127u) / 128u, 128, 0, st>>>(b->d_scenes, S);
     return cudaGetLastError();
@@ -280,7 +284,7 @@ cudaError_t build_graph(mb_batch* b, int which = 0) {
     cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e) return e;
     cudaError_t fe = cudaSuccess;
-    for (uint32_t f = 0; f < (which ? kChainFrames : 1u) && !fe; ++f) fe = enqueue_frame(b, b->cap_stream);
+    for (uint32_t f = 0; f < (which ? kChainFrames : 1u) && !fe; ++f) fe = enqueue_frame(b, b->cap_stream, !which);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(b->cap_stream, &g);
     if (fe) {
