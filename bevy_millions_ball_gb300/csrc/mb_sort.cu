@@ -58,20 +58,26 @@ struct HistParams {
 
 // ---------------------------------------------------------------- histogram
 // Digit counts of every pass in one read of the keys (shared-memory atomics; a
-// warp whose lanes share a digit adds once); the block that finishes last turns
+// warp whose lanes share a digit adds once, while that keeps happening); the block that finishes last turns
 // the counts into exclusive bases and zeroes them for the next sort.
-__device__ __forceinline__ void hist_key(uint32_t* s_hist, const HistParams& hp, uint32_t key, bool full_warp) {
-    for (int p = 0; p < hp.passes; ++p) {
+// Returns whether any digit of the key was warp-uniform (full_warp only).
+__device__ __forceinline__ bool hist_key(uint32_t* s_hist, const HistParams& hp, uint32_t key, bool full_warp) {
+    bool hit = false;
+#pragma unroll
+    for (int p = 0; p < kMaxPasses; ++p) {  // static indices: the parameters stay in registers
+        if (p >= hp.passes) break;
         const uint32_t d = (key >> hp.shift[p]) & ((1u << hp.bits[p]) - 1u);
         if (full_warp) {
             const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
             if (__all_sync(0xFFFFFFFFu, d == d0)) {
                 if ((threadIdx.x & 31u) == 0u) atomicAdd(&s_hist[hp.hist_off[p] + d], 32u);
+                hit = true;
                 continue;
             }
         }
         atomicAdd(&s_hist[hp.hist_off[p] + d], 1u);
     }
+    return hit;
 }
 
 __global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n,
@@ -89,15 +95,20 @@ __global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ 
     const uint32_t stride = gridDim.x * blockDim.x;
     const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0u;
     const uint32_t n4 = vec ? n / 4u : 0u;  // whole uint4 groups, read four keys at a time
+    // a warp stops looking for uniform digits once a group of its keys had none
+    // (random keys); nearly sorted keys keep hitting and keep the check
+    bool check = true;
     for (uint32_t g0 = blockIdx.x * blockDim.x; g0 < n4; g0 += stride) {
         const uint32_t g = g0 + tid;
         const bool full = g0 + blockDim.x <= n4;  // every lane of the block has a group
         if (g < n4) {
             const uint4 k4 = __ldg(reinterpret_cast<const uint4*>(keys) + g);
-            hist_key(s_hist, hp, k4.x, full);
-            hist_key(s_hist, hp, k4.y, full);
-            hist_key(s_hist, hp, k4.z, full);
-            hist_key(s_hist, hp, k4.w, full);
+            const bool c = full && check;
+            bool hit = hist_key(s_hist, hp, k4.x, c);
+            hit = hist_key(s_hist, hp, k4.y, c) || hit;
+            hit = hist_key(s_hist, hp, k4.z, c) || hit;
+            hit = hist_key(s_hist, hp, k4.w, c) || hit;
+            if (c) check = hit;
         }
     }
     for (uint32_t i = 4u * n4 + blockIdx.x * blockDim.x + tid; i < n; i += stride)
@@ -179,6 +190,7 @@ __global__ void __launch_bounds__(THREADS, 3)
     {
         uint32_t* wz = reinterpret_cast<uint32_t*>(s_whist);
         for (uint32_t i = tid; i < (uint32_t)WARPS * R / 2u; i += THREADS) wz[i] = 0u;
+        for (uint32_t d = tid; d < R; d += THREADS) s_cnt[d] = 0u;
     }
     __syncthreads();
     const uint32_t tile = s_tile;
@@ -191,7 +203,18 @@ __global__ void __launch_bounds__(THREADS, 3)
         uint32_t idx = wbase + (uint32_t)j * 32u + lane;
         bool valid = idx < n;
         k[j] = valid ? __ldg(keys_in + idx) : 0u;
+        // the value moves with the key at staging time; start pulling it into L2 now
+        if (valid && vals_in) asm volatile("prefetch.global.L2 [%0];" ::"l"(vals_in + idx));
     }
+    // the tile's digit counts first, published at once, so that later tiles'
+    // look-back finds them while this tile is still ranking its keys
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j)
+        if (wbase + (uint32_t)j * 32u + lane < n) atomicAdd(&s_cnt[(k[j] >> shift) & mask], 1u);
+    __syncthreads();
+    uint32_t* lb_tile = lookback + (size_t)tile * R;
+    for (uint32_t d = tid; d < R; d += THREADS)
+        st_relaxed(lb_tile + d, lb_pack(tile == 0 ? kFlagPrefix : kFlagAggregate, epoch, s_cnt[d]));
 
     // per-warp stable ranking; the lanes holding the same digit are found with one
     // ballot per digit bit (warp-level multi-split)
@@ -217,8 +240,7 @@ __global__ void __launch_bounds__(THREADS, 3)
     }
     __syncthreads();
 
-    // per digit: exclusive scan across warps, tile count, publish to look-back
-    uint32_t* lb_tile = lookback + (size_t)tile * R;
+    // per digit: exclusive scan across warps (the tile count is s_cnt already)
     for (uint32_t d = tid; d < R; d += THREADS) {
         uint32_t run = 0;
 #pragma unroll
@@ -227,8 +249,6 @@ __global__ void __launch_bounds__(THREADS, 3)
             s_whist[w * R + d] = (uint16_t)run;
             run += c;
         }
-        s_cnt[d] = run;
-        st_relaxed(lb_tile + d, lb_pack(tile == 0 ? kFlagPrefix : kFlagAggregate, epoch, run));
     }
     __syncthreads();
 
