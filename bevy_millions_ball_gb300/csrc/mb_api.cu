@@ -740,9 +740,9 @@ mb_status mb_sort_and_hash(mb_sort_plan* p, const uint32_t* keys, const uint32_t
         return fail(nullptr, MB_ERR_INVALID_ARG, "NULL key/value buffer");
     cudaStream_t st = (cudaStream_t)cuda_stream;
     mb::SortSchedule sch = mb::make_schedule(n, number_of_cells, p->digit_bits_max);
-    cudaError_t e = mb::sort_and_offsets(p->scratch, sch, keys, vals, sorted_keys, sorted_vals, st);
+    cudaError_t e = mb::sort_pairs(p->scratch, sch, keys, vals, sorted_keys, sorted_vals, st);
     if (e) return cuda_fail(nullptr, "mb_sort_and_hash", e);
-    if ((start || close) && (e = mb::offsets_to_start_close(p->scratch.offs, number_of_cells, start, close, st)))
+    if ((start || close) && (e = mb::hash_ranges(p->scratch, sorted_keys, n, number_of_cells, start, close, st)))
         return cuda_fail(nullptr, "mb_sort_and_hash", e);
     return MB_OK;
 }

@@ -89,6 +89,11 @@ cudaError_t sort_and_offsets(SortScratch& s, const SortSchedule& sch, const uint
                              cudaStream_t st);
 
 // start/close tables (spatial_hashing.wgsl semantics) from cell offsets.
+// start/close (nullable) of every cell straight from the sorted keys: 0xFFFFFFFF
+// for empty cells, else the first / last slot of the cell's run.
+// (scratch: its gap list, whose counter the sort's histogram cleared)
+cudaError_t hash_ranges(SortScratch& s, const uint32_t* sorted_keys, uint32_t n, uint32_t cells, uint32_t* start,
+                        uint32_t* close, cudaStream_t st);
 cudaError_t offsets_to_start_close(const uint32_t* offs, uint32_t cells, uint32_t* start,
                                    uint32_t* close, cudaStream_t st);
 

@@ -394,6 +394,53 @@ __global__ void k_offs_to_start_close(const uint32_t* __restrict__ offs, uint32_
     if (close) close[c] = full ? b - 1u : kInvalid;
 }
 
+// HASHING (spatial_hashing.wgsl:46-70) straight from the sorted keys, every cell
+// written once: thread i (i in [0, n], i = n a sentinel with key = cells) that
+// starts a run of key k writes start[k] = i, closes the previous run
+// (close[key[i-1]] = i - 1) and marks the empty cells between the two keys
+// (0xFFFFFFFF in both tables; runs of more than kGapCells empty cells are
+// listed for k_fill_empty).  Keys >= cells belong to no cell.
+__global__ void __launch_bounds__(256)
+    k_hash_ranges(const uint32_t* __restrict__ sorted_keys, uint32_t n, uint32_t cells, uint32_t* start,
+                  uint32_t* close, uint32_t* gaps, uint32_t gap_cap, uint32_t* gap_count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    const uint32_t k = i < n ? min(__ldg(sorted_keys + i), cells) : cells;
+    const uint32_t p = i > 0u ? min(__ldg(sorted_keys + i - 1u), cells) : 0xFFFFFFFFu;
+    const uint32_t from = p + 1u;  // first cell after the previous key (0 for i = 0)
+    if (i > 0u && p == k) return;  // inside a run
+    if (i > 0u && p < cells && close) close[p] = i - 1u;
+    if (k < cells && start) start[k] = i;
+    if (from >= k) return;  // no empty cells in between
+    if (k - from <= kGapCells) {
+        for (uint32_t c = from; c < k; ++c) {
+            if (start) start[c] = kInvalid;
+            if (close) close[c] = kInvalid;
+        }
+        return;
+    }
+    const uint32_t g = atomicAdd(gap_count, 1u);
+    if (g < gap_cap) {
+        gaps[3u * g] = from;
+        gaps[3u * g + 1u] = k - 1u;
+        gaps[3u * g + 2u] = kInvalid;
+    }
+}
+
+// The listed runs of empty cells (run e = blockIdx.x, + gridDim.x, ...).
+__global__ void __launch_bounds__(256)
+    k_fill_empty(const uint32_t* __restrict__ gaps, uint32_t gap_cap, const uint32_t* __restrict__ gap_count,
+                 uint32_t* start, uint32_t* close) {
+    const uint32_t m = min(*gap_count, gap_cap);
+    for (uint32_t e = blockIdx.x; e < m; e += gridDim.x) {
+        const uint32_t from = gaps[3u * e], to = gaps[3u * e + 1u];
+        for (uint32_t c = from + threadIdx.x; c <= to; c += blockDim.x) {
+            if (start) start[c] = kInvalid;
+            if (close) close[c] = kInvalid;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256)
     k_gather_state(const uint32_t* __restrict__ perm, uint32_t n, const float4* __restrict__ pos_in,
                    const uint4* __restrict__ vfme_in, float4* __restrict__ spos, uint4* __restrict__ svfme,
@@ -566,6 +613,20 @@ cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in,
     if (!n) return cudaSuccess;
     k_gather_state<<<(n + 255u) / 256u, 256, 0, st>>>(perm, n, pos_in, vfme_in, spos, svfme, sorted_keys, offs,
                                                       bands, N);
+    return cudaGetLastError();
+}
+
+cudaError_t hash_ranges(SortScratch& s, const uint32_t* sorted_keys, uint32_t n, uint32_t cells, uint32_t* start,
+                        uint32_t* close, cudaStream_t st) {
+    if (!start && !close) return cudaSuccess;
+    cudaError_t e;
+    // the gap counter is cleared by the sort's histogram kernel; an empty sort has none
+    if (n == 0 && (e = cudaMemsetAsync(s.ctl + kCtlGaps, 0, sizeof(uint32_t), st))) return e;
+    const uint32_t cap = gap_capacity(s.max_cells);
+    k_hash_ranges<<<(n + 256u) / 256u, 256, 0, st>>>(sorted_keys, n, cells, start, close, s.gaps, cap,
+                                                     s.ctl + kCtlGaps);
+    if ((e = cudaGetLastError())) return e;
+    k_fill_empty<<<(uint32_t)device_sm_count() * 4u, 256, 0, st>>>(s.gaps, cap, s.ctl + kCtlGaps, start, close);
     return cudaGetLastError();
 }
 

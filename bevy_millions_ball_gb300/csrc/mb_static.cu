@@ -105,8 +105,8 @@ extern "C" mb_status mb_sort_and_hash_static(const uint32_t* keys, const uint32_
         slot.ready = true;
     }
     mb::SortSchedule sch = mb::make_schedule(n, number_of_cells, kStaticDigitBits);
-    e = mb::sort_and_offsets(slot.view, sch, keys, vals, sorted_keys, sorted_vals, st);
-    if (!e && (start || close)) e = mb::offsets_to_start_close(slot.view.offs, number_of_cells, start, close, st);
+    e = mb::sort_pairs(slot.view, sch, keys, vals, sorted_keys, sorted_vals, st);
+    if (!e && (start || close)) e = mb::hash_ranges(slot.view, sorted_keys, n, number_of_cells, start, close, st);
     if (e) return fail(e == cudaErrorMemoryAllocation ? MB_ERR_OOM : MB_ERR_CUDA,
                        std::string("mb_sort_and_hash_static: ") + cudaGetErrorString(e));
     return MB_OK;

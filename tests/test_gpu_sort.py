@@ -124,3 +124,28 @@ def test_stage_rejects_oversize(cuda, plan):
 
     with pytest.raises(MbError):
         plan.run(0, None, (1 << 24) + 1, 16, 0, 0, None, None)
+
+
+def test_empty_input_leaves_every_cell_empty(cuda, plan):
+    """n = 0: no keys, so start and close are 0xFFFFFFFF everywhere (also after a
+    call that filled them)."""
+    rng = np.random.default_rng(3)
+    cells = 100_000
+    run_stage(cuda, plan, rng.integers(0, cells, 5000, dtype=np.uint64).astype(np.uint32), cells)
+    _, _, start, close = run_stage(cuda, plan, np.zeros(0, np.uint32), cells)
+    assert np.all(start == INV) and np.all(close == INV)
+
+
+def test_sparse_keys_long_empty_runs(cuda, plan):
+    """Few keys over many cells: long runs of empty cells between them (and before
+    the first, after the last) are filled by the gap pass."""
+    rng = np.random.default_rng(4)
+    cells = 1 << 22
+    keys = np.sort(rng.choice(cells, 300, replace=False)).astype(np.uint32)
+    keys = np.repeat(keys, rng.integers(1, 4, keys.size))[::-1].copy()
+    sk, perm, start, close = run_stage(cuda, plan, keys, cells)
+    ref = np.argsort(keys, kind="stable").astype(np.uint32)
+    np.testing.assert_array_equal(perm, ref)
+    rs, rc = oracle.spatial_hash(keys[ref], cells)
+    np.testing.assert_array_equal(start, rs)
+    np.testing.assert_array_equal(close, rc)
