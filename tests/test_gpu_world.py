@@ -178,13 +178,15 @@ def test_settings_change_midrun(built_lib, cuda):
 
 
 def test_crowded_cells_block_sort(built_lib, cuda):
-    """~200 spheres per cell: cells re-sorted by the block bitonic path."""
+    """~200 spheres per cell: cells put back in input order by the warp bitonic
+    fixup path (9-256 slots); the crowded-warp contact walk (six candidates per step)."""
     sc = scenes.plain_uniform(51_200, 16, grid_size=1, half_map_height=8, seed=31)
     run_pair(sc, 4, [1, 2, 4])
 
 
 def test_degenerate_cells_heapsort(built_lib, cuda):
-    """~9,000 spheres per cell (N=2): the bounded single-thread heapsort path."""
+    """~9,000 spheres per cell (N=2): the block fixup path (bitmaps of the input
+    indices, cells over 256 slots) and bands too wide to stage (global reads)."""
     sc = scenes.plain_uniform(36_000, 2, grid_size=4, half_map_height=8, seed=32)
     run_pair(sc, 3, [1, 2, 3])
 
