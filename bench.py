@@ -5,7 +5,8 @@ positions, N(0, 1) m/s velocities, rigid response, dt = 1/60 (runs as 0.016).
 A "step" is one frame of the pipeline over the whole scene.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload P-1M|P-small|P-4M] [--cpu-seconds S]
+                    [--workload P-1M|P-small|P-4M|batch|serving|sort|segments|render]
+                    [--cpu-seconds S]
 
 Timing: W untimed frames, then K frames, each bracketed by CUDA events on the
 world's stream; L2 is flushed (a 256 MB write, then a 256 MB read so that no dirty
@@ -589,13 +590,160 @@ def run_serving(args):
     return 0
 
 
+def run_segments(args):
+    """Stage workload: mb_assemble_segments (segment starts, key->segment map and
+    count) over 16,777,216 sorted keys drawn uniformly below 2^24 (sorted once by
+    the stage sort, outside the timing); the reference's segment assembly
+    (src/physics/assemble_segs.rs:314-430) at its largest hashing-test size."""
+    import numpy as np
+    import torch
+
+    from bevy_millions_ball_gb300 import SortPlan
+
+    torch.cuda.set_device(0)
+    n = cells = 1 << 24
+    plan = SortPlan(max_keys=n, max_cells=cells)
+    keys_np = np.random.default_rng(0).integers(0, cells, n).astype(np.uint32)
+    keys = torch.from_numpy(keys_np.view(np.int32)).cuda()
+    sk = torch.empty(n, dtype=torch.int32, device="cuda")
+    sv = torch.empty_like(sk)
+    segs = torch.empty(n, dtype=torch.int32, device="cuda")
+    kmap = torch.empty(cells, dtype=torch.int32, device="cuda")
+    num = torch.empty(1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    plan.run(keys.data_ptr(), None, n, cells, sk.data_ptr(), sv.data_ptr(), None, None, stream.cuda_stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    run = lambda: plan.assemble_segments(sk.data_ptr(), n, segs.data_ptr(), kmap.data_ptr(), num.data_ptr(),
+                                         stream.cuda_stream)
+    for _ in range(max(args.warmup, 3)):
+        run()
+    torch.cuda.synchronize()
+    sorted_np = np.sort(keys_np)
+    starts = np.flatnonzero(np.r_[True, sorted_np[1:] != sorted_np[:-1]]).astype(np.uint32)
+    m = int(num.cpu().numpy()[0])
+    assert m == starts.size and np.array_equal(segs[:m].cpu().numpy().view(np.uint32), starts)
+    K = min(args.steps, 50)
+    total = 0.0
+    for _ in range(K):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        run()
+        b.record(stream)
+        torch.cuda.synchronize()
+        total += a.elapsed_time(b)
+    plan.close()
+    ms = total / K
+    hbm, peak_kind = peaks()
+    # byte model: sorted keys read once (4 B/key), segment start and map entry written (8 B/segment)
+    model = 4 * n + 8 * m
+    achieved = model / (ms * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:  # the same assembly restated in numpy, one thread
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < min(args.cpu_seconds, 10.0) or reps == 0:
+            st = np.flatnonzero(np.r_[True, sorted_np[1:] != sorted_np[:-1]])
+            km = np.empty(cells, np.uint32)
+            km[sorted_np[st]] = np.arange(st.size, dtype=np.uint32)
+            reps += 1
+        dt = (time.perf_counter() - t0) / reps
+        cpu = {"value": n / dt, "unit": "keys/s", "cores": 1, "kind": "port",
+               "sample": f"{reps} numpy runs of the same 16,777,216 sorted keys, one thread"}
+    line = {
+        "metric": "keys/s (segment table)", "value": n / (ms * 1e-3), "unit": "keys/s", "n_gpus": 1,
+        "steps": K, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"stage: 16,777,216 sorted keys, uniform below 2^24 ({m:,} segments)",
+                   "l2": "flushed before every timed call (256 MB write, outside the events)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": peak_kind, "model_bytes": model},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_render(args):
+    """Headless impostor render (mb_render_topdown) of the settled 1,048,576-sphere
+    scene (P-1M after 300 frames) into a 2048 x 2048 RGBA8 image + height map in
+    device memory, the whole 1024 x 1024 map in view."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from bevy_millions_ball_gb300 import World, scenes
+    from bevy_millions_ball_gb300._abi import MB_DEVICE
+
+    torch.cuda.set_device(0)
+    sc = scenes.workload("P-1M")
+    stream = torch.cuda.current_stream()
+    W = H = 2048
+    w = World(sc.plugin, stream=stream.cuda_stream)
+    w.set_state(sc.pos_scale, sc.vfme)
+    w.step(300)
+    w.sync()
+    img = torch.empty(W * H, dtype=torch.int32, device="cuda")
+    hmap = torch.empty(W * H, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    run = lambda: w._check(w._lib.mb_render_topdown(w._h, W, H, -512.0, -512.0, 512.0, 512.0, img.data_ptr(),
+                                                    hmap.data_ptr(), MB_DEVICE))
+    for _ in range(max(args.warmup, 3)):
+        run()
+    torch.cuda.synchronize()
+    K = min(args.steps, 50)
+    total = 0.0
+    for _ in range(K):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        run()
+        b.record(stream)
+        torch.cuda.synchronize()
+        total += a.elapsed_time(b)
+    ms = total / K
+    pos, _ = w.get_state()
+    w.close()
+    hbm, peak_kind = peaks()
+    px = W * H
+    # byte model: spheres read once (16 B), z-buffer cleared, each covered pixel's
+    # atomic max (read + write 16 B; pi r^2 pixels per sphere at 2 px per unit),
+    # then per pixel the z-buffer read, the winning sphere read and 8 B written
+    covered = int(sc.n * np.pi * 0.25 * (W / 1024.0) ** 2)
+    model = 16 * sc.n + 8 * px + 16 * covered + px * (8 + 16 + 8)
+    achieved = model / (ms * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle
+
+        t0 = time.perf_counter()
+        oracle.render_topdown(pos, W, H, -512.0, -512.0, 512.0, 512.0)
+        dt = time.perf_counter() - t0
+        cpu = {"value": 1.0 / dt, "unit": "images/s", "cores": 1, "kind": "port",
+               "sample": "one oracle render of the same state and image size, one thread"}
+    line = {
+        "metric": "images/s (headless impostor render)", "value": 1e3 / ms, "unit": "images/s", "n_gpus": 1,
+        "steps": K, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "P-1M state after 300 frames, 2048 x 2048 top-down image of the whole map",
+                   "l2": "flushed before every timed call (256 MB write, outside the events)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": peak_kind, "model_bytes": model},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="P-1M", choices=["P-small", "P-1M", "P-4M", "batch", "serving", "sort"])
+    ap.add_argument("--workload", default="P-1M",
+                    choices=["P-small", "P-1M", "P-4M", "batch", "serving", "sort", "segments", "render"])
     ap.add_argument("--batch-scenes", type=int, default=512)
     ap.add_argument("--serve-requests", type=int, default=300)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
@@ -607,9 +755,11 @@ def main():
     args = ap.parse_args()
     rank, world_size, local_rank = env_rank()
     if args.impl == "reference":
-        if args.workload in ("batch", "serving", "sort"):
-            why = ("the reference's sort runs only as wgpu compute passes (no graphics stack on this box)"
-                   if args.workload == "sort" else
+        if args.workload in ("batch", "serving", "sort", "segments", "render"):
+            why = ("the reference's sort and segment passes run only as wgpu compute passes (no graphics stack "
+                   "on this box)" if args.workload in ("sort", "segments") else
+                   "the reference's impostor pass is a wgpu fragment shader: unavailable on this box"
+                   if args.workload == "render" else
                    "the reference runs one scene per app; batching/serving have no reference implementation")
             print(json.dumps({"impl": "reference", "unavailable": why}))
             return 0
@@ -623,6 +773,10 @@ def main():
         return run_serving(args)
     if args.workload == "sort":
         return run_sort(args)
+    if args.workload == "segments":
+        return run_segments(args)
+    if args.workload == "render":
+        return run_render(args)
     return run_ours(args, rank, world_size, local_rank)
 
 

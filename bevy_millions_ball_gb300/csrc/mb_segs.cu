@@ -8,7 +8,8 @@
 //
 // Three kernels: every block counts the run starts of its 4096 keys; one block
 // scans the block counts (and writes the total); every block then recounts its
-// run starts with a block-wide scan and writes its segments at its base.
+// run starts (per warp, in order, with ballots) and writes its segments at its
+// base.  Warps read their keys in coalesced chunks of 32.
 
 #include <cuda_runtime.h>
 
@@ -24,16 +25,6 @@ constexpr uint32_t kSegBlockKeys = kSegThreads * kSegItems;
 // key i of the block's range starts a run
 __device__ __forceinline__ bool run_start(const uint32_t* __restrict__ keys, uint32_t i) {
     return i == 0u || __ldg(keys + i) != __ldg(keys + i - 1u);
-}
-
-__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* s_w) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
-    if ((threadIdx.x & 31u) == 0u) s_w[threadIdx.x >> 5] = v;
-    __syncthreads();
-    uint32_t t = 0;
-    for (uint32_t w = 0; w < blockDim.x / 32u; ++w) t += s_w[w];
-    __syncthreads();
-    return t;
 }
 
 // exclusive prefix over the block (thread order) of v; *total = block sum
@@ -56,16 +47,38 @@ __device__ __forceinline__ uint32_t block_excl(uint32_t v, uint32_t* s_w, uint32
     return base + incl - v;
 }
 
-// Each thread owns kSegItems consecutive keys of the block's range.
+// A block covers kSegBlockKeys consecutive keys; warp w of it the kSegItems
+// chunks of 32 keys starting at w * 32 * kSegItems, lane l key l of each chunk
+// (coalesced loads).  run_flags returns, per lane, bit q = key l of chunk q starts
+// a run, and the warp's number of run starts.
+__device__ __forceinline__ uint32_t run_flags(const uint32_t* __restrict__ keys, uint32_t n, uint32_t wfirst,
+                                              uint32_t& warp_total) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t flags = 0, total = 0;
+#pragma unroll
+    for (uint32_t q = 0; q < kSegItems; ++q) {
+        const uint32_t i = wfirst + q * 32u + lane;
+        const bool f = i < n && run_start(keys, i);
+        flags |= (f ? 1u : 0u) << q;
+        total += (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, f));
+    }
+    warp_total = total;
+    return flags;
+}
+
 __global__ void __launch_bounds__(kSegThreads)
     k_seg_count(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ block_counts) {
     __shared__ uint32_t s_w[kSegThreads / 32];
-    const uint32_t first = blockIdx.x * kSegBlockKeys + threadIdx.x * kSegItems;
-    uint32_t c = 0;
-    for (uint32_t q = 0; q < kSegItems; ++q)
-        if (first + q < n && run_start(keys, first + q)) ++c;
-    const uint32_t t = block_sum(c, s_w);
-    if (threadIdx.x == 0) block_counts[blockIdx.x] = t;
+    const uint32_t warp = threadIdx.x >> 5;
+    uint32_t wt;
+    run_flags(keys, n, blockIdx.x * kSegBlockKeys + warp * 32u * kSegItems, wt);
+    if ((threadIdx.x & 31u) == 0u) s_w[warp] = wt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (uint32_t w = 0; w < kSegThreads / 32u; ++w) t += s_w[w];
+        block_counts[blockIdx.x] = t;
+    }
 }
 
 // One block: exclusive scan of the block counts in place, total to *num_segs.
@@ -88,19 +101,24 @@ __global__ void __launch_bounds__(kSegThreads)
     k_seg_assemble(const uint32_t* __restrict__ keys, uint32_t n, const uint32_t* __restrict__ block_base,
                    uint32_t* __restrict__ segs, uint32_t* __restrict__ key_seg_map) {
     __shared__ uint32_t s_w[kSegThreads / 32];
-    const uint32_t first = blockIdx.x * kSegBlockKeys + threadIdx.x * kSegItems;
-    uint32_t c = 0;
-    for (uint32_t q = 0; q < kSegItems; ++q)
-        if (first + q < n && run_start(keys, first + q)) ++c;
-    uint32_t total;
-    uint32_t s = __ldg(block_base + blockIdx.x) + block_excl(c, s_w, total);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, lt = (1u << lane) - 1u;
+    const uint32_t wfirst = blockIdx.x * kSegBlockKeys + warp * 32u * kSegItems;
+    uint32_t wt;
+    const uint32_t flags = run_flags(keys, n, wfirst, wt);
+    if (lane == 0u) s_w[warp] = wt;
+    __syncthreads();
+    uint32_t s = __ldg(block_base + blockIdx.x);  // the warp's first segment: block base + earlier warps
+    for (uint32_t w = 0; w < warp; ++w) s += s_w[w];
+#pragma unroll
     for (uint32_t q = 0; q < kSegItems; ++q) {
-        const uint32_t i = first + q;
-        if (i < n && run_start(keys, i)) {
-            segs[s] = i;
-            key_seg_map[__ldg(keys + i)] = s;
-            ++s;
+        const bool f = (flags >> q) & 1u;
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, f);
+        if (f) {
+            const uint32_t i = wfirst + q * 32u + lane, at = s + (uint32_t)__popc(m & lt);
+            segs[at] = i;
+            key_seg_map[__ldg(keys + i)] = at;
         }
+        s += (uint32_t)__popc(m);
     }
 }
 
