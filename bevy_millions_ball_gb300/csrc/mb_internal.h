@@ -83,10 +83,6 @@ cudaError_t sort_pairs(SortScratch& s, const SortSchedule& sch, const uint32_t* 
 // keys and the most significant digit's bases of the sort that produced them.
 cudaError_t cell_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t* sorted_keys,
                          cudaStream_t st);
-// sort_pairs then cell_offsets.
-cudaError_t sort_and_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t* keys,
-                             const uint32_t* vals, uint32_t* sorted_keys, uint32_t* sorted_vals,
-                             cudaStream_t st);
 
 // start/close tables (spatial_hashing.wgsl semantics) from cell offsets.
 // start/close (nullable) of every cell straight from the sorted keys: 0xFFFFFFFF

@@ -599,14 +599,6 @@ cudaError_t cell_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t
     return cudaGetLastError();
 }
 
-cudaError_t sort_and_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t* keys,
-                             const uint32_t* vals, uint32_t* sorted_keys, uint32_t* sorted_vals,
-                             cudaStream_t st) {
-    cudaError_t e = sort_pairs(s, sch, keys, vals, sorted_keys, sorted_vals, st);
-    if (e) return e;
-    return cell_offsets(s, sch, sorted_keys, st);
-}
-
 cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in, const uint4* vfme_in,
                          float4* spos, uint4* svfme, const uint32_t* sorted_keys, const uint32_t* offs,
                          uint4* bands, uint32_t N, cudaStream_t st) {
