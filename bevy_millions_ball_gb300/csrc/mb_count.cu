@@ -9,7 +9,7 @@
 //      it emits the keys (one red.add per sphere);
 //   2. k_cell_scan: one exclusive scan turns the counts into the cell offsets
 //      offs[c] (= start of cell c; offs[C] = n); each
-//      1024-cell chunk takes its base from per-4096-cell-tile counts emitted with
+//      2048-cell chunk takes its base from per-4096-cell-tile counts emitted with
 //      the per-cell ones (plus the counts of its tile's earlier chunks), so
 //      chunks never wait on each other;
 //   3. k_cell_scatter: each sphere claims a slot of its cell with one atomic per
@@ -36,8 +36,8 @@ namespace mb {
 namespace {
 
 // ---------------------------------------------------------------- scan
-// Block b of the scan covers the chunk of cells [1024 b, 1024 b + 1024) inside
-// tile t = b / 4 (cells [4096 t, 4096 t + 4096)).  coarse[t] holds the number of
+// Block b of the scan covers the chunk of cells [kScanChunk b, kScanChunk (b + 1))
+// inside tile t = b kScanChunk / 4096 (cells [4096 t, 4096 t + 4096)).  coarse[t] holds the number of
 // spheres in tile t (emitted with the per-cell counts), so a chunk finds its base
 // by summing coarse[0..t) and the counts of the tile's cells before it - no
 // look-back, no waiting on other blocks.  The counts are left in place (other
