@@ -9,7 +9,7 @@
 //      it emits the keys (one red.add per sphere);
 //   2. k_cell_scan: one exclusive scan turns the counts into the cell offsets
 //      offs[c] (= start of cell c; offs[C] = n); each
-//      2048-cell chunk takes its base from per-4096-cell-tile counts emitted with
+//      chunk of cells takes its base from per-4096-cell-tile counts emitted with
 //      the per-cell ones (plus the counts of its tile's earlier chunks), so
 //      chunks never wait on each other;
 //   3. k_cell_scatter: each sphere claims a slot of its cell with one atomic per

@@ -213,7 +213,7 @@ cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_sc
 
 // Counting sort of cell keys (mb_count.cu).
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 8;
+constexpr int kScanItems = 16;
 constexpr uint32_t kScanChunk = kScanThreads * kScanItems;  // cells per block of the scan
 constexpr uint32_t kScanTile = 4096;                        // cells per coarse count (tile base)
 static_assert(kScanTile % kScanChunk == 0, "scan chunks tile the coarse tiles");
