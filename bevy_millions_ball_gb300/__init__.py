@@ -362,6 +362,11 @@ class SortPlan:
                                                          sorted_keys_ptr, sorted_vals_ptr, start_ptr,
                                                          close_ptr, _stream_handle(stream)))
 
+    def status(self, stream=None) -> None:
+        """mb_sort_plan_status: raises MbError (MB_ERR_TIMEOUT) if a bounded device
+        wait of the plan's sorts gave up since the last check (and clears it)."""
+        _abi.check(self._lib, self._lib.mb_sort_plan_status(self._h, _stream_handle(stream)))
+
     def assemble_segments(self, sorted_keys_ptr: int, n: int, segs_ptr: int, key_seg_map_ptr: int,
                           num_segs_ptr: int, stream=None) -> None:
         """mb_assemble_segments: one segment per run of equal sorted keys (device pointers)."""

@@ -107,7 +107,10 @@ SIGNATURES = {
     "mb_sort_plan_create": (C.c_int, [u32, u32, C.POINTER(vp)]),
     "mb_sort_plan_destroy": (C.c_int, [vp]),
     "mb_sort_and_hash": (C.c_int, [vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]),
+    "mb_sort_plan_status": (C.c_int, [vp, vp]),
+    "mb_sort_plan_selftest_stall": (C.c_int, [vp, u32, vp]),
     "mb_sort_and_hash_static": (C.c_int, [vp, vp, u32, u32, vp, vp, vp, vp, vp]),
+    "mb_sort_static_status": (C.c_int, [vp]),
     "mb_assemble_segments": (C.c_int, [vp, vp, u32, vp, vp, vp, vp]),
     "mb_render_topdown": (C.c_int, [vp, u32, u32, C.c_float, C.c_float, C.c_float, C.c_float, vp, vp, C.c_int]),
     "mb_get_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),

@@ -747,6 +747,27 @@ mb_status mb_sort_and_hash(mb_sort_plan* p, const uint32_t* keys, const uint32_t
     return MB_OK;
 }
 
+mb_status mb_sort_plan_status(mb_sort_plan* p, void* cuda_stream) {
+    if (!p) return fail(nullptr, MB_ERR_INVALID_ARG, "plan is NULL");
+    uint32_t flags = 0;
+    cudaError_t e = mb::sort_take_error(p->scratch, (cudaStream_t)cuda_stream, &flags);
+    if (e) return cuda_fail(nullptr, "mb_sort_plan_status", e);
+    if (flags)
+        return fail(nullptr, MB_ERR_TIMEOUT,
+                    "mb_sort_plan_status: a bounded look-back wait of the sort gave up; the results of the "
+                    "plan's calls since the last status check are invalid");
+    return MB_OK;
+}
+
+mb_status mb_sort_plan_selftest_stall(mb_sort_plan* p, uint32_t spin_limit, void* cuda_stream) {
+    if (!p) return fail(nullptr, MB_ERR_INVALID_ARG, "plan is NULL");
+    if (spin_limit == 0 || spin_limit > (1u << 20))
+        return fail(nullptr, MB_ERR_INVALID_ARG, "spin_limit must be in [1, 2^20]");
+    cudaError_t e = mb::sort_stall_for_test(p->scratch, spin_limit, (cudaStream_t)cuda_stream);
+    if (e) return cuda_fail(nullptr, "mb_sort_plan_selftest_stall", e);
+    return MB_OK;
+}
+
 mb_status mb_assemble_segments(mb_sort_plan* p, const uint32_t* sorted_keys, uint32_t n, uint32_t* segs,
                                uint32_t* key_seg_map, uint32_t* num_segs, void* cuda_stream) {
     if (!p) return fail(nullptr, MB_ERR_INVALID_ARG, "plan is NULL");

@@ -64,8 +64,11 @@ struct SortScratch {
     uint32_t* offs = nullptr;       // [max_cells + 1] cell offsets (CSR)
     uint32_t* gaps = nullptr;       // [3 * gap_capacity(max_cells)] long runs of cells to fill
     size_t lookback_words_per_pass = 0;
-    uint32_t last_tiles = 0;        // tiles of the previous sort (look-back reuse check)
+    // layout of the previous sort's look-back words (reuse check): a table is
+    // reused only when the previous sort wrote every word this one reads
+    uint32_t last_tiles = 0;
     int last_passes = 0;
+    uint32_t last_bits[kMaxPasses] = {0, 0, 0, 0};
 };
 
 // Runs of more than kGapCells cells between consecutive sorted keys are written
@@ -76,9 +79,20 @@ cudaError_t scratch_alloc(SortScratch& s, uint32_t max_keys, uint32_t max_cells)
 void scratch_free(SortScratch& s);
 
 // Stable sort of (keys, vals or iota) -> (sorted_keys, sorted_vals).
+// clear_always: clear the look-back words this sort uses on the stream every
+// call instead of tracking the previous sort's layout on the host (for scratch
+// that calls recorded into graphs may replay in any order).
 cudaError_t sort_pairs(SortScratch& s, const SortSchedule& sch, const uint32_t* keys,
                        const uint32_t* vals, uint32_t* sorted_keys, uint32_t* sorted_vals,
-                       cudaStream_t st);
+                       cudaStream_t st, bool clear_always = false);
+// Reads and clears the scratch's error word (synchronises the stream first):
+// *flags != 0 when a bounded look-back wait gave up since the last read.  A
+// give-up also forces the next sort to start from a cleared look-back table.
+cudaError_t sort_take_error(SortScratch& s, cudaStream_t st, uint32_t* flags);
+// Test hook: one onesweep block takes tile 1 of a pass whose tile 0 never
+// publishes its look-back words, so its wait runs out after spin_limit polls and
+// sets the error word; nothing else is written.  The next sort clears the table.
+cudaError_t sort_stall_for_test(SortScratch& s, uint32_t spin_limit, cudaStream_t st);
 // Cell offsets offs[c] = number of keys < c for c in [0, cells], from the sorted
 // keys and the most significant digit's bases of the sort that produced them.
 cudaError_t cell_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t* sorted_keys,
@@ -297,6 +311,7 @@ cudaError_t assemble_segments(const uint32_t* sorted_keys, uint32_t n, uint32_t*
 cudaError_t render_topdown(const float4* pos, uint32_t n, uint32_t w, uint32_t h, float x0, float z0, float x1,
                            float z1, unsigned long long* zbuf, uint32_t* rgba, float* height, cudaStream_t st);
 
+// SM count of the current device (cached per device id).
 int device_sm_count();
 
 // Settings checks shared by worlds and batches ("" = valid).

@@ -32,7 +32,7 @@ namespace {
 constexpr uint32_t kFlagAggregate = 1u;
 constexpr uint32_t kFlagPrefix = 2u;
 constexpr uint32_t kValueMask = (1u << 28) - 1u;
-constexpr uint32_t kSpinLimit = 1u << 21;
+constexpr uint32_t kSpinLimit = 1u << 21;  // look-back polls before a wait gives up (~0.2 s)
 constexpr int kWindow = 8;  // look-back words loaded per step
 
 __device__ __forceinline__ uint32_t lb_pack(uint32_t flag, uint32_t epoch, uint32_t value) {
@@ -168,7 +168,8 @@ __global__ void __launch_bounds__(THREADS, 3)
     k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
                uint32_t shift, uint32_t bits, const uint32_t* __restrict__ bases,
-               uint32_t* lookback, uint32_t* tile_ticket, uint32_t* err, const uint32_t* epoch_word) {
+               uint32_t* lookback, uint32_t* tile_ticket, uint32_t* err, const uint32_t* epoch_word,
+               uint32_t spin_limit) {
     constexpr int WARPS = THREADS / 32;
     constexpr uint32_t TILE = THREADS * ITEMS;
     const uint32_t R = 1u << bits, mask = R - 1u;
@@ -281,7 +282,7 @@ __global__ void __launch_bounds__(THREADS, 3)
                     if (f == kFlagPrefix) found = true;
                 }
                 if (!ready) {  // a predecessor has not published yet: retry this window
-                    if (++spins > kSpinLimit) {
+                    if (++spins > spin_limit) {
                         atomicOr(err, 1u);
                         gave_up = true;
                     } else if (spins > 16u) {
@@ -461,14 +462,15 @@ size_t onesweep_smem(uint32_t R) {
 }  // namespace
 
 int device_sm_count() {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
-    return sms;
+    constexpr int kDevices = 64;
+    static int sms[kDevices] = {};  // 0: not looked up yet (benign race: every thread stores the same value)
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int got = (dev >= 0 && dev < kDevices) ? __atomic_load_n(&sms[dev], __ATOMIC_RELAXED) : 0;
+    if (got > 0) return got;
+    if (cudaDeviceGetAttribute(&got, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || got <= 0) got = 1;
+    if (dev >= 0 && dev < kDevices) __atomic_store_n(&sms[dev], got, __ATOMIC_RELAXED);
+    return got;
 }
 
 SortSchedule make_schedule(uint32_t n, uint32_t cells, uint32_t digit_bits_max) {
@@ -523,6 +525,31 @@ cudaError_t scratch_alloc(SortScratch& s, uint32_t max_keys, uint32_t max_cells)
     return cudaSuccess;
 }
 
+namespace {
+// Look-back words are tagged with the epoch of the sort that wrote them (1..3,
+// advanced by every sort's histogram kernel) and reused without clearing when
+// the previous sort had the same layout (tiles, passes and digit widths): it
+// then overwrote every word this sort reads with the previous epoch, so a word
+// not yet published by this sort never carries the current epoch.  Any other
+// layout could leave a word of the sort three epochs back in place, so the
+// table is cleared (and the epoch restarted) instead.
+bool same_layout(const SortScratch& s, const SortSchedule& sch) {
+    if (sch.tiles != s.last_tiles || sch.passes != s.last_passes) return false;
+    for (int p = 0; p < sch.passes; ++p)
+        if (sch.bits[p] != s.last_bits[p]) return false;
+    return true;
+}
+void remember_layout(SortScratch& s, const SortSchedule& sch) {
+    s.last_tiles = sch.tiles;
+    s.last_passes = sch.passes;
+    for (int p = 0; p < kMaxPasses; ++p) s.last_bits[p] = p < sch.passes ? sch.bits[p] : 0u;
+}
+void forget_layout(SortScratch& s) {
+    s.last_tiles = 0;
+    s.last_passes = 0;
+}
+}  // namespace
+
 void scratch_free(SortScratch& s) {
     cudaFree(s.alt_keys);
     cudaFree(s.alt_vals);
@@ -537,18 +564,23 @@ void scratch_free(SortScratch& s) {
 
 cudaError_t sort_pairs(SortScratch& s, const SortSchedule& sch, const uint32_t* keys,
                        const uint32_t* vals, uint32_t* sorted_keys, uint32_t* sorted_vals,
-                       cudaStream_t st) {
+                       cudaStream_t st, bool clear_always) {
     const uint32_t n = sch.n;
     if (n == 0) return cudaSuccess;
-    // look-back words are reused across sorts with an epoch tag; a different
-    // tile count or pass count could leave same-epoch words from older sorts.
-    if (sch.tiles != s.last_tiles || sch.passes != s.last_passes) {
+    if (clear_always) {
+        // every word this sort reads starts unpublished, whatever ran before
+        for (int p = 0; p < sch.passes; ++p) {
+            cudaError_t e = cudaMemsetAsync(s.lookback + (size_t)p * s.lookback_words_per_pass, 0,
+                                            sizeof(uint32_t) * (size_t)sch.tiles * (1u << sch.bits[p]), st);
+            if (e) return e;
+        }
+        forget_layout(s);
+    } else if (!same_layout(s, sch)) {
         cudaError_t e = cudaMemsetAsync(s.lookback, 0,
                                         sizeof(uint32_t) * kMaxPasses * s.lookback_words_per_pass, st);
         if (e) return e;
         if ((e = cudaMemsetAsync(s.ctl + kCtlEpoch, 0, sizeof(uint32_t), st))) return e;
-        s.last_tiles = sch.tiles;
-        s.last_passes = sch.passes;
+        remember_layout(s, sch);
     }
 
     HistParams hp;
@@ -578,12 +610,42 @@ cudaError_t sort_pairs(SortScratch& s, const SortSchedule& sch, const uint32_t* 
         k_onesweep<kSortThreads, kSortItems><<<sch.tiles, kSortThreads, onesweep_smem(R), st>>>(
             kin, vin, kout, vout, n, sch.shift[p], sch.bits[p], s.bases + p * (kMaxRadix + 1),
             s.lookback + (size_t)p * s.lookback_words_per_pass, s.ctl + kCtlTile0 + p,
-            s.ctl + kCtlError, s.ctl + kCtlEpoch);
+            s.ctl + kCtlError, s.ctl + kCtlEpoch, kSpinLimit);
         if ((e = cudaGetLastError())) return e;
         kin = kout;
         vin = vout;
     }
     return cudaSuccess;
+}
+
+cudaError_t sort_take_error(SortScratch& s, cudaStream_t st, uint32_t* flags) {
+    uint32_t f = 0;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (!e) e = cudaMemcpy(&f, s.ctl + kCtlError, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (!e && f) {
+        e = cudaMemset(s.ctl + kCtlError, 0, sizeof(uint32_t));
+        forget_layout(s);  // the look-back words of the failed sort may be half written
+    }
+    if (flags) *flags = e ? 0u : f;
+    return e;
+}
+
+cudaError_t sort_stall_for_test(SortScratch& s, uint32_t spin_limit, cudaStream_t st) {
+    // pass 0's words unpublished (tile 0 never runs), ticket 1 for the one block:
+    // it is tile 1 of a one-key sort, so it reads and writes no keys, and its
+    // look-back on tile 0 polls until spin_limit runs out
+    constexpr uint32_t kBits = 8, R = 1u << kBits;
+    if (2u * R > s.lookback_words_per_pass) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(s.lookback, 0, sizeof(uint32_t) * 2u * R, st);
+    if (e) return e;
+    const uint32_t one = 1u;
+    if ((e = cudaMemcpyAsync(s.ctl + kCtlTile0, &one, sizeof(uint32_t), cudaMemcpyHostToDevice, st))) return e;
+    k_onesweep<kSortThreads, kSortItems><<<1, kSortThreads, onesweep_smem(R), st>>>(
+        s.alt_keys, nullptr, s.alt_vals, s.alt_vals, 1u, 0u, kBits, s.bases, s.lookback, s.ctl + kCtlTile0,
+        s.ctl + kCtlError, s.ctl + kCtlEpoch, spin_limit);
+    if ((e = cudaGetLastError())) return e;
+    forget_layout(s);
+    return cudaStreamSynchronize(st);  // `one` lives on this stack frame
 }
 
 cudaError_t cell_offsets(SortScratch& s, const SortSchedule& sch, const uint32_t* sorted_keys,

@@ -18,7 +18,11 @@
 // Every call on a device shares the one array, and the array keeps what the
 // last call left in it.  Calls whose work overlaps on the GPU (different
 // streams, or host threads racing) corrupt each other's results; callers must
-// order them, e.g. by issuing them all on one stream.
+// order them, e.g. by issuing them all on one stream.  Each call clears, on its
+// stream, the part of the array whose stale contents could be misread (the sort's
+// look-back words), so recorded calls replayed in any order stay correct.
+// mb_sort_static_status reads (and clears) the array's error word: a bounded
+// device-side wait that gave up.
 
 #include <cuda_runtime.h>
 
@@ -105,9 +109,27 @@ extern "C" mb_status mb_sort_and_hash_static(const uint32_t* keys, const uint32_
         slot.ready = true;
     }
     mb::SortSchedule sch = mb::make_schedule(n, number_of_cells, kStaticDigitBits);
-    e = mb::sort_pairs(slot.view, sch, keys, vals, sorted_keys, sorted_vals, st);
+    e = mb::sort_pairs(slot.view, sch, keys, vals, sorted_keys, sorted_vals, st, /*clear_always=*/true);
     if (!e && (start || close)) e = mb::hash_ranges(slot.view, sorted_keys, n, number_of_cells, start, close, st);
     if (e) return fail(e == cudaErrorMemoryAllocation ? MB_ERR_OOM : MB_ERR_CUDA,
                        std::string("mb_sort_and_hash_static: ") + cudaGetErrorString(e));
+    return MB_OK;
+}
+
+extern "C" mb_status mb_sort_static_status(void* cuda_stream) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return fail(MB_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return fail(MB_ERR_INVALID_ARG, "mb_sort_static_status: device id too large");
+    std::lock_guard<std::mutex> lock(g_mu);
+    DeviceSlot& slot = g_dev[dev];
+    if (!slot.ready) return MB_OK;  // nothing ran on this device
+    uint32_t flags = 0;
+    e = mb::sort_take_error(slot.view, (cudaStream_t)cuda_stream, &flags);
+    if (e) return fail(MB_ERR_CUDA, std::string("mb_sort_static_status: ") + cudaGetErrorString(e));
+    if (flags)
+        return fail(MB_ERR_TIMEOUT,
+                    "mb_sort_static_status: a bounded look-back wait gave up; results of the calls since the "
+                    "last status check are invalid");
     return MB_OK;
 }

@@ -197,6 +197,27 @@ mb_status mb_sort_and_hash(mb_sort_plan* p, const uint32_t* keys, const uint32_t
                            uint32_t* start, uint32_t* close, void* cuda_stream);
 
 /*
+ * Status of a plan's sorts (the reference panics where a pass fails,
+ * src/physics/mod.rs:788-798; this reports instead).  Every wait of the sort's
+ * decoupled look-back is bounded: a wait that gives up sets an error word in the
+ * plan and the call's results are invalid.  mb_sort_plan_status waits for
+ * `cuda_stream`, reads and clears that word, and returns MB_ERR_TIMEOUT if it was
+ * set (the next sort then starts from a cleared look-back table), else MB_OK.
+ * Allocates nothing.
+ */
+mb_status mb_sort_plan_status(mb_sort_plan* p, void* cuda_stream);
+
+/*
+ * Diagnostic (no counterpart in the reference): makes one look-back wait of the
+ * plan's sort run out on purpose - a lone block takes the second tile of a pass
+ * whose first tile never publishes - with a wait limit of spin_limit polls
+ * (1 .. 2^20), so that the timeout path can be tested without a fault: the block
+ * gives up, sets the plan's error word and exits; mb_sort_plan_status then
+ * returns MB_ERR_TIMEOUT.  Synchronous.  Writes nothing the caller owns.
+ */
+mb_status mb_sort_plan_selftest_stall(mb_sort_plan* p, uint32_t spin_limit, void* cuda_stream);
+
+/*
  * Compacted segment table of sorted keys, the reference's segment assembly
  * (src/physics/assemble_segs.rs:314-430, assemble_segs.wgsl): each run of equal
  * keys in sorted_keys[0..n) is one segment, in slot order.  Device pointers:
@@ -232,6 +253,9 @@ mb_status mb_assemble_segments(mb_sort_plan* p, const uint32_t* sorted_keys, uin
 mb_status mb_sort_and_hash_static(const uint32_t* keys, const uint32_t* vals, uint32_t n,
                                   uint32_t number_of_cells, uint32_t* sorted_keys, uint32_t* sorted_vals,
                                   uint32_t* start, uint32_t* close, void* cuda_stream);
+/* mb_sort_plan_status for the fixed scratch of mb_sort_and_hash_static on the
+ * current device (MB_OK if no call ran there yet).  Allocates nothing. */
+mb_status mb_sort_static_status(void* cuda_stream);
 
 /* Per-world kernel choices (the autotuner's knobs). */
 typedef struct mb_tuning {

@@ -109,6 +109,47 @@ def test_sort_repeated_calls_and_sizes(cuda, plan):
         np.testing.assert_array_equal(perm, np.argsort(keys, kind="stable").astype(np.uint32))
 
 
+def test_sort_digit_split_changes_at_same_tile_count(cuda, plan):
+    """Same key count (same tile count) under cell counts whose digit schedules
+    differ (2^18 cells: 5 + 5 + 8 bits; 2^17: 5 + 4 + 8): a changed digit width
+    re-lays the look-back table, so words left by an older sort must not be read
+    as published ones."""
+    rng = np.random.default_rng(12)
+    n = 200_000
+    for cells in [1 << 18, 1 << 17, 1 << 17, 1 << 18, 1 << 17, 1 << 18, 1 << 18, 1 << 17, 1 << 18]:
+        keys = rng.integers(0, cells, n, dtype=np.uint64).astype(np.uint32)
+        sk, perm, start, close = run_stage(cuda, plan, keys, cells)
+        ref = np.argsort(keys, kind="stable").astype(np.uint32)
+        np.testing.assert_array_equal(perm, ref, err_msg=f"cells {cells}")
+        np.testing.assert_array_equal(sk, keys[ref])
+        rs, rc = oracle.spatial_hash(keys[ref], cells)
+        np.testing.assert_array_equal(start, rs)
+        np.testing.assert_array_equal(close, rc)
+    plan.status(cuda.current_stream().cuda_stream)  # no wait gave up
+
+
+def test_lookback_wait_runs_out_and_reports_timeout(cuda, plan, built_lib):
+    """A bounded look-back wait that runs out (a lone block whose predecessor tile
+    never publishes, 1000 polls) sets the plan's error word, which
+    mb_sort_plan_status reports as MB_ERR_TIMEOUT once; the plan keeps working."""
+    from bevy_millions_ball_gb300 import MbError
+
+    lib = built_lib
+    stream = cuda.current_stream().cuda_stream
+    plan.status(stream)
+    assert lib.mb_sort_plan_selftest_stall(plan._h, 1000, stream) == 0, lib.mb_last_error(None)
+    with pytest.raises(MbError) as e:
+        plan.status(stream)
+    assert e.value.status == 4 and "look-back" in str(e.value)
+    plan.status(stream)  # read once, then clear
+    rng = np.random.default_rng(13)
+    for n, cells in [(300_000, 1 << 20), (300_000, 1 << 20), (5000, 77)]:
+        keys = rng.integers(0, cells, n, dtype=np.uint64).astype(np.uint32)
+        sk, perm, start, close = run_stage(cuda, plan, keys, cells)
+        np.testing.assert_array_equal(perm, np.argsort(keys, kind="stable").astype(np.uint32))
+    plan.status(stream)
+
+
 def test_sort_with_values(cuda, plan):
     rng = np.random.default_rng(2)
     n, cells = 123_457, 5000

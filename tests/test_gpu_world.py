@@ -191,12 +191,6 @@ def test_degenerate_cells_heapsort(built_lib, cuda):
     run_pair(sc, 3, [1, 2, 3])
 
 
-def test_full_size_1m_frames_bit_exact(built_lib, cuda):
-    """1,048,576 spheres, N=1024: the benchmark workload, 3 frames against the oracle."""
-    sc = scenes.workload("P-1M")
-    run_pair(sc, 3, [1, 2, 3])
-
-
 def test_full_size_1m_properties(built_lib, cuda):
     """Size-independent properties after many frames at full size."""
     sc = scenes.workload("P-1M")

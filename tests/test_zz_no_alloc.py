@@ -59,6 +59,27 @@ def test_static_scratch_matches_planned_entry_point(built_lib, cuda):
         lib.mb_sort_plan_destroy(plan)
 
 
+def test_static_scratch_digit_split_changes(built_lib, cuda):
+    """The same key count under cell counts with different digit schedules
+    (2^18 cells: 5 + 5 + 8 bits; 2^17: 5 + 4 + 8), alternating: every call clears
+    the look-back words it uses, so none of an older call is misread."""
+    torch, lib = cuda, built_lib
+    plan = C.c_void_p()
+    assert lib.mb_sort_plan_create(1 << 18, 1 << 18, C.byref(plan)) == 0
+    rng = np.random.default_rng(77)
+    try:
+        for cells in [1 << 18, 1 << 17, 1 << 17, 1 << 18, 1 << 17, 1 << 18]:
+            keys = rng.integers(0, cells, 200_000, dtype=np.uint64).astype(np.uint32)
+            got = _run(torch, lib, lib.mb_sort_and_hash_static, keys, cells, None)
+            ref = _run(torch, lib, lib.mb_sort_and_hash, keys, cells, None, plan=plan)
+            for g, r, what in zip(got, ref, ["sorted keys", "sorted values", "start", "close"]):
+                np.testing.assert_array_equal(g, r, err_msg=f"{what}, cells {cells}")
+            np.testing.assert_array_equal(got[1], np.argsort(keys, kind="stable").astype(np.uint32))
+        assert lib.mb_sort_static_status(torch.cuda.current_stream().cuda_stream) == 0
+    finally:
+        lib.mb_sort_plan_destroy(plan)
+
+
 def test_static_scratch_rejects_sizes_beyond_its_limit(built_lib, cuda):
     lib = built_lib
     assert lib.mb_sort_and_hash_static(None, None, 262_145, 16, None, None, None, None, None) == 1
