@@ -1,8 +1,9 @@
 """Seeded synthetic scenes for the benchmark workloads (numpy PCG64).
 
-The reference's own default scene comes from ChaCha8 + rand 0.8 ``gen_range``
-(src/physics/mod.rs:172-212), a third-party generator not present here; these
-generators produce the workloads the benchmark names instead:
+The reference's own start-up scene (src/physics/mod.rs:172-212) is rebuilt by
+``reference_default`` with the reference's random stream (ChaCha8 seeded from
+0, rand 0.8's f32 ``gen_range``; see ``chacha``).  The benchmark workloads are
+seeded numpy PCG64 scenes:
 
 * ``plain_uniform``  — uniform positions, N(0, 1) m/s velocities (65,536 / 1,048,576 spheres)
 * ``plain_clustered`` — 16 Gaussian clusters, spring response (4,194,304 spheres)
@@ -122,10 +123,11 @@ def reference_default(plugin: PhysicsPlugin | None = None, seed: int = 0) -> Sce
     its default settings (16,384 spheres, N = 128, grid_size 8): a lattice of
     2^(L//2) x 2^(L - L//2) spheres (L = log2 n), x-major, 4 units apart, centred
     on the origin, at height 4, radius 1, mass 1, horizontal velocities (stored
-    as displacement per step, as the reference packs them) uniform in
-    [-0.8, 0.8) per axis, vertical 0.  The reference draws the velocities from
-    ChaCha8 (rand 0.8), which is not reproduced here: numpy's PCG64 draws the
-    same distribution, so the lattice is identical and the velocity stream is not."""
+    as displacement per step, as the reference packs them) from
+    ``ChaCha8Rng::seed_from_u64(seed)`` through rand 0.8's ``gen_range(-0.8..0.8)``
+    (x then z per sphere, mod.rs:198-205), vertical 0.  The stream restates the
+    crates' published algorithms (``chacha``); it is unpinned against a run of the
+    reference itself, which needs a Rust toolchain."""
     plugin = plugin or PhysicsPlugin()
     n = int(plugin.max_number_of_agents)
     if n <= 0 or n & (n - 1):
@@ -139,10 +141,9 @@ def reference_default(plugin: PhysicsPlugin | None = None, seed: int = 0) -> Sce
     pos[:, 1] = 4.0
     pos[:, 2] = np.tile(zs, cx)
     pos[:, 3] = 1.0
-    rng = np.random.default_rng(seed)
-    v = np.zeros((n, 3), np.float32)
-    v[:, 0] = rng.uniform(-0.8, 0.8, n).astype(np.float32)
-    v[:, 2] = rng.uniform(-0.8, 0.8, n).astype(np.float32)
+    from .chacha import reference_start_velocities
+
+    v = reference_start_velocities(n, seed)
     vfme = pack_vfme(v, np.zeros_like(v), 1.0)
     return Scene(plugin, pos, vfme, f"reference default lattice n={n}")
 

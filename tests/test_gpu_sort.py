@@ -125,7 +125,7 @@ def test_sort_digit_split_changes_at_same_tile_count(cuda, plan):
         rs, rc = oracle.spatial_hash(keys[ref], cells)
         np.testing.assert_array_equal(start, rs)
         np.testing.assert_array_equal(close, rc)
-    plan.status(cuda.current_stream().cuda_stream)  # no wait gave up
+    plan.status(cuda.cuda.current_stream().cuda_stream)  # no wait gave up
 
 
 def test_lookback_wait_runs_out_and_reports_timeout(cuda, plan, built_lib):
@@ -135,7 +135,7 @@ def test_lookback_wait_runs_out_and_reports_timeout(cuda, plan, built_lib):
     from bevy_millions_ball_gb300 import MbError
 
     lib = built_lib
-    stream = cuda.current_stream().cuda_stream
+    stream = cuda.cuda.current_stream().cuda_stream
     plan.status(stream)
     assert lib.mb_sort_plan_selftest_stall(plan._h, 1000, stream) == 0, lib.mb_last_error(None)
     with pytest.raises(MbError) as e:
