@@ -239,8 +239,11 @@ class World:
         return t
 
     def set_tuning(self, digit_bits_max: int | None = None, collide_block: int | None = None,
-                   sort_algorithm: int | None = None, frames_per_launch: int | None = None) -> None:
+                   sort_algorithm: int | None = None, frames_per_launch: int | None = None,
+                   state_gather: int | None = None) -> None:
         t = self.tuning
+        if state_gather is not None:
+            t.state_gather = state_gather
         if digit_bits_max is not None:
             t.digit_bits_max = digit_bits_max
         if collide_block is not None:

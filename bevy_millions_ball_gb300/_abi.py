@@ -59,10 +59,11 @@ class MbConsts(C.Structure):
 
 class MbTuning(C.Structure):
     _fields_ = [("digit_bits_max", u32), ("collide_block", u32), ("sort_algorithm", u32),
-                ("frames_per_launch", u32), ("reserved", u32 * 4)]
+                ("frames_per_launch", u32), ("state_gather", u32), ("reserved", u32 * 3)]
 
 
 MB_SORT_COUNTING, MB_SORT_ONESWEEP = 0, 1
+MB_GATHER_COPY, MB_GATHER_INDIRECT = 0, 1
 MB_TUNE_CANDIDATES = 12
 
 

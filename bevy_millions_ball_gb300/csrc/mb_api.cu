@@ -152,6 +152,8 @@ cudaError_t mark(mb_world* w, int i, cudaStream_t st, bool capturing) {
 }
 
 bool counting(const mb_world* w) { return w->tuning.sort_algorithm == MB_SORT_COUNTING; }
+// The physics pass reads the state through the permutation instead of a sorted copy.
+bool indirect(const mb_world* w) { return w->tuning.state_gather == MB_GATHER_INDIRECT; }
 
 // Enqueue one frame on `st`.  Profiling marks: [0] frame start, [1] after the
 // first ordering stage, [2] after the second, [3] after physics.  `chained`: the
@@ -176,7 +178,8 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         if ((e = mb::count_scan(w->cnt, w->scratch.ctl, w->cells, w->scratch.offs, st, pdl && chained))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
         if ((e = mb::count_scatter(w->cnt, w->keys, w->n, w->cells, w->scratch.offs, w->perm, w->pos[cur],
-                                   w->vfme[cur], w->spos, w->svfme, w->bands, w->P.N, st, pdl)))
+                                   w->vfme[cur], indirect(w) ? nullptr : w->spos, indirect(w) ? nullptr : w->svfme,
+                                   w->bands, w->P.N, st, pdl)))
             return e;
         hist = w->cnt.hist;
         coarse = w->cnt.coarse;
@@ -184,7 +187,8 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         if ((e = mb::sort_pairs(w->scratch, w->sched, w->keys, nullptr, w->sorted_keys, w->perm, st))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
         if ((e = mb::cell_offsets(w->scratch, w->sched, w->sorted_keys, st))) return e;
-        if (!init && (e = mb::gather_state(w->perm, w->n, w->pos[cur], w->vfme[cur], w->spos, w->svfme,
+        if (!init && (e = mb::gather_state(w->perm, w->n, w->pos[cur], w->vfme[cur],
+                                           indirect(w) ? nullptr : w->spos, indirect(w) ? nullptr : w->svfme,
                                            w->sorted_keys, w->scratch.offs, w->bands, w->P.N, st)))
             return e;
     }
@@ -194,10 +198,15 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         e = mb::launch_physics_init(w->P, w->n, w->perm, w->pos[cur], w->vfme[cur], w->pos[nxt],
                                     w->vfme[nxt], w->keys, hist, coarse, st);
         if (!e && hist) e = mb::count_tile_counts(w->cnt, w->cells, st);
-    } else
-        e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->spos, w->svfme, w->pos[nxt],
+    } else if (indirect(w)) {
+        e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->pos[cur], w->vfme[cur], w->perm,
+                                    w->pos[nxt], w->vfme[nxt], w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError,
+                                    st, pdl && counting(w));
+    } else {
+        e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->spos, w->svfme, nullptr, w->pos[nxt],
                                     w->vfme[nxt], w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError, st,
                                     pdl && counting(w));
+    }
     if (e) return e;
     return mark(w, 3, st, capturing);
 }
@@ -545,6 +554,8 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
     const uint32_t fpl = t->frames_per_launch;
     if (!(fpl == 0 || fpl == 1 || fpl == 2 || fpl == 4 || fpl == 8 || fpl == 16))
         return fail(w, MB_ERR_INVALID_ARG, "frames_per_launch must be 0, 1, 2, 4, 8 or 16");
+    if (t->state_gather != MB_GATHER_COPY && t->state_gather != MB_GATHER_INDIRECT)
+        return fail(w, MB_ERR_INVALID_ARG, "state_gather must be MB_GATHER_COPY or MB_GATHER_INDIRECT");
     drop_graphs(w);
     bool to_counting = t->sort_algorithm == MB_SORT_COUNTING && !counting(w);
     w->tuning = *t;

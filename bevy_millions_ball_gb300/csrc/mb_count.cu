@@ -158,7 +158,8 @@ __device__ __forceinline__ void mark_fix(uint32_t* __restrict__ fix_bits, uint32
     const uint32_t m = __ballot_sync(0xFFFFFFFFu, mark);
     if ((threadIdx.x & 31u) == 0u && i < n) fix_bits[i >> 5] = m;
 }
-// Also moves each sphere's state to its slot (sorted copy for the physics pass)
+// Also (spos != NULL) moves each sphere's state to its slot (a sorted copy for
+// the physics pass; without it the physics pass reads the state through perm)
 // and, where a slot begins or ends a physics tile, writes that side of the
 // tile's band table entry (the cell of a slot is final here; the fixup only
 // reorders slots inside a cell).
@@ -178,7 +179,7 @@ __global__ void __launch_bounds__(256)
         uint32_t k = valid ? __ldg(keys + i) : 0xFFFFFFFFu;
         float4 p;
         uint4 q;
-        if (valid) {
+        if (valid && spos) {
             p = __ldg(pos_in + i);
             q = __ldg(vfme_in + i);
         }
@@ -201,8 +202,10 @@ __global__ void __launch_bounds__(256)
             const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
             if (dst >= n) continue;  // only counts that disagree with the keys get here
             perm[dst] = i;
-            spos[dst] = p;
-            svfme[dst] = q;
+            if (spos) {
+                spos[dst] = p;
+                svfme[dst] = q;
+            }
             if (bands && !ident) write_band_bounds(bands, offs, N, n, dst, k);
         }
     }
@@ -307,9 +310,9 @@ __global__ void __launch_bounds__(kCollectThreads)
 
 // ---------------------------------------------------------------- fixup
 // The listed cells (see k_fix_collect) get their slots back in ascending input order
-// and re-gather their sorted state copy from the state source: one buffer (a
-// world), or each scene's current buffer (a batch, where cells and coarse tiles
-// of HOLD scenes are left alone).  Cells of up to kFixSmall slots: a thread
+// and (spos != NULL) re-gather their sorted state copy from the state source: one
+// buffer (a world), or each scene's current buffer (a batch, where cells and
+// coarse tiles of HOLD scenes are left alone).  Cells of up to kFixSmall slots: a thread
 // each (sorting network in registers); up to kFixWarp: a warp each (bitonic sort
 // in registers and shuffles); larger: a block each (bitmap of the input indices,
 // chunk by chunk of their range, read back in order).
@@ -420,14 +423,6 @@ __device__ __forceinline__ void warp_bitonic(uint32_t (&v)[kFixWarp / 32], uint3
 }
 
 template <class Src>
-__device__ __forceinline__ void regather(const Src& src, const uint32_t* perm, uint32_t lo, uint32_t j,
-                                         float4* __restrict__ spos, uint4* __restrict__ svfme) {
-    const uint32_t o = perm[lo + j];
-    spos[lo + j] = src.pos(o);
-    svfme[lo + j] = src.vfme(o);
-}
-
-template <class Src>
 __global__ void __launch_bounds__(kFixThreads)
     k_cell_fix(const uint32_t* __restrict__ offs, uint32_t* perm, uint32_t* __restrict__ hist, uint32_t cells,
                uint32_t* __restrict__ coarse, uint32_t tiles,
@@ -479,8 +474,10 @@ __global__ void __launch_bounds__(kFixThreads)
         for (uint32_t k = 0; k < kFixSmall; ++k) {
             if (k < m) {
                 perm[lo + k] = v[k];
-                spos[lo + k] = src.pos(v[k]);
-                svfme[lo + k] = src.vfme(v[k]);
+                if (spos) {
+                    spos[lo + k] = src.pos(v[k]);
+                    svfme[lo + k] = src.vfme(v[k]);
+                }
             }
         }
     }
@@ -520,8 +517,10 @@ __global__ void __launch_bounds__(kFixThreads)
             const uint32_t e = 32u * s + lane;
             if (e < m) {
                 perm[lo + e] = v[s];
-                spos[lo + e] = src.pos(v[s]);
-                svfme[lo + e] = src.vfme(v[s]);
+                if (spos) {
+                    spos[lo + e] = src.pos(v[s]);
+                    svfme[lo + e] = src.vfme(v[s]);
+                }
             }
         }
     }
@@ -575,8 +574,10 @@ __global__ void __launch_bounds__(kFixThreads)
                     for (uint32_t q = 0; q < 4; ++q) {
                         if (q < got) {
                             perm[at + q] = vv[q];
-                            spos[at + q] = src.pos(vv[q]);
-                            svfme[at + q] = src.vfme(vv[q]);
+                            if (spos) {
+                                spos[at + q] = src.pos(vv[q]);
+                                svfme[at + q] = src.vfme(vv[q]);
+                            }
                         }
                     }
                     at += got;

@@ -200,12 +200,14 @@ cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t*
                                 const float4* pos_in, const uint4* vfme_in, float4* pos_out,
                                 uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse,
                                 cudaStream_t st);
-// LOOP pass over the state in sorted order (spos/svfme, slot j = sorted slot j).
-// `bands` is the band table the sort wrote for this order.
+// LOOP pass.  perm == NULL: spos/svfme hold the state in sorted order (slot j =
+// sorted slot j, a copy the sort wrote); otherwise they hold it in the previous
+// frame's slot order and sorted slot j is spos[perm[j]].  `bands` is the band
+// table the sort wrote for this order.
 // `pdl`: launched as a programmatic dependent of the kernel before it.
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
-                                const float4* spos, const uint4* svfme, float4* pos_out, uint4* vfme_out,
-                                uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
+                                const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
+                                uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
                                 cudaStream_t st, bool pdl = false);
 // Compares the physics pass's division (div_exact) with IEEE division over
 // `count` generated cases on the current device (synchronous).
@@ -274,9 +276,9 @@ cudaError_t count_tile_counts_scenes(CountScratch& s, const SceneDev* scenes, co
 cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32_t* offs, uint32_t* perm,
                              cudaStream_t st);
 // perm := stable permutation sorting keys by cell, from the offsets of count_scan
-// and the counts in hist (counted back down to 0); spos/svfme := the state in that
-// order (spos[j] = pos_in[perm[j]]); bands (nullable) := the band table of that
-// order for an N x N grid; coarse := 0.
+// and the counts in hist (counted back down to 0); spos/svfme (nullable
+// together) := the state in that order (spos[j] = pos_in[perm[j]]); bands
+// (nullable) := the band table of that order for an N x N grid; coarse := 0.
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
                           float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,

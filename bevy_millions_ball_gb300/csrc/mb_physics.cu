@@ -250,6 +250,7 @@ constexpr int kTileThreads = kPhysicsTile;
 constexpr uint32_t kBandCap = 2 * kTileThreads;
 constexpr uint32_t kBandPad = 8;  // >= the widest look-ahead of the contact walk, minus one
 constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier wait (error flag on expiry)
+constexpr uint32_t kGatherUnroll = 2;      // band entries a thread gathers per step (loads in flight)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -306,16 +307,20 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 // is left to the exact test.  Slots past the row's end inside a step are read
 // but masked out: `bpos` must stay readable kLook - 1 slots past every row
 // (the shared bands are padded; global reads are clamped).
+//
+// kIndirect (global reads only): `bpos`/`bvfme` hold the state in the previous
+// frame's slot order and sorted slot j is read at perm[j] (clamped to nmax).
 __device__ __forceinline__ uint32_t cand_slot(uint32_t t, const uint32_t (&o)[3], uint32_t c0, uint32_t c01) {
     return t + (t < c0 ? o[0] : (t < c01 ? o[1] : o[2]));
 }
 
 constexpr float kNearScale = 1.0014989f;  // about sqrt(1.003): squared, a 0.3% margin on edge^2
 
-template <bool kShared, uint32_t kLook>
+template <bool kShared, uint32_t kLook, bool kIndirect>
 __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
-                                             uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself) {
+                                             uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself,
+                                             const uint32_t* __restrict__ perm, uint32_t nmax) {
     const float sk = a.scale * kNearScale;
     uint32_t t = 0;
     while (t < T) {
@@ -324,7 +329,14 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
         const uint32_t rem = (r0 ? c0 : (r01 ? c01 : T)) - t;  // candidates left in this row, >= 1
         float4 bp[kLook];
 #pragma unroll
-        for (uint32_t q = 0; q < kLook; ++q) bp[q] = kShared ? bpos[j0 + q] : __ldg(bpos + j0 + min(q, rem - 1u));
+        for (uint32_t q = 0; q < kLook; ++q) {
+            if (kShared) {
+                bp[q] = bpos[j0 + q];
+            } else {
+                const uint32_t j = j0 + min(q, rem - 1u);
+                bp[q] = __ldg(bpos + (kIndirect ? min(__ldg(perm + j), nmax) : j));
+            }
+        }
         uint32_t m = 0;
 #pragma unroll
         for (uint32_t q = 0; q < kLook; ++q) {
@@ -339,7 +351,12 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
             const uint32_t q = (uint32_t)(__ffs(m) - 1);
             t += q + 1u;
             const uint32_t j = j0 + q;
-            sphere(P, a, unpack(kShared ? bpos[j] : __ldg(bpos + j), kShared ? bvfme[j] : __ldg(bvfme + j)));
+            if (kShared) {
+                sphere(P, a, unpack(bpos[j], bvfme[j]));
+            } else {
+                const uint32_t sj = kIndirect ? min(__ldg(perm + j), nmax) : j;
+                sphere(P, a, unpack(__ldg(bpos + sj), __ldg(bvfme + sj)));
+            }
         } else {
             t += min(rem, kLook);
         }
@@ -351,14 +368,15 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
 // so its lanes run one loop.
 constexpr uint32_t kCrowdedT = 48, kLookSparse = 4, kLookCrowded = 6;
 
-template <bool kShared>
+template <bool kShared, bool kIndirect>
 __device__ __forceinline__ void contact_loop(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
-                                             uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself) {
+                                             uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself,
+                                             const uint32_t* __restrict__ perm, uint32_t nmax) {
     if (__any_sync(__activemask(), T >= kCrowdedT))
-        contact_walk<kShared, kLookCrowded>(P, a, bpos, bvfme, o, c0, c01, T, tself);
+        contact_walk<kShared, kLookCrowded, kIndirect>(P, a, bpos, bvfme, o, c0, c01, T, tself, perm, nmax);
     else
-        contact_walk<kShared, kLookSparse>(P, a, bpos, bvfme, o, c0, c01, T, tself);
+        contact_walk<kShared, kLookSparse, kIndirect>(P, a, bpos, bvfme, o, c0, c01, T, tself, perm, nmax);
 }
 
 // Slot ranges of the three candidate rows of a sphere in cell (cx, cz), key =
@@ -385,12 +403,15 @@ __device__ __forceinline__ void row_bounds(uint32_t N, const uint32_t* __restric
 // clamp, pack, store, new key and its counts.  The bands of its tile are staged
 // in b_pos/b_vfme ([3][kBandCap]: band 0 row below, 1 own row, 2 row above; band
 // b holds slots [b_lo[b], b_lo[b] + b_cnt[b])); rows outside them are read from
-// spos/svfme.  base_a / base_c: the scene's first slot and cell (0 for a world).
+// spos/svfme (through perm when kIndirect).  base_a / base_c: the scene's first
+// slot and cell (0 for a world).
+template <bool kIndirect>
 __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32_t i, uint32_t n, uint32_t base_a,
                                             uint32_t base_c, const uint32_t (&lo)[3], const uint32_t (&hi)[3],
                                             const float4* b_pos, const uint4* b_vfme, const uint32_t* b_lo,
                                             const uint32_t* b_cnt, const float4* __restrict__ spos,
-                                            const uint4* __restrict__ svfme, float4* __restrict__ pos_out,
+                                            const uint4* __restrict__ svfme, const uint32_t* __restrict__ perm,
+                                            float4* __restrict__ pos_out,
                                             uint4* __restrict__ vfme_out, uint32_t* __restrict__ keys_out,
                                             uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse) {
     // candidate rows in the reference's order: own row (band 1), below (0), above (2)
@@ -425,9 +446,9 @@ __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32
     // handle_collisions (physics.wgsl:119-169)
     V3 old_pos = a.position;
     if (shared)
-        contact_loop<true>(P, a, b_pos, b_vfme, o_s, c[0], c01, T, tself);
+        contact_loop<true, false>(P, a, b_pos, b_vfme, o_s, c[0], c01, T, tself, perm, n - 1u);
     else
-        contact_loop<false>(P, a, spos, svfme, o_g, c[0], c01, T, tself);
+        contact_loop<false, kIndirect>(P, a, spos, svfme, o_g, c[0], c01, T, tself, perm, n - 1u);
     V3 diff = a.position - old_pos;
     if (longer_than(diff, a.scale)) {
         // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337); the
@@ -472,8 +493,13 @@ __device__ __forceinline__ uint32_t scene_of(const SceneDev* __restrict__ scenes
 }
 
 // main (physics.wgsl:57-97) for one tile of kTileThreads consecutive sorted
-// slots, one thread per slot.  spos/svfme hold the state in sorted order
-// (agent_new(agent_index_sorted[i]) of the reference is spos[i]).
+// slots, one thread per slot.  agent_new(agent_index_sorted[i]) of the reference
+// is the state of sorted slot i:
+//   kIndirect = false: spos/svfme hold the state in sorted order (the sort wrote
+//     a copy), slot i is spos[i]; bands are copied with TMA bulk copies;
+//   kIndirect = true: spos/svfme hold the state in the previous frame's slot
+//     order and slot i is spos[perm[i]]; bands are gathered through perm by the
+//     block's threads (the sort writes no state copy).
 //
 // kBatched = false: one scene, parameters P, LOOP pipeline.
 // kBatched = true: many scenes in one flattened key space (scene s owns slots
@@ -481,14 +507,16 @@ __device__ __forceinline__ uint32_t scene_of(const SceneDev* __restrict__ scenes
 // its scene's mode: LOOP, INIT (re-pack, emit key) or HOLD (state carried over
 // unchanged, key re-emitted).  Slot indices inside a scene (the jitter hash)
 // are local, so every scene evolves exactly as it would alone.
-template <bool kBatched>
+template <bool kBatched, bool kIndirect>
 __global__ void __launch_bounds__(kTileThreads)
     k_physics_frame(const __grid_constant__ PhysParams P1, const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
                     uint32_t n, const uint32_t* __restrict__ offs, const uint4* __restrict__ bands,
                     const float4* __restrict__ spos,
-                    const uint4* __restrict__ svfme, float4* __restrict__ pos_out0, float4* __restrict__ pos_out1,
+                    const uint4* __restrict__ svfme, const uint32_t* __restrict__ perm, float4* __restrict__ pos_out0,
+                    float4* __restrict__ pos_out1,
                     uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1, uint32_t* __restrict__ keys_out,
                     uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse, uint32_t* __restrict__ err) {
+    static_assert(!(kBatched && kIndirect), "batches stage a sorted copy");
     __shared__ __align__(16) float4 s_pos[3 * kBandCap + kBandPad];  // padded: the walk reads past rows
     __shared__ __align__(16) uint4 s_vfme[3][kBandCap];
     __shared__ __align__(8) uint64_t s_bar;
@@ -517,7 +545,7 @@ __global__ void __launch_bounds__(kTileThreads)
     }
 
     const PhysParams& P = kBatched ? scenes[sc].P : P1;  // read where it lives, not copied
-    if (tid == 0) mbar_init(&s_bar, 1u);
+    if (!kIndirect && tid == 0) mbar_init(&s_bar, 1u);
     if (bands) {  // bounds from the band table: one load (a batch: tiles inside one LOOP scene)
         if (tid == 0) {
             bool stage = true;
@@ -542,7 +570,7 @@ __global__ void __launch_bounds__(kTileThreads)
             }
         }
     }
-    griddep_wait();  // the sort's outputs (the sorted state copy) are complete and visible
+    griddep_wait();  // the sort's outputs (order, state copy) are complete and visible
     if (!bands && tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
         uint32_t lo = 0, hi = 0;
         bool stage = true;
@@ -557,7 +585,9 @@ __global__ void __launch_bounds__(kTileThreads)
         }
         if (stage) {
             const uint32_t N = Q.N;
-            const uint32_t kf = key_of(Q, __ldg(spos + i0)), kl = key_of(Q, __ldg(spos + ilast));
+            const uint32_t sf0 = kIndirect ? min(__ldg(perm + i0), n - 1u) : i0;
+            const uint32_t sl0 = kIndirect ? min(__ldg(perm + ilast), n - 1u) : ilast;
+            const uint32_t kf = key_of(Q, __ldg(spos + sf0)), kl = key_of(Q, __ldg(spos + sl0));
             const uint32_t cxf = kf - (kf / N) * N, cxl = kl - (kl / N) * N;
             const uint32_t* of = offs + qc;
             if (tid == 1) {  // own row
@@ -585,16 +615,48 @@ __global__ void __launch_bounds__(kTileThreads)
         s_cnt[tid] = (hi > lo && hi - lo <= kBandCap) ? hi - lo : 0u;
     }
 
-    // own sphere: loads issued here overlap the band set-up; the copies start
-    // after the barrier (mbarrier initialised and bounds published by then)
+    // own sphere: loads issued here overlap the band set-up
     float4 own_p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     uint4 own_q = make_uint4(0u, 0u, 0u, 0u);
     if (valid) {
-        own_p = __ldg(spos + i);
-        own_q = __ldg(svfme + i);
+        const uint32_t o = kIndirect ? min(__ldg(perm + i), n - 1u) : i;
+        own_p = __ldg(spos + o);
+        own_q = __ldg(svfme + o);
     }
-    __syncthreads();
-    if (tid == 0) {
+    __syncthreads();  // band bounds published (and, copy mode, the mbarrier initialised)
+    if (kIndirect) {
+        // gather the bands through perm: every thread takes entries tid, tid + 128,
+        // ... of the three bands laid end to end, kGatherUnroll at a time (loads
+        // first, then stores)
+        const uint32_t c0 = s_cnt[0], c01 = c0 + s_cnt[1], tot = c01 + s_cnt[2];
+        for (uint32_t f0 = 0; f0 < tot; f0 += kGatherUnroll * kTileThreads) {
+            uint32_t dst[kGatherUnroll], src[kGatherUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kGatherUnroll; ++u) {
+                const uint32_t f = f0 + u * kTileThreads + tid;
+                const uint32_t b = f < c0 ? 0u : (f < c01 ? 1u : 2u);
+                const uint32_t j = f - (b == 0u ? 0u : (b == 1u ? c0 : c01));
+                dst[u] = b * kBandCap + j;
+                src[u] = f < tot ? min(__ldg(perm + s_lo[b] + j), n - 1u) : 0u;
+            }
+            float4 gp[kGatherUnroll];
+            uint4 gq[kGatherUnroll];
+#pragma unroll
+            for (uint32_t u = 0; u < kGatherUnroll; ++u) {
+                if (f0 + u * kTileThreads + tid < tot) {
+                    gp[u] = __ldg(spos + src[u]);
+                    gq[u] = __ldg(svfme + src[u]);
+                }
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < kGatherUnroll; ++u) {
+                if (f0 + u * kTileThreads + tid < tot) {
+                    s_pos[dst[u]] = gp[u];
+                    (&s_vfme[0][0])[dst[u]] = gq[u];
+                }
+            }
+        }
+    } else if (tid == 0) {
         uint32_t bytes = 0;
 #pragma unroll
         for (int b = 0; b < 3; ++b) bytes += s_cnt[b] * 32u;
@@ -619,7 +681,9 @@ __global__ void __launch_bounds__(kTileThreads)
         key = cz * N + cx;
         if (mode == kModeLoop) row_bounds(N, offs + base_c, key, cx, cz, lo, hi);
     }
-    {  // bounded wait for the bands (every thread, so all copies land before exit)
+    if (kIndirect) {
+        __syncthreads();  // bands gathered
+    } else {  // bounded wait for the bands (every thread, so all copies land before exit)
         uint32_t spins = 0;
         while (!mbar_try_wait(&s_bar, 0u)) {
             if (++spins > kWaitLimit) {
@@ -639,8 +703,8 @@ __global__ void __launch_bounds__(kTileThreads)
     }
     if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
 
-    step_sphere(P, a, i, n, base_a, base_c, lo, hi, s_pos, &s_vfme[0][0], s_lo, s_cnt, spos, svfme, pos_out,
-                vfme_out, keys_out, hist, coarse);
+    step_sphere<kIndirect>(P, a, i, n, base_a, base_c, lo, hi, s_pos, &s_vfme[0][0], s_lo, s_cnt, spos, svfme,
+                           perm, pos_out, vfme_out, keys_out, hist, coarse);
 }
 
 // Self-test of div_exact against IEEE division over count generated cases:
@@ -748,13 +812,18 @@ cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t*
 }
 
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
-                                const float4* spos, const uint4* svfme, float4* pos_out, uint4* vfme_out,
-                                uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
+                                const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
+                                uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
                                 cudaStream_t st, bool pdl) {
     if (!n) return cudaSuccess;
-    return launch_pdl(pdl, k_physics_frame<false>, dim3((n + kTileThreads - 1u) / kTileThreads), dim3(kTileThreads),
-                      0, st, p, (const SceneDev*)nullptr, (const uint32_t*)nullptr, n, offs, bands, spos, svfme,
-                      pos_out, (float4*)nullptr, vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
+    const dim3 grid((n + kTileThreads - 1u) / kTileThreads), block(kTileThreads);
+    if (perm)
+        return launch_pdl(pdl, k_physics_frame<false, true>, grid, block, 0, st, p, (const SceneDev*)nullptr,
+                          (const uint32_t*)nullptr, n, offs, bands, spos, svfme, perm, pos_out, (float4*)nullptr,
+                          vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
+    return launch_pdl(pdl, k_physics_frame<false, false>, grid, block, 0, st, p, (const SceneDev*)nullptr,
+                      (const uint32_t*)nullptr, n, offs, bands, spos, svfme, (const uint32_t*)nullptr, pos_out,
+                      (float4*)nullptr, vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
 }
 
 cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
@@ -763,9 +832,9 @@ cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_sc
                                  uint32_t* keys, uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st) {
     if (!n) return cudaSuccess;
     PhysParams unused{};
-    k_physics_frame<true><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
-        unused, scenes, tile_scene, n, offs, bands, spos, svfme, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, keys, hist,
-        coarse, err);
+    k_physics_frame<true, false><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
+        unused, scenes, tile_scene, n, offs, bands, spos, svfme, nullptr, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1,
+        keys, hist, coarse, err);
     return cudaGetLastError();
 }
 

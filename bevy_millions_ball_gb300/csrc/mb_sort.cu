@@ -449,9 +449,11 @@ __global__ void __launch_bounds__(256)
                    uint4* __restrict__ bands, uint32_t N) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t o = min(__ldg(perm + i), n - 1u);
-    spos[i] = __ldg(pos_in + o);
-    svfme[i] = __ldg(vfme_in + o);
+    if (spos) {  // the sorted state copy (none when the physics pass reads through perm)
+        const uint32_t o = min(__ldg(perm + i), n - 1u);
+        spos[i] = __ldg(pos_in + o);
+        svfme[i] = __ldg(vfme_in + o);
+    }
     if (bands) write_band_bounds(bands, offs, N, n, i, __ldg(sorted_keys + i));
 }
 

@@ -264,8 +264,19 @@ typedef struct mb_tuning {
     uint32_t sort_algorithm;   /* MB_SORT_COUNTING (default) or MB_SORT_ONESWEEP */
     uint32_t frames_per_launch; /* LOOP frames captured per graph launch in multi-frame steps:
                                    1, 2, 4, 8 (default; 0 reads as 8) or 16 */
-    uint32_t reserved[4];
+    uint32_t state_gather;     /* MB_GATHER_COPY or MB_GATHER_INDIRECT (below) */
+    uint32_t reserved[3];
 } mb_tuning;
+
+/* How the physics pass reads the state in this frame's sorted order:
+ *   MB_GATHER_COPY:     the sort writes a sorted copy of the state (32 B per
+ *                       sphere); the physics pass copies its tile's neighbour
+ *                       bands from it with bulk copies;
+ *   MB_GATHER_INDIRECT: the sort writes only the permutation; the physics pass
+ *                       gathers its bands (and its own spheres) through it.
+ * Both give identical results. */
+#define MB_GATHER_COPY 0u
+#define MB_GATHER_INDIRECT 1u
 
 /* Frame sort: both produce the identical stable permutation and cell ranges.
  *   MB_SORT_COUNTING: per-cell counts (emitted by the previous physics pass) ->

@@ -56,8 +56,10 @@ def test_world_matches_golden_fixtures(built_lib, cuda, name):
             np.testing.assert_array_equal(dbg["start"], d[f"f{f}_start"])
 
 
-def run_pair(scene, frames, checkpoints, world_kw=None):
+def run_pair(scene, frames, checkpoints, world_kw=None, tuning=None):
     with World(scene.plugin, **(world_kw or {})) as w:
+        if tuning:
+            w.set_tuning(**tuning)
         ow = oracle.OracleWorld(scene.plugin.to_c())
         w.set_state(scene.pos_scale, scene.vfme)
         ow.set_state(scene.pos_scale, scene.vfme)
@@ -189,6 +191,53 @@ def test_degenerate_cells_heapsort(built_lib, cuda):
     indices, cells over 256 slots) and bands too wide to stage (global reads)."""
     sc = scenes.plain_uniform(36_000, 2, grid_size=4, half_map_height=8, seed=32)
     run_pair(sc, 3, [1, 2, 3])
+
+
+INDIRECT = {"state_gather": 1}
+
+
+@pytest.mark.parametrize("case", ["small", "clustered", "crowded", "degenerate", "mixed", "sparse"])
+def test_indirect_state_gather(built_lib, cuda, case):
+    """MB_GATHER_INDIRECT: the sort writes only the permutation and the physics
+    pass gathers its bands and spheres through it (staged bands, and the global
+    reads of bands too wide to stage); bit-exact like the sorted-copy mode."""
+    if case == "small":
+        run_pair(scenes.workload("P-small"), 101, [1, 2, 11, 50, 101], tuning=INDIRECT)
+    elif case == "clustered":
+        run_pair(scenes.plain_clustered(262_144, 512, clusters=4, sigma_xz=16.0, seed=9), 40, [1, 2, 11, 40],
+                 tuning=INDIRECT)
+    elif case == "crowded":
+        run_pair(scenes.plain_uniform(51_200, 16, grid_size=1, half_map_height=8, seed=31), 4, [1, 2, 4],
+                 tuning=INDIRECT)
+    elif case == "degenerate":
+        run_pair(scenes.plain_uniform(36_000, 2, grid_size=4, half_map_height=8, seed=32), 3, [1, 2, 3],
+                 tuning=INDIRECT)
+    elif case == "mixed":
+        sc = scenes.plain_uniform(40_000, 128, half_map_height=4, seed=31, spring=True)
+        rng = np.random.default_rng(33)
+        from bevy_millions_ball_gb300 import unpack_vfme
+        v, f, _ = unpack_vfme(sc.vfme)
+        sc.vfme = pack_vfme(v, f, rng.choice(np.array([0.5, 1.0, 1.5, 2.0, 0.7], np.float32), sc.n))
+        sc.pos_scale[:, 3] = rng.choice(np.array([0.3, 0.45, 0.5, 0.6], np.float32), sc.n)
+        run_pair(sc, 30, [1, 2, 11, 30], tuning=INDIRECT)
+    else:
+        run_pair(scenes.plain_uniform(5_000, 512, seed=13), 25, [1, 2, 11, 25], tuning=INDIRECT)
+
+
+def test_indirect_with_onesweep_and_switches(built_lib, cuda):
+    """The gather mode with the onesweep sort, and switched mid-run both ways."""
+    sc = scenes.plain_clustered(120_000, 256, clusters=3, sigma_xz=12.0, seed=18)
+    with World(sc.plugin) as w:
+        ow = oracle.OracleWorld(sc.plugin.to_c())
+        w.set_state(sc.pos_scale, sc.vfme)
+        ow.set_state(sc.pos_scale, sc.vfme)
+        for alg, gather, k in [(1, 1, 3), (0, 1, 4), (0, 0, 2), (1, 0, 2), (0, 1, 5)]:
+            w.set_tuning(sort_algorithm=alg, state_gather=gather)
+            w.step(k)
+            ow.step(k)
+            compare(w, ow, ow.time)
+        with pytest.raises(MbError):
+            w.set_tuning(state_gather=2)
 
 
 def test_full_size_1m_properties(built_lib, cuda):
