@@ -240,10 +240,12 @@ class World:
 
     def set_tuning(self, digit_bits_max: int | None = None, collide_block: int | None = None,
                    sort_algorithm: int | None = None, frames_per_launch: int | None = None,
-                   state_gather: int | None = None) -> None:
+                   state_gather: int | None = None, frame_kernel: int | None = None) -> None:
         t = self.tuning
         if state_gather is not None:
             t.state_gather = state_gather
+        if frame_kernel is not None:
+            t.frame_kernel = frame_kernel
         if digit_bits_max is not None:
             t.digit_bits_max = digit_bits_max
         if collide_block is not None:
@@ -262,7 +264,8 @@ class World:
         tried = (MbTuning * _abi.MB_TUNE_CANDIDATES)()
         self._check(self._lib.mb_autotune(self._h, frames, C.byref(best), ms, tried))
         desc = lambda t: {"sort_algorithm": t.sort_algorithm, "digit_bits_max": t.digit_bits_max,
-                          "frames_per_launch": t.frames_per_launch}
+                          "frames_per_launch": t.frames_per_launch, "state_gather": t.state_gather,
+                          "frame_kernel": t.frame_kernel}
         return {"best": desc(best), "candidates": [dict(desc(t), ms_per_frame=float(m)) for t, m in zip(tried, ms)]}
 
     # -- state

@@ -37,7 +37,7 @@ UNITS = {
     "mb_batch.cu": [],
     "mb_physics.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
 }
-HEADERS = [CSRC / "mb_internal.h", ROOT / "include" / "millionsball.h"]
+HEADERS = [CSRC / "mb_internal.h", CSRC / "mb_count_dev.cuh", ROOT / "include" / "millionsball.h"]
 
 
 def nvcc() -> str:

@@ -63,6 +63,7 @@ struct mb_world {
     uint32_t* sorted_keys = nullptr;
     uint4* bands = nullptr;            // band table of the sorted order (written by the sort)
     uint32_t* perm = nullptr;
+    uint32_t* fused_bar = nullptr;     // grid barrier words of the fused frame kernel (2, zero between launches)
     mb::SortScratch scratch;      // onesweep sort scratch + the cell offsets (offs)
     mb::CountScratch cnt;         // counting-sort scratch (per-cell and per-tile counts, fixup lists)
     mb::SortSchedule sched;
@@ -154,6 +155,34 @@ cudaError_t mark(mb_world* w, int i, cudaStream_t st, bool capturing) {
 bool counting(const mb_world* w) { return w->tuning.sort_algorithm == MB_SORT_COUNTING; }
 // The physics pass reads the state through the permutation instead of a sorted copy.
 bool indirect(const mb_world* w) { return w->tuning.state_gather == MB_GATHER_INDIRECT; }
+// LOOP frames run as one cooperative kernel per step (profiling needs the
+// per-stage kernels, so it falls back to them).
+bool fused(const mb_world* w) { return w->tuning.frame_kernel == MB_FRAME_FUSED && !w->profiling; }
+constexpr uint32_t kFusedFramesPerLaunch = 256;
+
+cudaError_t enqueue_fused(mb_world* w, uint32_t frames) {
+    mb::FusedFrame f;
+    f.P = w->P;
+    f.n = w->n;
+    f.cells = w->cells;
+    f.frames = frames;
+    f.cur = (uint32_t)w->cur;
+    f.indirect = indirect(w);
+    f.keys = w->keys;
+    f.offs = w->scratch.offs;
+    f.perm = w->perm;
+    f.bands = w->bands;
+    f.cnt = &w->cnt;
+    for (int b = 0; b < 2; ++b) {
+        f.pos[b] = w->pos[b];
+        f.vfme[b] = w->vfme[b];
+    }
+    f.spos = w->spos;
+    f.svfme = w->svfme;
+    f.bar = w->fused_bar;
+    f.err = w->scratch.ctl + mb::kCtlError;
+    return mb::launch_frame_fused(f, w->stream);
+}
 
 // Enqueue one frame on `st`.  Profiling marks: [0] frame start, [1] after the
 // first ordering stage, [2] after the second, [3] after physics.  `chained`: the
@@ -319,6 +348,8 @@ mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out) {
         if ((e = cudaMalloc(&w->sorted_keys, sizeof(uint32_t) * n))) return e;
         if ((e = cudaMalloc(&w->bands, sizeof(uint4) * mb::band_table_entries(n)))) return e;
         if ((e = cudaMalloc(&w->perm, sizeof(uint32_t) * n))) return e;
+        if ((e = cudaMalloc(&w->fused_bar, sizeof(uint32_t) * 2u))) return e;
+        if ((e = cudaMemset(w->fused_bar, 0, sizeof(uint32_t) * 2u))) return e;
         if ((e = mb::scratch_alloc(w->scratch, w->n, w->cells))) return e;
         return mb::count_scratch_alloc(w->cnt, w->cells, w->n);
     };
@@ -349,6 +380,7 @@ mb_status mb_destroy(mb_world* w) {
     cudaFree(w->img);
     cudaFree(w->img_h);
     cudaFree(w->perm);
+    cudaFree(w->fused_bar);
     mb::scratch_free(w->scratch);
     mb::count_scratch_free(w->cnt);
     if (w->cap_stream) cudaStreamDestroy(w->cap_stream);
@@ -452,6 +484,14 @@ mb_status mb_step(mb_world* w, uint32_t k) {
     for (uint32_t f = 0; f < k;) {
         if (w->time == 0) {
             if ((e = enqueue_frame(w, w->stream, w->cur, true))) return cuda_fail(w, "mb_step(init)", e);
+        } else if (fused(w)) {  // the remaining LOOP frames, one cooperative launch per 256
+            const uint32_t fr = std::min(k - f, kFusedFramesPerLaunch);
+            if ((e = enqueue_fused(w, fr))) return cuda_fail(w, "mb_step(fused)", e);
+            f += fr;
+            w->time += fr;
+            w->cur ^= (int)(fr & 1u);
+            w->frame_done = true;
+            continue;
         } else if (chain_frames(w) > 1u && k - f >= chain_frames(w) && !w->profiling) {
             // a chain of LOOP frames, one launch
             const uint32_t cf = chain_frames(w);
@@ -483,12 +523,13 @@ mb_status mb_sync(mb_world* w) {
         return cuda_fail(w, "mb_sync", e);
     if (flag) {
         cudaMemset(w->scratch.ctl + mb::kCtlError, 0, sizeof(uint32_t));
+        cudaMemset(w->fused_bar, 0, sizeof(uint32_t) * 2u);  // a barrier that gave up leaves its count
         w->scratch.last_tiles = 0;  // force a clean look-back table next sort
         drop_graphs(w);
-        char msg[160];
+        char msg[192];
         std::snprintf(msg, sizeof msg,
-                      "a bounded device-side wait gave up (flags 0x%x: 1 sort look-back, 4 band copy); "
-                      "results since the last sync are invalid",
+                      "a bounded device-side wait gave up (flags 0x%x: 1 sort look-back, 4 band copy, 8 grid "
+                      "barrier of the fused frame); results since the last sync are invalid",
                       flag);
         return fail(w, MB_ERR_TIMEOUT, msg);
     }
@@ -556,6 +597,12 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
         return fail(w, MB_ERR_INVALID_ARG, "frames_per_launch must be 0, 1, 2, 4, 8 or 16");
     if (t->state_gather != MB_GATHER_COPY && t->state_gather != MB_GATHER_INDIRECT)
         return fail(w, MB_ERR_INVALID_ARG, "state_gather must be MB_GATHER_COPY or MB_GATHER_INDIRECT");
+    if (t->frame_kernel != MB_FRAME_GRAPH && t->frame_kernel != MB_FRAME_FUSED)
+        return fail(w, MB_ERR_INVALID_ARG, "frame_kernel must be MB_FRAME_GRAPH or MB_FRAME_FUSED");
+    if (t->frame_kernel == MB_FRAME_FUSED && t->sort_algorithm != MB_SORT_COUNTING)
+        return fail(w, MB_ERR_INVALID_ARG, "MB_FRAME_FUSED runs the counting sort (sort_algorithm 0)");
+    if (t->frame_kernel == MB_FRAME_FUSED && mb::fused_blocks_per_sm() <= 0)
+        return fail(w, MB_ERR_INVALID_ARG, "the fused frame kernel cannot be resident on this device");
     drop_graphs(w);
     bool to_counting = t->sort_algorithm == MB_SORT_COUNTING && !counting(w);
     w->tuning = *t;
@@ -616,18 +663,29 @@ mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* fram
     const mb_tuning start = w->tuning;
     mb_tuning cand[MB_TUNE_CANDIDATES];
     {
-        const uint32_t sorts[4][2] = {{MB_SORT_COUNTING, 8u}, {MB_SORT_ONESWEEP, 6u}, {MB_SORT_ONESWEEP, 8u},
-                                      {MB_SORT_ONESWEEP, 11u}};
-        const uint32_t fpl[3] = {1u, 8u, 16u};
-        uint32_t c = 0;
-        for (const auto& so : sorts)
-            for (uint32_t f : fpl) {
-                cand[c] = start;
-                cand[c].sort_algorithm = so[0];
-                cand[c].digit_bits_max = so[1];
-                cand[c].frames_per_launch = f;
-                ++c;
-            }
+        // {sort, digit bits, frames per graph launch, state gather, frame kernel}
+        const uint32_t c5[MB_TUNE_CANDIDATES][5] = {
+            {MB_SORT_COUNTING, 8u, 1u, MB_GATHER_COPY, MB_FRAME_GRAPH},
+            {MB_SORT_COUNTING, 8u, 8u, MB_GATHER_COPY, MB_FRAME_GRAPH},
+            {MB_SORT_COUNTING, 8u, 16u, MB_GATHER_COPY, MB_FRAME_GRAPH},
+            {MB_SORT_COUNTING, 8u, 8u, MB_GATHER_COPY, MB_FRAME_FUSED},
+            {MB_SORT_COUNTING, 8u, 8u, MB_GATHER_INDIRECT, MB_FRAME_GRAPH},
+            {MB_SORT_COUNTING, 8u, 16u, MB_GATHER_INDIRECT, MB_FRAME_GRAPH},
+            {MB_SORT_COUNTING, 8u, 8u, MB_GATHER_INDIRECT, MB_FRAME_FUSED},
+            {MB_SORT_ONESWEEP, 6u, 8u, MB_GATHER_COPY, MB_FRAME_GRAPH},
+            {MB_SORT_ONESWEEP, 8u, 1u, MB_GATHER_COPY, MB_FRAME_GRAPH},
+            {MB_SORT_ONESWEEP, 8u, 8u, MB_GATHER_COPY, MB_FRAME_GRAPH},
+            {MB_SORT_ONESWEEP, 8u, 8u, MB_GATHER_INDIRECT, MB_FRAME_GRAPH},
+            {MB_SORT_ONESWEEP, 11u, 8u, MB_GATHER_COPY, MB_FRAME_GRAPH},
+        };
+        for (uint32_t c = 0; c < MB_TUNE_CANDIDATES; ++c) {
+            cand[c] = start;
+            cand[c].sort_algorithm = c5[c][0];
+            cand[c].digit_bits_max = c5[c][1];
+            cand[c].frames_per_launch = c5[c][2];
+            cand[c].state_gather = c5[c][3];
+            cand[c].frame_kernel = c5[c][4];
+        }
     }
     // save what the frames overwrite
     const size_t n = w->n, C = w->cells;
@@ -824,6 +882,7 @@ mb_status mb_last_frame_times(mb_world* w, float* ms) {
 
 uint32_t mb_kernels_per_frame(const mb_world* w) {
     if (!w) return 0u;
+    if (fused(w)) return 1u;  // one launch per step, whatever its frame count
     // counting: scan + scatter + fixup listing + in-cell fixup + physics;
     // onesweep: histogram + one kernel per digit pass + cell offsets + gap fill + gather + physics
     return counting(w) ? 5u : (uint32_t)w->sched.passes + 5u;

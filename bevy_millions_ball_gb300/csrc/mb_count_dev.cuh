@@ -1,0 +1,515 @@
+// mb_count_dev.cuh - device code of the counting sort (see mb_count.cu), as
+// functions of an explicit block index so that both the per-stage kernels
+// (mb_count.cu) and the fused frame kernel (mb_physics.cu) run the same code.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mb_internal.h"
+
+namespace mb {
+namespace {
+
+// ---------------------------------------------------------------- scan
+// Block b of the scan covers the chunk of cells [kScanChunk b, kScanChunk (b + 1))
+// inside tile t = b kScanChunk / 4096 (cells [4096 t, 4096 t + 4096)).  coarse[t] holds the number of
+// spheres in tile t (emitted with the per-cell counts), so a chunk finds its base
+// by summing coarse[0..t) and the counts of the tile's cells before it - no
+// look-back, no waiting on other blocks.  The counts are left in place (other
+// chunks read them); the fixup kernel clears them.
+//
+// kScenes (a batch): every scene's cell range is padded to whole tiles, so a tile
+// belongs to one scene; its base is that scene's first slot plus the coarse
+// counts of the scene's earlier tiles, and tiles of HOLD scenes are left alone.
+// One chunk (kScanThreads threads); s_warp, s_base: kScanThreads / 32 words each.
+template <bool kScenes, bool kCg = false>
+__device__ __forceinline__ void scan_chunk(uint32_t chunk, const uint32_t* __restrict__ hist,
+                                           const uint32_t* __restrict__ coarse, uint32_t cells,
+                                           uint32_t* __restrict__ offs, uint32_t* fix_ctl,
+                                           const SceneDev* __restrict__ scenes,
+                                           const uint32_t* __restrict__ cell_tile_scene, uint32_t* s_warp,
+                                           uint32_t* s_base) {
+    constexpr int W = kScanThreads / 32;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t c0 = chunk * kScanChunk, tile = c0 / kScanTile;
+    __syncthreads();  // a previous chunk's partial sums are read (when one thread block runs several)
+    if (chunk == 0 && tid < (uint32_t)kFixLists) fix_ctl[tid] = 0u;  // fixup lists of this frame start empty
+    const uint32_t base = c0 + tid * kScanItems;
+
+    uint32_t first_tile = 0, base_slot = 0;
+    if (kScenes) {
+        const uint32_t sc = __ldg(cell_tile_scene + tile);
+        if (__ldg(&scenes[sc].mode) == kModeHold) return;
+        first_tile = __ldg(&scenes[sc].cell_base) / kScanTile;
+        base_slot = __ldg(&scenes[sc].agent_base);
+    }
+    // exclusive base of this chunk: the coarse counts of the earlier tiles, plus
+    // the counts of the tile's cells before the chunk
+    uint32_t bsum = 0;
+    for (uint32_t t = first_tile + tid; t < tile; t += kScanThreads) bsum += ld_in<kCg>(coarse + t);
+    for (uint32_t c = tile * kScanTile + tid * 4u; c < c0; c += kScanThreads * 4u) {
+        const uint4 x = __ldcg(reinterpret_cast<const uint4*>(hist + c));
+        bsum += (x.x + x.y) + (x.z + x.w);
+    }
+
+    uint32_t v[kScanItems];
+    if (base + kScanItems <= cells) {
+        const uint4* h4 = reinterpret_cast<const uint4*>(hist + base);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            uint4 x = __ldcg(h4 + q);
+            v[4 * q] = x.x;
+            v[4 * q + 1] = x.y;
+            v[4 * q + 2] = x.z;
+            v[4 * q + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < kScanItems; ++q) v[q] = (base + q < cells) ? __ldcg(hist + base + q) : 0u;
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) sum += v[q];
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) bsum += __shfl_xor_sync(0xFFFFFFFFu, bsum, o);
+    if (lane == 31u) s_warp[warp] = incl;
+    if (lane == 0u) s_base[warp] = bsum;
+    __syncthreads();
+    uint32_t run = base_slot + incl - sum;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        if ((uint32_t)w < warp) run += s_warp[w];
+        run += s_base[w];
+    }
+    if (base + kScanItems <= cells) {
+        uint4* o4 = reinterpret_cast<uint4*>(offs + base);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            uint4 x;
+            x.x = run; run += v[4 * q];
+            x.y = run; run += v[4 * q + 1];
+            x.z = run; run += v[4 * q + 2];
+            x.w = run; run += v[4 * q + 3];
+            o4[q] = x;
+        }
+        // end of the tile: the next tile's first offset, or the scene's / table's end
+        if (base + kScanItems == cells || (kScenes && tid == kScanThreads - 1)) offs[base + kScanItems] = run;
+    } else {
+        for (int q = 0; q < kScanItems; ++q) {
+            uint32_t c = base + q;
+            if (c < cells) {
+                offs[c] = run;
+                run += v[q];
+                if (c + 1u == cells) offs[cells] = run;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- scatter
+// Fixup lists, filled with one global atomic per list per block iteration.
+struct FixLists {
+    uint32_t* ctl;
+    uint32_t* list[kFixLists];
+    uint32_t cap[kFixLists];
+};
+
+// The run [b, b + g) of a cell with slots [lo, hi) ends the cell and did not
+// start it: other warps' runs came first, so the cell may be out of input order.
+// The run's leader marks its input slot in the fixup bitmap (once per cell: one
+// run ends it); k_fix_collect lists the marked cells.
+__device__ __forceinline__ bool listed(uint32_t lo, uint32_t hi, uint32_t b, uint32_t g) {
+    return b + g == hi && b != lo;
+}
+// One word of the bitmap per 32 input slots, written whole by the warp that
+// scatters them (every word below ceil(n / 32) is rewritten each frame, so
+// nothing is cleared and the scatter needs no atomics or barriers for it).
+__device__ __forceinline__ void mark_fix(uint32_t* __restrict__ fix_bits, uint32_t i, uint32_t n, bool mark) {
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, mark);
+    if ((threadIdx.x & 31u) == 0u && i < n) fix_bits[i >> 5] = m;
+}
+// Also (spos != NULL) moves each sphere's state to its slot (a sorted copy for
+// the physics pass; without it the physics pass reads the state through perm)
+// and, where a slot begins or ends a physics tile, writes that side of the
+// tile's band table entry (the cell of a slot is final here; the fixup only
+// reorders slots inside a cell).
+// Input slots [vb * 256, ...) with a stride of nvb * 256 (256-thread blocks).
+template <bool kCg = false>
+__device__ __forceinline__ void scatter_range(uint32_t vb, uint32_t nvb, const uint32_t* __restrict__ keys,
+                                              uint32_t n, uint32_t* __restrict__ hist,
+                                              uint32_t* __restrict__ perm, const float4* __restrict__ pos_in,
+                                              const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
+                                              uint4* __restrict__ svfme, const uint32_t* __restrict__ offs,
+                                              uint4* __restrict__ bands, uint32_t N,
+                                              uint32_t* __restrict__ fix_bits) {
+    const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
+    const uint32_t stride = nvb * blockDim.x;
+    for (uint32_t i0 = vb * blockDim.x; i0 < n; i0 += stride) {
+        uint32_t i = i0 + threadIdx.x;
+        bool valid = i < n;
+        uint32_t k = valid ? ld_in<kCg>(keys + i) : 0xFFFFFFFFu;
+        float4 p;
+        uint4 q;
+        if (valid && spos) {
+            p = ld_in<kCg>(pos_in + i);
+            q = ld_in<kCg>(vfme_in + i);
+        }
+        // a key flagged kInitKeyBit belongs to a scene in its INIT frame: all its
+        // keys are equal, so its stable order is the identity and the slot is i
+        const bool ident = valid && (k & kInitKeyBit);
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k);
+        uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+        uint32_t b = 0;
+        bool mark = false;
+        if (valid && !ident && lane == leader) {
+            const uint32_t g = (uint32_t)__popc(peers);
+            const uint32_t lo = ld_in<kCg>(offs + k), hi = ld_in<kCg>(offs + k + 1u);
+            b = hi - atomicSub(hist + k, g);  // the run's first slot
+            mark = listed(lo, hi, b, g);
+        }
+        b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
+        mark_fix(fix_bits, i, n, mark);
+        if (valid) {
+            const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
+            if (dst >= n) continue;  // only counts that disagree with the keys get here
+            perm[dst] = i;
+            if (spos) {
+                spos[dst] = p;
+                svfme[dst] = q;
+            }
+            if (bands && !ident) write_band_bounds<kCg>(bands, offs, N, n, dst, k);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- collect
+// Lists the cells marked in the fixup bitmap by size class (a marked input
+// slot's key is its cell).  A block reads kCollectWords words, a byte per
+// thread, stages the cells in shared memory and appends them to the global
+// lists with one atomic per list.
+constexpr uint32_t kCollectThreads = 256, kCollectWords = kCollectThreads / 4u;
+
+// One block of the listing (kCollectThreads threads); s_cell: kFixLists x
+// kCollectWords * 32 words, s_n and s_base: kFixLists words each.
+template <bool kCg = false>
+__device__ __forceinline__ void collect_block(uint32_t vb, const uint32_t* __restrict__ fix_bits,
+                                              const uint32_t* __restrict__ keys, uint32_t n,
+                                              const uint32_t* __restrict__ offs, const FixLists& lists,
+                                              uint32_t (*s_cell)[kCollectWords * 32u], uint32_t* s_n,
+                                              uint32_t* s_base) {
+    const uint32_t tid = threadIdx.x;
+    __syncthreads();  // a previous block's lists are read out (when one thread block runs several)
+    if (tid < (uint32_t)kFixLists) s_n[tid] = 0u;
+    __syncthreads();
+    const uint32_t words = (n + 31u) / 32u;
+    const uint32_t w = vb * kCollectWords + tid / 4u, sh = 8u * (tid & 3u);
+    uint32_t bits = w < words ? (__ldcg(fix_bits + w) >> sh) & 0xFFu : 0u;
+    while (bits) {
+        const uint32_t c = ld_in<kCg>(keys + 32u * w + sh + (uint32_t)(__ffs(bits) - 1));
+        bits &= bits - 1u;
+        const uint32_t m = ld_in<kCg>(offs + c + 1u) - ld_in<kCg>(offs + c);
+        const int cls = m <= kFixSmall ? kFixListSmall : (m <= kFixWarp ? kFixListWarp : kFixListHuge);
+        s_cell[cls][atomicAdd(&s_n[cls], 1u)] = c;  // at most 32 * kCollectWords marks per block
+    }
+    __syncthreads();
+    if (tid < (uint32_t)kFixLists && s_n[tid]) s_base[tid] = atomicAdd(lists.ctl + tid, s_n[tid]);
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < kFixLists; ++c) {
+        for (uint32_t j = tid; j < s_n[c]; j += kCollectThreads) {
+            const uint32_t at = s_base[c] + j;  // lists hold every cell that can qualify; the bound guards bad counts
+            if (at < lists.cap[c]) lists.list[c][at] = s_cell[c][j];
+        }
+    }
+}
+
+// ---------------------------------------------------------------- fixup
+// The listed cells (see k_fix_collect) get their slots back in ascending input order
+// and (spos != NULL) re-gather their sorted state copy from the state source: one
+// buffer (a world), or each scene's current buffer (a batch, where cells and
+// coarse tiles of HOLD scenes are left alone).  Cells of up to kFixSmall slots: a thread
+// each (sorting network in registers); up to kFixWarp: a warp each (bitonic sort
+// in registers and shuffles); larger: a block each (bitmap of the input indices,
+// chunk by chunk of their range, read back in order).
+constexpr uint32_t kFixThreads = 256;
+constexpr uint32_t kBitmapWords = 8192;                 // 32 KB of shared memory
+constexpr uint32_t kBitmapValues = kBitmapWords * 32u;  // input indices per bitmap chunk
+
+// Block-wide min (is_min) or max of v; every thread gets the result.
+__device__ __forceinline__ uint32_t block_reduce(uint32_t v, uint32_t* s_red, bool is_min) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint32_t u = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        v = is_min ? min(v, u) : max(v, u);
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31u) == 0u) s_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    v = s_red[0];
+    for (uint32_t w = 1; w < blockDim.x / 32u; ++w) v = is_min ? min(v, s_red[w]) : max(v, s_red[w]);
+    __syncthreads();
+    return v;
+}
+
+// Block-wide exclusive prefix sum of v; `total` receives the sum over the block.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_red, uint32_t& total) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31u) s_red[warp] = incl;
+    __syncthreads();
+    uint32_t base = 0, sum = 0;
+    for (uint32_t w = 0; w < blockDim.x / 32u; ++w) {
+        if (w < warp) base += s_red[w];
+        sum += s_red[w];
+    }
+    __syncthreads();
+    total = sum;
+    return base + incl - v;
+}
+
+template <bool kCg>
+struct OneBufferT {
+    const float4* p;
+    const uint4* q;
+    __device__ __forceinline__ bool tile_active(uint32_t) const { return true; }
+    __device__ __forceinline__ bool any_init() const { return false; }
+    __device__ __forceinline__ bool tile_init(uint32_t) const { return false; }
+    __device__ __forceinline__ float4 pos(uint32_t o) const { return ld_in<kCg>(p + o); }
+    __device__ __forceinline__ uint4 vfme(uint32_t o) const { return ld_in<kCg>(q + o); }
+};
+using OneBuffer = OneBufferT<false>;
+
+struct SceneBuffers {
+    const SceneDev* scenes;
+    const uint32_t* slot_tile_scene;  // scene of slot t * kPhysicsTile
+    const uint32_t* cell_tile_scene;  // scene of scan tile t
+    const float4* p0;
+    const float4* p1;
+    const uint4* q0;
+    const uint4* q1;
+    __device__ __forceinline__ bool tile_active(uint32_t t) const {
+        return __ldg(&scenes[__ldg(cell_tile_scene + t)].mode) != kModeHold;
+    }
+    __device__ __forceinline__ bool any_init() const { return true; }
+    __device__ __forceinline__ bool tile_init(uint32_t t) const {
+        return __ldg(&scenes[__ldg(cell_tile_scene + t)].mode) == kModeInit;
+    }
+    __device__ __forceinline__ uint32_t parity(uint32_t o) const {
+        uint32_t s = __ldg(slot_tile_scene + o / kPhysicsTile);
+        while (o >= __ldg(&scenes[s].agent_end)) ++s;
+        return __ldg(&scenes[s].parity);
+    }
+    __device__ __forceinline__ float4 pos(uint32_t o) const { return __ldg((parity(o) ? p1 : p0) + o); }
+    __device__ __forceinline__ uint4 vfme(uint32_t o) const { return __ldg((parity(o) ? q1 : q0) + o); }
+};
+
+// Ascending bitonic sort of the warp's 32 S keys, key e = 32 s + lane in v[s]
+// (S a power of two, at most kFixWarp / 32): partners e ^ j in other lanes are
+// exchanged with shuffles, partners in other registers of the same lane in place.
+template <uint32_t S>
+__device__ __forceinline__ void warp_bitonic(uint32_t (&v)[kFixWarp / 32], uint32_t lane) {
+#pragma unroll
+    for (uint32_t k = 2u; k <= 32u * S; k <<= 1) {
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0u; j >>= 1) {
+            if (j < 32u) {
+#pragma unroll
+                for (uint32_t s = 0; s < S; ++s) {
+                    const uint32_t e = 32u * s + lane;
+                    const uint32_t o = __shfl_xor_sync(0xFFFFFFFFu, v[s], (int)j);
+                    const bool up = (e & k) == 0u, low = (e & j) == 0u;
+                    v[s] = (low == up) ? min(v[s], o) : max(v[s], o);
+                }
+            } else {
+                const uint32_t js = j / 32u;
+#pragma unroll
+                for (uint32_t s = 0; s < S; ++s) {
+                    if (s & js) continue;
+                    const uint32_t e = 32u * s + lane;
+                    const uint32_t a = v[s], b = v[s | js];
+                    const bool up = (e & k) == 0u;
+                    v[s] = up ? min(a, b) : max(a, b);
+                    v[s | js] = up ? max(a, b) : min(a, b);
+                }
+            }
+        }
+    }
+}
+
+// Block vb of nvb (kFixThreads threads; the lists are shared out grid-stride);
+// s_v: kBitmapWords words, s_red: kFixThreads / 32 + 1 words.
+template <class Src, bool kCg = false>
+__device__ __forceinline__ void fix_block(uint32_t vb, uint32_t nvb, const uint32_t* __restrict__ offs,
+                                          uint32_t* perm, uint32_t* __restrict__ hist, uint32_t cells,
+                                          uint32_t* __restrict__ coarse, uint32_t tiles, const FixLists& lists,
+                                          uint32_t* __restrict__ tmp, const Src& src, float4* __restrict__ spos,
+                                          uint4* __restrict__ svfme, uint32_t* s_v, uint32_t* s_red) {
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    // the scan of this frame is over: clear the tile counts for the next one; the
+    // cell counts went back to zero in the scatter, except those of scenes in
+    // their INIT frame (placed in identity order, nothing subtracted)
+    if (vb == 0)
+        for (uint32_t t = tid; t < tiles; t += blockDim.x)
+            if (src.tile_active(t)) coarse[t] = 0u;
+    if (src.any_init())
+        for (uint32_t c = (vb * blockDim.x + tid) * 4u; c < cells; c += nvb * blockDim.x * 4u)
+            if (src.tile_init(c / kScanTile)) *reinterpret_cast<uint4*>(hist + c) = make_uint4(0u, 0u, 0u, 0u);
+
+    const uint32_t* __restrict__ small = lists.list[0];
+    const uint32_t* __restrict__ mid = lists.list[1];
+    const uint32_t* __restrict__ huge = lists.list[2];
+
+    // small cells: one thread each, the cell held in registers (a sorting
+    // network over kFixSmall slots; empty slots hold 0xFFFFFFFF and stay last)
+    const uint32_t n_small = min(ld_cur<kCg>(lists.ctl + kFixListSmall), lists.cap[0]);
+    for (uint32_t x = vb * blockDim.x + tid; x < n_small; x += nvb * blockDim.x) {
+        const uint32_t c = ld_cur<kCg>(small + x);
+        const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;
+        uint32_t v[kFixSmall];
+        bool sorted = true;
+#pragma unroll
+        for (uint32_t k = 0; k < kFixSmall; ++k) v[k] = k < m ? ld_cur<kCg>(perm + lo + k) : 0xFFFFFFFFu;
+#pragma unroll
+        for (uint32_t k = 1; k < kFixSmall; ++k) sorted = sorted && v[k - 1u] <= v[k];
+        if (sorted) continue;
+        // Batcher's odd-even merge sort of 8 keys (19 compare-exchanges)
+        constexpr uint8_t kNet[19][2] = {{0, 1}, {2, 3}, {4, 5}, {6, 7}, {0, 2}, {1, 3}, {4, 6}, {5, 7}, {1, 2},
+                                         {5, 6}, {0, 4}, {1, 5}, {2, 6}, {3, 7}, {2, 4}, {3, 5}, {1, 2}, {3, 4},
+                                         {5, 6}};
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const uint32_t a = v[kNet[q][0]], b = v[kNet[q][1]];
+            v[kNet[q][0]] = min(a, b);
+            v[kNet[q][1]] = max(a, b);
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kFixSmall; ++k) {
+            if (k < m) {
+                perm[lo + k] = v[k];
+                if (spos) {
+                    spos[lo + k] = src.pos(v[k]);
+                    svfme[lo + k] = src.vfme(v[k]);
+                }
+            }
+        }
+    }
+
+    // mid cells: one warp each, a bitonic sort of the cell's input indices held
+    // in registers (slot e = 32 s + lane is v[s]; padded with 0xFFFFFFFF to 32 S
+    // slots, S a power of two)
+    const uint32_t n_mid = min(ld_cur<kCg>(lists.ctl + kFixListWarp), lists.cap[1]);
+    const uint32_t warps = nvb * (blockDim.x / 32u);
+    for (uint32_t x = vb * (blockDim.x / 32u) + tid / 32u; x < n_mid; x += warps) {
+        const uint32_t c = ld_cur<kCg>(mid + x);
+        const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;  // 9 <= m <= kFixWarp
+        uint32_t v[kFixWarp / 32];
+#pragma unroll
+        for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
+            const uint32_t e = 32u * s + lane;
+            v[s] = e < m ? ld_cur<kCg>(perm + lo + e) : 0xFFFFFFFFu;
+        }
+        {  // the runs may have claimed their slots in input order already
+            bool ok = true;
+#pragma unroll
+            for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
+                const uint32_t down = __shfl_down_sync(0xFFFFFFFFu, v[s], 1);
+                const uint32_t wrap = s + 1u < kFixWarp / 32 ? __shfl_sync(0xFFFFFFFFu, v[s + 1u < kFixWarp / 32 ? s + 1u : s], 0)
+                                                              : 0xFFFFFFFFu;
+                ok = ok && v[s] <= (lane == 31u ? wrap : down);
+            }
+            if (__all_sync(0xFFFFFFFFu, ok)) continue;
+        }
+        if (m <= 32u) warp_bitonic<1>(v, lane);
+        else if (m <= 64u) warp_bitonic<2>(v, lane);
+        else if (m <= 128u) warp_bitonic<4>(v, lane);
+        else warp_bitonic<8>(v, lane);
+        __syncwarp();  // every lane has read the cell before any slot is rewritten
+#pragma unroll
+        for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
+            const uint32_t e = 32u * s + lane;
+            if (e < m) {
+                perm[lo + e] = v[s];
+                if (spos) {
+                    spos[lo + e] = src.pos(v[s]);
+                    svfme[lo + e] = src.vfme(v[s]);
+                }
+            }
+        }
+    }
+
+    // huge cells: one block each.  The cell's input indices are copied aside,
+    // then each chunk of their value range becomes a bitmap in shared memory: the
+    // set bits, read in order, are the chunk's indices in ascending order, and a
+    // block scan of per-thread bit counts gives every thread its output position.
+    const uint32_t n_huge = min(ld_cur<kCg>(lists.ctl + kFixListHuge), lists.cap[2]);
+    for (uint32_t x = vb; x < n_huge; x += nvb) {
+        const uint32_t c = ld_cur<kCg>(huge + x);
+        const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;
+        uint32_t vmin = 0xFFFFFFFFu, vmax = 0u;
+        for (uint32_t j = tid; j < m; j += blockDim.x) {
+            const uint32_t v = ld_cur<kCg>(perm + lo + j);
+            tmp[lo + j] = v;
+            vmin = min(vmin, v);
+            vmax = max(vmax, v);
+        }
+        vmin = block_reduce(vmin, s_red, true);
+        vmax = block_reduce(vmax, s_red, false);  // ends with a barrier: tmp is complete
+        uint32_t done = 0;
+        for (uint32_t c0 = vmin;; c0 += kBitmapValues) {
+            for (uint32_t w = tid; w < kBitmapWords; w += blockDim.x) s_v[w] = 0u;
+            __syncthreads();
+            for (uint32_t j = tid; j < m; j += blockDim.x) {
+                const uint32_t d = tmp[lo + j] - c0;
+                if (d < kBitmapValues) atomicOr(&s_v[d >> 5], 1u << (d & 31u));
+            }
+            __syncthreads();
+            constexpr uint32_t kWordsPer = kBitmapWords / kFixThreads;
+            uint32_t mine = 0;
+#pragma unroll 8
+            for (uint32_t w = 0; w < kWordsPer; ++w) mine += (uint32_t)__popc(s_v[tid * kWordsPer + w]);
+            uint32_t total;
+            const uint32_t before = block_exclusive_scan(mine, s_red, total);
+            uint32_t at = lo + done + before;
+            for (uint32_t w = 0; w < kWordsPer; ++w) {
+                uint32_t bits = s_v[tid * kWordsPer + w];
+                const uint32_t vb = c0 + (tid * kWordsPer + w) * 32u;
+                while (bits) {  // four at a time, so the state loads overlap
+                    uint32_t vv[4];
+                    uint32_t got = 0;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        vv[q] = bits ? vb + (uint32_t)(__ffs(bits) - 1) : 0u;
+                        got += bits ? 1u : 0u;
+                        bits &= bits - 1u;
+                    }
+#pragma unroll
+                    for (uint32_t q = 0; q < 4; ++q) {
+                        if (q < got) {
+                            perm[at + q] = vv[q];
+                            if (spos) {
+                                spos[at + q] = src.pos(vv[q]);
+                                svfme[at + q] = src.vfme(vv[q]);
+                            }
+                        }
+                    }
+                    at += got;
+                }
+            }
+            done += total;
+            __syncthreads();  // bitmap free for the next chunk
+            if (vmax - c0 < kBitmapValues) break;
+        }
+    }
+}
+
+}  // namespace
+}  // namespace mb

@@ -170,6 +170,29 @@ cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
+// Load of data the running kernel does not write.  kCg: the data may have been
+// written earlier in the same launch (the fused frame kernel, whose stages are
+// separated by grid barriers, not kernel boundaries), so it is read from L2
+// (ld.global.cg) instead of through the non-coherent read-only path.
+template <bool kCg, typename T>
+__device__ __forceinline__ T ld_in(const T* p) {
+    if constexpr (kCg)
+        return __ldcg(p);
+    else
+        return __ldg(p);
+}
+
+// Load of data that an earlier stage wrote: a plain load after a kernel
+// boundary; from L2 (ld.global.cg) inside the fused frame kernel (kCg).
+template <bool kCg, typename T>
+__device__ __forceinline__ T ld_cur(const T* p) {
+    if constexpr (kCg)
+        return __ldcg(p);
+    else
+        return *p;
+}
+
+template <bool kCg = false>
 __device__ __forceinline__ void write_band_bounds(uint4* __restrict__ bands, const uint32_t* __restrict__ offs,
                                                   uint32_t N, uint32_t n, uint32_t slot, uint32_t key) {
     const uint32_t r = slot % kPhysicsTile;
@@ -180,14 +203,14 @@ __device__ __forceinline__ void write_band_bounds(uint4* __restrict__ bands, con
     if (first) {
         const uint32_t l = cx > 0u ? 1u : 0u;
         const uint32_t f = max(key, N), lf = f % N > 0u ? 1u : 0u;  // row below: from column cx-1 of row cz-1
-        bands[2u * t] = make_uint4(__ldg(offs + f - N - lf), __ldg(offs + key - l),
-                                   key < top ? __ldg(offs + key + N - l) : n, 0u);
+        bands[2u * t] = make_uint4(ld_in<kCg>(offs + f - N - lf), ld_in<kCg>(offs + key - l),
+                                   key < top ? ld_in<kCg>(offs + key + N - l) : n, 0u);
     }
     if (last) {
         const uint32_t rr = cx < N - 1u ? 2u : 1u;
         const uint32_t a = min(key, top - 1u), ra = a % N < N - 1u ? 2u : 1u;  // row above: to column cx+1
-        bands[2u * t + 1u] = make_uint4(key >= N ? __ldg(offs + key - N + rr) : 0u, __ldg(offs + key + rr),
-                                        top ? __ldg(offs + a + N + ra) : 0u, 0u);
+        bands[2u * t + 1u] = make_uint4(key >= N ? ld_in<kCg>(offs + key - N + rr) : 0u, ld_in<kCg>(offs + key + rr),
+                                        top ? ld_in<kCg>(offs + a + N + ra) : 0u, 0u);
     }
 }
 #endif
@@ -209,6 +232,32 @@ cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t*
                                 const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
                                 uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
                                 cudaStream_t st, bool pdl = false);
+// LOOP frames of one world as a single cooperative kernel (all stages of every
+// frame, separated by grid barriers): `frames` frames from state buffer `cur`
+// (the last one lands in cur ^ (frames & 1)), counting sort, sorted copy or
+// (indirect) gather through perm.  bar: two zeroed words; err: the error word
+// (bit 8: a grid barrier gave up).
+struct CountScratch;
+struct FusedFrame {
+    PhysParams P;
+    uint32_t n, cells, frames, cur;
+    bool indirect;
+    uint32_t* keys;
+    uint32_t* offs;
+    uint32_t* perm;
+    uint4* bands;
+    const CountScratch* cnt;
+    float4* pos[2];
+    uint4* vfme[2];
+    float4* spos;
+    uint4* svfme;
+    uint32_t* bar;
+    uint32_t* err;
+};
+cudaError_t launch_frame_fused(const FusedFrame& f, cudaStream_t st);
+// Resident blocks per SM of the fused frame kernel (0: it cannot run).
+int fused_blocks_per_sm();
+
 // Compares the physics pass's division (div_exact) with IEEE division over
 // `count` generated cases on the current device (synchronous).
 cudaError_t selftest_divide(uint64_t seed, uint64_t count, uint64_t* mismatches, uint32_t* bad4);

@@ -14,6 +14,9 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
+#include "mb_count_dev.cuh"
 #include "mb_internal.h"
 
 namespace mb {
@@ -316,7 +319,7 @@ __device__ __forceinline__ uint32_t cand_slot(uint32_t t, const uint32_t (&o)[3]
 
 constexpr float kNearScale = 1.0014989f;  // about sqrt(1.003): squared, a 0.3% margin on edge^2
 
-template <bool kShared, uint32_t kLook, bool kIndirect>
+template <bool kShared, uint32_t kLook, bool kIndirect, bool kCg>
 __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
                                              uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself,
@@ -334,7 +337,7 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
                 bp[q] = bpos[j0 + q];
             } else {
                 const uint32_t j = j0 + min(q, rem - 1u);
-                bp[q] = __ldg(bpos + (kIndirect ? min(__ldg(perm + j), nmax) : j));
+                bp[q] = ld_in<kCg>(bpos + (kIndirect ? min(ld_in<kCg>(perm + j), nmax) : j));
             }
         }
         uint32_t m = 0;
@@ -354,8 +357,8 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
             if (kShared) {
                 sphere(P, a, unpack(bpos[j], bvfme[j]));
             } else {
-                const uint32_t sj = kIndirect ? min(__ldg(perm + j), nmax) : j;
-                sphere(P, a, unpack(__ldg(bpos + sj), __ldg(bvfme + sj)));
+                const uint32_t sj = kIndirect ? min(ld_in<kCg>(perm + j), nmax) : j;
+                sphere(P, a, unpack(ld_in<kCg>(bpos + sj), ld_in<kCg>(bvfme + sj)));
             }
         } else {
             t += min(rem, kLook);
@@ -368,33 +371,34 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
 // so its lanes run one loop.
 constexpr uint32_t kCrowdedT = 48, kLookSparse = 4, kLookCrowded = 6;
 
-template <bool kShared, bool kIndirect>
+template <bool kShared, bool kIndirect, bool kCg>
 __device__ __forceinline__ void contact_loop(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
                                              uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself,
                                              const uint32_t* __restrict__ perm, uint32_t nmax) {
     if (__any_sync(__activemask(), T >= kCrowdedT))
-        contact_walk<kShared, kLookCrowded, kIndirect>(P, a, bpos, bvfme, o, c0, c01, T, tself, perm, nmax);
+        contact_walk<kShared, kLookCrowded, kIndirect, kCg>(P, a, bpos, bvfme, o, c0, c01, T, tself, perm, nmax);
     else
-        contact_walk<kShared, kLookSparse, kIndirect>(P, a, bpos, bvfme, o, c0, c01, T, tself, perm, nmax);
+        contact_walk<kShared, kLookSparse, kIndirect, kCg>(P, a, bpos, bvfme, o, c0, c01, T, tself, perm, nmax);
 }
 
 // Slot ranges of the three candidate rows of a sphere in cell (cx, cz), key =
 // cz*N + cx (get_collision_grid_id's neighbourhood, physics.wgsl:122-160): own
 // row [0], row below [1], row above [2]; rows off the map stay empty.
+template <bool kCg>
 __device__ __forceinline__ void row_bounds(uint32_t N, const uint32_t* __restrict__ of, uint32_t key, uint32_t cx,
                                            uint32_t cz, uint32_t (&lo)[3], uint32_t (&hi)[3]) {
     const uint32_t l = cx > 0u ? 1u : 0u, rr = cx < N - 1u ? 2u : 1u;
-    lo[0] = __ldg(of + key - l);
-    hi[0] = __ldg(of + key + rr);
+    lo[0] = ld_in<kCg>(of + key - l);
+    hi[0] = ld_in<kCg>(of + key + rr);
     lo[1] = hi[1] = lo[2] = hi[2] = 0u;
     if (cz > 0u) {
-        lo[1] = __ldg(of + key - N - l);
-        hi[1] = __ldg(of + key - N + rr);
+        lo[1] = ld_in<kCg>(of + key - N - l);
+        hi[1] = ld_in<kCg>(of + key - N + rr);
     }
     if (cz < N - 1u) {
-        lo[2] = __ldg(of + key + N - l);
-        hi[2] = __ldg(of + key + N + rr);
+        lo[2] = ld_in<kCg>(of + key + N - l);
+        hi[2] = ld_in<kCg>(of + key + N + rr);
     }
 }
 
@@ -405,7 +409,7 @@ __device__ __forceinline__ void row_bounds(uint32_t N, const uint32_t* __restric
 // b holds slots [b_lo[b], b_lo[b] + b_cnt[b])); rows outside them are read from
 // spos/svfme (through perm when kIndirect).  base_a / base_c: the scene's first
 // slot and cell (0 for a world).
-template <bool kIndirect>
+template <bool kIndirect, bool kCg>
 __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32_t i, uint32_t n, uint32_t base_a,
                                             uint32_t base_c, const uint32_t (&lo)[3], const uint32_t (&hi)[3],
                                             const float4* b_pos, const uint4* b_vfme, const uint32_t* b_lo,
@@ -446,9 +450,9 @@ __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32
     // handle_collisions (physics.wgsl:119-169)
     V3 old_pos = a.position;
     if (shared)
-        contact_loop<true, false>(P, a, b_pos, b_vfme, o_s, c[0], c01, T, tself, perm, n - 1u);
+        contact_loop<true, false, kCg>(P, a, b_pos, b_vfme, o_s, c[0], c01, T, tself, perm, n - 1u);
     else
-        contact_loop<false, kIndirect>(P, a, spos, svfme, o_g, c[0], c01, T, tself, perm, n - 1u);
+        contact_loop<false, kIndirect, kCg>(P, a, spos, svfme, o_g, c[0], c01, T, tself, perm, n - 1u);
     V3 diff = a.position - old_pos;
     if (longer_than(diff, a.scale)) {
         // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337); the
@@ -507,33 +511,48 @@ __device__ __forceinline__ uint32_t scene_of(const SceneDev* __restrict__ scenes
 // its scene's mode: LOOP, INIT (re-pack, emit key) or HOLD (state carried over
 // unchanged, key re-emitted).  Slot indices inside a scene (the jitter hash)
 // are local, so every scene evolves exactly as it would alone.
-template <bool kBatched, bool kIndirect>
-__global__ void __launch_bounds__(kTileThreads)
-    k_physics_frame(const __grid_constant__ PhysParams P1, const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
-                    uint32_t n, const uint32_t* __restrict__ offs, const uint4* __restrict__ bands,
-                    const float4* __restrict__ spos,
-                    const uint4* __restrict__ svfme, const uint32_t* __restrict__ perm, float4* __restrict__ pos_out0,
-                    float4* __restrict__ pos_out1,
-                    uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1, uint32_t* __restrict__ keys_out,
-                    uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse, uint32_t* __restrict__ err) {
-    static_assert(!(kBatched && kIndirect), "batches stage a sorted copy");
-    __shared__ __align__(16) float4 s_pos[3 * kBandCap + kBandPad];  // padded: the walk reads past rows
-    __shared__ __align__(16) uint4 s_vfme[3][kBandCap];
-    __shared__ __align__(8) uint64_t s_bar;
-    __shared__ uint32_t s_lo[3], s_cnt[3];
+// Shared memory of one tile: bands (s_pos padded: the walk reads past rows) and
+// the band bounds.  (The mbarrier of the band copies is kept apart, so that the
+// fused frame kernel can reuse this memory for its other stages.)
+struct TileSmem {
+    float4 pos[3 * kBandCap + kBandPad];
+    uint4 vfme[3 * kBandCap];
+    uint32_t lo[3], cnt[3];
+};
 
-    const uint32_t tid = threadIdx.x;
-    const uint32_t i0 = blockIdx.x * kTileThreads;
+// One tile of the physics pass, run by kTileThreads threads (tid = 0..127 within
+// the group; the block's __syncthreads must be reached by every thread of the
+// block, so a block that runs two tiles side by side runs both halves through
+// this function together).  s_bar must have been initialised (copy mode);
+// bar_parity is the phase this tile's copies complete.  A tile at or past the
+// end (tile * 128 >= n) does nothing but take part in the barriers.
+template <bool kBatched, bool kIndirect, bool kCg = false>
+__device__ __forceinline__ void physics_tile(
+    uint32_t tile, uint32_t tid, uint32_t bar_parity, TileSmem* sm, uint64_t* s_bar, const PhysParams& P1,
+    const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene, uint32_t n,
+    const uint32_t* __restrict__ offs, const uint4* __restrict__ bands, const float4* __restrict__ spos,
+    const uint4* __restrict__ svfme, const uint32_t* __restrict__ perm, float4* __restrict__ pos_out0,
+    float4* __restrict__ pos_out1, uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1,
+    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
+    uint32_t* __restrict__ err) {
+    static_assert(!(kBatched && kIndirect), "batches stage a sorted copy");
+    float4* const s_pos = sm->pos;
+    uint4* const s_vfme = sm->vfme;
+    uint32_t* const s_lo = sm->lo;
+    uint32_t* const s_cnt = sm->cnt;
+
+    const uint32_t i0 = tile * kTileThreads;
+    const bool tile_ok = i0 < n;
     const uint32_t i = i0 + tid;
-    const uint32_t ilast = min(i0 + kTileThreads, n) - 1u;
-    const bool valid = i < n;
+    const uint32_t ilast = tile_ok ? min(i0 + kTileThreads, n) - 1u : 0u;
+    const bool valid = tile_ok && i < n;
 
     // this slot's scene; its output buffer is the one its current state is not in
     uint32_t sc = 0, base_a = 0, base_c = 0, mode = kModeLoop;
     float4* __restrict__ pos_out = pos_out0;
     uint4* __restrict__ vfme_out = vfme_out0;
-    if (kBatched) {
-        const uint32_t first = __ldg(tile_scene + blockIdx.x);
+    if (kBatched && tile_ok) {
+        const uint32_t first = __ldg(tile_scene + tile);
         sc = scene_of(scenes, first, valid ? i : ilast);
         base_a = scenes[sc].agent_base;
         base_c = scenes[sc].cell_base;
@@ -545,12 +564,15 @@ __global__ void __launch_bounds__(kTileThreads)
     }
 
     const PhysParams& P = kBatched ? scenes[sc].P : P1;  // read where it lives, not copied
-    if (!kIndirect && tid == 0) mbar_init(&s_bar, 1u);
-    if (bands) {  // bounds from the band table: one load (a batch: tiles inside one LOOP scene)
+    if (tid == 0 && !tile_ok) {
+#pragma unroll
+        for (int b = 0; b < 3; ++b) s_cnt[b] = 0u;  // nothing to stage
+    }
+    if (bands && tile_ok) {  // bounds from the band table: one load (a batch: tiles inside one LOOP scene)
         if (tid == 0) {
             bool stage = true;
             if (kBatched) {
-                const uint32_t first = __ldg(tile_scene + blockIdx.x);
+                const uint32_t first = __ldg(tile_scene + tile);
                 const uint32_t sf = scene_of(scenes, first, i0), sl = scene_of(scenes, first, ilast);
                 stage = sf == sl && __ldg(&scenes[sf].mode) == kModeLoop;
             }
@@ -559,8 +581,8 @@ __global__ void __launch_bounds__(kTileThreads)
             // completed before the kernel this one follows could start (the
             // fixups in between reorder slots inside cells, never tile bounds);
             // read through L2
-            const uint4 l = stage ? __ldcg(bands + 2u * blockIdx.x) : z;
-            const uint4 h = stage ? __ldcg(bands + 2u * blockIdx.x + 1u) : z;
+            const uint4 l = stage ? __ldcg(bands + 2u * tile) : z;
+            const uint4 h = stage ? __ldcg(bands + 2u * tile + 1u) : z;
             const uint32_t lo3[3] = {l.x, l.y, l.z}, hi3[3] = {h.x, h.y, h.z};
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
@@ -571,13 +593,13 @@ __global__ void __launch_bounds__(kTileThreads)
         }
     }
     griddep_wait();  // the sort's outputs (order, state copy) are complete and visible
-    if (!bands && tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
+    if (!bands && tile_ok && tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
         uint32_t lo = 0, hi = 0;
         bool stage = true;
         PhysParams Q = P;
         uint32_t qc = base_c;
         if (kBatched) {  // stage only tiles inside one LOOP scene
-            const uint32_t first = __ldg(tile_scene + blockIdx.x);
+            const uint32_t first = __ldg(tile_scene + tile);
             const uint32_t sf = scene_of(scenes, first, i0), sl = scene_of(scenes, first, ilast);
             stage = sf == sl && scenes[sf].mode == kModeLoop;
             Q = scenes[sf].P;
@@ -585,28 +607,28 @@ __global__ void __launch_bounds__(kTileThreads)
         }
         if (stage) {
             const uint32_t N = Q.N;
-            const uint32_t sf0 = kIndirect ? min(__ldg(perm + i0), n - 1u) : i0;
-            const uint32_t sl0 = kIndirect ? min(__ldg(perm + ilast), n - 1u) : ilast;
-            const uint32_t kf = key_of(Q, __ldg(spos + sf0)), kl = key_of(Q, __ldg(spos + sl0));
+            const uint32_t sf0 = kIndirect ? min(ld_in<kCg>(perm + i0), n - 1u) : i0;
+            const uint32_t sl0 = kIndirect ? min(ld_in<kCg>(perm + ilast), n - 1u) : ilast;
+            const uint32_t kf = key_of(Q, ld_in<kCg>(spos + sf0)), kl = key_of(Q, ld_in<kCg>(spos + sl0));
             const uint32_t cxf = kf - (kf / N) * N, cxl = kl - (kl / N) * N;
             const uint32_t* of = offs + qc;
             if (tid == 1) {  // own row
-                lo = of[kf - (cxf > 0u ? 1u : 0u)];
-                hi = of[kl + (cxl < N - 1u ? 2u : 1u)];
+                lo = ld_cur<kCg>(of + kf - (cxf > 0u ? 1u : 0u));
+                hi = ld_cur<kCg>(of + kl + (cxl < N - 1u ? 2u : 1u));
             } else if (tid == 0) {  // row below, for tile spheres with cz > 0
                 if (kl >= N) {
                     uint32_t f = max(kf, N);
                     uint32_t cf = f - (f / N) * N;
-                    lo = of[f - N - (cf > 0u ? 1u : 0u)];
-                    hi = of[kl - N + (cxl < N - 1u ? 2u : 1u)];
+                    lo = ld_cur<kCg>(of + f - N - (cf > 0u ? 1u : 0u));
+                    hi = ld_cur<kCg>(of + kl - N + (cxl < N - 1u ? 2u : 1u));
                 }
             } else {  // row above, for tile spheres with cz < N-1
                 const uint32_t top = N * (N - 1u);
                 if (kf < top) {
                     uint32_t l = min(kl, top - 1u);
                     uint32_t cl = l - (l / N) * N;
-                    lo = of[kf + N - (cxf > 0u ? 1u : 0u)];
-                    hi = of[l + N + (cl < N - 1u ? 2u : 1u)];
+                    lo = ld_cur<kCg>(of + kf + N - (cxf > 0u ? 1u : 0u));
+                    hi = ld_cur<kCg>(of + l + N + (cl < N - 1u ? 2u : 1u));
                 }
             }
         }
@@ -619,9 +641,9 @@ __global__ void __launch_bounds__(kTileThreads)
     float4 own_p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     uint4 own_q = make_uint4(0u, 0u, 0u, 0u);
     if (valid) {
-        const uint32_t o = kIndirect ? min(__ldg(perm + i), n - 1u) : i;
-        own_p = __ldg(spos + o);
-        own_q = __ldg(svfme + o);
+        const uint32_t o = kIndirect ? min(ld_in<kCg>(perm + i), n - 1u) : i;
+        own_p = ld_in<kCg>(spos + o);
+        own_q = ld_in<kCg>(svfme + o);
     }
     __syncthreads();  // band bounds published (and, copy mode, the mbarrier initialised)
     if (kIndirect) {
@@ -637,22 +659,22 @@ __global__ void __launch_bounds__(kTileThreads)
                 const uint32_t b = f < c0 ? 0u : (f < c01 ? 1u : 2u);
                 const uint32_t j = f - (b == 0u ? 0u : (b == 1u ? c0 : c01));
                 dst[u] = b * kBandCap + j;
-                src[u] = f < tot ? min(__ldg(perm + s_lo[b] + j), n - 1u) : 0u;
+                src[u] = f < tot ? min(ld_in<kCg>(perm + s_lo[b] + j), n - 1u) : 0u;
             }
             float4 gp[kGatherUnroll];
             uint4 gq[kGatherUnroll];
 #pragma unroll
             for (uint32_t u = 0; u < kGatherUnroll; ++u) {
                 if (f0 + u * kTileThreads + tid < tot) {
-                    gp[u] = __ldg(spos + src[u]);
-                    gq[u] = __ldg(svfme + src[u]);
+                    gp[u] = ld_in<kCg>(spos + src[u]);
+                    gq[u] = ld_in<kCg>(svfme + src[u]);
                 }
             }
 #pragma unroll
             for (uint32_t u = 0; u < kGatherUnroll; ++u) {
                 if (f0 + u * kTileThreads + tid < tot) {
                     s_pos[dst[u]] = gp[u];
-                    (&s_vfme[0][0])[dst[u]] = gq[u];
+                    s_vfme[dst[u]] = gq[u];
                 }
             }
         }
@@ -660,12 +682,12 @@ __global__ void __launch_bounds__(kTileThreads)
         uint32_t bytes = 0;
 #pragma unroll
         for (int b = 0; b < 3; ++b) bytes += s_cnt[b] * 32u;
-        mbar_arrive_expect_tx(&s_bar, bytes);
+        mbar_arrive_expect_tx(s_bar, bytes);
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
             if (s_cnt[b]) {
-                bulk_g2s(s_pos + b * kBandCap, spos + s_lo[b], s_cnt[b] * 16u, &s_bar);
-                bulk_g2s(s_vfme[b], svfme + s_lo[b], s_cnt[b] * 16u, &s_bar);
+                bulk_g2s(s_pos + b * kBandCap, spos + s_lo[b], s_cnt[b] * 16u, s_bar);
+                bulk_g2s(s_vfme + b * kBandCap, svfme + s_lo[b], s_cnt[b] * 16u, s_bar);
             }
         }
     }
@@ -679,13 +701,13 @@ __global__ void __launch_bounds__(kTileThreads)
         a = unpack(own_p, own_q);
         cell_of(P, a.position.x, a.position.z, cx, cz);
         key = cz * N + cx;
-        if (mode == kModeLoop) row_bounds(N, offs + base_c, key, cx, cz, lo, hi);
+        if (mode == kModeLoop) row_bounds<kCg>(N, offs + base_c, key, cx, cz, lo, hi);
     }
     if (kIndirect) {
         __syncthreads();  // bands gathered
     } else {  // bounded wait for the bands (every thread, so all copies land before exit)
         uint32_t spins = 0;
-        while (!mbar_try_wait(&s_bar, 0u)) {
+        while (!mbar_try_wait(s_bar, bar_parity)) {
             if (++spins > kWaitLimit) {
                 if (tid == 0) atomicOr(err, 4u);
                 break;
@@ -703,9 +725,168 @@ __global__ void __launch_bounds__(kTileThreads)
     }
     if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
 
-    step_sphere<kIndirect>(P, a, i, n, base_a, base_c, lo, hi, s_pos, &s_vfme[0][0], s_lo, s_cnt, spos, svfme,
-                           perm, pos_out, vfme_out, keys_out, hist, coarse);
+    step_sphere<kIndirect, kCg>(P, a, i, n, base_a, base_c, lo, hi, s_pos, s_vfme, s_lo, s_cnt, spos, svfme, perm,
+                                pos_out, vfme_out, keys_out, hist, coarse);
 }
+
+template <bool kBatched, bool kIndirect>
+__global__ void __launch_bounds__(kTileThreads)
+    k_physics_frame(const __grid_constant__ PhysParams P1, const SceneDev* __restrict__ scenes,
+                    const uint32_t* __restrict__ tile_scene, uint32_t n, const uint32_t* __restrict__ offs,
+                    const uint4* __restrict__ bands, const float4* __restrict__ spos,
+                    const uint4* __restrict__ svfme, const uint32_t* __restrict__ perm, float4* __restrict__ pos_out0,
+                    float4* __restrict__ pos_out1, uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1,
+                    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
+                    uint32_t* __restrict__ err) {
+    __shared__ __align__(16) TileSmem sm;
+    __shared__ __align__(8) uint64_t s_bar;
+    if (!kIndirect && threadIdx.x == 0) mbar_init(&s_bar, 1u);  // first copy after the tile's CTA barrier
+    physics_tile<kBatched, kIndirect>(blockIdx.x, threadIdx.x, 0u, &sm, &s_bar, P1, scenes, tile_scene, n, offs,
+                                      bands, spos, svfme, perm, pos_out0, pos_out1, vfme_out0, vfme_out1, keys_out,
+                                      hist, coarse, err);
+}
+
+// ---------------------------------------------------------------- fused frame
+// LOOP frames as one cooperative kernel: the five stages of a frame (count scan,
+// scatter, fixup listing, fixup, physics) run back to back in one launch,
+// separated by grid barriers instead of kernel boundaries, for as many frames
+// as the launch is given.  Every block is resident (cooperative launch), so a
+// block may wait for the others; each wait is bounded.  The stages run the same
+// device code as the per-stage kernels, reading data written earlier in the
+// launch from L2 (kCg), so the results are identical.
+constexpr uint32_t kFusedThreads = 256;
+constexpr uint32_t kBarrierLimit = 1u << 24;  // polls of a grid barrier before it gives up (~2 s)
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// bar[0] counts arrivals, bar[1] is the generation.  The last block to arrive
+// resets the count and advances the generation; the others wait for that.  A
+// wait that runs out (or sees that another block's wait ran out) sets bit 8 of
+// the error word and returns false: the caller then leaves the kernel.
+__device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* err, uint32_t* s_flag) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t ok = 1u;
+        const uint32_t gen = ld_acquire_gpu(bar + 1);
+        __threadfence();  // this block's writes before its arrival
+        if (atomicAdd(bar, 1u) == gridDim.x - 1u) {
+            __threadfence();  // every other block's writes (their arrivals are read above)
+            atomicExch(bar, 0u);
+            st_release_gpu(bar + 1, gen + 1u);
+        } else {
+            uint32_t spins = 0;
+            while (ld_acquire_gpu(bar + 1) == gen) {
+                ++spins;
+                if (spins > kBarrierLimit || ((spins & 1023u) == 0u && (ld_acquire_gpu(err) & 8u))) {
+                    atomicOr(err, 8u);
+                    ok = 0u;
+                    break;
+                }
+                if (spins > 32u) __nanosleep(64);
+            }
+        }
+        __threadfence();
+        *s_flag = ok;
+    }
+    __syncthreads();
+    return *s_flag != 0u;
+}
+
+struct FusedArgs {
+    PhysParams P;
+    uint32_t n, cells, chunks, scan_tiles, phys_tiles, collect_blocks, frames, cur;
+    uint32_t* keys;
+    uint32_t* hist;
+    uint32_t* coarse;
+    uint32_t* offs;
+    uint32_t* perm;
+    uint4* bands;
+    uint32_t* fix_bits;
+    uint32_t* fix_tmp;
+    FixLists lists;
+    float4* pos[2];
+    uint4* vfme[2];
+    float4* spos;   // sorted copy (copy mode)
+    uint4* svfme;
+    uint32_t* bar;  // [2] grid barrier words (zero between launches)
+    uint32_t* err;
+};
+
+union FusedSmem {
+    struct {
+        uint32_t warp[kScanThreads / 32], base[kScanThreads / 32];
+    } scan;
+    struct {
+        uint32_t cell[kFixLists][kCollectWords * 32u];
+        uint32_t n[kFixLists], base[kFixLists];
+    } collect;
+    struct {
+        uint32_t v[kBitmapWords];
+        uint32_t red[kFixThreads / 32 + 1];
+    } fix;
+    TileSmem tile[2];  // the physics stage runs two 128-slot tiles per block side by side
+};
+static_assert(kScanThreads == kFusedThreads && kCollectThreads == kFusedThreads && kFixThreads == kFusedThreads &&
+                  2u * kTileThreads == kFusedThreads,
+              "the fused kernel runs every stage with its block shape");
+
+template <bool kIndirect>
+__global__ void __launch_bounds__(kFusedThreads, 4) k_frame_fused(const __grid_constant__ FusedArgs A) {
+    extern __shared__ __align__(16) unsigned char fused_smem[];
+    FusedSmem& S = *reinterpret_cast<FusedSmem*>(fused_smem);
+    __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ uint32_t s_flag;
+    const uint32_t tid = threadIdx.x, half = tid / kTileThreads;
+    if (!kIndirect && tid % kTileThreads == 0u) mbar_init(&s_bar[half], 1u);
+    uint32_t parity = 0;
+    for (uint32_t f = 0; f < A.frames; ++f) {
+        const uint32_t cur = A.cur ^ (f & 1u), nxt = cur ^ 1u;
+        // cell offsets from the counts the previous frame emitted
+        for (uint32_t vb = blockIdx.x; vb < A.chunks; vb += gridDim.x)
+            scan_chunk<false, true>(vb, A.hist, A.coarse, A.cells, A.offs, A.lists.ctl, nullptr, nullptr, S.scan.warp,
+                                    S.scan.base);
+        if (!grid_barrier(A.bar, A.err, &s_flag)) return;
+        scatter_range<true>(blockIdx.x, gridDim.x, A.keys, A.n, A.hist, A.perm, A.pos[cur], A.vfme[cur],
+                            kIndirect ? nullptr : A.spos, kIndirect ? nullptr : A.svfme, A.offs, A.bands, A.P.N,
+                            A.fix_bits);
+        if (!grid_barrier(A.bar, A.err, &s_flag)) return;
+        for (uint32_t vb = blockIdx.x; vb < A.collect_blocks; vb += gridDim.x)
+            collect_block<true>(vb, A.fix_bits, A.keys, A.n, A.offs, A.lists, S.collect.cell, S.collect.n,
+                                S.collect.base);
+        if (!grid_barrier(A.bar, A.err, &s_flag)) return;
+        const OneBufferT<true> src{A.pos[cur], A.vfme[cur]};
+        fix_block<OneBufferT<true>, true>(blockIdx.x, gridDim.x, A.offs, A.perm, A.hist, A.cells, A.coarse,
+                                          A.scan_tiles, A.lists, A.fix_tmp, src, kIndirect ? nullptr : A.spos,
+                                          kIndirect ? nullptr : A.svfme, S.fix.v, S.fix.red);
+        if (!grid_barrier(A.bar, A.err, &s_flag)) return;
+        // the stages above wrote the sorted copy (global) and this block's shared
+        // memory through the generic proxy; the bulk copies read and write them
+        // through the async proxy
+        asm volatile("fence.proxy.async;" ::: "memory");
+        __syncthreads();
+        for (uint32_t t2 = blockIdx.x; 2u * t2 < A.phys_tiles; t2 += gridDim.x) {
+            physics_tile<false, kIndirect, true>(2u * t2 + half, tid % kTileThreads, parity, &S.tile[half],
+                                                 &s_bar[half], A.P, nullptr, nullptr, A.n, A.offs, A.bands,
+                                                 kIndirect ? A.pos[cur] : A.spos, kIndirect ? A.vfme[cur] : A.svfme,
+                                                 kIndirect ? A.perm : nullptr, A.pos[nxt], nullptr, A.vfme[nxt],
+                                                 nullptr, A.keys, A.hist, A.coarse, A.err);
+            parity ^= 1u;
+            __syncthreads();  // every thread is done with this tile's bands and bounds
+            asm volatile("fence.proxy.async;" ::: "memory");
+        }
+        if (f + 1u < A.frames && !grid_barrier(A.bar, A.err, &s_flag)) return;
+    }
+}
+
+
+
 
 // Self-test of div_exact against IEEE division over count generated cases:
 // operands from all float bit patterns, normal-range operands, power-of-two
@@ -824,6 +1005,66 @@ cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t*
     return launch_pdl(pdl, k_physics_frame<false, false>, grid, block, 0, st, p, (const SceneDev*)nullptr,
                       (const uint32_t*)nullptr, n, offs, bands, spos, svfme, (const uint32_t*)nullptr, pos_out,
                       (float4*)nullptr, vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
+}
+
+int fused_blocks_per_sm() {
+    static int per_sm = -1;  // same for every device of one architecture
+    if (per_sm < 0) {
+        int b = 0;
+        const size_t smem = sizeof(FusedSmem);
+        cudaError_t e = cudaFuncSetAttribute(k_frame_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (!e) e = cudaFuncSetAttribute(k_frame_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_frame_fused<false>, kFusedThreads, smem);
+        int b2 = 0;
+        if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_frame_fused<true>, kFusedThreads, smem);
+        per_sm = e ? 0 : std::min(b, b2);
+    }
+    return per_sm;
+}
+
+cudaError_t launch_frame_fused(const FusedFrame& f, cudaStream_t st) {
+    if (!f.frames || !f.n) return cudaSuccess;
+    const int per_sm = fused_blocks_per_sm();
+    if (per_sm <= 0) return cudaErrorCooperativeLaunchTooLarge;
+    FusedArgs A;
+    A.P = f.P;
+    A.n = f.n;
+    A.cells = f.cells;
+    A.chunks = (f.cells + kScanChunk - 1u) / kScanChunk;
+    A.scan_tiles = (f.cells + kScanTile - 1u) / kScanTile;
+    A.phys_tiles = (f.n + kTileThreads - 1u) / kTileThreads;
+    A.collect_blocks = ((f.n + 31u) / 32u + kCollectWords - 1u) / kCollectWords;
+    A.frames = f.frames;
+    A.cur = f.cur;
+    A.keys = f.keys;
+    A.hist = f.cnt->hist;
+    A.coarse = f.cnt->coarse;
+    A.offs = f.offs;
+    A.perm = f.perm;
+    A.bands = f.bands;
+    A.fix_bits = f.cnt->fix_bits;
+    A.fix_tmp = f.cnt->fix_tmp;
+    A.lists = FixLists{f.cnt->fix_ctl, {f.cnt->fix[0], f.cnt->fix[1], f.cnt->fix[2]},
+                       {f.cnt->fix_cap[0], f.cnt->fix_cap[1], f.cnt->fix_cap[2]}};
+    for (int b = 0; b < 2; ++b) {
+        A.pos[b] = f.pos[b];
+        A.vfme[b] = f.vfme[b];
+    }
+    A.spos = f.spos;
+    A.svfme = f.svfme;
+    A.bar = f.bar;
+    A.err = f.err;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((uint32_t)(per_sm * device_sm_count()));
+    cfg.blockDim = dim3(kFusedThreads);
+    cfg.dynamicSmemBytes = sizeof(FusedSmem);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return f.indirect ? cudaLaunchKernelEx(&cfg, k_frame_fused<true>, A) : cudaLaunchKernelEx(&cfg, k_frame_fused<false>, A);
 }
 
 cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,

@@ -265,8 +265,21 @@ typedef struct mb_tuning {
     uint32_t frames_per_launch; /* LOOP frames captured per graph launch in multi-frame steps:
                                    1, 2, 4, 8 (default; 0 reads as 8) or 16 */
     uint32_t state_gather;     /* MB_GATHER_COPY or MB_GATHER_INDIRECT (below) */
-    uint32_t reserved[3];
+    uint32_t frame_kernel;     /* MB_FRAME_GRAPH or MB_FRAME_FUSED (below) */
+    uint32_t reserved[2];
 } mb_tuning;
+
+/* How LOOP frames are launched:
+ *   MB_FRAME_GRAPH: one kernel per stage (count scan, scatter, fixup listing,
+ *                   fixup, physics), captured in CUDA graphs (default);
+ *   MB_FRAME_FUSED: every stage of every frame of an mb_step call in one
+ *                   cooperative kernel, the stages separated by grid barriers
+ *                   (bounded waits: a barrier that gives up is reported by
+ *                   mb_sync as MB_ERR_TIMEOUT).  Counting sort only; with
+ *                   profiling on, frames run as MB_FRAME_GRAPH.
+ * Both give identical results. */
+#define MB_FRAME_GRAPH 0u
+#define MB_FRAME_FUSED 1u
 
 /* How the physics pass reads the state in this frame's sorted order:
  *   MB_GATHER_COPY:     the sort writes a sorted copy of the state (32 B per
@@ -306,10 +319,12 @@ mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float 
 
 /*
  * Autotuner (no counterpart in the reference, whose sort and passes have fixed
- * workgroup shapes).  Times every candidate tuning on the world's own scene for
- * `frames` LOOP frames each (CUDA events on the world's stream, one warm-up
- * frame per candidate): the counting sort and the onesweep sort with 6-, 8- and
- * 11-bit digits, each with 1, 8 and 16 frames per graph launch.  The world's
+ * workgroup shapes, NUMBER_OF_THREADS_PER_WORKGROUP = 256 at src/physics/mod.rs:35).
+ * Times every candidate tuning on the world's own scene for `frames` LOOP frames
+ * each (CUDA events on the world's stream, one warm-up frame per candidate):
+ * twelve combinations of the sort (counting, or onesweep with 6-, 8- or 11-bit
+ * digits), frames per graph launch (1, 8, 16), state gather (sorted copy or
+ * through the permutation) and frame kernel (per-stage graph or fused).  The world's
  * state, keys, permutation, cell ranges and time are saved first and restored
  * afterwards, so the simulation continues exactly as if the tuner had not run.
  * The fastest candidate is applied and written to *best; frame_ms (nullable,

@@ -240,6 +240,71 @@ def test_indirect_with_onesweep_and_switches(built_lib, cuda):
             w.set_tuning(state_gather=2)
 
 
+FUSED = {"frame_kernel": 1}
+
+
+@pytest.mark.parametrize("gather", [0, 1])
+@pytest.mark.parametrize("case", ["small", "clustered", "crowded", "degenerate", "sparse", "mixed"])
+def test_fused_frame_kernel(built_lib, cuda, case, gather):
+    """MB_FRAME_FUSED: every stage of every frame of a step in one cooperative
+    kernel (grid barriers between the stages); bit-exact like the per-stage
+    kernels, with the sorted copy and with the gather through the permutation."""
+    tuning = dict(FUSED, state_gather=gather)
+    if case == "small":
+        run_pair(scenes.workload("P-small"), 101, [1, 2, 11, 50, 101], tuning=tuning)
+    elif case == "clustered":
+        run_pair(scenes.plain_clustered(262_144, 512, clusters=4, sigma_xz=16.0, seed=9), 40, [1, 2, 11, 40],
+                 tuning=tuning)
+    elif case == "crowded":
+        run_pair(scenes.plain_uniform(51_200, 16, grid_size=1, half_map_height=8, seed=31), 4, [1, 2, 4],
+                 tuning=tuning)
+    elif case == "degenerate":
+        run_pair(scenes.plain_uniform(36_000, 2, grid_size=4, half_map_height=8, seed=32), 3, [1, 2, 3],
+                 tuning=tuning)
+    elif case == "sparse":
+        run_pair(scenes.plain_uniform(5_000, 512, seed=13), 25, [1, 2, 11, 25], tuning=tuning)
+    else:
+        sc = scenes.plain_uniform(40_000, 128, half_map_height=4, seed=34, spring=True)
+        rng = np.random.default_rng(35)
+        from bevy_millions_ball_gb300 import unpack_vfme
+        v, f, _ = unpack_vfme(sc.vfme)
+        sc.vfme = pack_vfme(v, f, rng.choice(np.array([0.5, 1.0, 1.5, 2.0, 0.7], np.float32), sc.n))
+        sc.pos_scale[:, 3] = rng.choice(np.array([0.3, 0.45, 0.5, 0.6], np.float32), sc.n)
+        run_pair(sc, 30, [1, 2, 11, 30], tuning=tuning)
+
+
+def test_fused_switches_and_settings(built_lib, cuda):
+    """Fused and per-stage frames alternate mid-run (odd and even frame counts per
+    step, so both state buffers start fused launches), with a settings change
+    and a re-upload in between; the sort algorithm must stay counting."""
+    sc = scenes.plain_uniform(60_000, 256, seed=44)
+    with World(sc.plugin) as w:
+        ow = oracle.OracleWorld(sc.plugin.to_c())
+        w.set_state(sc.pos_scale, sc.vfme)
+        ow.set_state(sc.pos_scale, sc.vfme)
+        for kernel, k in [(1, 1), (1, 3), (0, 2), (1, 7), (0, 5), (1, 16)]:
+            w.set_tuning(frame_kernel=kernel)
+            w.step(k)
+            ow.step(k)
+            w.sync()
+            compare(w, ow, ow.time)
+        new = sc.plugin.replace(e_agent=0.4, number_of_grids_one_dimension=128, grid_size=2)
+        w.set_settings(new)
+        ow.set_settings(new.to_c())
+        w.step(9)
+        ow.step(9)
+        compare(w, ow, ow.time)
+        w.set_state(sc.pos_scale, sc.vfme)
+        ow.set_state(sc.pos_scale, sc.vfme)
+        w.step(12)
+        ow.step(12)
+        compare(w, ow, ow.time)
+        with pytest.raises(MbError):
+            w.set_tuning(sort_algorithm=1)  # fused frames run the counting sort
+        with pytest.raises(MbError):
+            w.set_tuning(frame_kernel=2)
+
+
 def test_full_size_1m_properties(built_lib, cuda):
     """Size-independent properties after many frames at full size."""
     sc = scenes.workload("P-1M")
@@ -404,7 +469,8 @@ def test_autotune_keeps_the_frame_sequence(built_lib, cuda):
         fastest = min(res["candidates"], key=lambda c: c["ms_per_frame"])
         assert res["best"] == {k: fastest[k] for k in res["best"]}
         t = w.tuning
-        assert (t.sort_algorithm, t.digit_bits_max, t.frames_per_launch) == tuple(res["best"].values())
+        assert (t.sort_algorithm, t.digit_bits_max, t.frames_per_launch, t.state_gather,
+                t.frame_kernel) == tuple(res["best"].values())
         assert w.time == 5
         compare(w, ow, 5)
         w.step(21)
