@@ -276,6 +276,10 @@ def run_ours(args, rank, world_size, local_rank):
     w.set_profiling(False)
     value = world_size * n * args.steps / (total_ms * 1e-3)
     kernels = w.kernels_per_frame
+    # candidate pairs the physics pass tests per frame (the last profiled frame's cell ranges)
+    from bevy_millions_ball_gb300 import stats as mbstats
+    dbg = w.debug()
+    pair_tests = mbstats.candidate_tests(dbg["start"], dbg["close"], p.number_of_grids_one_dimension)
 
     # e2e through the public API with host buffers (pinned)
     e2e = None
@@ -326,6 +330,20 @@ def run_ours(args, rank, world_size, local_rank):
                   "achieved_gbs": frame_bytes / (total_ms / args.steps * 1e-3) / 1e9,
                   "frac": frame_bytes / (total_ms / args.steps * 1e-3) / 1e9 / hbm},
     }
+    # pair-test rate of the physics pass against an issue ceiling: one candidate
+    # test is at least 10 lane-instructions (3 differences, the squared distance
+    # in 3 multiply/FMA steps, the bound FMA, compare, mask), and an SM issues 4
+    # warp-instructions (128 lane-instructions) per clock
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    sm_mhz = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("sm_max_mhz", 2070.0)) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else 2070.0
+    test_ceiling = props.multi_processor_count * 128 * sm_mhz * 1e6 / 10.0
+    pairs = {"tests_per_frame": pair_tests, "tests_per_sphere": pair_tests / n,
+             "achieved_per_s": pair_tests / (phys_ms * 1e-3), "ceiling_per_s": test_ceiling,
+             "frac": pair_tests / (phys_ms * 1e-3) / test_ceiling,
+             "how": "candidate pairs of the 3 x 3 cell neighbourhoods from the last profiled frame's cell "
+                    "ranges, over the physics kernel's mean event time; ceiling = SMs x 128 lane-instructions "
+                    "per clock x max SM clock / 10 lane-instructions per test"}
     cpu = None
     if world_size == 1 and not args.no_cpu_baseline:
         v, frames, el, thr = cpu_oracle_run(sc, args.cpu_seconds)
@@ -348,6 +366,7 @@ def run_ours(args, rank, world_size, local_rank):
                       "how": "CUDA events inside the frame graph, on the world's stream, in a second pass of "
                              f"{prof_frames} frames right after the timed region"},
         "roofline": roofline,
+        "pair_tests": pairs,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(kernels * args.steps),

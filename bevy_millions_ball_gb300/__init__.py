@@ -265,7 +265,7 @@ class World:
         self._check(self._lib.mb_autotune(self._h, frames, C.byref(best), ms, tried))
         desc = lambda t: {"sort_algorithm": t.sort_algorithm, "digit_bits_max": t.digit_bits_max,
                           "frames_per_launch": t.frames_per_launch, "state_gather": t.state_gather,
-                          "frame_kernel": t.frame_kernel}
+                          "frame_kernel": t.frame_kernel, "collide_block": t.collide_block}
         return {"best": desc(best), "candidates": [dict(desc(t), ms_per_frame=float(m)) for t, m in zip(tried, ms)]}
 
     # -- state

@@ -65,7 +65,7 @@ class MbTuning(C.Structure):
 MB_SORT_COUNTING, MB_SORT_ONESWEEP = 0, 1
 MB_GATHER_COPY, MB_GATHER_INDIRECT = 0, 1
 MB_FRAME_GRAPH, MB_FRAME_FUSED = 0, 1
-MB_TUNE_CANDIDATES = 12
+MB_TUNE_CANDIDATES = 16
 
 
 class MbServerConfig(C.Structure):

@@ -230,11 +230,11 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
     } else if (indirect(w)) {
         e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->pos[cur], w->vfme[cur], w->perm,
                                     w->pos[nxt], w->vfme[nxt], w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError,
-                                    st, pdl && counting(w));
+                                    st, pdl && counting(w), w->tuning.collide_block);
     } else {
         e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->spos, w->svfme, nullptr, w->pos[nxt],
                                     w->vfme[nxt], w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError, st,
-                                    pdl && counting(w));
+                                    pdl && counting(w), w->tuning.collide_block);
     }
     if (e) return e;
     return mark(w, 3, st, capturing);
@@ -588,8 +588,8 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
     if (!w || !t) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
     if (t->digit_bits_max < 4 || t->digit_bits_max > mb::kMaxDigitBits)
         return fail(w, MB_ERR_INVALID_ARG, "digit_bits_max must be in [4, 11]");
-    if (t->collide_block < 32 || t->collide_block > 256 || (t->collide_block & 31u))
-        return fail(w, MB_ERR_INVALID_ARG, "collide_block must be a multiple of 32 in [32, 256]");
+    if (t->collide_block != 64u && t->collide_block != 128u && t->collide_block != 256u)
+        return fail(w, MB_ERR_INVALID_ARG, "collide_block must be 64, 128 or 256");
     if (t->sort_algorithm != MB_SORT_COUNTING && t->sort_algorithm != MB_SORT_ONESWEEP)
         return fail(w, MB_ERR_INVALID_ARG, "sort_algorithm must be MB_SORT_COUNTING or MB_SORT_ONESWEEP");
     const uint32_t fpl = t->frames_per_launch;
@@ -663,28 +663,25 @@ mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* fram
     const mb_tuning start = w->tuning;
     mb_tuning cand[MB_TUNE_CANDIDATES];
     {
-        // {sort, digit bits, frames per graph launch, state gather, frame kernel}
-        const uint32_t c5[MB_TUNE_CANDIDATES][5] = {
-            {MB_SORT_COUNTING, 8u, 1u, MB_GATHER_COPY, MB_FRAME_GRAPH},
-            {MB_SORT_COUNTING, 8u, 8u, MB_GATHER_COPY, MB_FRAME_GRAPH},
-            {MB_SORT_COUNTING, 8u, 16u, MB_GATHER_COPY, MB_FRAME_GRAPH},
-            {MB_SORT_COUNTING, 8u, 8u, MB_GATHER_COPY, MB_FRAME_FUSED},
-            {MB_SORT_COUNTING, 8u, 8u, MB_GATHER_INDIRECT, MB_FRAME_GRAPH},
-            {MB_SORT_COUNTING, 8u, 16u, MB_GATHER_INDIRECT, MB_FRAME_GRAPH},
-            {MB_SORT_COUNTING, 8u, 8u, MB_GATHER_INDIRECT, MB_FRAME_FUSED},
-            {MB_SORT_ONESWEEP, 6u, 8u, MB_GATHER_COPY, MB_FRAME_GRAPH},
-            {MB_SORT_ONESWEEP, 8u, 1u, MB_GATHER_COPY, MB_FRAME_GRAPH},
-            {MB_SORT_ONESWEEP, 8u, 8u, MB_GATHER_COPY, MB_FRAME_GRAPH},
-            {MB_SORT_ONESWEEP, 8u, 8u, MB_GATHER_INDIRECT, MB_FRAME_GRAPH},
-            {MB_SORT_ONESWEEP, 11u, 8u, MB_GATHER_COPY, MB_FRAME_GRAPH},
+        // {sort, digit bits, frames per graph launch, state gather, frame kernel, physics tile}
+        const uint32_t C = MB_SORT_COUNTING, O = MB_SORT_ONESWEEP, CP = MB_GATHER_COPY, IN = MB_GATHER_INDIRECT,
+                       G = MB_FRAME_GRAPH, F = MB_FRAME_FUSED;
+        const uint32_t c6[MB_TUNE_CANDIDATES][6] = {
+            {C, 8u, 1u, CP, G, 128u},  {C, 8u, 8u, CP, G, 128u},  {C, 8u, 16u, CP, G, 128u},
+            {C, 8u, 8u, CP, G, 64u},   {C, 8u, 8u, CP, G, 256u},  {C, 8u, 16u, CP, G, 256u},
+            {C, 8u, 8u, CP, F, 128u},  {C, 8u, 8u, IN, G, 128u},  {C, 8u, 16u, IN, G, 128u},
+            {C, 8u, 8u, IN, G, 256u},  {C, 8u, 8u, IN, F, 128u},  {O, 6u, 8u, CP, G, 128u},
+            {O, 8u, 1u, CP, G, 128u},  {O, 8u, 8u, CP, G, 128u},  {O, 8u, 8u, IN, G, 128u},
+            {O, 11u, 8u, CP, G, 128u},
         };
         for (uint32_t c = 0; c < MB_TUNE_CANDIDATES; ++c) {
             cand[c] = start;
-            cand[c].sort_algorithm = c5[c][0];
-            cand[c].digit_bits_max = c5[c][1];
-            cand[c].frames_per_launch = c5[c][2];
-            cand[c].state_gather = c5[c][3];
-            cand[c].frame_kernel = c5[c][4];
+            cand[c].sort_algorithm = c6[c][0];
+            cand[c].digit_bits_max = c6[c][1];
+            cand[c].frames_per_launch = c6[c][2];
+            cand[c].state_gather = c6[c][3];
+            cand[c].frame_kernel = c6[c][4];
+            cand[c].collide_block = c6[c][5];
         }
     }
     // save what the frames overwrite

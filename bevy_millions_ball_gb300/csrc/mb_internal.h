@@ -227,11 +227,12 @@ cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t*
 // sorted slot j, a copy the sort wrote); otherwise they hold it in the previous
 // frame's slot order and sorted slot j is spos[perm[j]].  `bands` is the band
 // table the sort wrote for this order.
-// `pdl`: launched as a programmatic dependent of the kernel before it.
+// `pdl`: launched as a programmatic dependent of the kernel before it.  tile:
+// slots per thread block (64, 128 or 256).
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                 const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
                                 uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
-                                cudaStream_t st, bool pdl = false);
+                                cudaStream_t st, bool pdl = false, uint32_t tile = kPhysicsTile);
 // LOOP frames of one world as a single cooperative kernel (all stages of every
 // frame, separated by grid barriers): `frames` frames from state buffer `cur`
 // (the last one lands in cur ^ (frames & 1)), counting sort, sorted copy or

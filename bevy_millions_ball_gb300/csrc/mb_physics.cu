@@ -249,8 +249,14 @@ __global__ void __launch_bounds__(256)
 // Bands of at most kBandCap slots are copied to shared memory with TMA bulk
 // copies (cp.async.bulk, completion on one mbarrier); wider bands (a tile
 // spanning a row boundary) are read from global memory instead.
-constexpr int kTileThreads = kPhysicsTile;
-constexpr uint32_t kBandCap = 2 * kTileThreads;
+constexpr int kTileThreads = kPhysicsTile;  // slots per tile (batched and fused passes: always)
+// Slots a staged band holds, for tiles of kTile slots (the world's collide_block:
+// 64, 128 or 256).
+template <uint32_t kTile>
+__host__ __device__ constexpr uint32_t band_cap() {
+    return kTile == 256u ? 384u : 2u * kTile;
+}
+constexpr uint32_t kBandCap = band_cap<kTileThreads>();
 constexpr uint32_t kBandPad = 8;  // >= the widest look-ahead of the contact walk, minus one
 constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier wait (error flag on expiry)
 constexpr uint32_t kGatherUnroll = 2;      // band entries a thread gathers per step (loads in flight)
@@ -405,11 +411,11 @@ __device__ __forceinline__ void row_bounds(uint32_t N, const uint32_t* __restric
 // One sphere's LOOP step (physics.wgsl:57-90) at sorted slot i, state `a`
 // unpacked from it: Verlet, contacts against its candidate rows, jitter, walls,
 // clamp, pack, store, new key and its counts.  The bands of its tile are staged
-// in b_pos/b_vfme ([3][kBandCap]: band 0 row below, 1 own row, 2 row above; band
+// in b_pos/b_vfme ([3][kCap]: band 0 row below, 1 own row, 2 row above; band
 // b holds slots [b_lo[b], b_lo[b] + b_cnt[b])); rows outside them are read from
 // spos/svfme (through perm when kIndirect).  base_a / base_c: the scene's first
 // slot and cell (0 for a world).
-template <bool kIndirect, bool kCg>
+template <bool kIndirect, bool kCg, uint32_t kCap>
 __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32_t i, uint32_t n, uint32_t base_a,
                                             uint32_t base_c, const uint32_t (&lo)[3], const uint32_t (&hi)[3],
                                             const float4* b_pos, const uint4* b_vfme, const uint32_t* b_lo,
@@ -431,7 +437,7 @@ __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32
             c[r] = h > lo[r] ? h - lo[r] : 0u;
             if (r == 0 && !(i >= lo[0] && i < lo[0] + c[0])) c[0] = 0u;  // inconsistent input: drop
             shared = shared && (c[r] == 0u || (lo[r] >= b_lo[b] && h <= b_lo[b] + b_cnt[b]));
-            o_s[r] = b * kBandCap + lo[r] - b_lo[b] - start;
+            o_s[r] = b * kCap + lo[r] - b_lo[b] - start;
             o_g[r] = lo[r] - start;
             start += c[r];
         }
@@ -496,7 +502,19 @@ __device__ __forceinline__ uint32_t scene_of(const SceneDev* __restrict__ scenes
     return s;
 }
 
-// main (physics.wgsl:57-97) for one tile of kTileThreads consecutive sorted
+// Shared memory of one tile of kTile slots: bands (pos padded: the walk reads
+// past rows) and the band bounds.  (The mbarrier of the band copies is kept
+// apart, so that the fused frame kernel can reuse this memory for its other
+// stages.)
+template <uint32_t kTile>
+struct TileSmemT {
+    float4 pos[3 * band_cap<kTile>() + kBandPad];
+    uint4 vfme[3 * band_cap<kTile>()];
+    uint32_t lo[3], cnt[3];
+};
+using TileSmem = TileSmemT<kTileThreads>;
+
+// main (physics.wgsl:57-97) for one tile of kTile consecutive sorted
 // slots, one thread per slot.  agent_new(agent_index_sorted[i]) of the reference
 // is the state of sorted slot i:
 //   kIndirect = false: spos/svfme hold the state in sorted order (the sort wrote
@@ -511,24 +529,18 @@ __device__ __forceinline__ uint32_t scene_of(const SceneDev* __restrict__ scenes
 // its scene's mode: LOOP, INIT (re-pack, emit key) or HOLD (state carried over
 // unchanged, key re-emitted).  Slot indices inside a scene (the jitter hash)
 // are local, so every scene evolves exactly as it would alone.
-// Shared memory of one tile: bands (s_pos padded: the walk reads past rows) and
-// the band bounds.  (The mbarrier of the band copies is kept apart, so that the
-// fused frame kernel can reuse this memory for its other stages.)
-struct TileSmem {
-    float4 pos[3 * kBandCap + kBandPad];
-    uint4 vfme[3 * kBandCap];
-    uint32_t lo[3], cnt[3];
-};
 
-// One tile of the physics pass, run by kTileThreads threads (tid = 0..127 within
+// One tile of the physics pass, run by kTile threads (tid = 0 .. kTile-1 within
 // the group; the block's __syncthreads must be reached by every thread of the
 // block, so a block that runs two tiles side by side runs both halves through
 // this function together).  s_bar must have been initialised (copy mode);
 // bar_parity is the phase this tile's copies complete.  A tile at or past the
-// end (tile * 128 >= n) does nothing but take part in the barriers.
-template <bool kBatched, bool kIndirect, bool kCg = false>
+// end (tile * kTile >= n) does nothing but take part in the barriers.  The band
+// table holds bounds per 128-slot tile: a 256-slot tile joins two entries, a
+// 64-slot tile derives its own from its first and last cells.
+template <bool kBatched, bool kIndirect, bool kCg = false, uint32_t kTile = kTileThreads>
 __device__ __forceinline__ void physics_tile(
-    uint32_t tile, uint32_t tid, uint32_t bar_parity, TileSmem* sm, uint64_t* s_bar, const PhysParams& P1,
+    uint32_t tile, uint32_t tid, uint32_t bar_parity, TileSmemT<kTile>* sm, uint64_t* s_bar, const PhysParams& P1,
     const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene, uint32_t n,
     const uint32_t* __restrict__ offs, const uint4* __restrict__ bands, const float4* __restrict__ spos,
     const uint4* __restrict__ svfme, const uint32_t* __restrict__ perm, float4* __restrict__ pos_out0,
@@ -536,15 +548,18 @@ __device__ __forceinline__ void physics_tile(
     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
     uint32_t* __restrict__ err) {
     static_assert(!(kBatched && kIndirect), "batches stage a sorted copy");
+    static_assert(kTile == 64u || kTile == 128u || kTile == 256u, "tiles of 64, 128 or 256 slots");
+    constexpr uint32_t kCap = band_cap<kTile>();
+    const uint4* __restrict__ btab = kTile == 64u ? nullptr : bands;
     float4* const s_pos = sm->pos;
     uint4* const s_vfme = sm->vfme;
     uint32_t* const s_lo = sm->lo;
     uint32_t* const s_cnt = sm->cnt;
 
-    const uint32_t i0 = tile * kTileThreads;
+    const uint32_t i0 = tile * kTile;
     const bool tile_ok = i0 < n;
     const uint32_t i = i0 + tid;
-    const uint32_t ilast = tile_ok ? min(i0 + kTileThreads, n) - 1u : 0u;
+    const uint32_t ilast = tile_ok ? min(i0 + kTile, n) - 1u : 0u;
     const bool valid = tile_ok && i < n;
 
     // this slot's scene; its output buffer is the one its current state is not in
@@ -568,7 +583,7 @@ __device__ __forceinline__ void physics_tile(
 #pragma unroll
         for (int b = 0; b < 3; ++b) s_cnt[b] = 0u;  // nothing to stage
     }
-    if (bands && tile_ok) {  // bounds from the band table: one load (a batch: tiles inside one LOOP scene)
+    if (btab && tile_ok) {  // bounds from the band table: one load (a batch: tiles inside one LOOP scene)
         if (tid == 0) {
             bool stage = true;
             if (kBatched) {
@@ -581,19 +596,21 @@ __device__ __forceinline__ void physics_tile(
             // completed before the kernel this one follows could start (the
             // fixups in between reorder slots inside cells, never tile bounds);
             // read through L2
-            const uint4 l = stage ? __ldcg(bands + 2u * tile) : z;
-            const uint4 h = stage ? __ldcg(bands + 2u * tile + 1u) : z;
+            constexpr uint32_t kPer = kTile / kPhysicsTile;  // 128-slot table tiles per tile
+            const uint32_t tl = tile * kPer, th = min(tl + kPer - 1u, (n - 1u) / kPhysicsTile);
+            const uint4 l = stage ? __ldcg(btab + 2u * tl) : z;
+            const uint4 h = stage ? __ldcg(btab + 2u * th + 1u) : z;
             const uint32_t lo3[3] = {l.x, l.y, l.z}, hi3[3] = {h.x, h.y, h.z};
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
                 const uint32_t hb = min(hi3[b], n);
                 s_lo[b] = lo3[b];
-                s_cnt[b] = (hb > lo3[b] && hb - lo3[b] <= kBandCap) ? hb - lo3[b] : 0u;
+                s_cnt[b] = (hb > lo3[b] && hb - lo3[b] <= kCap) ? hb - lo3[b] : 0u;
             }
         }
     }
     griddep_wait();  // the sort's outputs (order, state copy) are complete and visible
-    if (!bands && tile_ok && tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
+    if (!btab && tile_ok && tid < 3) {  // band b: keys of the tile's first and last sphere, then offsets
         uint32_t lo = 0, hi = 0;
         bool stage = true;
         PhysParams Q = P;
@@ -634,7 +651,7 @@ __device__ __forceinline__ void physics_tile(
         }
         hi = min(hi, n);
         s_lo[tid] = lo;
-        s_cnt[tid] = (hi > lo && hi - lo <= kBandCap) ? hi - lo : 0u;
+        s_cnt[tid] = (hi > lo && hi - lo <= kCap) ? hi - lo : 0u;
     }
 
     // own sphere: loads issued here overlap the band set-up
@@ -651,28 +668,28 @@ __device__ __forceinline__ void physics_tile(
         // ... of the three bands laid end to end, kGatherUnroll at a time (loads
         // first, then stores)
         const uint32_t c0 = s_cnt[0], c01 = c0 + s_cnt[1], tot = c01 + s_cnt[2];
-        for (uint32_t f0 = 0; f0 < tot; f0 += kGatherUnroll * kTileThreads) {
+        for (uint32_t f0 = 0; f0 < tot; f0 += kGatherUnroll * kTile) {
             uint32_t dst[kGatherUnroll], src[kGatherUnroll];
 #pragma unroll
             for (uint32_t u = 0; u < kGatherUnroll; ++u) {
-                const uint32_t f = f0 + u * kTileThreads + tid;
+                const uint32_t f = f0 + u * kTile + tid;
                 const uint32_t b = f < c0 ? 0u : (f < c01 ? 1u : 2u);
                 const uint32_t j = f - (b == 0u ? 0u : (b == 1u ? c0 : c01));
-                dst[u] = b * kBandCap + j;
+                dst[u] = b * kCap + j;
                 src[u] = f < tot ? min(ld_in<kCg>(perm + s_lo[b] + j), n - 1u) : 0u;
             }
             float4 gp[kGatherUnroll];
             uint4 gq[kGatherUnroll];
 #pragma unroll
             for (uint32_t u = 0; u < kGatherUnroll; ++u) {
-                if (f0 + u * kTileThreads + tid < tot) {
+                if (f0 + u * kTile + tid < tot) {
                     gp[u] = ld_in<kCg>(spos + src[u]);
                     gq[u] = ld_in<kCg>(svfme + src[u]);
                 }
             }
 #pragma unroll
             for (uint32_t u = 0; u < kGatherUnroll; ++u) {
-                if (f0 + u * kTileThreads + tid < tot) {
+                if (f0 + u * kTile + tid < tot) {
                     s_pos[dst[u]] = gp[u];
                     s_vfme[dst[u]] = gq[u];
                 }
@@ -686,8 +703,8 @@ __device__ __forceinline__ void physics_tile(
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
             if (s_cnt[b]) {
-                bulk_g2s(s_pos + b * kBandCap, spos + s_lo[b], s_cnt[b] * 16u, s_bar);
-                bulk_g2s(s_vfme + b * kBandCap, svfme + s_lo[b], s_cnt[b] * 16u, s_bar);
+                bulk_g2s(s_pos + b * kCap, spos + s_lo[b], s_cnt[b] * 16u, s_bar);
+                bulk_g2s(s_vfme + b * kCap, svfme + s_lo[b], s_cnt[b] * 16u, s_bar);
             }
         }
     }
@@ -725,12 +742,12 @@ __device__ __forceinline__ void physics_tile(
     }
     if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
 
-    step_sphere<kIndirect, kCg>(P, a, i, n, base_a, base_c, lo, hi, s_pos, s_vfme, s_lo, s_cnt, spos, svfme, perm,
+    step_sphere<kIndirect, kCg, kCap>(P, a, i, n, base_a, base_c, lo, hi, s_pos, s_vfme, s_lo, s_cnt, spos, svfme, perm,
                                 pos_out, vfme_out, keys_out, hist, coarse);
 }
 
-template <bool kBatched, bool kIndirect>
-__global__ void __launch_bounds__(kTileThreads)
+template <bool kBatched, bool kIndirect, uint32_t kTile = kTileThreads>
+__global__ void __launch_bounds__(kTile)
     k_physics_frame(const __grid_constant__ PhysParams P1, const SceneDev* __restrict__ scenes,
                     const uint32_t* __restrict__ tile_scene, uint32_t n, const uint32_t* __restrict__ offs,
                     const uint4* __restrict__ bands, const float4* __restrict__ spos,
@@ -738,10 +755,10 @@ __global__ void __launch_bounds__(kTileThreads)
                     float4* __restrict__ pos_out1, uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1,
                     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
                     uint32_t* __restrict__ err) {
-    __shared__ __align__(16) TileSmem sm;
+    __shared__ __align__(16) TileSmemT<kTile> sm;
     __shared__ __align__(8) uint64_t s_bar;
     if (!kIndirect && threadIdx.x == 0) mbar_init(&s_bar, 1u);  // first copy after the tile's CTA barrier
-    physics_tile<kBatched, kIndirect>(blockIdx.x, threadIdx.x, 0u, &sm, &s_bar, P1, scenes, tile_scene, n, offs,
+    physics_tile<kBatched, kIndirect, false, kTile>(blockIdx.x, threadIdx.x, 0u, &sm, &s_bar, P1, scenes, tile_scene, n, offs,
                                       bands, spos, svfme, perm, pos_out0, pos_out1, vfme_out0, vfme_out1, keys_out,
                                       hist, coarse, err);
 }
@@ -992,19 +1009,34 @@ cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t*
     return cudaGetLastError();
 }
 
+template <uint32_t kTile>
+cudaError_t launch_physics_tiles(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
+                                 const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
+                                 uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse,
+                                 uint32_t* err, cudaStream_t st, bool pdl) {
+    const dim3 grid((n + kTile - 1u) / kTile), block(kTile);
+    if (perm)
+        return launch_pdl(pdl, k_physics_frame<false, true, kTile>, grid, block, 0, st, p, (const SceneDev*)nullptr,
+                          (const uint32_t*)nullptr, n, offs, bands, spos, svfme, perm, pos_out, (float4*)nullptr,
+                          vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
+    return launch_pdl(pdl, k_physics_frame<false, false, kTile>, grid, block, 0, st, p, (const SceneDev*)nullptr,
+                      (const uint32_t*)nullptr, n, offs, bands, spos, svfme, (const uint32_t*)nullptr, pos_out,
+                      (float4*)nullptr, vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
+}
+
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                 const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
                                 uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
-                                cudaStream_t st, bool pdl) {
+                                cudaStream_t st, bool pdl, uint32_t tile) {
     if (!n) return cudaSuccess;
-    const dim3 grid((n + kTileThreads - 1u) / kTileThreads), block(kTileThreads);
-    if (perm)
-        return launch_pdl(pdl, k_physics_frame<false, true>, grid, block, 0, st, p, (const SceneDev*)nullptr,
-                          (const uint32_t*)nullptr, n, offs, bands, spos, svfme, perm, pos_out, (float4*)nullptr,
-                          vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
-    return launch_pdl(pdl, k_physics_frame<false, false>, grid, block, 0, st, p, (const SceneDev*)nullptr,
-                      (const uint32_t*)nullptr, n, offs, bands, spos, svfme, (const uint32_t*)nullptr, pos_out,
-                      (float4*)nullptr, vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
+    if (tile == 64u)
+        return launch_physics_tiles<64u>(p, n, offs, bands, spos, svfme, perm, pos_out, vfme_out, keys_out, hist,
+                                         coarse, err, st, pdl);
+    if (tile == 256u)
+        return launch_physics_tiles<256u>(p, n, offs, bands, spos, svfme, perm, pos_out, vfme_out, keys_out, hist,
+                                          coarse, err, st, pdl);
+    return launch_physics_tiles<128u>(p, n, offs, bands, spos, svfme, perm, pos_out, vfme_out, keys_out, hist,
+                                      coarse, err, st, pdl);
 }
 
 int fused_blocks_per_sm() {

@@ -81,3 +81,20 @@ def compare(a: dict, b: dict) -> dict:
 
 def within_bounds(a: dict, b: dict) -> bool:
     return all(ok for _, _, ok in compare(a, b).values())
+
+
+def candidate_tests(start: np.ndarray, close: np.ndarray, grids: int) -> int:
+    """Candidate pairs one physics pass tests, from a frame's cell ranges.
+
+    The reference tests every sphere against every other sphere in the 3 x 3
+    cells around its own (physics.wgsl:122-160, the three row ranges of
+    handle_collisions).  With m[c] spheres in cell c and M[c] the sum of m over
+    c's 3 x 3 neighbourhood, a frame tests sum(m[c] * (M[c] - 1)) pairs.  start
+    and close are the frame's tables (0xFFFFFFFF for empty cells, close
+    inclusive)."""
+    st = np.asarray(start, np.int64).reshape(grids, grids)
+    cl = np.asarray(close, np.int64).reshape(grids, grids)
+    m = np.where(st == 0xFFFFFFFF, 0, cl - st + 1)
+    pad = np.pad(m, 1)
+    nb = sum(pad[1 + dz:1 + dz + grids, 1 + dx:1 + dx + grids] for dz in (-1, 0, 1) for dx in (-1, 0, 1))
+    return int(np.sum(m * (nb - 1)))

@@ -260,7 +260,8 @@ mb_status mb_sort_static_status(void* cuda_stream);
 /* Per-world kernel choices (the autotuner's knobs). */
 typedef struct mb_tuning {
     uint32_t digit_bits_max;   /* widest radix digit of the onesweep sort, 4..11 */
-    uint32_t collide_block;    /* reserved: the physics kernel's tile is fixed at 128 slots */
+    uint32_t collide_block;    /* sorted slots per thread block of the physics pass: 64, 128
+                                  (default) or 256; MB_FRAME_FUSED frames run 128 */
     uint32_t sort_algorithm;   /* MB_SORT_COUNTING (default) or MB_SORT_ONESWEEP */
     uint32_t frames_per_launch; /* LOOP frames captured per graph launch in multi-frame steps:
                                    1, 2, 4, 8 (default; 0 reads as 8) or 16 */
@@ -322,9 +323,10 @@ mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float 
  * workgroup shapes, NUMBER_OF_THREADS_PER_WORKGROUP = 256 at src/physics/mod.rs:35).
  * Times every candidate tuning on the world's own scene for `frames` LOOP frames
  * each (CUDA events on the world's stream, one warm-up frame per candidate):
- * twelve combinations of the sort (counting, or onesweep with 6-, 8- or 11-bit
+ * sixteen combinations of the sort (counting, or onesweep with 6-, 8- or 11-bit
  * digits), frames per graph launch (1, 8, 16), state gather (sorted copy or
- * through the permutation) and frame kernel (per-stage graph or fused).  The world's
+ * through the permutation), frame kernel (per-stage graph or fused) and physics
+ * tile (64, 128 or 256 slots per thread block).  The world's
  * state, keys, permutation, cell ranges and time are saved first and restored
  * afterwards, so the simulation continues exactly as if the tuner had not run.
  * The fastest candidate is applied and written to *best; frame_ms (nullable,
@@ -332,7 +334,7 @@ mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float 
  * order of tried[] (nullable, same length).  Needs a frame to have run since the
  * last upload (MB_ERR_NOT_READY otherwise).  Allocates temporary device memory.
  */
-#define MB_TUNE_CANDIDATES 12u
+#define MB_TUNE_CANDIDATES 16u
 mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* frame_ms, mb_tuning* tried);
 
 /*

@@ -240,6 +240,31 @@ def test_indirect_with_onesweep_and_switches(built_lib, cuda):
             w.set_tuning(state_gather=2)
 
 
+@pytest.mark.parametrize("tile", [64, 256])
+@pytest.mark.parametrize("case", ["small", "clustered", "crowded", "degenerate", "sparse"])
+def test_collide_block_sizes(built_lib, cuda, case, tile):
+    """Physics tiles of 64 and 256 slots per thread block (collide_block), with
+    the sorted copy and with the gather through the permutation: bit-exact."""
+    for gather in (0, 1):
+        tuning = {"collide_block": tile, "state_gather": gather}
+        if case == "small":
+            run_pair(scenes.workload("P-small"), 51, [1, 2, 11, 51], tuning=tuning)
+        elif case == "clustered":
+            run_pair(scenes.plain_clustered(262_144, 512, clusters=4, sigma_xz=16.0, seed=9), 20, [1, 2, 20],
+                     tuning=tuning)
+        elif case == "crowded":
+            run_pair(scenes.plain_uniform(51_200, 16, grid_size=1, half_map_height=8, seed=31), 4, [1, 2, 4],
+                     tuning=tuning)
+        elif case == "degenerate":
+            run_pair(scenes.plain_uniform(36_000, 2, grid_size=4, half_map_height=8, seed=32), 3, [1, 2, 3],
+                     tuning=tuning)
+        else:
+            run_pair(scenes.plain_uniform(5_000 + tile, 512, seed=13), 25, [1, 2, 25], tuning=tuning)
+    with World(scenes.plain_uniform(1000, 32).plugin) as w:
+        with pytest.raises(MbError):
+            w.set_tuning(collide_block=96)
+
+
 FUSED = {"frame_kernel": 1}
 
 
@@ -465,12 +490,12 @@ def test_autotune_keeps_the_frame_sequence(built_lib, cuda):
         w.step(5)
         ow.step(5)
         res = w.autotune(frames=8)
-        assert len(res["candidates"]) == 12 and all(c["ms_per_frame"] > 0 for c in res["candidates"])
+        assert len(res["candidates"]) == 16 and all(c["ms_per_frame"] > 0 for c in res["candidates"])
         fastest = min(res["candidates"], key=lambda c: c["ms_per_frame"])
         assert res["best"] == {k: fastest[k] for k in res["best"]}
         t = w.tuning
         assert (t.sort_algorithm, t.digit_bits_max, t.frames_per_launch, t.state_gather,
-                t.frame_kernel) == tuple(res["best"].values())
+                t.frame_kernel, t.collide_block) == tuple(res["best"].values())
         assert w.time == 5
         compare(w, ow, 5)
         w.step(21)

@@ -54,3 +54,25 @@ def test_diverged_runs_keep_their_statistics():
     assert a["contacts"] > 10_000
     cmp = stats.compare(a, b)
     assert all(ok for _, _, ok in cmp.values()), cmp
+
+
+def test_candidate_tests_counts_the_reference_neighbourhood():
+    """Brute-force count of (sphere, candidate) pairs in the 3 x 3 cells around
+    each sphere's cell against the closed form."""
+    rng = np.random.default_rng(7)
+    N = 9
+    cells = rng.integers(0, N * N, 300)
+    keys = np.sort(cells)
+    start = np.full(N * N, 0xFFFFFFFF, np.uint32)
+    close = np.full(N * N, 0xFFFFFFFF, np.uint32)
+    for c in np.unique(keys):
+        idx = np.flatnonzero(keys == c)
+        start[c], close[c] = idx[0], idx[-1]
+    want = 0
+    for c in keys:
+        cz, cx = divmod(int(c), N)
+        for d in keys:
+            dz, dx = divmod(int(d), N)
+            want += abs(dz - cz) <= 1 and abs(dx - cx) <= 1
+        want -= 1
+    assert stats.candidate_tests(start, close, N) == want
