@@ -451,6 +451,30 @@ class Batch:
         self._check(self._lib.mb_batch_memory(self._h, C.byref(b)))
         return b.value
 
+    @property
+    def tuning(self) -> MbTuning:
+        t = MbTuning()
+        self._check(self._lib.mb_batch_get_tuning(self._h, C.byref(t)))
+        return t
+
+    def set_tuning(self, frames_per_launch: int | None = None, collide_block: int | None = None) -> None:
+        t = self.tuning
+        if frames_per_launch is not None:
+            t.frames_per_launch = frames_per_launch
+        if collide_block is not None:
+            t.collide_block = collide_block
+        self._check(self._lib.mb_batch_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self, frames: int = 16) -> dict:
+        """mb_batch_autotune: time frames_per_launch x collide_block on the pool's own
+        scenes (states restored), apply the fastest; returns it and every candidate's
+        ms/frame."""
+        n = _abi.MB_BATCH_TUNE_CANDIDATES
+        best, ms, tried = MbTuning(), (C.c_float * n)(), (MbTuning * n)()
+        self._check(self._lib.mb_batch_autotune(self._h, frames, C.byref(best), ms, tried))
+        desc = lambda t: {"frames_per_launch": t.frames_per_launch, "collide_block": t.collide_block}
+        return {"best": desc(best), "candidates": [dict(desc(t), ms_per_frame=float(m)) for t, m in zip(tried, ms)]}
+
     def close(self) -> None:
         if self._h:
             self._lib.mb_batch_destroy(self._h)

@@ -66,6 +66,7 @@ MB_SORT_COUNTING, MB_SORT_ONESWEEP = 0, 1
 MB_GATHER_COPY, MB_GATHER_INDIRECT = 0, 1
 MB_FRAME_GRAPH, MB_FRAME_FUSED = 0, 1
 MB_TUNE_CANDIDATES = 16
+MB_BATCH_TUNE_CANDIDATES = 9
 
 
 class MbServerConfig(C.Structure):
@@ -133,6 +134,9 @@ SIGNATURES = {
     "mb_batch_sync": (C.c_int, [vp]),
     "mb_batch_time": (i64, [vp, u32]),
     "mb_batch_get_debug": (C.c_int, [vp, u32, vp, vp, vp, vp, C.c_int]),
+    "mb_batch_get_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),
+    "mb_batch_set_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),
+    "mb_batch_autotune": (C.c_int, [vp, u32, C.POINTER(MbTuning), C.POINTER(C.c_float), C.POINTER(MbTuning)]),
     "mb_server_create": (C.c_int, [C.POINTER(MbServerConfig), vp, C.POINTER(vp)]),
     "mb_server_destroy": (C.c_int, [vp]),
     "mb_server_submit_create": (C.c_int, [vp, C.POINTER(MbSettings), vp, vp, C.POINTER(u32), C.POINTER(C.c_uint64)]),

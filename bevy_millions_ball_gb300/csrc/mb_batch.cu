@@ -103,6 +103,7 @@ struct mb_batch {
     bool layout_dirty = true;             // scene ranges changed: re-upload tiles, re-capture
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     std::vector<uint32_t> last_modes;
+    mb_tuning tuning{};                   // frames_per_launch (chain length) and collide_block are used
     std::string err;
 };
 
@@ -265,7 +266,7 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st, bool may_init) {
         return e;
     if ((e = mb::launch_physics_batch(b->d_scenes, b->d_tile_scene, b->n_total, b->offs, b->bands, b->spos, b->svfme,
                                       b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->keys, b->cnt.hist,
-                                      b->cnt.coarse, b->ctl + mb::kCtlError, st)))
+                                      b->cnt.coarse, b->ctl + mb::kCtlError, st, b->tuning.collide_block)))
         return e;
     // INIT scenes emitted cell counts only: their tile counts from the cell counts
     if (may_init &&
@@ -276,15 +277,17 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st, bool may_init) {
     return cudaGetLastError();
 }
 
-// graph[0]: one frame; graph[1]: kChainFrames frames back to back (used while no
-// scene changes mode; even, so every scene ends in the buffer it started from).
-constexpr uint32_t kChainFrames = 8;
+// graph[0]: one frame; graph[1]: chain_frames(b) frames back to back (used while
+// no scene changes mode; 1, 2, 4, 8 (default) or 16).
+uint32_t chain_frames(const mb_batch* b) {
+    return b->tuning.frames_per_launch ? b->tuning.frames_per_launch : 8u;
+}
 
 cudaError_t build_graph(mb_batch* b, int which = 0) {
     cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e) return e;
     cudaError_t fe = cudaSuccess;
-    for (uint32_t f = 0; f < (which ? kChainFrames : 1u) && !fe; ++f) fe = enqueue_frame(b, b->cap_stream, !which);
+    for (uint32_t f = 0; f < (which ? chain_frames(b) : 1u) && !fe; ++f) fe = enqueue_frame(b, b->cap_stream, !which);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(b->cap_stream, &g);
     if (fe) {
@@ -304,11 +307,11 @@ cudaError_t recount(mb_batch* b) {
     return e;
 }
 
-// One frame over every scene (frames = 1), or kChainFrames frames with the same
-// modes and no INIT among them (frames = kChainFrames); modes[i] is scene i's mode.
+// One frame over every scene (frames = 1), or chain_frames(b) frames with the same
+// modes and no INIT among them; modes[i] is scene i's mode.
 mb_status run_frame(mb_batch* b, const std::vector<uint32_t>& modes, uint32_t frames = 1) {
     cudaError_t e;
-    const int which = frames == 1 ? 0 : 1;
+    const int which = frames == 1 ? 0 : 1;  // (a chain of one frame is graph 0)
     if (!b->counts_valid && (e = recount(b))) return bcuda(b, "batch recount", e);
     if ((e = sync_tables(b, modes))) return bcuda(b, "batch tables", e);
     if (!b->graph[which] && (e = build_graph(b, which))) return bcuda(b, "batch capture", e);
@@ -377,6 +380,9 @@ mb_status mb_batch_create(const mb_settings* scenes, uint32_t num_scenes, uint32
     b->cap_cells = (uint32_t)cells;
     b->cap_scenes = std::max(num_scenes, capacity_scenes);
     b->stream = (cudaStream_t)cuda_stream;
+    b->tuning.digit_bits_max = 8;
+    b->tuning.collide_block = mb::kPhysicsTile;
+    b->tuning.frames_per_launch = 8;
     cudaError_t e = alloc_pool(b);
     if (e) {
         mb_status st = bcuda(nullptr, "mb_batch_create", e);
@@ -452,7 +458,8 @@ mb_status mb_batch_step(mb_batch* b, uint32_t k) {
             modes[i] = !run ? mb::kModeHold : (h.init_pending ? mb::kModeInit : mb::kModeLoop);
             init = init || modes[i] == mb::kModeInit;
         }
-        const uint32_t frames = (!init && k - f >= kChainFrames) ? kChainFrames : 1u;
+        const uint32_t cf = chain_frames(b);
+        const uint32_t frames = (!init && cf > 1u && k - f >= cf) ? cf : 1u;
         mb_status st = run_frame(b, modes, frames);
         if (st != MB_OK) return st;
         f += frames;
@@ -508,6 +515,134 @@ mb_status mb_batch_get_debug(mb_batch* b, uint32_t scene, uint32_t* keys, uint32
         cudaFree(tmp);
     }
     if (e) return bcuda(b, "batch debug", e);
+    return MB_OK;
+}
+
+mb_status mb_batch_get_tuning(const mb_batch* b, mb_tuning* out) {
+    if (!b || !out) return MB_ERR_INVALID_ARG;
+    *out = b->tuning;
+    return MB_OK;
+}
+
+mb_status mb_batch_set_tuning(mb_batch* b, const mb_tuning* t) {
+    if (!b || !t) return bfail(b, MB_ERR_INVALID_ARG, "NULL argument");
+    const uint32_t fpl = t->frames_per_launch;
+    if (!(fpl == 0 || fpl == 1 || fpl == 2 || fpl == 4 || fpl == 8 || fpl == 16))
+        return bfail(b, MB_ERR_INVALID_ARG, "frames_per_launch must be 0, 1, 2, 4, 8 or 16");
+    if (t->collide_block != 64u && t->collide_block != 128u && t->collide_block != 256u)
+        return bfail(b, MB_ERR_INVALID_ARG, "collide_block must be 64, 128 or 256");
+    if (t->sort_algorithm != MB_SORT_COUNTING || t->state_gather != MB_GATHER_COPY ||
+        t->frame_kernel != MB_FRAME_GRAPH)
+        return bfail(b, MB_ERR_INVALID_ARG,
+                     "a batch runs the counting sort, the sorted copy and per-stage kernels");
+    drop_graphs(b);
+    b->tuning = *t;
+    return MB_OK;
+}
+
+mb_status mb_batch_autotune(mb_batch* b, uint32_t frames, mb_tuning* best, float* frame_ms, mb_tuning* tried) {
+    if (!b || !best) return bfail(b, MB_ERR_INVALID_ARG, "NULL argument");
+    if (frames == 0) return bfail(b, MB_ERR_INVALID_ARG, "frames must be positive");
+    if (b->scenes.empty()) return bfail(b, MB_ERR_NOT_READY, "the batch has no scene");
+    for (const SceneHost& h : b->scenes)
+        if (!h.has_state || h.init_pending || !h.frame_done)
+            return bfail(b, MB_ERR_NOT_READY, "run a frame of every scene before autotuning");
+    const mb_tuning start = b->tuning;
+    mb_tuning cand[MB_BATCH_TUNE_CANDIDATES];
+    {
+        const uint32_t fpl[3] = {1u, 8u, 16u}, tiles[3] = {64u, 128u, 256u};
+        uint32_t c = 0;
+        for (uint32_t f : fpl)
+            for (uint32_t t : tiles) {
+                cand[c] = start;
+                cand[c].frames_per_launch = f;
+                cand[c].collide_block = t;
+                ++c;
+            }
+    }
+    // save what the frames overwrite: both state buffers (scenes keep their own
+    // parity), keys, order, cell offsets and the host view of every scene
+    const size_t A = b->n_total, Cc = (size_t)b->cells_total + 1u;
+    float4* pos[2] = {nullptr, nullptr};
+    uint4* vfme[2] = {nullptr, nullptr};
+    uint32_t *keys = nullptr, *perm = nullptr, *offs = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    auto release = [&]() {
+        for (int i = 0; i < 2; ++i) {
+            cudaFree(pos[i]);
+            cudaFree(vfme[i]);
+        }
+        cudaFree(keys);
+        cudaFree(perm);
+        cudaFree(offs);
+        for (auto& x : ev)
+            if (x) cudaEventDestroy(x);
+    };
+    const std::vector<SceneHost> saved = b->scenes;
+    auto snap = [&](bool save) -> cudaError_t {
+        cudaError_t r;
+        auto cp = [&](void* a, void* d, size_t bytes) {
+            return cudaMemcpyAsync(save ? a : d, save ? d : a, bytes, cudaMemcpyDeviceToDevice, b->stream);
+        };
+        for (int i = 0; i < 2; ++i) {
+            if ((r = cp(pos[i], b->pos[i], sizeof(float4) * A))) return r;
+            if ((r = cp(vfme[i], b->vfme[i], sizeof(uint4) * A))) return r;
+        }
+        if ((r = cp(keys, b->keys, sizeof(uint32_t) * A))) return r;
+        if ((r = cp(perm, b->perm, sizeof(uint32_t) * A))) return r;
+        return cp(offs, b->offs, sizeof(uint32_t) * Cc);
+    };
+    auto restore_host = [&]() {
+        b->scenes = saved;
+        b->last_modes.clear();  // the scene table (parities) is uploaded again before the next frame
+        b->counts_valid = false;
+    };
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 2 && !e; ++i) {
+        if (!e) e = cudaMalloc(&pos[i], sizeof(float4) * A);
+        if (!e) e = cudaMalloc(&vfme[i], sizeof(uint4) * A);
+    }
+    if (!e) e = cudaMalloc(&keys, sizeof(uint32_t) * A);
+    if (!e) e = cudaMalloc(&perm, sizeof(uint32_t) * A);
+    if (!e) e = cudaMalloc(&offs, sizeof(uint32_t) * Cc);
+    if (!e) e = cudaEventCreate(&ev[0]);
+    if (!e) e = cudaEventCreate(&ev[1]);
+    if (!e) e = snap(true);
+    if (e) {
+        release();
+        return bcuda(b, "mb_batch_autotune", e);
+    }
+    float best_ms = 0.0f;
+    uint32_t best_i = 0;
+    mb_status st = MB_OK;
+    for (uint32_t c = 0; c < MB_BATCH_TUNE_CANDIDATES && st == MB_OK; ++c) {
+        if ((e = snap(false))) break;  // every candidate starts from the saved frame
+        restore_host();
+        if ((st = mb_batch_set_tuning(b, &cand[c])) != MB_OK) break;
+        if ((st = mb_batch_step(b, 1)) != MB_OK) break;  // warm-up: graphs built
+        if ((e = cudaEventRecord(ev[0], b->stream))) break;
+        if ((st = mb_batch_step(b, frames)) != MB_OK) break;
+        if ((e = cudaEventRecord(ev[1], b->stream)) || (e = cudaEventSynchronize(ev[1]))) break;
+        float ms = 0.0f;
+        if ((e = cudaEventElapsedTime(&ms, ev[0], ev[1]))) break;
+        ms /= (float)frames;
+        if (frame_ms) frame_ms[c] = ms;
+        if (tried) tried[c] = cand[c];
+        if (c == 0 || ms < best_ms) {
+            best_ms = ms;
+            best_i = c;
+        }
+    }
+    cudaError_t e2 = snap(false);
+    restore_host();
+    const mb_status st2 = mb_batch_set_tuning(b, (e || st != MB_OK) ? &start : &cand[best_i]);
+    if (!e2) e2 = cudaStreamSynchronize(b->stream);
+    release();
+    if (e) return bcuda(b, "mb_batch_autotune", e);
+    if (st != MB_OK) return st;
+    if (e2) return bcuda(b, "mb_batch_autotune", e2);
+    if (st2 != MB_OK) return st2;
+    *best = cand[best_i];
     return MB_OK;
 }
 
@@ -652,9 +787,8 @@ void worker_loop(mb_server* s) {
                 if (run) least = std::min<int64_t>(least, sc.pending);
             }
             // a chain of frames while every running scene owes that many and none is new
-            const uint32_t chain = (!init && least >= (int64_t)kChainFrames && frames - f >= (int64_t)kChainFrames)
-                                       ? kChainFrames
-                                       : 1u;
+            const int64_t cf = (int64_t)chain_frames(b);
+            const uint32_t chain = (!init && cf > 1 && least >= cf && frames - f >= cf) ? (uint32_t)cf : 1u;
             for (size_t i = 0; i < S; ++i)
                 if (modes[i] == mb::kModeLoop) agent_steps += (uint64_t)b->scenes[i].n * chain;
             if (run_frame(b, modes, chain) != MB_OK) {

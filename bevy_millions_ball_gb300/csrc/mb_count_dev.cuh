@@ -22,6 +22,7 @@ namespace {
 // belongs to one scene; its base is that scene's first slot plus the coarse
 // counts of the scene's earlier tiles, and tiles of HOLD scenes are left alone.
 // One chunk (kScanThreads threads); s_warp, s_base: kScanThreads / 32 words each.
+// A block that runs several chunks must synchronise between them.
 template <bool kScenes, bool kCg = false>
 __device__ __forceinline__ void scan_chunk(uint32_t chunk, const uint32_t* __restrict__ hist,
                                            const uint32_t* __restrict__ coarse, uint32_t cells,
@@ -32,7 +33,6 @@ __device__ __forceinline__ void scan_chunk(uint32_t chunk, const uint32_t* __res
     constexpr int W = kScanThreads / 32;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t c0 = chunk * kScanChunk, tile = c0 / kScanTile;
-    __syncthreads();  // a previous chunk's partial sums are read (when one thread block runs several)
     if (chunk == 0 && tid < (uint32_t)kFixLists) fix_ctl[tid] = 0u;  // fixup lists of this frame start empty
     const uint32_t base = c0 + tid * kScanItems;
 
@@ -196,7 +196,8 @@ __device__ __forceinline__ void scatter_range(uint32_t vb, uint32_t nvb, const u
 constexpr uint32_t kCollectThreads = 256, kCollectWords = kCollectThreads / 4u;
 
 // One block of the listing (kCollectThreads threads); s_cell: kFixLists x
-// kCollectWords * 32 words, s_n and s_base: kFixLists words each.
+// kCollectWords * 32 words, s_n and s_base: kFixLists words each.  A block that
+// runs several must synchronise between them.
 template <bool kCg = false>
 __device__ __forceinline__ void collect_block(uint32_t vb, const uint32_t* __restrict__ fix_bits,
                                               const uint32_t* __restrict__ keys, uint32_t n,
@@ -204,7 +205,6 @@ __device__ __forceinline__ void collect_block(uint32_t vb, const uint32_t* __res
                                               uint32_t (*s_cell)[kCollectWords * 32u], uint32_t* s_n,
                                               uint32_t* s_base) {
     const uint32_t tid = threadIdx.x;
-    __syncthreads();  // a previous block's lists are read out (when one thread block runs several)
     if (tid < (uint32_t)kFixLists) s_n[tid] = 0u;
     __syncthreads();
     const uint32_t words = (n + 31u) / 32u;

@@ -274,7 +274,8 @@ cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_sc
                                  const uint32_t* offs, const uint4* bands, const float4* spos, const uint4* svfme,
                                  float4* pos_buf0,
                                  float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1, uint32_t* keys,
-                                 uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st);
+                                 uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st,
+                                 uint32_t tile = kPhysicsTile);
 
 
 // Counting sort of cell keys (mb_count.cu).

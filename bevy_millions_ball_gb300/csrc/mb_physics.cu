@@ -567,7 +567,7 @@ __device__ __forceinline__ void physics_tile(
     float4* __restrict__ pos_out = pos_out0;
     uint4* __restrict__ vfme_out = vfme_out0;
     if (kBatched && tile_ok) {
-        const uint32_t first = __ldg(tile_scene + tile);
+        const uint32_t first = __ldg(tile_scene + tile * kTile / kPhysicsTile);
         sc = scene_of(scenes, first, valid ? i : ilast);
         base_a = scenes[sc].agent_base;
         base_c = scenes[sc].cell_base;
@@ -587,7 +587,7 @@ __device__ __forceinline__ void physics_tile(
         if (tid == 0) {
             bool stage = true;
             if (kBatched) {
-                const uint32_t first = __ldg(tile_scene + tile);
+                const uint32_t first = __ldg(tile_scene + tile * kTile / kPhysicsTile);
                 const uint32_t sf = scene_of(scenes, first, i0), sl = scene_of(scenes, first, ilast);
                 stage = sf == sl && __ldg(&scenes[sf].mode) == kModeLoop;
             }
@@ -616,7 +616,7 @@ __device__ __forceinline__ void physics_tile(
         PhysParams Q = P;
         uint32_t qc = base_c;
         if (kBatched) {  // stage only tiles inside one LOOP scene
-            const uint32_t first = __ldg(tile_scene + tile);
+            const uint32_t first = __ldg(tile_scene + tile * kTile / kPhysicsTile);
             const uint32_t sf = scene_of(scenes, first, i0), sl = scene_of(scenes, first, ilast);
             stage = sf == sl && scenes[sf].mode == kModeLoop;
             Q = scenes[sf].P;
@@ -866,17 +866,21 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_frame_fused(const __grid_c
     for (uint32_t f = 0; f < A.frames; ++f) {
         const uint32_t cur = A.cur ^ (f & 1u), nxt = cur ^ 1u;
         // cell offsets from the counts the previous frame emitted
-        for (uint32_t vb = blockIdx.x; vb < A.chunks; vb += gridDim.x)
+        for (uint32_t vb = blockIdx.x; vb < A.chunks; vb += gridDim.x) {
             scan_chunk<false, true>(vb, A.hist, A.coarse, A.cells, A.offs, A.lists.ctl, nullptr, nullptr, S.scan.warp,
                                     S.scan.base);
+            __syncthreads();  // partial sums read before the next chunk writes them
+        }
         if (!grid_barrier(A.bar, A.err, &s_flag)) return;
         scatter_range<true>(blockIdx.x, gridDim.x, A.keys, A.n, A.hist, A.perm, A.pos[cur], A.vfme[cur],
                             kIndirect ? nullptr : A.spos, kIndirect ? nullptr : A.svfme, A.offs, A.bands, A.P.N,
                             A.fix_bits);
         if (!grid_barrier(A.bar, A.err, &s_flag)) return;
-        for (uint32_t vb = blockIdx.x; vb < A.collect_blocks; vb += gridDim.x)
+        for (uint32_t vb = blockIdx.x; vb < A.collect_blocks; vb += gridDim.x) {
             collect_block<true>(vb, A.fix_bits, A.keys, A.n, A.offs, A.lists, S.collect.cell, S.collect.n,
                                 S.collect.base);
+            __syncthreads();  // lists read out before the next block's counters reset
+        }
         if (!grid_barrier(A.bar, A.err, &s_flag)) return;
         const OneBufferT<true> src{A.pos[cur], A.vfme[cur]};
         fix_block<OneBufferT<true>, true>(blockIdx.x, gridDim.x, A.offs, A.perm, A.hist, A.cells, A.coarse,
@@ -1099,16 +1103,32 @@ cudaError_t launch_frame_fused(const FusedFrame& f, cudaStream_t st) {
     return f.indirect ? cudaLaunchKernelEx(&cfg, k_frame_fused<true>, A) : cudaLaunchKernelEx(&cfg, k_frame_fused<false>, A);
 }
 
-cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
-                                 const uint32_t* offs, const uint4* bands, const float4* spos, const uint4* svfme,
-                                 float4* pos_buf0, float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1,
-                                 uint32_t* keys, uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st) {
-    if (!n) return cudaSuccess;
+template <uint32_t kTile>
+cudaError_t launch_batch_tiles(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n, const uint32_t* offs,
+                               const uint4* bands, const float4* spos, const uint4* svfme, float4* pos_buf0,
+                               float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1, uint32_t* keys, uint32_t* hist,
+                               uint32_t* coarse, uint32_t* err, cudaStream_t st) {
     PhysParams unused{};
-    k_physics_frame<true, false><<<(n + kTileThreads - 1u) / kTileThreads, kTileThreads, 0, st>>>(
+    k_physics_frame<true, false, kTile><<<(n + kTile - 1u) / kTile, kTile, 0, st>>>(
         unused, scenes, tile_scene, n, offs, bands, spos, svfme, nullptr, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1,
         keys, hist, coarse, err);
     return cudaGetLastError();
+}
+
+cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
+                                 const uint32_t* offs, const uint4* bands, const float4* spos, const uint4* svfme,
+                                 float4* pos_buf0, float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1,
+                                 uint32_t* keys, uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st,
+                                 uint32_t tile) {
+    if (!n) return cudaSuccess;
+    if (tile == 64u)
+        return launch_batch_tiles<64u>(scenes, tile_scene, n, offs, bands, spos, svfme, pos_buf0, pos_buf1, vfme_buf0,
+                                       vfme_buf1, keys, hist, coarse, err, st);
+    if (tile == 256u)
+        return launch_batch_tiles<256u>(scenes, tile_scene, n, offs, bands, spos, svfme, pos_buf0, pos_buf1,
+                                        vfme_buf0, vfme_buf1, keys, hist, coarse, err, st);
+    return launch_batch_tiles<128u>(scenes, tile_scene, n, offs, bands, spos, svfme, pos_buf0, pos_buf1, vfme_buf0,
+                                    vfme_buf1, keys, hist, coarse, err, st);
 }
 
 cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,

@@ -183,3 +183,37 @@ def test_batch_long_steps_chain_frames(built_lib, cuda):
         for i, s in enumerate(scs):
             assert b.time(i) == frames[i]
             assert_same(b, i, alone(s, frames[i]), f"scene {i}")
+
+
+@pytest.mark.parametrize("tile,fpl", [(64, 1), (256, 16), (64, 8)])
+def test_batch_tuning_keeps_results(built_lib, cuda, tile, fpl):
+    """A pool with other physics tiles and chain lengths gives each scene exactly
+    its lone-world result."""
+    scs = mixed_scenes(7, seed=21)
+    with Batch([s.plugin for s in scs]) as b:
+        b.set_tuning(frames_per_launch=fpl, collide_block=tile)
+        for i, s in enumerate(scs):
+            b.set_state(i, s.pos_scale, s.vfme)
+        b.step(37)
+        for i, s in enumerate(scs):
+            assert_same(b, i, alone(s, 37), f"scene {i}, tile {tile}, {fpl} frames per launch")
+        with pytest.raises(MbError):
+            b.set_tuning(collide_block=100)
+
+
+def test_batch_autotune_restores_the_pool(built_lib, cuda):
+    """mb_batch_autotune times its nine candidates on the pool and restores every
+    scene (state, parity, time): the pool then continues exactly like lone worlds."""
+    scs = mixed_scenes(8, seed=22)
+    with Batch([s.plugin for s in scs]) as b:
+        for i, s in enumerate(scs):
+            b.set_state(i, s.pos_scale, s.vfme)
+        b.step(5)
+        res = b.autotune(frames=8)
+        assert len(res["candidates"]) == 9 and all(c["ms_per_frame"] > 0 for c in res["candidates"])
+        t = b.tuning
+        assert {"frames_per_launch": t.frames_per_launch, "collide_block": t.collide_block} == res["best"]
+        assert all(b.time(i) == 5 for i in range(len(scs)))
+        b.step(20)
+        for i, s in enumerate(scs):
+            assert_same(b, i, alone(s, 25), f"scene {i} after autotune")
