@@ -20,9 +20,12 @@
 //      state is copied to that slot; the run that
 //      fills a cell last marks the cell (a bit per input slot) if earlier runs
 //      of other warps got there first (only such cells can be out of order);
-//   4. k_fix_collect: the marked cells are listed by size;
-//   5. k_cell_fix: the listed cells' slots are put back in ascending input order
-//      (what a stable sort yields), re-gathering their state copy.
+//   4. k_fix_marked: the marked cells' slots are put back in ascending input
+//      order (what a stable sort yields), re-gathering their state copy - cells
+//      of up to 8 slots by the thread that reads the mark; larger ones are
+//      listed by size;
+//   5. k_cell_fix: the listed cells, a warp each up to 256 slots, a block each
+//      above; clears the counts for the next frame.
 //
 // The result is bit-identical to a stable sort; offs[] replaces start/close.
 
@@ -117,14 +120,14 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+template <class Src>
 __global__ void __launch_bounds__(kCollectThreads)
-    k_fix_collect(const uint32_t* __restrict__ fix_bits, const uint32_t* __restrict__ keys, uint32_t n,
-                  const uint32_t* __restrict__ offs, FixLists lists) {
-    __shared__ uint32_t s_cell[kFixLists][kCollectWords * 32u];
-    __shared__ uint32_t s_n[kFixLists], s_base[kFixLists];
-    griddep_wait();  // the scatter's bitmap is complete
+    k_fix_marked(const uint32_t* __restrict__ fix_bits, const uint32_t* __restrict__ keys, uint32_t n,
+                 const uint32_t* __restrict__ offs, uint32_t* perm, FixLists lists, Src src,
+                 float4* __restrict__ spos, uint4* __restrict__ svfme) {
+    griddep_wait();  // the scatter's bitmap and order are complete
     griddep_launch();
-    collect_block(blockIdx.x, fix_bits, keys, n, offs, lists, s_cell, s_n, s_base);
+    fix_marked_block<Src>(blockIdx.x, fix_bits, keys, n, offs, perm, lists, src, spos, svfme);
 }
 
 template <class Src>
@@ -300,8 +303,9 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
         if ((e = launch_pdl(pdl, k_cell_scatter, dim3(blocks), dim3(256), 0, st, keys, n, s.hist, perm, pos_in,
                             vfme_in, spos, svfme, offs, bands, N, s.fix_bits)))
             return e;
-        if ((e = launch_pdl(pdl, k_fix_collect, dim3(collect_grid(n)), dim3(kCollectThreads), 0, st,
-                            (const uint32_t*)s.fix_bits, keys, n, offs, fix_lists(s))))
+        const OneBuffer src{pos_in, vfme_in};
+        if ((e = launch_pdl(pdl, k_fix_marked<OneBuffer>, dim3(collect_grid(n)), dim3(kCollectThreads), 0, st,
+                            (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s), src, spos, svfme)))
             return e;
     }
     OneBuffer src{pos_in, vfme_in};
@@ -329,7 +333,9 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
                                                       pos_buf1, vfme_buf0, vfme_buf1, spos, svfme, offs,
                                                       s.fix_bits, bands);
         if ((e = cudaGetLastError())) return e;
-        k_fix_collect<<<collect_grid(n), kCollectThreads, 0, st>>>(s.fix_bits, keys, n, offs, fix_lists(s));
+        const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
+        k_fix_marked<SceneBuffers><<<collect_grid(n), kCollectThreads, 0, st>>>(s.fix_bits, keys, n, offs, perm,
+                                                                                fix_lists(s), src, spos, svfme);
         if ((e = cudaGetLastError())) return e;
     }
     SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};

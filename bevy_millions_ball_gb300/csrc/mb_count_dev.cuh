@@ -123,7 +123,7 @@ struct FixLists {
 // The run [b, b + g) of a cell with slots [lo, hi) ends the cell and did not
 // start it: other warps' runs came first, so the cell may be out of input order.
 // The run's leader marks its input slot in the fixup bitmap (once per cell: one
-// run ends it); k_fix_collect lists the marked cells.
+// run ends it); k_fix_marked puts the marked cells back in order.
 __device__ __forceinline__ bool listed(uint32_t lo, uint32_t hi, uint32_t b, uint32_t g) {
     return b + g == hi && b != lo;
 }
@@ -188,49 +188,12 @@ __device__ __forceinline__ void scatter_range(uint32_t vb, uint32_t nvb, const u
     }
 }
 
-// ---------------------------------------------------------------- collect
-// Lists the cells marked in the fixup bitmap by size class (a marked input
-// slot's key is its cell).  A block reads kCollectWords words, a byte per
-// thread, stages the cells in shared memory and appends them to the global
-// lists with one atomic per list.
+// The marked cells are read kCollectWords bitmap words per block of
+// kCollectThreads threads, a byte (8 input slots) per thread.
 constexpr uint32_t kCollectThreads = 256, kCollectWords = kCollectThreads / 4u;
 
-// One block of the listing (kCollectThreads threads); s_cell: kFixLists x
-// kCollectWords * 32 words, s_n and s_base: kFixLists words each.  A block that
-// runs several must synchronise between them.
-template <bool kCg = false>
-__device__ __forceinline__ void collect_block(uint32_t vb, const uint32_t* __restrict__ fix_bits,
-                                              const uint32_t* __restrict__ keys, uint32_t n,
-                                              const uint32_t* __restrict__ offs, const FixLists& lists,
-                                              uint32_t (*s_cell)[kCollectWords * 32u], uint32_t* s_n,
-                                              uint32_t* s_base) {
-    const uint32_t tid = threadIdx.x;
-    if (tid < (uint32_t)kFixLists) s_n[tid] = 0u;
-    __syncthreads();
-    const uint32_t words = (n + 31u) / 32u;
-    const uint32_t w = vb * kCollectWords + tid / 4u, sh = 8u * (tid & 3u);
-    uint32_t bits = w < words ? (__ldcg(fix_bits + w) >> sh) & 0xFFu : 0u;
-    while (bits) {
-        const uint32_t c = ld_in<kCg>(keys + 32u * w + sh + (uint32_t)(__ffs(bits) - 1));
-        bits &= bits - 1u;
-        const uint32_t m = ld_in<kCg>(offs + c + 1u) - ld_in<kCg>(offs + c);
-        const int cls = m <= kFixSmall ? kFixListSmall : (m <= kFixWarp ? kFixListWarp : kFixListHuge);
-        s_cell[cls][atomicAdd(&s_n[cls], 1u)] = c;  // at most 32 * kCollectWords marks per block
-    }
-    __syncthreads();
-    if (tid < (uint32_t)kFixLists && s_n[tid]) s_base[tid] = atomicAdd(lists.ctl + tid, s_n[tid]);
-    __syncthreads();
-#pragma unroll
-    for (int c = 0; c < kFixLists; ++c) {
-        for (uint32_t j = tid; j < s_n[c]; j += kCollectThreads) {
-            const uint32_t at = s_base[c] + j;  // lists hold every cell that can qualify; the bound guards bad counts
-            if (at < lists.cap[c]) lists.list[c][at] = s_cell[c][j];
-        }
-    }
-}
-
 // ---------------------------------------------------------------- fixup
-// The listed cells (see k_fix_collect) get their slots back in ascending input order
+// The listed cells get their slots back in ascending input order
 // and (spos != NULL) re-gather their sorted state copy from the state source: one
 // buffer (a world), or each scene's current buffer (a batch, where cells and
 // coarse tiles of HOLD scenes are left alone).  Cells of up to kFixSmall slots: a thread
@@ -345,6 +308,133 @@ __device__ __forceinline__ void warp_bitonic(uint32_t (&v)[kFixWarp / 32], uint3
     }
 }
 
+// A cell of m <= kFixSmall slots from lo back in input order, by one thread (a
+// sorting network over kFixSmall slots held in registers; empty slots hold
+// 0xFFFFFFFF and stay last), with its sorted state copy re-gathered (spos != NULL).
+template <class Src, bool kCg>
+__device__ __forceinline__ void fix_small_cell(uint32_t lo, uint32_t m, uint32_t* perm, const Src& src,
+                                               float4* __restrict__ spos, uint4* __restrict__ svfme) {
+    uint32_t v[kFixSmall];
+    bool sorted = true;
+#pragma unroll
+    for (uint32_t k = 0; k < kFixSmall; ++k) v[k] = k < m ? ld_cur<kCg>(perm + lo + k) : 0xFFFFFFFFu;
+#pragma unroll
+    for (uint32_t k = 1; k < kFixSmall; ++k) sorted = sorted && v[k - 1u] <= v[k];
+    if (sorted) return;
+    // Batcher's odd-even merge sort of 8 keys (19 compare-exchanges)
+    constexpr uint8_t kNet[19][2] = {{0, 1}, {2, 3}, {4, 5}, {6, 7}, {0, 2}, {1, 3}, {4, 6}, {5, 7}, {1, 2},
+                                     {5, 6}, {0, 4}, {1, 5}, {2, 6}, {3, 7}, {2, 4}, {3, 5}, {1, 2}, {3, 4},
+                                     {5, 6}};
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const uint32_t a = v[kNet[q][0]], b = v[kNet[q][1]];
+        v[kNet[q][0]] = min(a, b);
+        v[kNet[q][1]] = max(a, b);
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kFixSmall; ++k) {
+        if (k < m) {
+            perm[lo + k] = v[k];
+            if (spos) {
+                spos[lo + k] = src.pos(v[k]);
+                svfme[lo + k] = src.vfme(v[k]);
+            }
+        }
+    }
+}
+
+// A cell of kFixSmall < m <= kFixWarp slots from lo back in input order, by one
+// whole warp (a bitonic sort of the cell's input indices in registers: slot
+// e = 32 s + lane is v[s], padded with 0xFFFFFFFF to 32 S slots, S a power of two).
+template <class Src, bool kCg>
+__device__ __forceinline__ void fix_warp_cell(uint32_t lo, uint32_t m, uint32_t lane, uint32_t* perm, const Src& src,
+                                              float4* __restrict__ spos, uint4* __restrict__ svfme) {
+    uint32_t v[kFixWarp / 32];
+#pragma unroll
+    for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
+        const uint32_t e = 32u * s + lane;
+        v[s] = e < m ? ld_cur<kCg>(perm + lo + e) : 0xFFFFFFFFu;
+    }
+    {  // the runs may have claimed their slots in input order already
+        bool ok = true;
+#pragma unroll
+        for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
+            const uint32_t down = __shfl_down_sync(0xFFFFFFFFu, v[s], 1);
+            const uint32_t wrap = s + 1u < kFixWarp / 32 ? __shfl_sync(0xFFFFFFFFu, v[s + 1u < kFixWarp / 32 ? s + 1u : s], 0)
+                                                          : 0xFFFFFFFFu;
+            ok = ok && v[s] <= (lane == 31u ? wrap : down);
+        }
+        if (__all_sync(0xFFFFFFFFu, ok)) return;
+    }
+    if (m <= 32u) warp_bitonic<1>(v, lane);
+    else if (m <= 64u) warp_bitonic<2>(v, lane);
+    else if (m <= 128u) warp_bitonic<4>(v, lane);
+    else warp_bitonic<8>(v, lane);
+    __syncwarp();  // every lane has read the cell before any slot is rewritten
+#pragma unroll
+    for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
+        const uint32_t e = 32u * s + lane;
+        if (e < m) {
+            perm[lo + e] = v[s];
+            if (spos) {
+                spos[lo + e] = src.pos(v[s]);
+                svfme[lo + e] = src.vfme(v[s]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- marked cells
+// One block (kCollectThreads threads) of the fixup of the marked cells: it reads
+// kCollectWords words of the bitmap, a byte (8 input slots) per thread.  A
+// marked input slot names a cell (its key) that runs of several warps filled.
+// The thread that finds a cell of up to kFixSmall slots puts it back in input
+// order itself; larger cells are listed by size (one atomic per list per warp)
+// for fix_block, which shares them out over the whole grid (crowded scenes mark
+// many of them close together in the input).
+template <class Src, bool kCg = false>
+__device__ __forceinline__ void fix_marked_block(uint32_t vb, const uint32_t* __restrict__ fix_bits,
+                                                 const uint32_t* __restrict__ keys, uint32_t n,
+                                                 const uint32_t* __restrict__ offs, uint32_t* perm,
+                                                 const FixLists& lists, const Src& src, float4* __restrict__ spos,
+                                                 uint4* __restrict__ svfme) {
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    const uint32_t words = (n + 31u) / 32u;
+    const uint32_t w = vb * kCollectWords + tid / 4u, sh = 8u * (tid & 3u);
+    const uint32_t byte = w < words ? (__ldcg(fix_bits + w) >> sh) & 0xFFu : 0u;
+    uint32_t big[2] = {0u, 0u};  // bits of this thread's byte whose cell goes to list 1 (warp) / 2 (block)
+    uint32_t cell[8];
+    for (uint32_t bits = byte; bits; bits &= bits - 1u) {
+        const uint32_t q = (uint32_t)(__ffs(bits) - 1);
+        const uint32_t c = ld_in<kCg>(keys + 32u * w + sh + q);
+        const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;
+        if (m <= kFixSmall) {
+            fix_small_cell<Src, kCg>(lo, m, perm, src, spos, svfme);
+        } else {
+            big[m <= kFixWarp ? 0 : 1] |= 1u << q;
+            cell[q] = c;
+        }
+    }
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        const int cls = l == 0 ? kFixListWarp : kFixListHuge;
+        const uint32_t cnt = (uint32_t)__popc(big[l]);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        if (!total) continue;
+        uint32_t base = 0;
+        if (lane == 31u) base = atomicAdd(lists.ctl + cls, total);
+        base = __shfl_sync(0xFFFFFFFFu, base, 31) + incl - cnt;
+        for (uint32_t bits = big[l]; bits; bits &= bits - 1u, ++base)  // lists hold every cell that can qualify
+            if (base < lists.cap[cls]) lists.list[cls][base] = cell[__ffs(bits) - 1];
+    }
+}
+
 // Block vb of nvb (kFixThreads threads; the lists are shared out grid-stride);
 // s_v: kBitmapWords words, s_red: kFixThreads / 32 + 1 words.
 template <class Src, bool kCg = false>
@@ -374,33 +464,7 @@ __device__ __forceinline__ void fix_block(uint32_t vb, uint32_t nvb, const uint3
     for (uint32_t x = vb * blockDim.x + tid; x < n_small; x += nvb * blockDim.x) {
         const uint32_t c = ld_cur<kCg>(small + x);
         const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;
-        uint32_t v[kFixSmall];
-        bool sorted = true;
-#pragma unroll
-        for (uint32_t k = 0; k < kFixSmall; ++k) v[k] = k < m ? ld_cur<kCg>(perm + lo + k) : 0xFFFFFFFFu;
-#pragma unroll
-        for (uint32_t k = 1; k < kFixSmall; ++k) sorted = sorted && v[k - 1u] <= v[k];
-        if (sorted) continue;
-        // Batcher's odd-even merge sort of 8 keys (19 compare-exchanges)
-        constexpr uint8_t kNet[19][2] = {{0, 1}, {2, 3}, {4, 5}, {6, 7}, {0, 2}, {1, 3}, {4, 6}, {5, 7}, {1, 2},
-                                         {5, 6}, {0, 4}, {1, 5}, {2, 6}, {3, 7}, {2, 4}, {3, 5}, {1, 2}, {3, 4},
-                                         {5, 6}};
-#pragma unroll
-        for (int q = 0; q < 19; ++q) {
-            const uint32_t a = v[kNet[q][0]], b = v[kNet[q][1]];
-            v[kNet[q][0]] = min(a, b);
-            v[kNet[q][1]] = max(a, b);
-        }
-#pragma unroll
-        for (uint32_t k = 0; k < kFixSmall; ++k) {
-            if (k < m) {
-                perm[lo + k] = v[k];
-                if (spos) {
-                    spos[lo + k] = src.pos(v[k]);
-                    svfme[lo + k] = src.vfme(v[k]);
-                }
-            }
-        }
+        fix_small_cell<Src, kCg>(lo, m, perm, src, spos, svfme);
     }
 
     // mid cells: one warp each, a bitonic sort of the cell's input indices held
@@ -411,39 +475,7 @@ __device__ __forceinline__ void fix_block(uint32_t vb, uint32_t nvb, const uint3
     for (uint32_t x = vb * (blockDim.x / 32u) + tid / 32u; x < n_mid; x += warps) {
         const uint32_t c = ld_cur<kCg>(mid + x);
         const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;  // 9 <= m <= kFixWarp
-        uint32_t v[kFixWarp / 32];
-#pragma unroll
-        for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
-            const uint32_t e = 32u * s + lane;
-            v[s] = e < m ? ld_cur<kCg>(perm + lo + e) : 0xFFFFFFFFu;
-        }
-        {  // the runs may have claimed their slots in input order already
-            bool ok = true;
-#pragma unroll
-            for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
-                const uint32_t down = __shfl_down_sync(0xFFFFFFFFu, v[s], 1);
-                const uint32_t wrap = s + 1u < kFixWarp / 32 ? __shfl_sync(0xFFFFFFFFu, v[s + 1u < kFixWarp / 32 ? s + 1u : s], 0)
-                                                              : 0xFFFFFFFFu;
-                ok = ok && v[s] <= (lane == 31u ? wrap : down);
-            }
-            if (__all_sync(0xFFFFFFFFu, ok)) continue;
-        }
-        if (m <= 32u) warp_bitonic<1>(v, lane);
-        else if (m <= 64u) warp_bitonic<2>(v, lane);
-        else if (m <= 128u) warp_bitonic<4>(v, lane);
-        else warp_bitonic<8>(v, lane);
-        __syncwarp();  // every lane has read the cell before any slot is rewritten
-#pragma unroll
-        for (uint32_t s = 0; s < kFixWarp / 32; ++s) {
-            const uint32_t e = 32u * s + lane;
-            if (e < m) {
-                perm[lo + e] = v[s];
-                if (spos) {
-                    spos[lo + e] = src.pos(v[s]);
-                    svfme[lo + e] = src.vfme(v[s]);
-                }
-            }
-        }
+        fix_warp_cell<Src, kCg>(lo, m, lane, perm, src, spos, svfme);
     }
 
     // huge cells: one block each.  The cell's input indices are copied aside,

@@ -134,14 +134,23 @@ __device__ __forceinline__ bool longer_than(V3 v, float s) {
     return sqrtf(d) > s;
 }
 
+// Response model of a kernel instantiation: rigid, spring, or read from the
+// parameters at run time (batches mix scenes of both).
+enum : int { kRigid = 0, kSpring = 1, kSpringRuntime = 2 };
+template <int kResp>
+__device__ __forceinline__ bool spring_of(const PhysParams& P) {
+    return kResp == kSpringRuntime ? P.spring != 0u : kResp == kSpring;
+}
+
 // solve_sphere_constraint (physics.wgsl:300-331)
+template <int kResp>
 __device__ __forceinline__ void sphere(const PhysParams& P, Agent& a, const Agent& b) {
     float edge = b.scale + a.scale;
     V3 tpos = a.position - b.position;
     float dist = len3(tpos);
     if (dist <= edge) {
         V3 norm = normalize3(tpos);
-        if (!P.spring) {
+        if (!spring_of<kResp>(P)) {
             float m1 = a.massv, m2 = b.massv;
             V3 rvel = a.velocity - b.velocity;
             float rspd = dot3(rvel, norm);
@@ -169,6 +178,7 @@ __device__ __forceinline__ void sphere(const PhysParams& P, Agent& a, const Agen
 }
 
 // solve_cube_constraint (physics.wgsl:269-298)
+template <int kResp>
 __device__ __forceinline__ void cube(const PhysParams& P, Agent& a) {
     V3 edge = V3{P.half_map_size, P.half_map_height, P.half_map_size} - splat(a.scale);
     V3 cetr = {0.0f, P.half_map_height, 0.0f};
@@ -176,7 +186,7 @@ __device__ __forceinline__ void cube(const PhysParams& P, Agent& a) {
     V3 makeup = {edge.x - fabsf(tpos.x), edge.y - fabsf(tpos.y), edge.z - fabsf(tpos.z)};
     bool tx = makeup.x < 0.0f, ty = makeup.y < 0.0f, tz = makeup.z < 0.0f;
     if (!(tx || ty || tz)) return;
-    if (!P.spring) {
+    if (!spring_of<kResp>(P)) {
         a.position = V3{wclamp(tpos.x, -edge.x, edge.x), wclamp(tpos.y, -edge.y, edge.y),
                         wclamp(tpos.z, -edge.z, edge.z)} + cetr;
         float ne = -P.e_envir;
@@ -325,7 +335,7 @@ __device__ __forceinline__ uint32_t cand_slot(uint32_t t, const uint32_t (&o)[3]
 
 constexpr float kNearScale = 1.0014989f;  // about sqrt(1.003): squared, a 0.3% margin on edge^2
 
-template <bool kShared, uint32_t kLook, bool kIndirect, bool kCg>
+template <bool kShared, uint32_t kLook, bool kIndirect, bool kCg, int kResp>
 __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
                                              uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself,
@@ -361,10 +371,10 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
             t += q + 1u;
             const uint32_t j = j0 + q;
             if (kShared) {
-                sphere(P, a, unpack(bpos[j], bvfme[j]));
+                sphere<kResp>(P, a, unpack(bpos[j], bvfme[j]));
             } else {
                 const uint32_t sj = kIndirect ? min(ld_in<kCg>(perm + j), nmax) : j;
-                sphere(P, a, unpack(ld_in<kCg>(bpos + sj), ld_in<kCg>(bvfme + sj)));
+                sphere<kResp>(P, a, unpack(ld_in<kCg>(bpos + sj), ld_in<kCg>(bvfme + sj)));
             }
         } else {
             t += min(rem, kLook);
@@ -377,15 +387,15 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
 // so its lanes run one loop.
 constexpr uint32_t kCrowdedT = 48, kLookSparse = 4, kLookCrowded = 6;
 
-template <bool kShared, bool kIndirect, bool kCg>
+template <bool kShared, bool kIndirect, bool kCg, int kResp>
 __device__ __forceinline__ void contact_loop(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
                                              uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself,
                                              const uint32_t* __restrict__ perm, uint32_t nmax) {
     if (__any_sync(__activemask(), T >= kCrowdedT))
-        contact_walk<kShared, kLookCrowded, kIndirect, kCg>(P, a, bpos, bvfme, o, c0, c01, T, tself, perm, nmax);
+        contact_walk<kShared, kLookCrowded, kIndirect, kCg, kResp>(P, a, bpos, bvfme, o, c0, c01, T, tself, perm, nmax);
     else
-        contact_walk<kShared, kLookSparse, kIndirect, kCg>(P, a, bpos, bvfme, o, c0, c01, T, tself, perm, nmax);
+        contact_walk<kShared, kLookSparse, kIndirect, kCg, kResp>(P, a, bpos, bvfme, o, c0, c01, T, tself, perm, nmax);
 }
 
 // Slot ranges of the three candidate rows of a sphere in cell (cx, cz), key =
@@ -415,7 +425,7 @@ __device__ __forceinline__ void row_bounds(uint32_t N, const uint32_t* __restric
 // b holds slots [b_lo[b], b_lo[b] + b_cnt[b])); rows outside them are read from
 // spos/svfme (through perm when kIndirect).  base_a / base_c: the scene's first
 // slot and cell (0 for a world).
-template <bool kIndirect, bool kCg, uint32_t kCap>
+template <bool kIndirect, bool kCg, uint32_t kCap, int kResp>
 __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32_t i, uint32_t n, uint32_t base_a,
                                             uint32_t base_c, const uint32_t (&lo)[3], const uint32_t (&hi)[3],
                                             const float4* b_pos, const uint4* b_vfme, const uint32_t* b_lo,
@@ -456,9 +466,9 @@ __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32
     // handle_collisions (physics.wgsl:119-169)
     V3 old_pos = a.position;
     if (shared)
-        contact_loop<true, false, kCg>(P, a, b_pos, b_vfme, o_s, c[0], c01, T, tself, perm, n - 1u);
+        contact_loop<true, false, kCg, kResp>(P, a, b_pos, b_vfme, o_s, c[0], c01, T, tself, perm, n - 1u);
     else
-        contact_loop<false, kIndirect, kCg>(P, a, spos, svfme, o_g, c[0], c01, T, tself, perm, n - 1u);
+        contact_loop<false, kIndirect, kCg, kResp>(P, a, spos, svfme, o_g, c[0], c01, T, tself, perm, n - 1u);
     V3 diff = a.position - old_pos;
     if (longer_than(diff, a.scale)) {
         // hash3f1u(new_agent_index) * 2 - 1 (physics.wgsl:166, 334-337); the
@@ -472,7 +482,7 @@ __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32
         a.position = a.position + normalize3(jitter);
     }
 
-    cube(P, a);
+    cube<kResp>(P, a);
 
     const float lim = 65504.0f;  // CLAMP_F16
     a.velocity = {wclamp(a.velocity.x, -lim, lim), wclamp(a.velocity.y, -lim, lim),
@@ -538,7 +548,8 @@ using TileSmem = TileSmemT<kTileThreads>;
 // end (tile * kTile >= n) does nothing but take part in the barriers.  The band
 // table holds bounds per 128-slot tile: a 256-slot tile joins two entries, a
 // 64-slot tile derives its own from its first and last cells.
-template <bool kBatched, bool kIndirect, bool kCg = false, uint32_t kTile = kTileThreads>
+template <bool kBatched, bool kIndirect, bool kCg = false, uint32_t kTile = kTileThreads,
+          int kResp = kSpringRuntime>
 __device__ __forceinline__ void physics_tile(
     uint32_t tile, uint32_t tid, uint32_t bar_parity, TileSmemT<kTile>* sm, uint64_t* s_bar, const PhysParams& P1,
     const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene, uint32_t n,
@@ -742,11 +753,11 @@ __device__ __forceinline__ void physics_tile(
     }
     if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
 
-    step_sphere<kIndirect, kCg, kCap>(P, a, i, n, base_a, base_c, lo, hi, s_pos, s_vfme, s_lo, s_cnt, spos, svfme, perm,
+    step_sphere<kIndirect, kCg, kCap, kResp>(P, a, i, n, base_a, base_c, lo, hi, s_pos, s_vfme, s_lo, s_cnt, spos, svfme, perm,
                                 pos_out, vfme_out, keys_out, hist, coarse);
 }
 
-template <bool kBatched, bool kIndirect, uint32_t kTile = kTileThreads>
+template <bool kBatched, bool kIndirect, uint32_t kTile = kTileThreads, int kResp = kSpringRuntime>
 __global__ void __launch_bounds__(kTile)
     k_physics_frame(const __grid_constant__ PhysParams P1, const SceneDev* __restrict__ scenes,
                     const uint32_t* __restrict__ tile_scene, uint32_t n, const uint32_t* __restrict__ offs,
@@ -758,14 +769,14 @@ __global__ void __launch_bounds__(kTile)
     __shared__ __align__(16) TileSmemT<kTile> sm;
     __shared__ __align__(8) uint64_t s_bar;
     if (!kIndirect && threadIdx.x == 0) mbar_init(&s_bar, 1u);  // first copy after the tile's CTA barrier
-    physics_tile<kBatched, kIndirect, false, kTile>(blockIdx.x, threadIdx.x, 0u, &sm, &s_bar, P1, scenes, tile_scene, n, offs,
+    physics_tile<kBatched, kIndirect, false, kTile, kResp>(blockIdx.x, threadIdx.x, 0u, &sm, &s_bar, P1, scenes, tile_scene, n, offs,
                                       bands, spos, svfme, perm, pos_out0, pos_out1, vfme_out0, vfme_out1, keys_out,
                                       hist, coarse, err);
 }
 
 // ---------------------------------------------------------------- fused frame
 // LOOP frames as one cooperative kernel: the five stages of a frame (count scan,
-// scatter, fixup listing, fixup, physics) run back to back in one launch,
+// scatter, marked-cell fixup, large-cell fixup, physics) run back to back in one launch,
 // separated by grid barriers instead of kernel boundaries, for as many frames
 // as the launch is given.  Every block is resident (cooperative launch), so a
 // block may wait for the others; each wait is bounded.  The stages run the same
@@ -841,10 +852,6 @@ union FusedSmem {
         uint32_t warp[kScanThreads / 32], base[kScanThreads / 32];
     } scan;
     struct {
-        uint32_t cell[kFixLists][kCollectWords * 32u];
-        uint32_t n[kFixLists], base[kFixLists];
-    } collect;
-    struct {
         uint32_t v[kBitmapWords];
         uint32_t red[kFixThreads / 32 + 1];
     } fix;
@@ -876,13 +883,11 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_frame_fused(const __grid_c
                             kIndirect ? nullptr : A.spos, kIndirect ? nullptr : A.svfme, A.offs, A.bands, A.P.N,
                             A.fix_bits);
         if (!grid_barrier(A.bar, A.err, &s_flag)) return;
-        for (uint32_t vb = blockIdx.x; vb < A.collect_blocks; vb += gridDim.x) {
-            collect_block<true>(vb, A.fix_bits, A.keys, A.n, A.offs, A.lists, S.collect.cell, S.collect.n,
-                                S.collect.base);
-            __syncthreads();  // lists read out before the next block's counters reset
-        }
-        if (!grid_barrier(A.bar, A.err, &s_flag)) return;
         const OneBufferT<true> src{A.pos[cur], A.vfme[cur]};
+        for (uint32_t vb = blockIdx.x; vb < A.collect_blocks; vb += gridDim.x)
+            fix_marked_block<OneBufferT<true>, true>(vb, A.fix_bits, A.keys, A.n, A.offs, A.perm, A.lists, src,
+                                                     kIndirect ? nullptr : A.spos, kIndirect ? nullptr : A.svfme);
+        if (!grid_barrier(A.bar, A.err, &s_flag)) return;
         fix_block<OneBufferT<true>, true>(blockIdx.x, gridDim.x, A.offs, A.perm, A.hist, A.cells, A.coarse,
                                           A.scan_tiles, A.lists, A.fix_tmp, src, kIndirect ? nullptr : A.spos,
                                           kIndirect ? nullptr : A.svfme, S.fix.v, S.fix.red);
@@ -1013,19 +1018,33 @@ cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t*
     return cudaGetLastError();
 }
 
+template <uint32_t kTile, int kResp>
+cudaError_t launch_physics_resp(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
+                                const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
+                                uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse,
+                                uint32_t* err, cudaStream_t st, bool pdl) {
+    const dim3 grid((n + kTile - 1u) / kTile), block(kTile);
+    if (perm)
+        return launch_pdl(pdl, k_physics_frame<false, true, kTile, kResp>, grid, block, 0, st, p, (const SceneDev*)nullptr,
+                          (const uint32_t*)nullptr, n, offs, bands, spos, svfme, perm, pos_out, (float4*)nullptr,
+                          vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
+    return launch_pdl(pdl, k_physics_frame<false, false, kTile, kResp>, grid, block, 0, st, p,
+                      (const SceneDev*)nullptr, (const uint32_t*)nullptr, n, offs, bands, spos, svfme,
+                      (const uint32_t*)nullptr, pos_out, (float4*)nullptr, vfme_out, (uint4*)nullptr, keys_out, hist,
+                      coarse, err);
+}
+
+// One world's response model is known on the host: the kernel is compiled for it.
 template <uint32_t kTile>
 cudaError_t launch_physics_tiles(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                  const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
                                  uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse,
                                  uint32_t* err, cudaStream_t st, bool pdl) {
-    const dim3 grid((n + kTile - 1u) / kTile), block(kTile);
-    if (perm)
-        return launch_pdl(pdl, k_physics_frame<false, true, kTile>, grid, block, 0, st, p, (const SceneDev*)nullptr,
-                          (const uint32_t*)nullptr, n, offs, bands, spos, svfme, perm, pos_out, (float4*)nullptr,
-                          vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
-    return launch_pdl(pdl, k_physics_frame<false, false, kTile>, grid, block, 0, st, p, (const SceneDev*)nullptr,
-                      (const uint32_t*)nullptr, n, offs, bands, spos, svfme, (const uint32_t*)nullptr, pos_out,
-                      (float4*)nullptr, vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
+    if (p.spring)
+        return launch_physics_resp<kTile, kSpring>(p, n, offs, bands, spos, svfme, perm, pos_out, vfme_out,
+                                                   keys_out, hist, coarse, err, st, pdl);
+    return launch_physics_resp<kTile, kRigid>(p, n, offs, bands, spos, svfme, perm, pos_out, vfme_out, keys_out,
+                                              hist, coarse, err, st, pdl);
 }
 
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
