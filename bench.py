@@ -325,6 +325,7 @@ def run_ours(args, rank, world_size, local_rank):
         "bound": "hbm", "kernel": "k_physics_frame", "achieved": achieved, "peak": hbm, "unit": "GB/s",
         "frac": achieved / hbm, "peak_kind": peak_kind,
         "traffic": ncu_traffic("k_physics_frame", args.workload),
+        "traffic_from": f"profiles/k_physics_frame_{args.workload}.txt (one ncu capture; its header names the frame)",
         "algorithmic_bytes_per_launch": phys_bytes,
         "frame": {"algorithmic_bytes": frame_bytes,
                   "achieved_gbs": frame_bytes / (total_ms / args.steps * 1e-3) / 1e9,
@@ -406,6 +407,9 @@ def run_batch(args, rank=0, world_size=1, local_rank=0):
         b.set_state(i, s.pos_scale, s.vfme)
     b.step(1 + max(args.warmup, 3))
     b.sync()
+    # frames per graph launch and physics tile from the batch autotuner (states restored)
+    tuned = b.autotune(frames=8)
+    b.sync()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if dist:
         dist.barrier()
@@ -453,6 +457,7 @@ def run_batch(args, rank=0, world_size=1, local_rank=0):
         "config": {"workload": f"batch: {len(scs)} scenes, n log-uniform [1024, 262144], total {total:,} spheres, "
                                "N = next_pow2(sqrt n), H in {4,8,16}, e in [0.5,0.95], half spring",
                    "spheres_total": int(total), "median_scene": int(np.median(sizes)), "pool_bytes": int(mem),
+                   "tuning": dict(tuned["best"], how="mb_batch_autotune, 8 frames per candidate"),
                    "l2": "pool larger than L2",
                    "parallelism": f"scene shards x{world_size} (no collective)" if world_size > 1 else "single"},
         "plain_loop": {"value": total * K / t_plain, "ms_per_step": 1e3 * t_plain / K,

@@ -125,9 +125,10 @@ __global__ void __launch_bounds__(kCollectThreads)
     k_fix_marked(const uint32_t* __restrict__ fix_bits, const uint32_t* __restrict__ keys, uint32_t n,
                  const uint32_t* __restrict__ offs, uint32_t* perm, FixLists lists, Src src,
                  float4* __restrict__ spos, uint4* __restrict__ svfme) {
+    __shared__ uint32_t s_slot[kCollectThreads * 8u], s_big[2u * kCollectThreads * 8u], s_cnt[4];
     griddep_wait();  // the scatter's bitmap and order are complete
     griddep_launch();
-    fix_marked_block<Src>(blockIdx.x, fix_bits, keys, n, offs, perm, lists, src, spos, svfme);
+    fix_marked_block<Src>(blockIdx.x, fix_bits, keys, n, offs, perm, lists, src, spos, svfme, s_slot, s_big, s_cnt);
 }
 
 template <class Src>

@@ -388,50 +388,58 @@ __device__ __forceinline__ void fix_warp_cell(uint32_t lo, uint32_t m, uint32_t 
 // One block (kCollectThreads threads) of the fixup of the marked cells: it reads
 // kCollectWords words of the bitmap, a byte (8 input slots) per thread.  A
 // marked input slot names a cell (its key) that runs of several warps filled.
-// The thread that finds a cell of up to kFixSmall slots puts it back in input
-// order itself; larger cells are listed by size (one atomic per list per warp)
-// for fix_block, which shares them out over the whole grid (crowded scenes mark
-// many of them close together in the input).
+// Each warp gathers the marked slots of its 256 input slots in shared memory and
+// deals them out to its lanes, so a lane usually has one cell at most: cells of
+// up to kFixSmall slots are put back in input order by that lane; larger cells
+// are listed by size (one atomic per list per block) for fix_block, which shares
+// them out over the whole grid (crowded scenes mark many close together).
+// s_slot: kCollectThreads * 8 words; s_big: 2 x kCollectThreads * 8 words;
+// s_cnt: 4 words.
 template <class Src, bool kCg = false>
 __device__ __forceinline__ void fix_marked_block(uint32_t vb, const uint32_t* __restrict__ fix_bits,
                                                  const uint32_t* __restrict__ keys, uint32_t n,
                                                  const uint32_t* __restrict__ offs, uint32_t* perm,
                                                  const FixLists& lists, const Src& src, float4* __restrict__ spos,
-                                                 uint4* __restrict__ svfme) {
-    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+                                                 uint4* __restrict__ svfme, uint32_t* s_slot, uint32_t* s_big,
+                                                 uint32_t* s_cnt) {
+    constexpr uint32_t kPerWarp = 32u * 8u;  // input slots a warp reads the marks of
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t words = (n + 31u) / 32u;
     const uint32_t w = vb * kCollectWords + tid / 4u, sh = 8u * (tid & 3u);
-    const uint32_t byte = w < words ? (__ldcg(fix_bits + w) >> sh) & 0xFFu : 0u;
-    uint32_t big[2] = {0u, 0u};  // bits of this thread's byte whose cell goes to list 1 (warp) / 2 (block)
-    uint32_t cell[8];
-    for (uint32_t bits = byte; bits; bits &= bits - 1u) {
-        const uint32_t q = (uint32_t)(__ffs(bits) - 1);
-        const uint32_t c = ld_in<kCg>(keys + 32u * w + sh + q);
+    uint32_t byte = w < words ? (__ldcg(fix_bits + w) >> sh) & 0xFFu : 0u;
+    if (tid < 2u) s_cnt[tid] = 0u;
+    // compact the warp's marked slots
+    const uint32_t cnt = (uint32_t)__popc(byte);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    uint32_t* const my = s_slot + warp * kPerWarp;
+    for (uint32_t at = incl - cnt; byte; byte &= byte - 1u, ++at) my[at] = 32u * w + sh + (uint32_t)(__ffs(byte) - 1);
+    __syncthreads();  // slots written; list counters cleared
+    for (uint32_t k = lane; k < total; k += 32u) {
+        const uint32_t c = ld_in<kCg>(keys + my[k]);
         const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;
         if (m <= kFixSmall) {
             fix_small_cell<Src, kCg>(lo, m, perm, src, spos, svfme);
         } else {
-            big[m <= kFixWarp ? 0 : 1] |= 1u << q;
-            cell[q] = c;
+            const uint32_t l = m <= kFixWarp ? 0u : 1u;
+            s_big[l * kCollectThreads * 8u + atomicAdd(&s_cnt[l], 1u)] = c;
         }
     }
+    __syncthreads();
+    if (tid < 2u && s_cnt[tid]) s_cnt[2u + tid] = atomicAdd(lists.ctl + (tid == 0u ? kFixListWarp : kFixListHuge), s_cnt[tid]);
+    __syncthreads();
 #pragma unroll
-    for (int l = 0; l < 2; ++l) {
-        const int cls = l == 0 ? kFixListWarp : kFixListHuge;
-        const uint32_t cnt = (uint32_t)__popc(big[l]);
-        uint32_t incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= (uint32_t)o) incl += y;
+    for (uint32_t l = 0; l < 2u; ++l) {
+        const int cls = l == 0u ? kFixListWarp : kFixListHuge;
+        for (uint32_t j = tid; j < s_cnt[l]; j += kCollectThreads) {
+            const uint32_t at = s_cnt[2u + l] + j;  // lists hold every cell that can qualify
+            if (at < lists.cap[cls]) lists.list[cls][at] = s_big[l * kCollectThreads * 8u + j];
         }
-        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        if (!total) continue;
-        uint32_t base = 0;
-        if (lane == 31u) base = atomicAdd(lists.ctl + cls, total);
-        base = __shfl_sync(0xFFFFFFFFu, base, 31) + incl - cnt;
-        for (uint32_t bits = big[l]; bits; bits &= bits - 1u, ++base)  // lists hold every cell that can qualify
-            if (base < lists.cap[cls]) lists.list[cls][base] = cell[__ffs(bits) - 1];
     }
 }
 

@@ -852,6 +852,9 @@ union FusedSmem {
         uint32_t warp[kScanThreads / 32], base[kScanThreads / 32];
     } scan;
     struct {
+        uint32_t slot[kCollectThreads * 8u], big[2u * kCollectThreads * 8u], cnt[4];
+    } marked;
+    struct {
         uint32_t v[kBitmapWords];
         uint32_t red[kFixThreads / 32 + 1];
     } fix;
@@ -884,9 +887,12 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_frame_fused(const __grid_c
                             A.fix_bits);
         if (!grid_barrier(A.bar, A.err, &s_flag)) return;
         const OneBufferT<true> src{A.pos[cur], A.vfme[cur]};
-        for (uint32_t vb = blockIdx.x; vb < A.collect_blocks; vb += gridDim.x)
+        for (uint32_t vb = blockIdx.x; vb < A.collect_blocks; vb += gridDim.x) {
             fix_marked_block<OneBufferT<true>, true>(vb, A.fix_bits, A.keys, A.n, A.offs, A.perm, A.lists, src,
-                                                     kIndirect ? nullptr : A.spos, kIndirect ? nullptr : A.svfme);
+                                                     kIndirect ? nullptr : A.spos, kIndirect ? nullptr : A.svfme,
+                                                     S.marked.slot, S.marked.big, S.marked.cnt);
+            __syncthreads();  // the lists are written out before the next block's counters reset
+        }
         if (!grid_barrier(A.bar, A.err, &s_flag)) return;
         fix_block<OneBufferT<true>, true>(blockIdx.x, gridDim.x, A.offs, A.perm, A.hist, A.cells, A.coarse,
                                           A.scan_tiles, A.lists, A.fix_tmp, src, kIndirect ? nullptr : A.spos,
