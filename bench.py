@@ -360,7 +360,8 @@ def run_ours(args, rank, world_size, local_rank):
         "config": {"workload": workload_desc(args.workload, sc), "n": n, "grids": p.number_of_grids_one_dimension,
                    "cells": cells, "parallelism": f"replicas{world_size}" if world_size > 1 else "single",
                    "l2": "flushed before every timed frame (256 MB write then 256 MB read, outside the events)",
-                   "digit_bits_max": w.tuning.digit_bits_max, "collide_block": w.tuning.collide_block},
+                   "digit_bits_max": w.tuning.digit_bits_max, "collide_block": w.tuning.collide_block,
+                   "scatter_agents": max(w.tuning.scatter_agents, 1)},
         "stages_ms": {"sort": float(stage[:, 0].mean()), "cells": float(stage[:, 1].mean()),
                       "physics": phys_ms, "frames": prof_frames,
                       "ms_per_step_with_stage_events": prof_ms / prof_frames,

@@ -240,8 +240,11 @@ class World:
 
     def set_tuning(self, digit_bits_max: int | None = None, collide_block: int | None = None,
                    sort_algorithm: int | None = None, frames_per_launch: int | None = None,
-                   state_gather: int | None = None, frame_kernel: int | None = None) -> None:
+                   state_gather: int | None = None, frame_kernel: int | None = None,
+                   scatter_agents: int | None = None) -> None:
         t = self.tuning
+        if scatter_agents is not None:
+            t.scatter_agents = scatter_agents
         if state_gather is not None:
             t.state_gather = state_gather
         if frame_kernel is not None:
@@ -265,7 +268,8 @@ class World:
         self._check(self._lib.mb_autotune(self._h, frames, C.byref(best), ms, tried))
         desc = lambda t: {"sort_algorithm": t.sort_algorithm, "digit_bits_max": t.digit_bits_max,
                           "frames_per_launch": t.frames_per_launch, "state_gather": t.state_gather,
-                          "frame_kernel": t.frame_kernel, "collide_block": t.collide_block}
+                          "frame_kernel": t.frame_kernel, "collide_block": t.collide_block,
+                          "scatter_agents": max(t.scatter_agents, 1)}
         return {"best": desc(best), "candidates": [dict(desc(t), ms_per_frame=float(m)) for t, m in zip(tried, ms)]}
 
     # -- state
@@ -457,8 +461,11 @@ class Batch:
         self._check(self._lib.mb_batch_get_tuning(self._h, C.byref(t)))
         return t
 
-    def set_tuning(self, frames_per_launch: int | None = None, collide_block: int | None = None) -> None:
+    def set_tuning(self, frames_per_launch: int | None = None, collide_block: int | None = None,
+                   scatter_agents: int | None = None) -> None:
         t = self.tuning
+        if scatter_agents is not None:
+            t.scatter_agents = scatter_agents
         if frames_per_launch is not None:
             t.frames_per_launch = frames_per_launch
         if collide_block is not None:
@@ -466,13 +473,14 @@ class Batch:
         self._check(self._lib.mb_batch_set_tuning(self._h, C.byref(t)))
 
     def autotune(self, frames: int = 16) -> dict:
-        """mb_batch_autotune: time frames_per_launch x collide_block on the pool's own
-        scenes (states restored), apply the fastest; returns it and every candidate's
-        ms/frame."""
+        """mb_batch_autotune: time frames_per_launch x collide_block (and scatter_agents)
+        on the pool's own scenes (states restored), apply the fastest; returns it and
+        every candidate's ms/frame."""
         n = _abi.MB_BATCH_TUNE_CANDIDATES
         best, ms, tried = MbTuning(), (C.c_float * n)(), (MbTuning * n)()
         self._check(self._lib.mb_batch_autotune(self._h, frames, C.byref(best), ms, tried))
-        desc = lambda t: {"frames_per_launch": t.frames_per_launch, "collide_block": t.collide_block}
+        desc = lambda t: {"frames_per_launch": t.frames_per_launch, "collide_block": t.collide_block,
+                          "scatter_agents": max(t.scatter_agents, 1)}
         return {"best": desc(best), "candidates": [dict(desc(t), ms_per_frame=float(m)) for t, m in zip(tried, ms)]}
 
     def close(self) -> None:

@@ -59,14 +59,15 @@ class MbConsts(C.Structure):
 
 class MbTuning(C.Structure):
     _fields_ = [("digit_bits_max", u32), ("collide_block", u32), ("sort_algorithm", u32),
-                ("frames_per_launch", u32), ("state_gather", u32), ("frame_kernel", u32), ("reserved", u32 * 2)]
+                ("frames_per_launch", u32), ("state_gather", u32), ("frame_kernel", u32),
+                ("scatter_agents", u32), ("reserved", u32)]
 
 
 MB_SORT_COUNTING, MB_SORT_ONESWEEP = 0, 1
 MB_GATHER_COPY, MB_GATHER_INDIRECT = 0, 1
 MB_FRAME_GRAPH, MB_FRAME_FUSED = 0, 1
-MB_TUNE_CANDIDATES = 16
-MB_BATCH_TUNE_CANDIDATES = 9
+MB_TUNE_CANDIDATES = 19
+MB_BATCH_TUNE_CANDIDATES = 11
 
 
 class MbServerConfig(C.Structure):

@@ -208,7 +208,7 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         if ((e = mark(w, 1, st, capturing))) return e;
         if ((e = mb::count_scatter(w->cnt, w->keys, w->n, w->cells, w->scratch.offs, w->perm, w->pos[cur],
                                    w->vfme[cur], indirect(w) ? nullptr : w->spos, indirect(w) ? nullptr : w->svfme,
-                                   w->bands, w->P.N, st, pdl)))
+                                   w->bands, w->P.N, st, pdl, w->tuning.scatter_agents)))
             return e;
         hist = w->cnt.hist;
         coarse = w->cnt.coarse;
@@ -599,6 +599,8 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
         return fail(w, MB_ERR_INVALID_ARG, "state_gather must be MB_GATHER_COPY or MB_GATHER_INDIRECT");
     if (t->frame_kernel != MB_FRAME_GRAPH && t->frame_kernel != MB_FRAME_FUSED)
         return fail(w, MB_ERR_INVALID_ARG, "frame_kernel must be MB_FRAME_GRAPH or MB_FRAME_FUSED");
+    if (t->scatter_agents > 4u || t->scatter_agents == 3u)
+        return fail(w, MB_ERR_INVALID_ARG, "scatter_agents must be 0, 1, 2 or 4");
     if (t->frame_kernel == MB_FRAME_FUSED && t->sort_algorithm != MB_SORT_COUNTING)
         return fail(w, MB_ERR_INVALID_ARG, "MB_FRAME_FUSED runs the counting sort (sort_algorithm 0)");
     if (t->frame_kernel == MB_FRAME_FUSED && mb::fused_blocks_per_sm() <= 0)
@@ -663,16 +665,18 @@ mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* fram
     const mb_tuning start = w->tuning;
     mb_tuning cand[MB_TUNE_CANDIDATES];
     {
-        // {sort, digit bits, frames per graph launch, state gather, frame kernel, physics tile}
+        // {sort, digit bits, frames per graph launch, state gather, frame kernel, physics tile,
+        //  scatter spheres per thread}
         const uint32_t C = MB_SORT_COUNTING, O = MB_SORT_ONESWEEP, CP = MB_GATHER_COPY, IN = MB_GATHER_INDIRECT,
                        G = MB_FRAME_GRAPH, F = MB_FRAME_FUSED;
-        const uint32_t c6[MB_TUNE_CANDIDATES][6] = {
-            {C, 8u, 1u, CP, G, 128u},  {C, 8u, 8u, CP, G, 128u},  {C, 8u, 16u, CP, G, 128u},
-            {C, 8u, 8u, CP, G, 64u},   {C, 8u, 8u, CP, G, 256u},  {C, 8u, 16u, CP, G, 256u},
-            {C, 8u, 8u, CP, F, 128u},  {C, 8u, 8u, IN, G, 128u},  {C, 8u, 16u, IN, G, 128u},
-            {C, 8u, 8u, IN, G, 256u},  {C, 8u, 8u, IN, F, 128u},  {O, 6u, 8u, CP, G, 128u},
-            {O, 8u, 1u, CP, G, 128u},  {O, 8u, 8u, CP, G, 128u},  {O, 8u, 8u, IN, G, 128u},
-            {O, 11u, 8u, CP, G, 128u},
+        const uint32_t c6[MB_TUNE_CANDIDATES][7] = {
+            {C, 8u, 1u, CP, G, 128u, 1u},  {C, 8u, 8u, CP, G, 128u, 1u},  {C, 8u, 16u, CP, G, 128u, 1u},
+            {C, 8u, 8u, CP, G, 64u, 1u},   {C, 8u, 8u, CP, G, 256u, 1u},  {C, 8u, 16u, CP, G, 256u, 1u},
+            {C, 8u, 8u, CP, G, 128u, 2u},  {C, 8u, 8u, CP, G, 128u, 4u},  {C, 8u, 16u, CP, G, 256u, 2u},
+            {C, 8u, 8u, CP, F, 128u, 1u},  {C, 8u, 8u, IN, G, 128u, 1u},  {C, 8u, 16u, IN, G, 128u, 1u},
+            {C, 8u, 8u, IN, G, 256u, 1u},  {C, 8u, 8u, IN, F, 128u, 1u},  {O, 6u, 8u, CP, G, 128u, 1u},
+            {O, 8u, 1u, CP, G, 128u, 1u},  {O, 8u, 8u, CP, G, 128u, 1u},  {O, 8u, 8u, IN, G, 128u, 1u},
+            {O, 11u, 8u, CP, G, 128u, 1u},
         };
         for (uint32_t c = 0; c < MB_TUNE_CANDIDATES; ++c) {
             cand[c] = start;
@@ -682,6 +686,7 @@ mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* fram
             cand[c].state_gather = c6[c][3];
             cand[c].frame_kernel = c6[c][4];
             cand[c].collide_block = c6[c][5];
+            cand[c].scatter_agents = c6[c][6];
         }
     }
     // save what the frames overwrite

@@ -262,7 +262,7 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st, bool may_init) {
         return e;
     if ((e = mb::count_scatter_scenes(b->cnt, b->d_scenes, b->d_tile_scene, b->d_cell_tile_scene, b->keys, b->n_total,
                                       b->cells_total, b->offs, b->perm, b->pos[0], b->pos[1], b->vfme[0],
-                                      b->vfme[1], b->spos, b->svfme, b->bands, st)))
+                                      b->vfme[1], b->spos, b->svfme, b->bands, st, b->tuning.scatter_agents)))
         return e;
     if ((e = mb::launch_physics_batch(b->d_scenes, b->d_tile_scene, b->n_total, b->offs, b->bands, b->spos, b->svfme,
                                       b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->keys, b->cnt.hist,
@@ -531,6 +531,8 @@ mb_status mb_batch_set_tuning(mb_batch* b, const mb_tuning* t) {
         return bfail(b, MB_ERR_INVALID_ARG, "frames_per_launch must be 0, 1, 2, 4, 8 or 16");
     if (t->collide_block != 64u && t->collide_block != 128u && t->collide_block != 256u)
         return bfail(b, MB_ERR_INVALID_ARG, "collide_block must be 64, 128 or 256");
+    if (t->scatter_agents > 4u || t->scatter_agents == 3u)
+        return bfail(b, MB_ERR_INVALID_ARG, "scatter_agents must be 0, 1, 2 or 4");
     if (t->sort_algorithm != MB_SORT_COUNTING || t->state_gather != MB_GATHER_COPY ||
         t->frame_kernel != MB_FRAME_GRAPH)
         return bfail(b, MB_ERR_INVALID_ARG,
@@ -557,8 +559,16 @@ mb_status mb_batch_autotune(mb_batch* b, uint32_t frames, mb_tuning* best, float
                 cand[c] = start;
                 cand[c].frames_per_launch = f;
                 cand[c].collide_block = t;
+                cand[c].scatter_agents = 1u;
                 ++c;
             }
+        for (uint32_t a : {2u, 4u}) {  // spheres per scatter thread
+            cand[c] = start;
+            cand[c].frames_per_launch = 8u;
+            cand[c].collide_block = 128u;
+            cand[c].scatter_agents = a;
+            ++c;
+        }
     }
     // save what the frames overwrite: both state buffers (scenes keep their own
     // parity), keys, order, cell offsets and the host view of every scene

@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(kScanThreads)
     scan_chunk<kScenes>(blockIdx.x, hist, coarse, cells, offs, fix_ctl, scenes, cell_tile_scene, s_warp, s_base);
 }
 
+template <uint32_t kPer>
 __global__ void __launch_bounds__(256)
     k_cell_scatter(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
                    uint32_t* __restrict__ perm, const float4* __restrict__ pos_in,
@@ -58,12 +59,14 @@ __global__ void __launch_bounds__(256)
                    uint32_t N, uint32_t* __restrict__ fix_bits) {
     griddep_wait();
     griddep_launch();
-    scatter_range(blockIdx.x, gridDim.x, keys, n, hist, perm, pos_in, vfme_in, spos, svfme, offs, bands, N,
-                  fix_bits);
+    scatter_range<false, kPer>(blockIdx.x, gridDim.x, keys, n, hist, perm, pos_in, vfme_in, spos, svfme, offs, bands,
+                               N, fix_bits);
 }
 
 // The same for a batch: slot i's scene (from the tile table) gives the buffer
-// holding its state; spheres of HOLD scenes are left alone.
+// holding its state; spheres of HOLD scenes are left alone.  kPer inputs per
+// thread per step, as in scatter_range.
+template <uint32_t kPer>
 __global__ void __launch_bounds__(256)
     k_cell_scatter_scenes(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
                           const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
@@ -73,48 +76,56 @@ __global__ void __launch_bounds__(256)
                           const uint32_t* __restrict__ offs, uint32_t* __restrict__ fix_bits,
                           uint4* __restrict__ bands) {
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
-        uint32_t i = i0 + threadIdx.x;
-        bool valid = i < n;
-        uint32_t mode = kModeHold, parity = 0, sc = 0;
-        if (valid) {
-            uint32_t s = __ldg(tile_scene + i / kPhysicsTile);
-            while (i >= __ldg(&scenes[s].agent_end)) ++s;
-            mode = __ldg(&scenes[s].mode);
-            parity = __ldg(&scenes[s].parity);
-            sc = s;
+    const uint32_t stride = gridDim.x * blockDim.x * kPer;
+    for (uint32_t i0 = blockIdx.x * blockDim.x * kPer; i0 < n; i0 += stride) {
+        uint32_t k[kPer], sc[kPer];
+        bool act[kPer];
+        float4 p[kPer];
+        uint4 q[kPer];
+#pragma unroll
+        for (uint32_t r = 0; r < kPer; ++r) {
+            const uint32_t i = i0 + r * blockDim.x + threadIdx.x;
+            uint32_t mode = kModeHold, parity = 0, s = 0;
+            if (i < n) {
+                s = __ldg(tile_scene + i / kPhysicsTile);
+                while (i >= __ldg(&scenes[s].agent_end)) ++s;
+                mode = __ldg(&scenes[s].mode);
+                parity = __ldg(&scenes[s].parity);
+            }
+            sc[r] = s;
+            act[r] = i < n && mode != kModeHold;
+            k[r] = act[r] ? __ldg(keys + i) : 0xFFFFFFFFu;
+            if (act[r]) {
+                p[r] = __ldg((parity ? pos1 : pos0) + i);
+                q[r] = __ldg((parity ? vfme1 : vfme0) + i);
+            }
         }
-        valid = valid && mode != kModeHold;
-        uint32_t k = valid ? __ldg(keys + i) : 0xFFFFFFFFu;
-        float4 p;
-        uint4 q;
-        if (valid) {
-            p = __ldg((parity ? pos1 : pos0) + i);
-            q = __ldg((parity ? vfme1 : vfme0) + i);
-        }
-        const bool ident = valid && (k & kInitKeyBit);
-        uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k);
-        uint32_t leader = (uint32_t)(__ffs(peers) - 1);
-        uint32_t b = 0;
-        bool mark = false;
-        if (valid && !ident && lane == leader) {
-            const uint32_t g = (uint32_t)__popc(peers);
-            const uint32_t lo = __ldg(offs + k), hi = __ldg(offs + k + 1u);
-            b = hi - atomicSub(hist + k, g);  // the run's first slot
-            mark = listed(lo, hi, b, g);
-        }
-        b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
-        mark_fix(fix_bits, i, n, mark);
-        if (valid) {
+#pragma unroll
+        for (uint32_t r = 0; r < kPer; ++r) {
+            const uint32_t i = i0 + r * blockDim.x + threadIdx.x;
+            const bool valid = act[r];
+            const bool ident = valid && (k[r] & kInitKeyBit);
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k[r]);
+            const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+            uint32_t b = 0;
+            bool mark = false;
+            if (valid && !ident && lane == leader) {
+                const uint32_t g = (uint32_t)__popc(peers);
+                const uint32_t lo = __ldg(offs + k[r]), hi = __ldg(offs + k[r] + 1u);
+                b = hi - atomicSub(hist + k[r], g);  // the run's first slot
+                mark = listed(lo, hi, b, g);
+            }
+            b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
+            mark_fix(fix_bits, i, n, mark);
             const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
-            if (dst >= n) continue;  // only counts that disagree with the keys get here
-            perm[dst] = i;
-            spos[dst] = p;
-            svfme[dst] = q;
-            if (bands && !ident) {  // the scene's band table entries, in its own cell coordinates
-                const uint32_t cb = __ldg(&scenes[sc].cell_base);
-                write_band_bounds(bands, offs + cb, __ldg(&scenes[sc].P.N), n, dst, k - cb);
+            if (valid && dst < n) {  // only counts that disagree with the keys fail dst < n
+                perm[dst] = i;
+                spos[dst] = p[r];
+                svfme[dst] = q[r];
+                if (bands && !ident) {  // the scene's band table entries, in its own cell coordinates
+                    const uint32_t cb = __ldg(&scenes[sc[r]].cell_base);
+                    write_band_bounds(bands, offs + cb, __ldg(&scenes[sc[r]].P.N), n, dst, k[r] - cb);
+                }
             }
         }
     }
@@ -297,12 +308,16 @@ cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t*
 
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
-                          float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st, bool pdl) {
+                          float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st, bool pdl,
+                          uint32_t per_thread) {
     cudaError_t e;
     if (n) {
-        uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
-        if ((e = launch_pdl(pdl, k_cell_scatter, dim3(blocks), dim3(256), 0, st, keys, n, s.hist, perm, pos_in,
-                            vfme_in, spos, svfme, offs, bands, N, s.fix_bits)))
+        const uint32_t per = per_thread == 4u ? 4u : (per_thread == 2u ? 2u : 1u);
+        const uint32_t blocks = std::min<uint32_t>((n + 256u * per - 1u) / (256u * per),
+                                                   (uint32_t)device_sm_count() * 8u);
+        auto* kern = per == 4u ? k_cell_scatter<4> : (per == 2u ? k_cell_scatter<2> : k_cell_scatter<1>);
+        if ((e = launch_pdl(pdl, kern, dim3(blocks), dim3(256), 0, st, keys, n, s.hist, perm, pos_in, vfme_in, spos,
+                            svfme, offs, bands, N, s.fix_bits)))
             return e;
         const OneBuffer src{pos_in, vfme_in};
         if ((e = launch_pdl(pdl, k_fix_marked<OneBuffer>, dim3(collect_grid(n)), dim3(kCollectThreads), 0, st,
@@ -326,13 +341,16 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
                                  const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
                                  const uint32_t* offs, uint32_t* perm, const float4* pos_buf0,
                                  const float4* pos_buf1, const uint4* vfme_buf0, const uint4* vfme_buf1,
-                                 float4* spos, uint4* svfme, uint4* bands, cudaStream_t st) {
+                                 float4* spos, uint4* svfme, uint4* bands, cudaStream_t st, uint32_t per_thread) {
     cudaError_t e;
     if (n) {
-        uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
-        k_cell_scatter_scenes<<<blocks, 256, 0, st>>>(scenes, tile_scene, keys, n, s.hist, perm, pos_buf0,
-                                                      pos_buf1, vfme_buf0, vfme_buf1, spos, svfme, offs,
-                                                      s.fix_bits, bands);
+        const uint32_t per = per_thread == 4u ? 4u : (per_thread == 2u ? 2u : 1u);
+        const uint32_t blocks = std::min<uint32_t>((n + 256u * per - 1u) / (256u * per),
+                                                   (uint32_t)device_sm_count() * 8u);
+        auto* kern = per == 4u ? k_cell_scatter_scenes<4>
+                               : (per == 2u ? k_cell_scatter_scenes<2> : k_cell_scatter_scenes<1>);
+        kern<<<blocks, 256, 0, st>>>(scenes, tile_scene, keys, n, s.hist, perm, pos_buf0, pos_buf1, vfme_buf0,
+                                     vfme_buf1, spos, svfme, offs, s.fix_bits, bands);
         if ((e = cudaGetLastError())) return e;
         const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
         k_fix_marked<SceneBuffers><<<collect_grid(n), kCollectThreads, 0, st>>>(s.fix_bits, keys, n, offs, perm,

@@ -139,8 +139,10 @@ __device__ __forceinline__ void mark_fix(uint32_t* __restrict__ fix_bits, uint32
 // and, where a slot begins or ends a physics tile, writes that side of the
 // tile's band table entry (the cell of a slot is final here; the fixup only
 // reorders slots inside a cell).
-// Input slots [vb * 256, ...) with a stride of nvb * 256 (256-thread blocks).
-template <bool kCg = false>
+// Input slots [vb * 256 kPer, ...) with a stride of nvb * 256 kPer (256-thread
+// blocks): each thread takes kPer inputs 256 apart per step, their loads issued
+// together (the agents-per-thread knob; warps still see 32 consecutive inputs).
+template <bool kCg = false, uint32_t kPer = 1>
 __device__ __forceinline__ void scatter_range(uint32_t vb, uint32_t nvb, const uint32_t* __restrict__ keys,
                                               uint32_t n, uint32_t* __restrict__ hist,
                                               uint32_t* __restrict__ perm, const float4* __restrict__ pos_in,
@@ -149,41 +151,49 @@ __device__ __forceinline__ void scatter_range(uint32_t vb, uint32_t nvb, const u
                                               uint4* __restrict__ bands, uint32_t N,
                                               uint32_t* __restrict__ fix_bits) {
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
-    const uint32_t stride = nvb * blockDim.x;
-    for (uint32_t i0 = vb * blockDim.x; i0 < n; i0 += stride) {
-        uint32_t i = i0 + threadIdx.x;
-        bool valid = i < n;
-        uint32_t k = valid ? ld_in<kCg>(keys + i) : 0xFFFFFFFFu;
-        float4 p;
-        uint4 q;
-        if (valid && spos) {
-            p = ld_in<kCg>(pos_in + i);
-            q = ld_in<kCg>(vfme_in + i);
-        }
-        // a key flagged kInitKeyBit belongs to a scene in its INIT frame: all its
-        // keys are equal, so its stable order is the identity and the slot is i
-        const bool ident = valid && (k & kInitKeyBit);
-        uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k);
-        uint32_t leader = (uint32_t)(__ffs(peers) - 1);
-        uint32_t b = 0;
-        bool mark = false;
-        if (valid && !ident && lane == leader) {
-            const uint32_t g = (uint32_t)__popc(peers);
-            const uint32_t lo = ld_in<kCg>(offs + k), hi = ld_in<kCg>(offs + k + 1u);
-            b = hi - atomicSub(hist + k, g);  // the run's first slot
-            mark = listed(lo, hi, b, g);
-        }
-        b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
-        mark_fix(fix_bits, i, n, mark);
-        if (valid) {
-            const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
-            if (dst >= n) continue;  // only counts that disagree with the keys get here
-            perm[dst] = i;
-            if (spos) {
-                spos[dst] = p;
-                svfme[dst] = q;
+    const uint32_t stride = nvb * blockDim.x * kPer;
+    for (uint32_t i0 = vb * blockDim.x * kPer; i0 < n; i0 += stride) {
+        uint32_t k[kPer];
+        float4 p[kPer];
+        uint4 q[kPer];
+#pragma unroll
+        for (uint32_t r = 0; r < kPer; ++r) {
+            const uint32_t i = i0 + r * blockDim.x + threadIdx.x;
+            const bool valid = i < n;
+            k[r] = valid ? ld_in<kCg>(keys + i) : 0xFFFFFFFFu;
+            if (valid && spos) {
+                p[r] = ld_in<kCg>(pos_in + i);
+                q[r] = ld_in<kCg>(vfme_in + i);
             }
-            if (bands && !ident) write_band_bounds<kCg>(bands, offs, N, n, dst, k);
+        }
+#pragma unroll
+        for (uint32_t r = 0; r < kPer; ++r) {
+            const uint32_t i = i0 + r * blockDim.x + threadIdx.x;
+            const bool valid = i < n;
+            // a key flagged kInitKeyBit belongs to a scene in its INIT frame: all its
+            // keys are equal, so its stable order is the identity and the slot is i
+            const bool ident = valid && (k[r] & kInitKeyBit);
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, ident ? 0xFFFFFFFEu : k[r]);
+            const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+            uint32_t b = 0;
+            bool mark = false;
+            if (valid && !ident && lane == leader) {
+                const uint32_t g = (uint32_t)__popc(peers);
+                const uint32_t lo = ld_in<kCg>(offs + k[r]), hi = ld_in<kCg>(offs + k[r] + 1u);
+                b = hi - atomicSub(hist + k[r], g);  // the run's first slot
+                mark = listed(lo, hi, b, g);
+            }
+            b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
+            mark_fix(fix_bits, i, n, mark);
+            const uint32_t dst = ident ? i : b + (uint32_t)__popc(peers & lt);
+            if (valid && dst < n) {  // only counts that disagree with the keys fail dst < n
+                perm[dst] = i;
+                if (spos) {
+                    spos[dst] = p[r];
+                    svfme[dst] = q[r];
+                }
+                if (bands && !ident) write_band_bounds<kCg>(bands, offs, N, n, dst, k[r]);
+            }
         }
     }
 }

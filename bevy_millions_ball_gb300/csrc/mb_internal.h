@@ -330,10 +330,11 @@ cudaError_t count_init_order(CountScratch& s, uint32_t n, uint32_t cells, uint32
 // and the counts in hist (counted back down to 0); spos/svfme (nullable
 // together) := the state in that order (spos[j] = pos_in[perm[j]]); bands
 // (nullable) := the band table of that order for an N x N grid; coarse := 0.
+// per_thread: inputs each scatter thread takes per step (1, 2 or 4).
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
                           float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,
-                          bool pdl = false);
+                          bool pdl = false, uint32_t per_thread = 1);
 // Batched count scan: scene cell ranges are padded to whole scan tiles
 // (cell_tile_scene[t] = scene of tile t); tiles of HOLD scenes are skipped.
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
@@ -344,7 +345,8 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
                                  const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
                                  const uint32_t* offs, uint32_t* perm, const float4* pos_buf0,
                                  const float4* pos_buf1, const uint4* vfme_buf0, const uint4* vfme_buf1,
-                                 float4* spos, uint4* svfme, uint4* bands, cudaStream_t st);
+                                 float4* spos, uint4* svfme, uint4* bands, cudaStream_t st,
+                                 uint32_t per_thread = 1);
 // spos/svfme := pos_in/vfme_in gathered through perm (after the onesweep sort);
 // bands (nullable) := the band table of the sorted keys for an N x N grid.
 cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in, const uint4* vfme_in,

@@ -267,7 +267,10 @@ typedef struct mb_tuning {
                                    1, 2, 4, 8 (default; 0 reads as 8) or 16 */
     uint32_t state_gather;     /* MB_GATHER_COPY or MB_GATHER_INDIRECT (below) */
     uint32_t frame_kernel;     /* MB_FRAME_GRAPH or MB_FRAME_FUSED (below) */
-    uint32_t reserved[2];
+    uint32_t scatter_agents;   /* spheres each thread of the counting sort's scatter takes per
+                                  step: 1 (default; 0 reads as 1), 2 or 4; MB_FRAME_FUSED
+                                  frames run 1 */
+    uint32_t reserved;
 } mb_tuning;
 
 /* How LOOP frames are launched:
@@ -334,7 +337,7 @@ mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float 
  * order of tried[] (nullable, same length).  Needs a frame to have run since the
  * last upload (MB_ERR_NOT_READY otherwise).  Allocates temporary device memory.
  */
-#define MB_TUNE_CANDIDATES 16u
+#define MB_TUNE_CANDIDATES 19u
 mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* frame_ms, mb_tuning* tried);
 
 /*
@@ -391,20 +394,21 @@ mb_status mb_batch_get_debug(mb_batch* b, uint32_t scene, uint32_t* keys, uint32
 /*
  * Kernel choices of a batch (the knobs of mb_tuning that apply to a pool):
  * frames_per_launch (frames captured per graph launch while no scene changes
- * mode: 1, 2, 4, 8 (default) or 16) and collide_block (physics tile: 64, 128
- * (default) or 256 slots).  The other fields must keep their defaults
- * (counting sort, sorted copy, per-stage kernels).
+ * mode: 1, 2, 4, 8 (default) or 16), collide_block (physics tile: 64, 128
+ * (default) or 256 slots) and scatter_agents (1, 2 or 4).  The other fields
+ * must keep their defaults (counting sort, sorted copy, per-stage kernels).
  *
  * mb_batch_autotune: the world autotuner's counterpart for a pool (no
  * counterpart in the reference, whose passes have fixed workgroup shapes,
  * src/physics/mod.rs:35): times frames_per_launch {1, 8, 16} x collide_block
- * {64, 128, 256} on the pool's own scenes for `frames` frames each (one warm-up
+ * {64, 128, 256}, then scatter_agents 2 and 4 at 8 frames per launch and
+ * 128-slot tiles, on the pool's own scenes for `frames` frames each (one warm-up
  * frame per candidate), restoring every scene's state, keys, order, cell ranges
  * and time before each and at the end, then applies the fastest.  Every scene
  * needs a frame since its upload.  frame_ms / tried (nullable) receive
  * MB_BATCH_TUNE_CANDIDATES entries.  Allocates temporary device memory.
  */
-#define MB_BATCH_TUNE_CANDIDATES 9u
+#define MB_BATCH_TUNE_CANDIDATES 11u
 mb_status mb_batch_get_tuning(const mb_batch* b, mb_tuning* out);
 mb_status mb_batch_set_tuning(mb_batch* b, const mb_tuning* t);
 mb_status mb_batch_autotune(mb_batch* b, uint32_t frames, mb_tuning* best, float* frame_ms, mb_tuning* tried);

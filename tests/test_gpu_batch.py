@@ -6,7 +6,7 @@ import math
 import numpy as np
 import pytest
 
-from bevy_millions_ball_gb300 import Batch, MbError, Server, World, scenes
+from bevy_millions_ball_gb300 import Batch, MbError, Server, World, _abi, scenes
 
 pytestmark = pytest.mark.gpu
 INV = 0xFFFFFFFF
@@ -201,8 +201,23 @@ def test_batch_tuning_keeps_results(built_lib, cuda, tile, fpl):
             b.set_tuning(collide_block=100)
 
 
+@pytest.mark.parametrize("agents", [2, 4])
+def test_batch_scatter_agents(built_lib, cuda, agents):
+    """2 or 4 spheres per scatter thread in a pool: each scene exactly its lone-world result."""
+    scs = mixed_scenes(7, seed=23)
+    with Batch([s.plugin for s in scs]) as b:
+        b.set_tuning(scatter_agents=agents)
+        for i, s in enumerate(scs):
+            b.set_state(i, s.pos_scale, s.vfme)
+        b.step(19)
+        for i, s in enumerate(scs):
+            assert_same(b, i, alone(s, 19), f"scene {i}, {agents} spheres per scatter thread")
+        with pytest.raises(MbError):
+            b.set_tuning(scatter_agents=3)
+
+
 def test_batch_autotune_restores_the_pool(built_lib, cuda):
-    """mb_batch_autotune times its nine candidates on the pool and restores every
+    """mb_batch_autotune times its candidates on the pool and restores every
     scene (state, parity, time): the pool then continues exactly like lone worlds."""
     scs = mixed_scenes(8, seed=22)
     with Batch([s.plugin for s in scs]) as b:
@@ -210,9 +225,11 @@ def test_batch_autotune_restores_the_pool(built_lib, cuda):
             b.set_state(i, s.pos_scale, s.vfme)
         b.step(5)
         res = b.autotune(frames=8)
-        assert len(res["candidates"]) == 9 and all(c["ms_per_frame"] > 0 for c in res["candidates"])
+        assert len(res["candidates"]) == _abi.MB_BATCH_TUNE_CANDIDATES
+        assert all(c["ms_per_frame"] > 0 for c in res["candidates"])
         t = b.tuning
-        assert {"frames_per_launch": t.frames_per_launch, "collide_block": t.collide_block} == res["best"]
+        assert {"frames_per_launch": t.frames_per_launch, "collide_block": t.collide_block,
+                "scatter_agents": max(t.scatter_agents, 1)} == res["best"]
         assert all(b.time(i) == 5 for i in range(len(scs)))
         b.step(20)
         for i, s in enumerate(scs):

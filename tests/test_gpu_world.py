@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import oracle
-from bevy_millions_ball_gb300 import MbError, PhysicsPlugin, World, pack_vfme, scenes
+from bevy_millions_ball_gb300 import MbError, PhysicsPlugin, World, _abi, pack_vfme, scenes
 from tests.conftest import GOLDEN
 from tests.test_oracle import settings_from_fixture
 
@@ -265,6 +265,30 @@ def test_collide_block_sizes(built_lib, cuda, case, tile):
             w.set_tuning(collide_block=96)
 
 
+@pytest.mark.parametrize("agents", [2, 4])
+@pytest.mark.parametrize("case", ["small", "clustered", "crowded", "ragged"])
+def test_scatter_agents(built_lib, cuda, case, agents):
+    """scatter_agents: 2 or 4 spheres per thread of the counting sort's scatter
+    (grid-stride steps of 256 x agents inputs, ragged tails); bit-exact against
+    the oracle, with the sorted copy and with the gather through the permutation."""
+    for gather in (0, 1):
+        tuning = {"scatter_agents": agents, "state_gather": gather}
+        if case == "small":
+            run_pair(scenes.workload("P-small"), 21, [1, 2, 21], tuning=tuning)
+        elif case == "clustered":
+            run_pair(scenes.plain_clustered(262_144, 512, clusters=4, sigma_xz=16.0, seed=9), 12, [1, 2, 12],
+                     tuning=tuning)
+        elif case == "crowded":
+            run_pair(scenes.plain_uniform(51_200, 16, grid_size=1, half_map_height=8, seed=31), 4, [1, 2, 4],
+                     tuning=tuning)
+        else:  # n not a multiple of the step, smaller than one block's step
+            run_pair(scenes.plain_uniform(777 + 256 * agents + 3, 64, seed=14), 25, [1, 2, 25], tuning=tuning)
+    with World(scenes.plain_uniform(1000, 32).plugin) as w:
+        for bad in (3, 5, 8):
+            with pytest.raises(MbError):
+                w.set_tuning(scatter_agents=bad)
+
+
 FUSED = {"frame_kernel": 1}
 
 
@@ -490,12 +514,13 @@ def test_autotune_keeps_the_frame_sequence(built_lib, cuda):
         w.step(5)
         ow.step(5)
         res = w.autotune(frames=8)
-        assert len(res["candidates"]) == 16 and all(c["ms_per_frame"] > 0 for c in res["candidates"])
+        assert len(res["candidates"]) == _abi.MB_TUNE_CANDIDATES
+        assert all(c["ms_per_frame"] > 0 for c in res["candidates"])
         fastest = min(res["candidates"], key=lambda c: c["ms_per_frame"])
         assert res["best"] == {k: fastest[k] for k in res["best"]}
         t = w.tuning
         assert (t.sort_algorithm, t.digit_bits_max, t.frames_per_launch, t.state_gather,
-                t.frame_kernel, t.collide_block) == tuple(res["best"].values())
+                t.frame_kernel, t.collide_block, max(t.scatter_agents, 1)) == tuple(res["best"].values())
         assert w.time == 5
         compare(w, ow, 5)
         w.step(21)
