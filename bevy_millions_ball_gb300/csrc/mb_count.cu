@@ -22,10 +22,9 @@
 //      of other warps got there first (only such cells can be out of order);
 //   4. k_fix_marked: the marked cells' slots are put back in ascending input
 //      order (what a stable sort yields), re-gathering their state copy - cells
-//      of up to 8 slots by the thread that reads the mark; larger ones are
-//      listed by size;
-//   5. k_cell_fix: the listed cells, a warp each up to 256 slots, a block each
-//      above; clears the counts for the next frame.
+//      of up to 8 slots by the thread that reads the mark, up to 256 by a warp
+//      of the block that found them, larger ones by the last block to finish;
+//      it also clears the tile counts for the next frame.
 //
 // The result is bit-identical to a stable sort; offs[] replaces start/close.
 
@@ -134,26 +133,15 @@ __global__ void __launch_bounds__(256)
 template <class Src>
 __global__ void __launch_bounds__(kCollectThreads)
     k_fix_marked(const uint32_t* __restrict__ fix_bits, const uint32_t* __restrict__ keys, uint32_t n,
-                 const uint32_t* __restrict__ offs, uint32_t* perm, FixLists lists, Src src,
-                 float4* __restrict__ spos, uint4* __restrict__ svfme) {
-    __shared__ uint32_t s_slot[kCollectThreads * 8u], s_big[2u * kCollectThreads * 8u], s_cnt[4];
+                 const uint32_t* __restrict__ offs, uint32_t* perm, FixLists lists, uint32_t* __restrict__ tmp,
+                 Src src, float4* __restrict__ spos, uint4* __restrict__ svfme, uint32_t* __restrict__ hist,
+                 uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles) {
+    __shared__ MarkedSmem S;
     griddep_wait();  // the scatter's bitmap and order are complete
     griddep_launch();
-    fix_marked_block<Src>(blockIdx.x, fix_bits, keys, n, offs, perm, lists, src, spos, svfme, s_slot, s_big, s_cnt);
-}
-
-template <class Src>
-__global__ void __launch_bounds__(kFixThreads)
-    k_cell_fix(const uint32_t* __restrict__ offs, uint32_t* perm, uint32_t* __restrict__ hist, uint32_t cells,
-               uint32_t* __restrict__ coarse, uint32_t tiles,
-               FixLists lists, uint32_t* __restrict__ tmp, Src src,
-               float4* __restrict__ spos, uint4* __restrict__ svfme) {
-    __shared__ uint32_t s_v[kBitmapWords];
-    __shared__ uint32_t s_red[kFixThreads / 32 + 1];
-    griddep_wait();
-    griddep_launch();
-    fix_block(blockIdx.x, gridDim.x, offs, perm, hist, cells, coarse, tiles, lists, tmp, src, spos, svfme, s_v,
-              s_red);
+    clear_counts(blockIdx.x, gridDim.x, src, hist, cells, coarse, tiles);
+    fix_marked_block<Src, false, true>(blockIdx.x, gridDim.x, fix_bits, keys, n, offs, perm, lists, tmp, src, spos,
+                                       svfme, S);
 }
 
 // INIT frame after an upload: every key is 0, so the stable order is the
@@ -229,19 +217,18 @@ namespace {
 FixLists fix_lists(const CountScratch& s) {
     return FixLists{s.fix_ctl, {s.fix[0], s.fix[1], s.fix[2]}, {s.fix_cap[0], s.fix_cap[1], s.fix_cap[2]}};
 }
-uint32_t fix_blocks() { return (uint32_t)device_sm_count() * 4u; }
 uint32_t fix_words(uint32_t max_keys) { return max_keys / 32u + 1u; }
 uint32_t collect_grid(uint32_t n) { return ((n + 31u) / 32u + kCollectWords - 1u) / kCollectWords; }
 uint32_t scan_tiles(uint32_t cells) { return (cells + kScanTile - 1u) / kScanTile; }
 uint32_t fix_capacity(int cls, uint32_t max_cells, uint32_t max_keys) {
-    const uint32_t per = cls == kFixListSmall ? 2u : (cls == kFixListWarp ? kFixSmall + 1u : kFixWarp + 1u);
-    return std::min(max_cells, max_keys / per) + 1u;
+    if (cls != kFixListHuge) return 1u;  // only cells above kFixWarp slots are listed
+    return std::min(max_cells, max_keys / (kFixWarp + 1u)) + 1u;
 }
 }  // namespace
 
 uint64_t count_scratch_bytes(uint32_t max_cells, uint32_t max_keys) {
     const uint64_t padded = ((uint64_t)max_cells + kScanTile) & ~(uint64_t)15;
-    uint64_t b = 4u * (padded + (max_cells + kScanTile - 1u) / kScanTile + 1u + kFixLists);
+    uint64_t b = 4u * (padded + (max_cells + kScanTile - 1u) / kScanTile + 1u + kFixCtlWords);
     for (int c = 0; c < kFixLists; ++c) b += 4u * fix_capacity(c, max_cells, max_keys);
     return b + 4u * ((uint64_t)max_keys + 1u) + 4u * (uint64_t)fix_words(max_keys);
 }
@@ -253,7 +240,7 @@ cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells, uint32_t ma
     cudaError_t e;
     if ((e = cudaMalloc(&s.hist, sizeof(uint32_t) * padded))) return e;
     if ((e = cudaMalloc(&s.coarse, sizeof(uint32_t) * (s.tiles + 1u)))) return e;
-    if ((e = cudaMalloc(&s.fix_ctl, sizeof(uint32_t) * kFixLists))) return e;
+    if ((e = cudaMalloc(&s.fix_ctl, sizeof(uint32_t) * kFixCtlWords))) return e;
     if ((e = cudaMalloc(&s.fix_tmp, sizeof(uint32_t) * ((size_t)max_keys + 1u)))) return e;
     if ((e = cudaMalloc(&s.fix_bits, sizeof(uint32_t) * fix_words(max_keys)))) return e;
     for (int c = 0; c < kFixLists; ++c) {
@@ -262,7 +249,7 @@ cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells, uint32_t ma
     }
     if ((e = cudaMemset(s.hist, 0, sizeof(uint32_t) * padded))) return e;
     if ((e = cudaMemset(s.coarse, 0, sizeof(uint32_t) * (s.tiles + 1u)))) return e;
-    if ((e = cudaMemset(s.fix_ctl, 0, sizeof(uint32_t) * kFixLists))) return e;
+    if ((e = cudaMemset(s.fix_ctl, 0, sizeof(uint32_t) * kFixCtlWords))) return e;
     return cudaSuccess;
 }
 
@@ -319,14 +306,11 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
         if ((e = launch_pdl(pdl, kern, dim3(blocks), dim3(256), 0, st, keys, n, s.hist, perm, pos_in, vfme_in, spos,
                             svfme, offs, bands, N, s.fix_bits)))
             return e;
-        const OneBuffer src{pos_in, vfme_in};
-        if ((e = launch_pdl(pdl, k_fix_marked<OneBuffer>, dim3(collect_grid(n)), dim3(kCollectThreads), 0, st,
-                            (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s), src, spos, svfme)))
-            return e;
     }
-    OneBuffer src{pos_in, vfme_in};
-    return launch_pdl(pdl && n, k_cell_fix<OneBuffer>, dim3(fix_blocks()), dim3(kFixThreads), 0, st, offs, perm,
-                      s.hist, cells, s.coarse, scan_tiles(cells), fix_lists(s), s.fix_tmp, src, spos, svfme);
+    const OneBuffer src{pos_in, vfme_in};
+    return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(std::max(collect_grid(n), 1u)),
+                      dim3(kCollectThreads), 0, st, (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s),
+                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells));
 }
 
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
@@ -352,15 +336,11 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
         kern<<<blocks, 256, 0, st>>>(scenes, tile_scene, keys, n, s.hist, perm, pos_buf0, pos_buf1, vfme_buf0,
                                      vfme_buf1, spos, svfme, offs, s.fix_bits, bands);
         if ((e = cudaGetLastError())) return e;
-        const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
-        k_fix_marked<SceneBuffers><<<collect_grid(n), kCollectThreads, 0, st>>>(s.fix_bits, keys, n, offs, perm,
-                                                                                fix_lists(s), src, spos, svfme);
-        if ((e = cudaGetLastError())) return e;
     }
-    SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
-    k_cell_fix<SceneBuffers><<<fix_blocks(), kFixThreads, 0, st>>>(offs, perm, s.hist, cells, s.coarse,
-                                                                   scan_tiles(cells),
-                                                                   fix_lists(s), s.fix_tmp, src, spos, svfme);
+    const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
+    k_fix_marked<SceneBuffers><<<std::max(collect_grid(n), 1u), kCollectThreads, 0, st>>>(
+        s.fix_bits, keys, n, offs, perm, fix_lists(s), s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse,
+        scan_tiles(cells));
     return cudaGetLastError();
 }
 

@@ -201,6 +201,7 @@ __device__ __forceinline__ void scatter_range(uint32_t vb, uint32_t nvb, const u
 // The marked cells are read kCollectWords bitmap words per block of
 // kCollectThreads threads, a byte (8 input slots) per thread.
 constexpr uint32_t kCollectThreads = 256, kCollectWords = kCollectThreads / 4u;
+constexpr uint32_t kMarkedBitmapWords = 2u * kCollectThreads * 8u;  // the last block's bitmap: 16 KB
 
 // ---------------------------------------------------------------- fixup
 // The listed cells get their slots back in ascending input order
@@ -395,118 +396,44 @@ __device__ __forceinline__ void fix_warp_cell(uint32_t lo, uint32_t m, uint32_t 
 }
 
 // ---------------------------------------------------------------- marked cells
-// One block (kCollectThreads threads) of the fixup of the marked cells: it reads
-// kCollectWords words of the bitmap, a byte (8 input slots) per thread.  A
-// marked input slot names a cell (its key) that runs of several warps filled.
-// Each warp gathers the marked slots of its 256 input slots in shared memory and
-// deals them out to its lanes, so a lane usually has one cell at most: cells of
-// up to kFixSmall slots are put back in input order by that lane; larger cells
-// are listed by size (one atomic per list per block) for fix_block, which shares
-// them out over the whole grid (crowded scenes mark many close together).
-// s_slot: kCollectThreads * 8 words; s_big: 2 x kCollectThreads * 8 words;
-// s_cnt: 4 words.
-template <class Src, bool kCg = false>
-__device__ __forceinline__ void fix_marked_block(uint32_t vb, const uint32_t* __restrict__ fix_bits,
-                                                 const uint32_t* __restrict__ keys, uint32_t n,
-                                                 const uint32_t* __restrict__ offs, uint32_t* perm,
-                                                 const FixLists& lists, const Src& src, float4* __restrict__ spos,
-                                                 uint4* __restrict__ svfme, uint32_t* s_slot, uint32_t* s_big,
-                                                 uint32_t* s_cnt) {
-    constexpr uint32_t kPerWarp = 32u * 8u;  // input slots a warp reads the marks of
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t words = (n + 31u) / 32u;
-    const uint32_t w = vb * kCollectWords + tid / 4u, sh = 8u * (tid & 3u);
-    uint32_t byte = w < words ? (__ldcg(fix_bits + w) >> sh) & 0xFFu : 0u;
-    if (tid < 2u) s_cnt[tid] = 0u;
-    // compact the warp's marked slots
-    const uint32_t cnt = (uint32_t)__popc(byte);
-    uint32_t incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= (uint32_t)o) incl += y;
-    }
-    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    uint32_t* const my = s_slot + warp * kPerWarp;
-    for (uint32_t at = incl - cnt; byte; byte &= byte - 1u, ++at) my[at] = 32u * w + sh + (uint32_t)(__ffs(byte) - 1);
-    __syncthreads();  // slots written; list counters cleared
-    for (uint32_t k = lane; k < total; k += 32u) {
-        const uint32_t c = ld_in<kCg>(keys + my[k]);
-        const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;
-        if (m <= kFixSmall) {
-            fix_small_cell<Src, kCg>(lo, m, perm, src, spos, svfme);
-        } else {
-            const uint32_t l = m <= kFixWarp ? 0u : 1u;
-            s_big[l * kCollectThreads * 8u + atomicAdd(&s_cnt[l], 1u)] = c;
-        }
-    }
-    __syncthreads();
-    if (tid < 2u && s_cnt[tid]) s_cnt[2u + tid] = atomicAdd(lists.ctl + (tid == 0u ? kFixListWarp : kFixListHuge), s_cnt[tid]);
-    __syncthreads();
-#pragma unroll
-    for (uint32_t l = 0; l < 2u; ++l) {
-        const int cls = l == 0u ? kFixListWarp : kFixListHuge;
-        for (uint32_t j = tid; j < s_cnt[l]; j += kCollectThreads) {
-            const uint32_t at = s_cnt[2u + l] + j;  // lists hold every cell that can qualify
-            if (at < lists.cap[cls]) lists.list[cls][at] = s_big[l * kCollectThreads * 8u + j];
-        }
-    }
-}
-
-// Block vb of nvb (kFixThreads threads; the lists are shared out grid-stride);
-// s_v: kBitmapWords words, s_red: kFixThreads / 32 + 1 words.
-template <class Src, bool kCg = false>
-__device__ __forceinline__ void fix_block(uint32_t vb, uint32_t nvb, const uint32_t* __restrict__ offs,
-                                          uint32_t* perm, uint32_t* __restrict__ hist, uint32_t cells,
-                                          uint32_t* __restrict__ coarse, uint32_t tiles, const FixLists& lists,
-                                          uint32_t* __restrict__ tmp, const Src& src, float4* __restrict__ spos,
-                                          uint4* __restrict__ svfme, uint32_t* s_v, uint32_t* s_red) {
-    const uint32_t tid = threadIdx.x, lane = tid & 31u;
-    // the scan of this frame is over: clear the tile counts for the next one; the
-    // cell counts went back to zero in the scatter, except those of scenes in
-    // their INIT frame (placed in identity order, nothing subtracted)
+// The sort of this frame is past its scan: clear the tile counts for the next
+// frame's physics pass (block 0) and the cell counts of scenes in their INIT
+// frame, which the scatter does not count down (they keep identity order).
+template <class Src>
+__device__ __forceinline__ void clear_counts(uint32_t vb, uint32_t nvb, const Src& src, uint32_t* __restrict__ hist,
+                                             uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles) {
+    const uint32_t tid = threadIdx.x;
     if (vb == 0)
         for (uint32_t t = tid; t < tiles; t += blockDim.x)
             if (src.tile_active(t)) coarse[t] = 0u;
     if (src.any_init())
         for (uint32_t c = (vb * blockDim.x + tid) * 4u; c < cells; c += nvb * blockDim.x * 4u)
             if (src.tile_init(c / kScanTile)) *reinterpret_cast<uint4*>(hist + c) = make_uint4(0u, 0u, 0u, 0u);
+}
 
-    const uint32_t* __restrict__ small = lists.list[0];
-    const uint32_t* __restrict__ mid = lists.list[1];
-    const uint32_t* __restrict__ huge = lists.list[2];
-
-    // small cells: one thread each, the cell held in registers (a sorting
-    // network over kFixSmall slots; empty slots hold 0xFFFFFFFF and stay last)
-    const uint32_t n_small = min(ld_cur<kCg>(lists.ctl + kFixListSmall), lists.cap[0]);
-    for (uint32_t x = vb * blockDim.x + tid; x < n_small; x += nvb * blockDim.x) {
-        const uint32_t c = ld_cur<kCg>(small + x);
-        const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;
-        fix_small_cell<Src, kCg>(lo, m, perm, src, spos, svfme);
-    }
-
-    // mid cells: one warp each, a bitonic sort of the cell's input indices held
-    // in registers (slot e = 32 s + lane is v[s]; padded with 0xFFFFFFFF to 32 S
-    // slots, S a power of two)
-    const uint32_t n_mid = min(ld_cur<kCg>(lists.ctl + kFixListWarp), lists.cap[1]);
-    const uint32_t warps = nvb * (blockDim.x / 32u);
-    for (uint32_t x = vb * (blockDim.x / 32u) + tid / 32u; x < n_mid; x += warps) {
-        const uint32_t c = ld_cur<kCg>(mid + x);
-        const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;  // 9 <= m <= kFixWarp
-        fix_warp_cell<Src, kCg>(lo, m, lane, perm, src, spos, svfme);
-    }
-
-    // huge cells: one block each.  The cell's input indices are copied aside,
-    // then each chunk of their value range becomes a bitmap in shared memory: the
-    // set bits, read in order, are the chunk's indices in ascending order, and a
-    // block scan of per-thread bit counts gives every thread its output position.
-    const uint32_t n_huge = min(ld_cur<kCg>(lists.ctl + kFixListHuge), lists.cap[2]);
+// Cells of more than kFixWarp slots listed in lists.list[kFixListHuge], one block
+// each (block vb of nvb; kFixThreads threads, kWords a multiple of them).  The
+// cell's input indices are copied aside, then each chunk of their value range
+// becomes a bitmap in shared memory: the set bits, read in order, are the chunk's
+// indices in ascending order, and a block scan of per-thread bit counts gives
+// every thread its output position.  The list was written by other blocks of
+// the same launch or an earlier one: read from L2.  s_v: kWords words, s_red:
+// kFixThreads / 32 + 1 words.
+template <class Src, bool kCg, uint32_t kWords>
+__device__ __forceinline__ void fix_huge(uint32_t vb, uint32_t nvb, const FixLists& lists,
+                                         const uint32_t* __restrict__ offs, uint32_t* perm,
+                                         uint32_t* __restrict__ tmp, const Src& src, float4* __restrict__ spos,
+                                         uint4* __restrict__ svfme, uint32_t* s_v, uint32_t* s_red) {
+    constexpr uint32_t kValues = kWords * 32u, kWordsPer = kWords / kFixThreads;
+    static_assert(kWords % kFixThreads == 0, "bitmap words per thread");
+    const uint32_t tid = threadIdx.x;
+    const uint32_t n_huge = min(__ldcg(lists.ctl + kFixListHuge), lists.cap[kFixListHuge]);
     for (uint32_t x = vb; x < n_huge; x += nvb) {
-        const uint32_t c = ld_cur<kCg>(huge + x);
+        const uint32_t c = __ldcg(lists.list[kFixListHuge] + x);
         const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;
         uint32_t vmin = 0xFFFFFFFFu, vmax = 0u;
         for (uint32_t j = tid; j < m; j += blockDim.x) {
-            const uint32_t v = ld_cur<kCg>(perm + lo + j);
+            const uint32_t v = __ldcg(perm + lo + j);
             tmp[lo + j] = v;
             vmin = min(vmin, v);
             vmax = max(vmax, v);
@@ -514,15 +441,14 @@ __device__ __forceinline__ void fix_block(uint32_t vb, uint32_t nvb, const uint3
         vmin = block_reduce(vmin, s_red, true);
         vmax = block_reduce(vmax, s_red, false);  // ends with a barrier: tmp is complete
         uint32_t done = 0;
-        for (uint32_t c0 = vmin;; c0 += kBitmapValues) {
-            for (uint32_t w = tid; w < kBitmapWords; w += blockDim.x) s_v[w] = 0u;
+        for (uint32_t c0 = vmin;; c0 += kValues) {
+            for (uint32_t w = tid; w < kWords; w += blockDim.x) s_v[w] = 0u;
             __syncthreads();
             for (uint32_t j = tid; j < m; j += blockDim.x) {
                 const uint32_t d = tmp[lo + j] - c0;
-                if (d < kBitmapValues) atomicOr(&s_v[d >> 5], 1u << (d & 31u));
+                if (d < kValues) atomicOr(&s_v[d >> 5], 1u << (d & 31u));
             }
             __syncthreads();
-            constexpr uint32_t kWordsPer = kBitmapWords / kFixThreads;
             uint32_t mine = 0;
 #pragma unroll 8
             for (uint32_t w = 0; w < kWordsPer; ++w) mine += (uint32_t)__popc(s_v[tid * kWordsPer + w]);
@@ -531,13 +457,13 @@ __device__ __forceinline__ void fix_block(uint32_t vb, uint32_t nvb, const uint3
             uint32_t at = lo + done + before;
             for (uint32_t w = 0; w < kWordsPer; ++w) {
                 uint32_t bits = s_v[tid * kWordsPer + w];
-                const uint32_t vb = c0 + (tid * kWordsPer + w) * 32u;
+                const uint32_t vb0 = c0 + (tid * kWordsPer + w) * 32u;
                 while (bits) {  // four at a time, so the state loads overlap
                     uint32_t vv[4];
                     uint32_t got = 0;
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        vv[q] = bits ? vb + (uint32_t)(__ffs(bits) - 1) : 0u;
+                        vv[q] = bits ? vb0 + (uint32_t)(__ffs(bits) - 1) : 0u;
                         got += bits ? 1u : 0u;
                         bits &= bits - 1u;
                     }
@@ -556,7 +482,88 @@ __device__ __forceinline__ void fix_block(uint32_t vb, uint32_t nvb, const uint3
             }
             done += total;
             __syncthreads();  // bitmap free for the next chunk
-            if (vmax - c0 < kBitmapValues) break;
+            if (vmax - c0 < kValues) break;
+        }
+    }
+}
+
+// One block (kCollectThreads threads) of the fixup of the marked cells: it reads
+// kCollectWords words of the bitmap, a byte (8 input slots) per thread.  A
+// marked input slot names a cell (its key) that runs of several warps filled.
+// Each warp gathers the marked slots of its 256 input slots in shared memory and
+// deals them out to its lanes, so a lane usually has one cell at most: cells of
+// up to kFixSmall slots are put back in input order by that lane; cells of up to
+// kFixWarp slots are collected for the block, whose eight warps then take one
+// each in turn (crowded scenes mark many close together, so the block shares
+// them out rather than the warp that found them); larger cells are listed
+// (fix_huge).  kLast: the last block to finish fixes the listed cells (the
+// per-stage kernel); otherwise the caller does after a grid barrier.
+struct MarkedSmem {
+    union {
+        struct {
+            uint32_t slot[kCollectThreads * 8u];  // each warp's marked input slots
+            uint32_t mid[kCollectThreads * 8u];   // the block's cells of kFixSmall+1 .. kFixWarp slots
+        } a;
+        uint32_t v[kMarkedBitmapWords];           // the last block's bitmap (fix_huge)
+    } u;
+    uint32_t red[kCollectThreads / 32 + 1];
+    uint32_t cnt[4];  // [0] mid cells, [1] huge cells, [2] list base, [3] last block
+};
+template <class Src, bool kCg = false, bool kLast = false>
+__device__ __forceinline__ void fix_marked_block(uint32_t vb, uint32_t nvb, const uint32_t* __restrict__ fix_bits,
+                                                 const uint32_t* __restrict__ keys, uint32_t n,
+                                                 const uint32_t* __restrict__ offs, uint32_t* perm,
+                                                 const FixLists& lists, uint32_t* __restrict__ tmp, const Src& src,
+                                                 float4* __restrict__ spos, uint4* __restrict__ svfme,
+                                                 MarkedSmem& S) {
+    constexpr uint32_t kPerWarp = 32u * 8u;  // input slots a warp reads the marks of
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t words = (n + 31u) / 32u;
+    const uint32_t w = vb * kCollectWords + tid / 4u, sh = 8u * (tid & 3u);
+    uint32_t byte = w < words ? (__ldcg(fix_bits + w) >> sh) & 0xFFu : 0u;
+    if (tid < 2u) S.cnt[tid] = 0u;
+    // compact the warp's marked slots
+    const uint32_t cnt = (uint32_t)__popc(byte);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    uint32_t* const my = S.u.a.slot + warp * kPerWarp;
+    for (uint32_t at = incl - cnt; byte; byte &= byte - 1u, ++at) my[at] = 32u * w + sh + (uint32_t)(__ffs(byte) - 1);
+    __syncthreads();  // slots written; counters cleared
+    for (uint32_t k = lane; k < total; k += 32u) {
+        const uint32_t c = ld_in<kCg>(keys + my[k]);
+        const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;
+        if (m <= kFixSmall) {
+            fix_small_cell<Src, kCg>(lo, m, perm, src, spos, svfme);
+        } else if (m <= kFixWarp) {
+            S.u.a.mid[atomicAdd(&S.cnt[0], 1u)] = c;
+        } else {
+            const uint32_t at = atomicAdd(lists.ctl + kFixListHuge, 1u);
+            if (at < lists.cap[kFixListHuge]) lists.list[kFixListHuge][at] = c;  // holds every cell that can qualify
+        }
+    }
+    __syncthreads();  // the block's mid cells are collected
+    const uint32_t n_mid = S.cnt[0];
+    for (uint32_t x = warp; x < n_mid; x += kCollectThreads / 32u) {
+        const uint32_t c = S.u.a.mid[x];
+        const uint32_t lo = ld_cur<kCg>(offs + c), m = ld_cur<kCg>(offs + c + 1u) - lo;
+        fix_warp_cell<Src, kCg>(lo, m, lane, perm, src, spos, svfme);
+    }
+    if (kLast) {
+        __syncthreads();  // every warp is done with the shared lists
+        if (tid == 0) {
+            __threadfence();  // this block's list entries before it counts itself finished
+            S.cnt[3] = atomicAdd(lists.ctl + kFixListDone, 1u) == nvb - 1u ? 1u : 0u;
+        }
+        __syncthreads();
+        if (S.cnt[3]) {
+            __threadfence();  // every other block's list entries
+            if (tid == 0) lists.ctl[kFixListDone] = 0u;
+            fix_huge<Src, kCg, kMarkedBitmapWords>(0u, 1u, lists, offs, perm, tmp, src, spos, svfme, S.u.v, S.red);
         }
     }
 }

@@ -286,17 +286,20 @@ constexpr uint32_t kScanTile = 4096;                        // cells per coarse 
 static_assert(kScanTile % kScanChunk == 0, "scan chunks tile the coarse tiles");
 
 // Cells the scatter filled from several warp runs are marked (one bit per input
-// slot), then listed for the in-cell fixup by size: up to kFixSmall slots (a
+// slot); the fixup puts them back in order by size: up to kFixSmall slots (a
 // thread each), up to kFixWarp (a warp each), larger (a block each).
 constexpr uint32_t kFixSmall = 8;
 constexpr uint32_t kFixWarp = 256;
-enum : int { kFixListSmall = 0, kFixListWarp = 1, kFixListHuge = 2, kFixLists = 3 };
+// fix_ctl words: list lengths (cleared by each frame's scan), then a count of
+// finished fixup blocks (kFixListDone: the last one resets it).  Only the list
+// of cells above kFixWarp slots is filled.
+enum : int { kFixListSmall = 0, kFixListWarp = 1, kFixListHuge = 2, kFixLists = 3, kFixListDone = 3, kFixCtlWords = 4 };
 
 struct CountScratch {
     uint32_t max_cells = 0;
     uint32_t* hist = nullptr;     // [max_cells] counts of the keys of the next sort
     uint32_t* coarse = nullptr;   // [tiles] counts per 4096-cell scan tile
-    uint32_t* fix_ctl = nullptr;  // [kFixLists] lengths of the fixup lists
+    uint32_t* fix_ctl = nullptr;  // [kFixCtlWords] lengths of the fixup lists, finished fixup blocks
     uint32_t* fix[kFixLists] = {nullptr, nullptr, nullptr};  // listed cells, by size class
     uint32_t fix_cap[kFixLists] = {0u, 0u, 0u};                // their capacities
     uint32_t* fix_tmp = nullptr;  // [max_keys] copy of a large cell's input indices

@@ -775,8 +775,8 @@ __global__ void __launch_bounds__(kTile)
 }
 
 // ---------------------------------------------------------------- fused frame
-// LOOP frames as one cooperative kernel: the five stages of a frame (count scan,
-// scatter, marked-cell fixup, large-cell fixup, physics) run back to back in one launch,
+// LOOP frames as one cooperative kernel: the stages of a frame (count scan,
+// scatter, marked-cell fixup, cells above 256 slots if any, physics) run back to back in one launch,
 // separated by grid barriers instead of kernel boundaries, for as many frames
 // as the launch is given.  Every block is resident (cooperative launch), so a
 // block may wait for the others; each wait is bounded.  The stages run the same
@@ -851,9 +851,7 @@ union FusedSmem {
     struct {
         uint32_t warp[kScanThreads / 32], base[kScanThreads / 32];
     } scan;
-    struct {
-        uint32_t slot[kCollectThreads * 8u], big[2u * kCollectThreads * 8u], cnt[4];
-    } marked;
+    MarkedSmem marked;
     struct {
         uint32_t v[kBitmapWords];
         uint32_t red[kFixThreads / 32 + 1];
@@ -887,17 +885,21 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_frame_fused(const __grid_c
                             A.fix_bits);
         if (!grid_barrier(A.bar, A.err, &s_flag)) return;
         const OneBufferT<true> src{A.pos[cur], A.vfme[cur]};
+        clear_counts(blockIdx.x, gridDim.x, src, A.hist, A.cells, A.coarse, A.scan_tiles);
         for (uint32_t vb = blockIdx.x; vb < A.collect_blocks; vb += gridDim.x) {
-            fix_marked_block<OneBufferT<true>, true>(vb, A.fix_bits, A.keys, A.n, A.offs, A.perm, A.lists, src,
-                                                     kIndirect ? nullptr : A.spos, kIndirect ? nullptr : A.svfme,
-                                                     S.marked.slot, S.marked.big, S.marked.cnt);
-            __syncthreads();  // the lists are written out before the next block's counters reset
+            fix_marked_block<OneBufferT<true>, true, false>(vb, A.collect_blocks, A.fix_bits, A.keys, A.n, A.offs,
+                                                            A.perm, A.lists, A.fix_tmp, src,
+                                                            kIndirect ? nullptr : A.spos,
+                                                            kIndirect ? nullptr : A.svfme, S.marked);
+            __syncthreads();  // the shared lists are done before the next block's counters reset
         }
         if (!grid_barrier(A.bar, A.err, &s_flag)) return;
-        fix_block<OneBufferT<true>, true>(blockIdx.x, gridDim.x, A.offs, A.perm, A.hist, A.cells, A.coarse,
-                                          A.scan_tiles, A.lists, A.fix_tmp, src, kIndirect ? nullptr : A.spos,
-                                          kIndirect ? nullptr : A.svfme, S.fix.v, S.fix.red);
-        if (!grid_barrier(A.bar, A.err, &s_flag)) return;
+        if (__ldcg(A.lists.ctl + kFixListHuge) != 0u) {  // cells above kFixWarp slots (the same count in every block)
+            fix_huge<OneBufferT<true>, true, kBitmapWords>(blockIdx.x, gridDim.x, A.lists, A.offs, A.perm, A.fix_tmp,
+                                                           src, kIndirect ? nullptr : A.spos,
+                                                           kIndirect ? nullptr : A.svfme, S.fix.v, S.fix.red);
+            if (!grid_barrier(A.bar, A.err, &s_flag)) return;
+        }
         // the stages above wrote the sorted copy (global) and this block's shared
         // memory through the generic proxy; the bulk copies read and write them
         // through the async proxy

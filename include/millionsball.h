@@ -275,7 +275,7 @@ typedef struct mb_tuning {
 
 /* How LOOP frames are launched:
  *   MB_FRAME_GRAPH: one kernel per stage (count scan, scatter, marked-cell fixup,
- *                   large-cell fixup, physics), captured in CUDA graphs (default);
+ *                   physics), captured in CUDA graphs (default);
  *   MB_FRAME_FUSED: every stage of every frame of an mb_step call in one
  *                   cooperative kernel, the stages separated by grid barriers
  *                   (bounded waits: a barrier that gives up is reported by
