@@ -74,6 +74,18 @@ __device__ __forceinline__ Agent unpack(float4 p, uint4 q) {
     return a;
 }
 
+// A neighbour as the spring response reads it (solve_sphere_constraint's
+// spring branch, physics.wgsl:320-330, uses its position and scale only).
+__device__ __forceinline__ Agent unpack_pos(float4 p) {
+    Agent a;
+    a.position = {p.x, p.y, p.z};
+    a.scale = p.w;
+    a.velocity = splat(0.0f);
+    a.force = splat(0.0f);
+    a.massv = 0.0f;
+    return a;
+}
+
 // pack_vfme (physics.wgsl:235-242)
 __device__ __forceinline__ uint4 pack(const Agent& a) {
     uint4 q;
@@ -370,7 +382,14 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
             const uint32_t q = (uint32_t)(__ffs(m) - 1);
             t += q + 1u;
             const uint32_t j = j0 + q;
-            if (kShared) {
+            if constexpr (kResp == kSpring) {  // the neighbour's packed state is not read
+                if (kShared) {
+                    sphere<kResp>(P, a, unpack_pos(bpos[j]));
+                } else {
+                    const uint32_t sj = kIndirect ? min(ld_in<kCg>(perm + j), nmax) : j;
+                    sphere<kResp>(P, a, unpack_pos(ld_in<kCg>(bpos + sj)));
+                }
+            } else if (kShared) {
                 sphere<kResp>(P, a, unpack(bpos[j], bvfme[j]));
             } else {
                 const uint32_t sj = kIndirect ? min(ld_in<kCg>(perm + j), nmax) : j;
@@ -513,13 +532,16 @@ __device__ __forceinline__ uint32_t scene_of(const SceneDev* __restrict__ scenes
 }
 
 // Shared memory of one tile of kTile slots: bands (pos padded: the walk reads
-// past rows) and the band bounds.  (The mbarrier of the band copies is kept
-// apart, so that the fused frame kernel can reuse this memory for its other
-// stages.)
-template <uint32_t kTile>
+// past rows) and the band bounds.  kPosOnly (a world of the spring model, whose
+// contacts read the neighbours' positions only): the bands hold positions
+// alone, twice as many slots in the same memory.  (The mbarrier of the band
+// copies is kept apart, so that the fused frame kernel can reuse this memory for
+// its other stages.)
+template <uint32_t kTile, bool kPosOnly = false>
 struct TileSmemT {
-    float4 pos[3 * band_cap<kTile>() + kBandPad];
-    uint4 vfme[3 * band_cap<kTile>()];
+    static constexpr uint32_t kCap = kPosOnly ? 2u * band_cap<kTile>() : band_cap<kTile>();
+    float4 pos[3 * kCap + kBandPad];
+    uint4 vfme[kPosOnly ? 1u : 3 * kCap];
     uint32_t lo[3], cnt[3];
 };
 using TileSmem = TileSmemT<kTileThreads>;
@@ -551,7 +573,8 @@ using TileSmem = TileSmemT<kTileThreads>;
 template <bool kBatched, bool kIndirect, bool kCg = false, uint32_t kTile = kTileThreads,
           int kResp = kSpringRuntime>
 __device__ __forceinline__ void physics_tile(
-    uint32_t tile, uint32_t tid, uint32_t bar_parity, TileSmemT<kTile>* sm, uint64_t* s_bar, const PhysParams& P1,
+    uint32_t tile, uint32_t tid, uint32_t bar_parity, TileSmemT<kTile, kResp == kSpring>* sm, uint64_t* s_bar,
+    const PhysParams& P1,
     const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene, uint32_t n,
     const uint32_t* __restrict__ offs, const uint4* __restrict__ bands, const float4* __restrict__ spos,
     const uint4* __restrict__ svfme, const uint32_t* __restrict__ perm, float4* __restrict__ pos_out0,
@@ -560,7 +583,8 @@ __device__ __forceinline__ void physics_tile(
     uint32_t* __restrict__ err) {
     static_assert(!(kBatched && kIndirect), "batches stage a sorted copy");
     static_assert(kTile == 64u || kTile == 128u || kTile == 256u, "tiles of 64, 128 or 256 slots");
-    constexpr uint32_t kCap = band_cap<kTile>();
+    constexpr bool kPosOnly = kResp == kSpring;
+    constexpr uint32_t kCap = TileSmemT<kTile, kPosOnly>::kCap;
     const uint4* __restrict__ btab = kTile == 64u ? nullptr : bands;
     float4* const s_pos = sm->pos;
     uint4* const s_vfme = sm->vfme;
@@ -695,27 +719,27 @@ __device__ __forceinline__ void physics_tile(
             for (uint32_t u = 0; u < kGatherUnroll; ++u) {
                 if (f0 + u * kTile + tid < tot) {
                     gp[u] = ld_in<kCg>(spos + src[u]);
-                    gq[u] = ld_in<kCg>(svfme + src[u]);
+                    if (!kPosOnly) gq[u] = ld_in<kCg>(svfme + src[u]);
                 }
             }
 #pragma unroll
             for (uint32_t u = 0; u < kGatherUnroll; ++u) {
                 if (f0 + u * kTile + tid < tot) {
                     s_pos[dst[u]] = gp[u];
-                    s_vfme[dst[u]] = gq[u];
+                    if (!kPosOnly) s_vfme[dst[u]] = gq[u];
                 }
             }
         }
     } else if (tid == 0) {
         uint32_t bytes = 0;
 #pragma unroll
-        for (int b = 0; b < 3; ++b) bytes += s_cnt[b] * 32u;
+        for (int b = 0; b < 3; ++b) bytes += s_cnt[b] * (kPosOnly ? 16u : 32u);
         mbar_arrive_expect_tx(s_bar, bytes);
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
             if (s_cnt[b]) {
                 bulk_g2s(s_pos + b * kCap, spos + s_lo[b], s_cnt[b] * 16u, s_bar);
-                bulk_g2s(s_vfme + b * kCap, svfme + s_lo[b], s_cnt[b] * 16u, s_bar);
+                if (!kPosOnly) bulk_g2s(s_vfme + b * kCap, svfme + s_lo[b], s_cnt[b] * 16u, s_bar);
             }
         }
     }
@@ -766,7 +790,7 @@ __global__ void __launch_bounds__(kTile)
                     float4* __restrict__ pos_out1, uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1,
                     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
                     uint32_t* __restrict__ err) {
-    __shared__ __align__(16) TileSmemT<kTile> sm;
+    __shared__ __align__(16) TileSmemT<kTile, kResp == kSpring> sm;
     __shared__ __align__(8) uint64_t s_bar;
     if (!kIndirect && threadIdx.x == 0) mbar_init(&s_bar, 1u);  // first copy after the tile's CTA barrier
     physics_tile<kBatched, kIndirect, false, kTile, kResp>(blockIdx.x, threadIdx.x, 0u, &sm, &s_bar, P1, scenes, tile_scene, n, offs,
