@@ -322,6 +322,20 @@ class World:
                                                 hmap.ctypes.data, MB_HOST))
         return img.view(np.uint8).reshape(height, width, 4), hmap
 
+    def render_view(self, width: int, height: int, eye=None, target=None, fov_y_degrees: float = 0.0):
+        """mb_render_view: a width x height RGBA8 image (H, W, 4) uint8 and the depth
+        (distance along each pixel's ray, 0 for the clear colour) (H, W) float32 of
+        the current state through a perspective camera; by default the reference
+        view (eye (0, 64, 64) looking at the origin, 45-degree field of view)."""
+        img = np.empty((height, width), np.uint32)
+        depth = np.empty((height, width), np.float32)
+        e = None if eye is None else np.ascontiguousarray(eye, np.float32)
+        t = None if target is None else np.ascontiguousarray(target, np.float32)
+        self._check(self._lib.mb_render_view(self._h, width, height, None if e is None else e.ctypes.data,
+                                             None if t is None else t.ctypes.data, float(fov_y_degrees),
+                                             img.ctypes.data, depth.ctypes.data, MB_HOST))
+        return img.view(np.uint8).reshape(height, width, 4), depth
+
     # -- stepping
     def step(self, k: int = 1) -> None:
         self._check(self._lib.mb_step(self._h, int(k)))

@@ -117,6 +117,7 @@ SIGNATURES = {
     "mb_sort_static_status": (C.c_int, [vp]),
     "mb_assemble_segments": (C.c_int, [vp, vp, u32, vp, vp, vp, vp]),
     "mb_render_topdown": (C.c_int, [vp, u32, u32, C.c_float, C.c_float, C.c_float, C.c_float, vp, vp, C.c_int]),
+    "mb_render_view": (C.c_int, [vp, u32, u32, vp, vp, C.c_float, vp, vp, C.c_int]),
     "mb_get_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),
     "mb_set_tuning": (C.c_int, [vp, C.POINTER(MbTuning)]),
     "mb_autotune": (C.c_int, [vp, u32, C.POINTER(MbTuning), C.POINTER(C.c_float), C.POINTER(MbTuning)]),

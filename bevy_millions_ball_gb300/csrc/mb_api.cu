@@ -616,6 +616,33 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
     return MB_OK;
 }
 
+// The per-world image buffers of the renderers, grown on demand.
+cudaError_t image_buffers(mb_world* w, size_t px) {
+    if (px <= w->zbuf_pixels) return cudaSuccess;
+    cudaFree(w->zbuf);
+    cudaFree(w->img);
+    cudaFree(w->img_h);
+    w->zbuf = nullptr;
+    w->img = nullptr;
+    w->img_h = nullptr;
+    w->zbuf_pixels = 0;
+    cudaError_t e;
+    if ((e = cudaMalloc(&w->zbuf, sizeof(unsigned long long) * px)) ||
+        (e = cudaMalloc(&w->img, sizeof(uint32_t) * px)) || (e = cudaMalloc(&w->img_h, sizeof(float) * px)))
+        return e;
+    w->zbuf_pixels = px;
+    return cudaSuccess;
+}
+
+// Copies a rendered image (and its float plane) back to the host, synchronously.
+cudaError_t image_to_host(mb_world* w, size_t px, uint32_t* rgba, const uint32_t* out, float* plane,
+                          const float* out_plane) {
+    cudaError_t e = cudaMemcpyAsync(rgba, out, sizeof(uint32_t) * px, cudaMemcpyDeviceToHost, w->stream);
+    if (!e && plane) e = cudaMemcpyAsync(plane, out_plane, sizeof(float) * px, cudaMemcpyDeviceToHost, w->stream);
+    if (!e) e = cudaStreamSynchronize(w->stream);
+    return e;
+}
+
 mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float x0, float z0, float x1, float z1,
                             uint32_t* rgba, float* height_map, mb_memory where) {
     if (!w || !rgba) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
@@ -627,33 +654,47 @@ mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float 
         return fail(w, MB_ERR_INVALID_ARG, "window must satisfy x0 < x1, z0 < z1 (finite)");
     const size_t px = (size_t)width * height;
     cudaError_t e;
-    if (px > w->zbuf_pixels) {
-        cudaFree(w->zbuf);
-        cudaFree(w->img);
-        cudaFree(w->img_h);
-        w->zbuf = nullptr;
-        w->img = nullptr;
-        w->img_h = nullptr;
-        w->zbuf_pixels = 0;
-        if ((e = cudaMalloc(&w->zbuf, sizeof(unsigned long long) * px)) ||
-            (e = cudaMalloc(&w->img, sizeof(uint32_t) * px)) || (e = cudaMalloc(&w->img_h, sizeof(float) * px)))
-            return cuda_fail(w, "mb_render_topdown", e);
-        w->zbuf_pixels = px;
-    }
+    if ((e = image_buffers(w, px))) return cuda_fail(w, "mb_render_topdown", e);
     const bool host = where == MB_HOST;
     uint32_t* out = host ? w->img : rgba;
     float* out_h = host ? w->img_h : (height_map ? height_map : w->img_h);
     if ((e = mb::render_topdown(w->pos[w->cur], w->n, width, height, x0, z0, x1, z1, w->zbuf, out, out_h,
                                 w->stream)))
         return cuda_fail(w, "mb_render_topdown", e);
-    if (host) {
-        if ((e = cudaMemcpyAsync(rgba, out, sizeof(uint32_t) * px, cudaMemcpyDeviceToHost, w->stream)))
-            return cuda_fail(w, "mb_render_topdown", e);
-        if (height_map &&
-            (e = cudaMemcpyAsync(height_map, out_h, sizeof(float) * px, cudaMemcpyDeviceToHost, w->stream)))
-            return cuda_fail(w, "mb_render_topdown", e);
-        if ((e = cudaStreamSynchronize(w->stream))) return cuda_fail(w, "mb_render_topdown", e);
-    }
+    if (host && (e = image_to_host(w, px, rgba, out, height_map, out_h))) return cuda_fail(w, "mb_render_topdown", e);
+    return MB_OK;
+}
+
+mb_status mb_render_view(mb_world* w, uint32_t width, uint32_t height, const float* eye, const float* target,
+                         float fov_y_degrees, uint32_t* rgba, float* depth, mb_memory where) {
+    if (!w || !rgba) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
+    if (!w->has_state) return fail(w, MB_ERR_NOT_READY, "no state uploaded");
+    if (width == 0 || height == 0 || (uint64_t)width * height > (1ull << 28))
+        return fail(w, MB_ERR_INVALID_ARG, "image must have 1 .. 2^28 pixels");
+    float e3[3], t3[3], fov, to_light[3];
+    mb::reference_view(e3, t3, &fov, to_light);
+    if (eye) std::copy(eye, eye + 3, e3);
+    if (target) std::copy(target, target + 3, t3);
+    if (fov_y_degrees > 0.0f) fov = fov_y_degrees;
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(e3[k]) || !std::isfinite(t3[k]))
+            return fail(w, MB_ERR_INVALID_ARG, "eye and target must be finite");
+    const float fx = t3[0] - e3[0], fy = t3[1] - e3[1], fz = t3[2] - e3[2];
+    if (!(fx * fx + fz * fz > 1e-12f * (fx * fx + fy * fy + fz * fz)))  // also eye == target
+        return fail(w, MB_ERR_INVALID_ARG, "the view direction must not be vertical (the image's up is +y)");
+    if (!(fov < 180.0f) || !std::isfinite(fov))
+        return fail(w, MB_ERR_INVALID_ARG, "fov_y_degrees must be below 180 (0 or less: 45)");
+    const float tan_half = (float)std::tan((double)fov * 3.14159265358979323846 / 360.0);
+    const size_t px = (size_t)width * height;
+    cudaError_t e;
+    if ((e = image_buffers(w, px))) return cuda_fail(w, "mb_render_view", e);
+    const bool host = where == MB_HOST;
+    uint32_t* out = host ? w->img : rgba;
+    float* out_d = host ? (depth ? w->img_h : nullptr) : depth;
+    if ((e = mb::render_view(w->pos[w->cur], w->n, width, height, e3, t3, tan_half, to_light, w->c.half_map_size,
+                             2.0f * w->c.half_map_height, w->zbuf, out, out_d, w->stream)))
+        return cuda_fail(w, "mb_render_view", e);
+    if (host && (e = image_to_host(w, px, rgba, out, depth, out_d))) return cuda_fail(w, "mb_render_view", e);
     return MB_OK;
 }
 

@@ -368,6 +368,18 @@ cudaError_t assemble_segments(const uint32_t* sorted_keys, uint32_t n, uint32_t*
 // height: w*h outputs on the device.
 cudaError_t render_topdown(const float4* pos, uint32_t n, uint32_t w, uint32_t h, float x0, float z0, float x1,
                            float z1, unsigned long long* zbuf, uint32_t* rgba, float* height, cudaStream_t st);
+// Perspective view (mb_render_view): eye and target (+y up), tan of half the
+// vertical field of view, unit vector towards the light, the box |x|,|z| <=
+// half_map_size, 0 <= y <= map_top; depth (nullable): distance along each
+// pixel's ray (0: clear colour).
+cudaError_t render_view(const float4* pos, uint32_t n, uint32_t w, uint32_t h, const float eye[3],
+                        const float target[3], float tan_half_fov, const float to_light[3], float half_map_size,
+                        float map_top, unsigned long long* zbuf, uint32_t* rgba, float* depth, cudaStream_t st);
+// The reference view's constants (src/main.rs:65-89): camera (0, 64, 64) looking
+// at the origin, Bevy's default vertical field of view (45 degrees), and the unit
+// vector towards its directional light (rotation Euler ZYX (0, -0.15 pi,
+// -0.15 pi) applied to -z, negated).
+void reference_view(float eye[3], float target[3], float* fov_degrees, float to_light[3]);
 
 // SM count of the current device (cached per device id).
 int device_sm_count();

@@ -322,6 +322,23 @@ mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float 
                             uint32_t* rgba, float* height_map, mb_memory where);
 
 /*
+ * The same impostors seen through a perspective camera: by default the
+ * reference's own view (src/main.rs:65-89: eye (0, 64, 64) looking at the
+ * origin with +y up, Bevy's default 45-degree vertical field of view, clear
+ * colour sRGB (248, 151, 184), its directional light); eye / target (nullable,
+ * 3 floats each) and fov_y_degrees (> 0) override it.  Per pixel the nearest
+ * sphere along the pixel's ray is marched and its normal taken as the shader
+ * does; the light is a GGX lobe (the material's roughness 0.435, F0 0.04) plus
+ * Lambert and ambient terms standing in for Bevy's PBR pass, sRGB-encoded; the
+ * box interior (base colour 0.8, 0.7, 0.6) shows behind the spheres.  rgba:
+ * width*height u32 (R in the low byte, A = 255); depth (nullable): distance
+ * along each pixel's ray (0 where only the clear colour shows).  The view
+ * direction must not be vertical.  where and buffers as for mb_render_topdown.
+ */
+mb_status mb_render_view(mb_world* w, uint32_t width, uint32_t height, const float* eye, const float* target,
+                         float fov_y_degrees, uint32_t* rgba, float* depth, mb_memory where);
+
+/*
  * Autotuner (no counterpart in the reference, whose sort and passes have fixed
  * workgroup shapes, NUMBER_OF_THREADS_PER_WORKGROUP = 256 at src/physics/mod.rs:35).
  * Times every candidate tuning on the world's own scene for `frames` LOOP frames

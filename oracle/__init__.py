@@ -39,6 +39,8 @@ _SIG = {
     "mbo_time": (i64, [vp]),
     "mbo_hardware_threads": (C.c_int, []),
     "mbo_render_topdown": (None, [vp, u32, u32, u32, C.c_float, C.c_float, C.c_float, C.c_float, vp, vp, vp]),
+    "mbo_reference_view": (None, [vp, vp, vp, vp]),
+    "mbo_render_view": (None, [vp, u32, u32, u32, vp, vp, C.c_float, vp, C.c_float, C.c_float, vp, vp, vp]),
 }
 
 _lib = None
@@ -144,6 +146,30 @@ def render_topdown(pos: np.ndarray, width: int, height: int, x0: float, z0: floa
     win = np.empty((height, width), np.uint32)
     lib().mbo_render_topdown(_p(p), p.shape[0], width, height, x0, z0, x1, z1, _p(rgba), _p(hmap), _p(win))
     return rgba, hmap, win
+
+
+def reference_view():
+    """The reference's camera and light: (eye (3,), target (3,), fov degrees, unit vector towards the light (3,))."""
+    eye, target, light = (np.empty(3, np.float32) for _ in range(3))
+    fov = np.empty(1, np.float32)
+    lib().mbo_reference_view(_p(eye), _p(target), _p(fov), _p(light))
+    return eye, target, float(fov[0]), light
+
+
+def render_view(pos: np.ndarray, width: int, height: int, half_map_size: float, map_top: float, eye=None,
+                target=None, fov_degrees: float = 0.0):
+    """Perspective impostor render: (rgba u32 (h, w), depth f32 (h, w), winner u32 (h, w): sphere index + 1)."""
+    e0, t0, f0, light = reference_view()
+    eye = e0 if eye is None else np.ascontiguousarray(eye, np.float32)
+    target = t0 if target is None else np.ascontiguousarray(target, np.float32)
+    fov = f0 if fov_degrees <= 0 else float(fov_degrees)
+    p = np.ascontiguousarray(pos, np.float32)
+    rgba = np.empty((height, width), np.uint32)
+    depth = np.empty((height, width), np.float32)
+    win = np.empty((height, width), np.uint32)
+    lib().mbo_render_view(_p(p), p.shape[0], width, height, _p(eye), _p(target), fov, _p(light), half_map_size,
+                          map_top, _p(rgba), _p(depth), _p(win))
+    return rgba, depth, win
 
 
 def hardware_threads() -> int:

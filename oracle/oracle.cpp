@@ -749,3 +749,219 @@ extern "C" void mbo_render_topdown(const float* pos4, uint32_t n, uint32_t w, ui
         height[p] = hy;
     }
 }
+
+// CPU restatement of the perspective view (mb_render_view), in the library's
+// operation order: camera basis, pixel rays, nearest sphere per pixel (ties to
+// the lower index), the shader's march and normal along the pixel's ray, GGX +
+// Lambert + ambient lighting, sRGB encoding, the box interior behind.
+namespace {
+struct RCam {
+    float ex, ey, ez, gx, gy, gz, th, ta, lx, ly, lz, hs, top;
+    uint32_t w, h;
+    float fx, fy, fz, rx, ry, rz, ux, uy, uz;
+};
+void rbasis(RCam& C) {
+    float fx = C.gx - C.ex, fy = C.gy - C.ey, fz = C.gz - C.ez;
+    float l = len3r(fx, fy, fz);
+    C.fx = fx / l;
+    C.fy = fy / l;
+    C.fz = fz / l;
+    float rx = -C.fz, rz = C.fx;
+    l = std::sqrt(rx * rx + rz * rz);
+    C.rx = rx / l;
+    C.ry = 0.0f;
+    C.rz = rz / l;
+    C.ux = C.ry * C.fz - C.rz * C.fy;
+    C.uy = C.rz * C.fx - C.rx * C.fz;
+    C.uz = C.rx * C.fy - C.ry * C.fx;
+}
+void rray(const RCam& C, uint32_t u, uint32_t v, float& dx, float& dy, float& dz) {
+    const float sx = (2.0f * ((float)u + 0.5f) / (float)C.w - 1.0f) * C.ta;
+    const float sy = (1.0f - 2.0f * ((float)v + 0.5f) / (float)C.h) * C.th;
+    const float x = C.fx + sx * C.rx + sy * C.ux, y = C.fy + sx * C.ry + sy * C.uy, z = C.fz + sx * C.rz + sy * C.uz;
+    const float l = len3r(x, y, z);
+    dx = x / l;
+    dy = y / l;
+    dz = z / l;
+}
+float rsphere(const RCam& C, float dx, float dy, float dz, const RSphere& s) {
+    const float ox = C.ex - s.x, oy = C.ey - s.y, oz = C.ez - s.z;
+    const float b = ox * dx + oy * dy + oz * dz;
+    const float c = (ox * ox + oy * oy + oz * oz) - s.r * s.r;
+    const float disc = b * b - c;
+    if (!(disc >= 0.0f)) return -1.0f;
+    return -b - std::sqrt(disc);
+}
+float rsrgb8(float x) {
+    x = std::fmin(std::fmax(x, 0.0f), 1.0f);
+    const float e = x <= 0.0031308f ? 12.92f * x : 1.055f * std::pow(x, 1.0f / 2.4f) - 0.055f;
+    return std::fmin(255.0f * e + 0.5f, 255.0f);
+}
+uint32_t rrgba8(float r, float g, float b) {
+    return 0xFF000000u | (uint32_t)rsrgb8(r) | ((uint32_t)rsrgb8(g) << 8) | ((uint32_t)rsrgb8(b) << 16);
+}
+}  // namespace
+
+extern "C" void mbo_reference_view(float* eye, float* target, float* fov_degrees, float* to_light) {
+    eye[0] = 0.0f;
+    eye[1] = 64.0f;
+    eye[2] = 64.0f;
+    target[0] = target[1] = target[2] = 0.0f;
+    *fov_degrees = 45.0f;
+    const double pi = 3.14159265358979323846, b = -0.15 * pi, c = -0.15 * pi;
+    const double x = -std::cos(c) * std::sin(b), y = std::sin(c), z = -std::cos(c) * std::cos(b);
+    to_light[0] = (float)-x;
+    to_light[1] = (float)-y;
+    to_light[2] = (float)-z;
+}
+
+extern "C" void mbo_render_view(const float* pos4, uint32_t n, uint32_t w, uint32_t h, const float* eye,
+                                const float* target, float fov_degrees, const float* to_light, float half_map_size,
+                                float map_top, uint32_t* rgba, float* depth, uint32_t* winner) {
+    RCam C{};
+    C.ex = eye[0];
+    C.ey = eye[1];
+    C.ez = eye[2];
+    C.gx = target[0];
+    C.gy = target[1];
+    C.gz = target[2];
+    C.th = (float)std::tan((double)fov_degrees * 3.14159265358979323846 / 360.0);
+    C.ta = C.th * ((float)w / (float)h);
+    C.lx = to_light[0];
+    C.ly = to_light[1];
+    C.lz = to_light[2];
+    C.hs = half_map_size;
+    C.top = map_top;
+    C.w = w;
+    C.h = h;
+    rbasis(C);
+    std::vector<uint64_t> zb((size_t)w * h, ~0ull);
+    for (uint32_t i = 0; i < n; ++i) {
+        const RSphere s = grown(pos4 + 4 * (size_t)i);
+        if (!(s.r > 0.0f)) continue;
+        const float px = s.x - C.ex, py = s.y - C.ey, pz = s.z - C.ez;
+        const float cx = px * C.rx + py * C.ry + pz * C.rz, cy = px * C.ux + py * C.uy + pz * C.uz,
+                    cz = px * C.fx + py * C.fy + pz * C.fz;
+        if (!(cz - s.r > 1e-3f)) continue;
+        const float zn = cz - s.r, zf = cz + s.r;
+        const float xl = cx - s.r, xh = cx + s.r, yl = cy - s.r, yh = cy + s.r;
+        const float sxl = xl / (xl >= 0.0f ? zf : zn), sxh = xh / (xh >= 0.0f ? zn : zf);
+        const float syl = yl / (yl >= 0.0f ? zf : zn), syh = yh / (yh >= 0.0f ? zn : zf);
+        const float ua = (sxl / C.ta + 1.0f) * 0.5f * (float)w - 1.5f, ub = (sxh / C.ta + 1.0f) * 0.5f * (float)w + 0.5f;
+        const float va = (1.0f - syh / C.th) * 0.5f * (float)h - 1.5f, vb = (1.0f - syl / C.th) * 0.5f * (float)h + 0.5f;
+        if (!(ub >= 0.0f && vb >= 0.0f && ua < (float)w && va < (float)h)) continue;
+        const int u0 = (int)std::fmax(std::ceil(ua), 0.0f), u1 = (int)std::fmin(std::floor(ub), (float)w - 1.0f);
+        const int v0 = (int)std::fmax(std::ceil(va), 0.0f), v1 = (int)std::fmin(std::floor(vb), (float)h - 1.0f);
+        for (int v = v0; v <= v1; ++v) {
+            for (int u = u0; u <= u1; ++u) {
+                float dx, dy, dz;
+                rray(C, (uint32_t)u, (uint32_t)v, dx, dy, dz);
+                const float t = rsphere(C, dx, dy, dz, s);
+                if (!(t > 0.0f)) continue;
+                uint32_t bits;
+                std::memcpy(&bits, &t, 4);
+                const uint64_t key = ((uint64_t)bits << 32) | (uint64_t)(i + 1u);
+                uint64_t& z = zb[(size_t)v * w + u];
+                if (key < z) z = key;
+            }
+        }
+    }
+    const float K = 0.08f, kAmbient = 0.2f, kAlpha = 0.435f * 0.435f, kF0 = 0.04f, kPi = 3.14159265f;
+    for (size_t p = 0; p < (size_t)w * h; ++p) {
+        const uint32_t u = (uint32_t)(p % w), v = (uint32_t)(p / w);
+        float dx, dy, dz;
+        rray(C, u, v, dx, dy, dz);
+        const uint64_t key = zb[p];
+        if (winner) winner[p] = key == ~0ull ? 0u : (uint32_t)(key & 0xFFFFFFFFull);
+        if (key != ~0ull) {
+            const RSphere s = grown(pos4 + 4 * (size_t)((uint32_t)(key & 0xFFFFFFFFull) - 1u));
+            const uint32_t tb = (uint32_t)(key >> 32);
+            float t;
+            std::memcpy(&t, &tb, 4);
+            float hx = C.ex + t * dx, hy = C.ey + t * dy, hz = C.ez + t * dz;
+            float nx = hx - s.x, ny = hy - s.y, nz = hz - s.z;
+            const float nl = len3r(nx, ny, nz);
+            nx /= nl;
+            ny /= nl;
+            nz /= nl;
+            float sd_sphere = 0.0f, sd_plane = -hy, walked = 0.0f;
+            bool hit = false;
+            for (int it = 0; it < 16; ++it) {
+                const float d = smooth_max_r(sd_sphere, sd_plane, K);
+                hx += d * dx;
+                hy += d * dy;
+                hz += d * dz;
+                walked += d;
+                if (d < 0.001f) {
+                    hit = true;
+                    break;
+                }
+                sd_sphere = len3r(hx - s.x, hy - s.y, hz - s.z) - s.r;
+                sd_plane = -hy;
+            }
+            if (hit) {
+                const float hh = (sd_plane - sd_sphere) / K;
+                const float pa = 1.0f / (1.0f + std::exp2(hh)), pb = 1.0f / (1.0f + std::exp2(-hh));
+                float gx = pa * nx, gy = pa * ny - pb, gz = pa * nz;
+                const float gl = len3r(gx, gy, gz);
+                if (gl > 0.0f) {
+                    gx /= gl;
+                    gy /= gl;
+                    gz /= gl;
+                }
+                const float vx = -dx, vy = -dy, vz = -dz;
+                const float nl_ = std::fmax(gx * C.lx + gy * C.ly + gz * C.lz, 0.0f);
+                const float nv = std::fmax(gx * vx + gy * vy + gz * vz, 1e-4f);
+                float ax = vx + C.lx, ay = vy + C.ly, az = vz + C.lz;
+                const float al = len3r(ax, ay, az);
+                float spec = 0.0f;
+                if (al > 0.0f && nl_ > 0.0f) {
+                    ax /= al;
+                    ay /= al;
+                    az /= al;
+                    const float nh = std::fmax(gx * ax + gy * ay + gz * az, 0.0f),
+                                vh = std::fmax(vx * ax + vy * ay + vz * az, 0.0f);
+                    const float a2 = kAlpha * kAlpha, dd = nh * nh * (a2 - 1.0f) + 1.0f;
+                    const float D = a2 / (kPi * dd * dd);
+                    const float vis =
+                        0.5f / (nl_ * std::sqrt(nv * nv * (1.0f - a2) + a2) + nv * std::sqrt(nl_ * nl_ * (1.0f - a2) + a2));
+                    const float m = 1.0f - vh, m2 = m * m;
+                    const float F = kF0 + (1.0f - kF0) * (m2 * m2 * m);
+                    spec = D * vis * F * nl_;
+                }
+                const float lit = kAmbient + nl_;
+                rgba[p] = rrgba8(1.0f * lit + spec, (191.0f / 255.0f) * lit + spec, spec);
+                if (depth) depth[p] = t + walked;
+                continue;
+            }
+        }
+        float tn = 0.0f, tf = 3.0e38f;
+        int axis = -1;
+        const float lo[3] = {-C.hs, 0.0f, -C.hs}, hi[3] = {C.hs, C.top, C.hs}, e[3] = {C.ex, C.ey, C.ez},
+                    d[3] = {dx, dy, dz};
+        for (int k = 0; k < 3; ++k) {
+            if (d[k] != 0.0f) {
+                float t0 = (lo[k] - e[k]) / d[k], t1 = (hi[k] - e[k]) / d[k];
+                if (t0 > t1) std::swap(t0, t1);
+                tn = std::fmax(tn, t0);
+                if (t1 < tf) {
+                    tf = t1;
+                    axis = k;
+                }
+            } else if (e[k] < lo[k] || e[k] > hi[k]) {
+                tn = 3.0e38f;
+            }
+        }
+        if (axis >= 0 && tf > tn) {
+            const float bx = axis == 0 ? (dx > 0.0f ? -1.0f : 1.0f) : 0.0f;
+            const float by = axis == 1 ? (dy > 0.0f ? -1.0f : 1.0f) : 0.0f;
+            const float bz = axis == 2 ? (dz > 0.0f ? -1.0f : 1.0f) : 0.0f;
+            const float lit = kAmbient + std::fmax(bx * C.lx + by * C.ly + bz * C.lz, 0.0f);
+            rgba[p] = rrgba8(0.8f * lit, 0.7f * lit, 0.6f * lit);
+            if (depth) depth[p] = tf;
+            continue;
+        }
+        rgba[p] = 0xFF000000u | 248u | (151u << 8) | (184u << 16);
+        if (depth) depth[p] = 0.0f;
+    }
+}
