@@ -477,6 +477,7 @@ mb_status mb_get_state(mb_world* w, float* pos_scale, uint32_t* vfme, mb_memory 
 }
 
 mb_status mb_step(mb_world* w, uint32_t k) {
+    mb::NvtxRange nvtx_range("mb_step");
     if (!w) return fail(nullptr, MB_ERR_INVALID_ARG, "world is NULL");
     if (!w->has_state) return fail(w, MB_ERR_NOT_READY, "no state uploaded");
     if (!w->s.enable_simulation) return MB_OK;
@@ -645,6 +646,7 @@ cudaError_t image_to_host(mb_world* w, size_t px, uint32_t* rgba, const uint32_t
 
 mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float x0, float z0, float x1, float z1,
                             uint32_t* rgba, float* height_map, mb_memory where) {
+    mb::NvtxRange nvtx_range("mb_render_topdown");
     if (!w || !rgba) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
     if (!w->has_state) return fail(w, MB_ERR_NOT_READY, "no state uploaded");
     if (width == 0 || height == 0 || (uint64_t)width * height > (1ull << 28))
@@ -667,6 +669,7 @@ mb_status mb_render_topdown(mb_world* w, uint32_t width, uint32_t height, float 
 
 mb_status mb_render_view(mb_world* w, uint32_t width, uint32_t height, const float* eye, const float* target,
                          float fov_y_degrees, uint32_t* rgba, float* depth, mb_memory where) {
+    mb::NvtxRange nvtx_range("mb_render_view");
     if (!w || !rgba) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
     if (!w->has_state) return fail(w, MB_ERR_NOT_READY, "no state uploaded");
     if (width == 0 || height == 0 || (uint64_t)width * height > (1ull << 28))
@@ -699,6 +702,7 @@ mb_status mb_render_view(mb_world* w, uint32_t width, uint32_t height, const flo
 }
 
 mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* frame_ms, mb_tuning* tried) {
+    mb::NvtxRange nvtx_range("mb_autotune");
     if (!w || !best) return fail(w, MB_ERR_INVALID_ARG, "NULL argument");
     if (frames == 0) return fail(w, MB_ERR_INVALID_ARG, "frames must be positive");
     if (!w->frame_done || w->time == 0) return fail(w, MB_ERR_NOT_READY, "run a frame before autotuning");
@@ -845,6 +849,7 @@ mb_status mb_sort_plan_destroy(mb_sort_plan* p) {
 mb_status mb_sort_and_hash(mb_sort_plan* p, const uint32_t* keys, const uint32_t* vals, uint32_t n,
                            uint32_t number_of_cells, uint32_t* sorted_keys, uint32_t* sorted_vals,
                            uint32_t* start, uint32_t* close, void* cuda_stream) {
+    mb::NvtxRange nvtx_range("mb_sort_and_hash");
     if (!p) return fail(nullptr, MB_ERR_INVALID_ARG, "plan is NULL");
     if (n > p->scratch.max_keys || number_of_cells == 0 || number_of_cells > p->scratch.max_cells)
         return fail(nullptr, MB_ERR_INVALID_ARG, "n or number_of_cells exceeds the plan");

@@ -446,6 +446,7 @@ mb_status mb_batch_set_active(mb_batch* b, uint32_t scene, int active) {
 }
 
 mb_status mb_batch_step(mb_batch* b, uint32_t k) {
+    mb::NvtxRange nvtx_range("mb_batch_step");
     if (!b) return bfail(nullptr, MB_ERR_INVALID_ARG, "batch is NULL");
     for (const SceneHost& h : b->scenes)
         if (!h.has_state) return bfail(b, MB_ERR_NOT_READY, "every scene needs a state before stepping");
@@ -543,6 +544,7 @@ mb_status mb_batch_set_tuning(mb_batch* b, const mb_tuning* t) {
 }
 
 mb_status mb_batch_autotune(mb_batch* b, uint32_t frames, mb_tuning* best, float* frame_ms, mb_tuning* tried) {
+    mb::NvtxRange nvtx_range("mb_batch_autotune");
     if (!b || !best) return bfail(b, MB_ERR_INVALID_ARG, "NULL argument");
     if (frames == 0) return bfail(b, MB_ERR_INVALID_ARG, "frames must be positive");
     if (b->scenes.empty()) return bfail(b, MB_ERR_NOT_READY, "the batch has no scene");

@@ -1,6 +1,7 @@
 // mb_internal.h — host-side interfaces between the library's translation units.
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -383,6 +384,15 @@ void reference_view(float eye[3], float target[3], float* fov_degrees, float to_
 
 // SM count of the current device (cached per device id).
 int device_sm_count();
+
+// Names the host-side span of a library call (NVTX range) for Nsight tools;
+// without a tool attached the push and pop return at once.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Settings checks shared by worlds and batches ("" = valid).
 bool settings_valid(const mb_settings* s, std::string& why);
