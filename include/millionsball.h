@@ -343,10 +343,11 @@ mb_status mb_render_view(mb_world* w, uint32_t width, uint32_t height, const flo
  * workgroup shapes, NUMBER_OF_THREADS_PER_WORKGROUP = 256 at src/physics/mod.rs:35).
  * Times every candidate tuning on the world's own scene for `frames` LOOP frames
  * each (CUDA events on the world's stream, one warm-up frame per candidate):
- * sixteen combinations of the sort (counting, or onesweep with 6-, 8- or 11-bit
+ * nineteen combinations of the sort (counting, or onesweep with 6-, 8- or 11-bit
  * digits), frames per graph launch (1, 8, 16), state gather (sorted copy or
- * through the permutation), frame kernel (per-stage graph or fused) and physics
- * tile (64, 128 or 256 slots per thread block).  The world's
+ * through the permutation), frame kernel (per-stage graph or fused), physics
+ * tile (64, 128 or 256 slots per thread block) and spheres per scatter thread
+ * (1, 2, 4).  The world's
  * state, keys, permutation, cell ranges and time are saved first and restored
  * afterwards, so the simulation continues exactly as if the tuner had not run.
  * The fastest candidate is applied and written to *best; frame_ms (nullable,
