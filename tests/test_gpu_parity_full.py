@@ -9,7 +9,7 @@
   and 99th-percentile depth 10 %, maximum depth 50 %, kinetic energy 5 %), which
   bit-exact states meet with zero difference.
 * P-4M (4,194,304 spheres in 16 Gaussian clusters, N = 2048, spring k = 1000,
-  c = 5): bit-exact at frames 1, 2, 3 and 12.
+  c = 5): bit-exact at frames 1, 2, 3, 12 and 30.
 * A batch of 20 mixed scenes compared with the oracle scene by scene (not with
   a lone GPU world), including scenes held for a few frames.
 
@@ -59,7 +59,7 @@ def test_p4m_clustered_spring_bit_exact(built_lib, cuda):
     """The 4,194,304-sphere clustered spring workload at full size: cells near the
     cluster centres hold ~100 spheres (crowded-warp walk, bands too wide to stage,
     large fixup cells)."""
-    run_pair(scenes.workload("P-4M"), 12, [1, 2, 3, 12])
+    run_pair(scenes.workload("P-4M"), 30, [1, 2, 3, 12, 30])
 
 
 def _compare_scene(b: Batch, i: int, ow: "oracle.OracleWorld", what: str):
