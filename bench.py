@@ -47,6 +47,7 @@ sys.path.insert(0, str(ROOT))
 PHYSICS_BYTES_PER_AGENT = 72
 FRAME_BYTES_PER_AGENT = 136
 FRAME_BYTES_PER_CELL = 4
+SORTS = {"counting": 0, "onesweep": 1, "rank": 2}  # mb_tuning.sort_algorithm
 
 
 def env_rank():
@@ -219,6 +220,8 @@ def run_ours(args, rank, world_size, local_rank):
     cells = p.number_of_grids_one_dimension ** 2
     stream = torch.cuda.current_stream()
     w = World(p, stream=stream.cuda_stream)
+    if args.sort != "default":
+        w.set_tuning(sort_algorithm=SORTS[args.sort])
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     flush_read = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB
 
@@ -361,6 +364,7 @@ def run_ours(args, rank, world_size, local_rank):
                    "cells": cells, "parallelism": f"replicas{world_size}" if world_size > 1 else "single",
                    "l2": "flushed before every timed frame (256 MB write then 256 MB read, outside the events)",
                    "digit_bits_max": w.tuning.digit_bits_max, "collide_block": w.tuning.collide_block,
+                   "sort_algorithm": {v: k for k, v in SORTS.items()}[w.tuning.sort_algorithm],
                    "scatter_agents": max(w.tuning.scatter_agents, 1)},
         "stages_ms": {"sort": float(stage[:, 0].mean()), "cells": float(stage[:, 1].mean()),
                       "physics": phys_ms, "frames": prof_frames,
@@ -806,6 +810,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-frames", type=int, default=100)
     ap.add_argument("--e2e-reps", type=int, default=5)
+    ap.add_argument("--sort", choices=["default", *SORTS], default="default",
+                    help="frame sort of the world workloads (default: the library's)")
     args = ap.parse_args()
     rank, world_size, local_rank = env_rank()
     if args.impl == "reference":

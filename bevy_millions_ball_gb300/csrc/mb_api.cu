@@ -72,6 +72,7 @@ struct mb_world {
     int64_t time = -1;
     bool has_state = false;
     bool frame_done = false;           // a frame ran since the last upload
+    bool rank_ready = false;           // cnt.far[cur] lists the far moves of the frame before (MB_SORT_RANK)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaGraphExec_t chain[2] = {nullptr, nullptr};  // chained LOOP frames from each parity
     unsigned long long* zbuf = nullptr;             // render depth buffer (grown on demand)
@@ -152,7 +153,10 @@ cudaError_t mark(mb_world* w, int i, cudaStream_t st, bool capturing) {
                      : cudaEventRecord(w->prof_ev[i], st);
 }
 
-bool counting(const mb_world* w) { return w->tuning.sort_algorithm == MB_SORT_COUNTING; }
+// Counting sort (claim-and-fixup or rank placement) rather than the radix sort.
+bool counting(const mb_world* w) { return w->tuning.sort_algorithm != MB_SORT_ONESWEEP; }
+// LOOP frames place spheres by rank (falling back to claim-and-fixup by themselves).
+bool rank(const mb_world* w) { return w->tuning.sort_algorithm == MB_SORT_RANK; }
 // The physics pass reads the state through the permutation instead of a sorted copy.
 bool indirect(const mb_world* w) { return w->tuning.state_gather == MB_GATHER_INDIRECT; }
 // LOOP frames run as one cooperative kernel per step (profiling needs the
@@ -202,6 +206,19 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         if ((e = mark(w, 1, st, capturing))) return e;
         hist = w->cnt.hist;
         coarse = w->cnt.coarse;
+    } else if (rank(w)) {
+        // cell offsets (keeping the previous frame's), then the order by rank in
+        // the old neighbourhoods; this frame's physics pass lists its far moves
+        // in cnt.far[cur ^ 1] for the next frame
+        if ((e = mb::count_scan_keep(w->cnt, w->cells, w->scratch.offs, w->cnt.far[cur ^ 1], st, pdl && chained)))
+            return e;
+        if ((e = mark(w, 1, st, capturing))) return e;
+        if ((e = mb::count_rank(w->cnt, w->keys, w->n, w->cells, w->scratch.offs, w->cnt.far[cur], w->perm,
+                                w->pos[cur], w->vfme[cur], indirect(w) ? nullptr : w->spos,
+                                indirect(w) ? nullptr : w->svfme, w->bands, w->P.N, st, pdl)))
+            return e;
+        hist = w->cnt.hist;
+        coarse = w->cnt.coarse;
     } else if (counting(w)) {
         // cell offsets first (scan of the counts), then the permutation
         if ((e = mb::count_scan(w->cnt, w->scratch.ctl, w->cells, w->scratch.offs, st, pdl && chained))) return e;
@@ -230,11 +247,13 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
     } else if (indirect(w)) {
         e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->pos[cur], w->vfme[cur], w->perm,
                                     w->pos[nxt], w->vfme[nxt], w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError,
-                                    st, pdl && counting(w), w->tuning.collide_block);
+                                    st, pdl && counting(w), w->tuning.collide_block,
+                                    rank(w) ? w->cnt.far[nxt] : nullptr);
     } else {
         e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->spos, w->svfme, nullptr, w->pos[nxt],
                                     w->vfme[nxt], w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError, st,
-                                    pdl && counting(w), w->tuning.collide_block);
+                                    pdl && counting(w), w->tuning.collide_block,
+                                    rank(w) ? w->cnt.far[nxt] : nullptr);
     }
     if (e) return e;
     return mark(w, 3, st, capturing);
@@ -351,7 +370,8 @@ mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out) {
         if ((e = cudaMalloc(&w->fused_bar, sizeof(uint32_t) * 2u))) return e;
         if ((e = cudaMemset(w->fused_bar, 0, sizeof(uint32_t) * 2u))) return e;
         if ((e = mb::scratch_alloc(w->scratch, w->n, w->cells))) return e;
-        return mb::count_scratch_alloc(w->cnt, w->cells, w->n);
+        if ((e = mb::count_scratch_alloc(w->cnt, w->cells, w->n))) return e;
+        return mb::count_rank_alloc(w->cnt);
     };
     cudaError_t e = alloc_all();
     if (e) {
@@ -406,7 +426,7 @@ mb_status mb_set_settings(mb_world* w, const mb_settings* s) {
         if ((e = cudaMalloc(&offs, sizeof(uint32_t) * ((size_t)new_cells + 1u))))
             return cuda_fail(w, "mb_set_settings", e);
         mb::CountScratch cnt;
-        if ((e = mb::count_scratch_alloc(cnt, new_cells, w->n))) {
+        if ((e = mb::count_scratch_alloc(cnt, new_cells, w->n)) || (e = mb::count_rank_alloc(cnt))) {
             cudaFree(offs);
             mb::count_scratch_free(cnt);
             return cuda_fail(w, "mb_set_settings", e);
@@ -419,6 +439,7 @@ mb_status mb_set_settings(mb_world* w, const mb_settings* s) {
     }
     drop_graphs(w);
     apply_settings(w, *s);
+    w->rank_ready = false;
     // keys emitted under the old grid are re-derived under the new one
     if (grid_changed && w->has_state) {
         cudaError_t e = cudaSuccess;
@@ -454,6 +475,7 @@ mb_status mb_set_state(mb_world* w, const float* pos_scale, const uint32_t* vfme
     if ((e = cudaMemsetAsync(w->keys, 0, sizeof(uint32_t) * w->n, w->stream)))
         return cuda_fail(w, "mb_set_state", e);
     w->frame_done = false;
+    w->rank_ready = false;
     if ((e = recount(w))) return cuda_fail(w, "mb_set_state", e);
     if (where == MB_HOST && (e = cudaStreamSynchronize(w->stream)))
         return cuda_fail(w, "mb_set_state", e);
@@ -485,6 +507,7 @@ mb_status mb_step(mb_world* w, uint32_t k) {
     for (uint32_t f = 0; f < k;) {
         if (w->time == 0) {
             if ((e = enqueue_frame(w, w->stream, w->cur, true))) return cuda_fail(w, "mb_step(init)", e);
+            w->rank_ready = false;  // the next frame sorts keys in upload order
         } else if (fused(w)) {  // the remaining LOOP frames, one cooperative launch per 256
             const uint32_t fr = std::min(k - f, kFusedFramesPerLaunch);
             if ((e = enqueue_fused(w, fr))) return cuda_fail(w, "mb_step(fused)", e);
@@ -492,6 +515,14 @@ mb_status mb_step(mb_world* w, uint32_t k) {
             w->time += fr;
             w->cur ^= (int)(fr & 1u);
             w->frame_done = true;
+            w->rank_ready = false;
+            continue;
+        } else if (rank(w) && !w->rank_ready) {
+            // no far list describes this frame's input yet: mark it overflowed, so the
+            // frame claims slots and fixes cells (its physics pass then lists far moves)
+            if ((e = cudaMemsetAsync(w->cnt.far[w->cur], 0xFF, sizeof(uint32_t), w->stream)))
+                return cuda_fail(w, "mb_step", e);
+            w->rank_ready = true;
             continue;
         } else if (chain_frames(w) > 1u && k - f >= chain_frames(w) && !w->profiling) {
             // a chain of LOOP frames, one launch
@@ -591,8 +622,9 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
         return fail(w, MB_ERR_INVALID_ARG, "digit_bits_max must be in [4, 11]");
     if (t->collide_block != 64u && t->collide_block != 128u && t->collide_block != 256u)
         return fail(w, MB_ERR_INVALID_ARG, "collide_block must be 64, 128 or 256");
-    if (t->sort_algorithm != MB_SORT_COUNTING && t->sort_algorithm != MB_SORT_ONESWEEP)
-        return fail(w, MB_ERR_INVALID_ARG, "sort_algorithm must be MB_SORT_COUNTING or MB_SORT_ONESWEEP");
+    if (t->sort_algorithm != MB_SORT_COUNTING && t->sort_algorithm != MB_SORT_ONESWEEP &&
+        t->sort_algorithm != MB_SORT_RANK)
+        return fail(w, MB_ERR_INVALID_ARG, "sort_algorithm must be MB_SORT_COUNTING, MB_SORT_ONESWEEP or MB_SORT_RANK");
     const uint32_t fpl = t->frames_per_launch;
     if (!(fpl == 0 || fpl == 1 || fpl == 2 || fpl == 4 || fpl == 8 || fpl == 16))
         return fail(w, MB_ERR_INVALID_ARG, "frames_per_launch must be 0, 1, 2, 4, 8 or 16");
@@ -607,8 +639,9 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
     if (t->frame_kernel == MB_FRAME_FUSED && mb::fused_blocks_per_sm() <= 0)
         return fail(w, MB_ERR_INVALID_ARG, "the fused frame kernel cannot be resident on this device");
     drop_graphs(w);
-    bool to_counting = t->sort_algorithm == MB_SORT_COUNTING && !counting(w);
+    bool to_counting = t->sort_algorithm != MB_SORT_ONESWEEP && !counting(w);
     w->tuning = *t;
+    w->rank_ready = false;
     w->sched = mb::make_schedule(w->n, w->cells, w->tuning.digit_bits_max);
     if (to_counting && w->has_state) {  // counts were not kept while the radix sort ran
         cudaError_t e = recount(w);

@@ -38,15 +38,112 @@
 namespace mb {
 namespace {
 
+// keep (nullable): the replaced offsets are copied there (rank placement);
+// far_reset (nullable): a far-move list emptied for this frame's physics pass.
 template <bool kScenes>
 __global__ void __launch_bounds__(kScanThreads)
     k_cell_scan(const uint32_t* __restrict__ hist, const uint32_t* __restrict__ coarse, uint32_t cells,
                 uint32_t* __restrict__ offs, uint32_t* fix_ctl,
-                const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ cell_tile_scene) {
+                const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ cell_tile_scene,
+                uint32_t* __restrict__ keep, uint32_t* __restrict__ far_reset) {
     __shared__ uint32_t s_warp[kScanThreads / 32], s_base[kScanThreads / 32];
     griddep_wait();  // after the previous frame's physics pass, when chained to it
     griddep_launch();
-    scan_chunk<kScenes>(blockIdx.x, hist, coarse, cells, offs, fix_ctl, scenes, cell_tile_scene, s_warp, s_base);
+    if (far_reset && blockIdx.x == 0 && threadIdx.x == 0) *far_reset = 0u;
+    scan_chunk<kScenes>(blockIdx.x, hist, coarse, cells, offs, fix_ctl, scenes, cell_tile_scene, s_warp, s_base,
+                        keep);
+}
+
+// Rank placement of one world's spheres (MB_SORT_RANK), one sphere per thread
+// per step.  The input is the previous frame's sorted order, described by
+// offs_old; a sphere of new cell k = (kx, kz) that moved at most one cell sits
+// in the old ranges of cells (kx-1..kx+1, kz-1..kz+1), three slot ranges, one
+// per row.  Its stable slot is offs[k] plus the spheres with key k before it in
+// those ranges, plus the listed far moves with key k before it (a per-block
+// bit filter of their cells spares the others the list).  No atomics, no
+// marks: the order is final, so the band table is written here too.  The first
+// sphere of each cell clears its count for the next frame.  A far list that
+// overflowed (more than kFarCap moves, or forced after an upload or a grid
+// change) sends every block down the claim-and-fixup path instead (the fixup
+// kernel after this one then runs too).
+__device__ __forceinline__ uint32_t bloom_bit(uint32_t k) { return (k * 2654435761u) >> 20; }  // 12 bits
+
+__global__ void __launch_bounds__(256)
+    k_cell_rank(const uint32_t* __restrict__ keys, uint32_t n, uint32_t cells, uint32_t* __restrict__ hist,
+                uint32_t* __restrict__ perm, const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in,
+                float4* __restrict__ spos, uint4* __restrict__ svfme, const uint32_t* __restrict__ offs,
+                const uint32_t* __restrict__ offs_old, const uint32_t* __restrict__ far, uint4* __restrict__ bands,
+                uint32_t N, uint32_t* __restrict__ fix_bits) {
+    __shared__ uint32_t s_key[kFarCap], s_slot[kFarCap], s_bloom[kBloomWords];
+    griddep_wait();  // the scan's offsets, the previous physics pass's keys and far moves
+    griddep_launch();
+    const uint32_t F = __ldcg(far);
+    if (F > kFarCap) {
+        scatter_range<false, 1>(blockIdx.x, gridDim.x, keys, n, hist, perm, pos_in, vfme_in, spos, svfme, offs,
+                                bands, N, fix_bits);
+        return;
+    }
+    const uint32_t tid = threadIdx.x;
+    if (F) {
+        for (uint32_t t = tid; t < kBloomWords; t += blockDim.x) s_bloom[t] = 0u;
+        __syncthreads();
+        for (uint32_t t = tid; t < F; t += blockDim.x) {
+            const uint32_t sl = min(__ldcg(far + 1u + t), n - 1u), k = __ldg(keys + sl);
+            s_slot[t] = sl;
+            s_key[t] = k;
+            const uint32_t b = bloom_bit(k);
+            atomicOr(&s_bloom[b >> 5], 1u << (b & 31u));
+        }
+        __syncthreads();
+    }
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + tid; i < n; i += stride) {
+        const uint32_t k = __ldg(keys + i);
+        if (k >= cells) continue;  // keys the physics pass cannot emit
+        float4 p;
+        uint4 q;
+        if (spos) {
+            p = __ldg(pos_in + i);
+            q = __ldg(vfme_in + i);
+        }
+        const uint32_t base = __ldg(offs + k);
+        const uint32_t kz = k / N, kx = k - kz * N;
+        const uint32_t c0 = kx > 0u ? kx - 1u : 0u, c1 = (kx + 1u < N ? kx + 1u : kx) + 1u;
+        uint32_t lo[3], hi[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const bool row = d == 0 ? kz > 0u : (d == 2 ? kz + 1u < N : true);
+            const uint32_t r = kz + (uint32_t)d - 1u;
+            lo[d] = row ? __ldg(offs_old + r * N + c0) : 0u;
+            hi[d] = row ? min(__ldg(offs_old + r * N + c1), i) : 0u;
+        }
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            for (uint32_t j = lo[d]; j < hi[d]; j += 4u) {
+                uint32_t kk[4];
+#pragma unroll
+                for (uint32_t u = 0; u < 4u; ++u) kk[u] = __ldg(keys + min(j + u, hi[d] - 1u));
+#pragma unroll
+                for (uint32_t u = 0; u < 4u; ++u) cnt += (j + u < hi[d] && kk[u] == k) ? 1u : 0u;
+            }
+        }
+        if (F) {
+            const uint32_t b = bloom_bit(k);
+            if (s_bloom[b >> 5] & (1u << (b & 31u)))
+                for (uint32_t t = 0; t < F; ++t) cnt += (s_key[t] == k && s_slot[t] < i) ? 1u : 0u;
+        }
+        if (cnt == 0u) hist[k] = 0u;  // the cell's first sphere
+        const uint32_t dst = base + cnt;
+        if (dst < n) {
+            perm[dst] = i;
+            if (spos) {
+                spos[dst] = p;
+                svfme[dst] = q;
+            }
+            if (bands) write_band_bounds(bands, offs, N, n, dst, k);
+        }
+    }
 }
 
 template <uint32_t kPer>
@@ -130,16 +227,19 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// gate (nullable): the far list rank placement read; unless it overflowed the
+// order is final and only the counts are cleared.
 template <class Src>
 __global__ void __launch_bounds__(kCollectThreads)
     k_fix_marked(const uint32_t* __restrict__ fix_bits, const uint32_t* __restrict__ keys, uint32_t n,
                  const uint32_t* __restrict__ offs, uint32_t* perm, FixLists lists, uint32_t* __restrict__ tmp,
                  Src src, float4* __restrict__ spos, uint4* __restrict__ svfme, uint32_t* __restrict__ hist,
-                 uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles) {
+                 uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles, const uint32_t* __restrict__ gate) {
     __shared__ MarkedSmem S;
     griddep_wait();  // the scatter's bitmap and order are complete
     griddep_launch();
     clear_counts(blockIdx.x, gridDim.x, src, hist, cells, coarse, tiles);
+    if (gate && __ldcg(gate) <= kFarCap) return;
     fix_marked_block<Src, false, true>(blockIdx.x, gridDim.x, fix_bits, keys, n, offs, perm, lists, tmp, src, spos,
                                        svfme, S);
 }
@@ -253,12 +353,26 @@ cudaError_t count_scratch_alloc(CountScratch& s, uint32_t max_cells, uint32_t ma
     return cudaSuccess;
 }
 
+cudaError_t count_rank_alloc(CountScratch& s) {
+    if (s.offs_old) return cudaSuccess;
+    cudaError_t e;
+    const size_t padded = ((size_t)s.max_cells + kScanTile) & ~(size_t)15;
+    if ((e = cudaMalloc(&s.offs_old, sizeof(uint32_t) * padded))) return e;
+    for (auto*& l : s.far) {
+        if ((e = cudaMalloc(&l, sizeof(uint32_t) * kFarWords))) return e;
+        if ((e = cudaMemset(l, 0xFF, sizeof(uint32_t)))) return e;  // overflowed: no order to rank from yet
+    }
+    return cudaSuccess;
+}
+
 void count_scratch_free(CountScratch& s) {
     cudaFree(s.hist);
     cudaFree(s.coarse);
     cudaFree(s.fix_ctl);
     cudaFree(s.fix_tmp);
     cudaFree(s.fix_bits);
+    cudaFree(s.offs_old);
+    for (auto* l : s.far) cudaFree(l);
     for (auto* l : s.fix) cudaFree(l);
     s = CountScratch();
 }
@@ -290,7 +404,31 @@ cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t*
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
     return launch_pdl(pdl, k_cell_scan<false>, dim3(chunks), dim3(kScanThreads), 0, st, (const uint32_t*)s.hist,
                       (const uint32_t*)s.coarse, cells, offs, s.fix_ctl, (const SceneDev*)nullptr,
-                      (const uint32_t*)nullptr);
+                      (const uint32_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr);
+}
+
+cudaError_t count_scan_keep(CountScratch& s, uint32_t cells, uint32_t* offs, uint32_t* far_reset, cudaStream_t st,
+                            bool pdl) {
+    const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
+    return launch_pdl(pdl, k_cell_scan<false>, dim3(chunks), dim3(kScanThreads), 0, st, (const uint32_t*)s.hist,
+                      (const uint32_t*)s.coarse, cells, offs, s.fix_ctl, (const SceneDev*)nullptr,
+                      (const uint32_t*)nullptr, s.offs_old, far_reset);
+}
+
+cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells, const uint32_t* offs,
+                       const uint32_t* far, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
+                       float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st, bool pdl) {
+    cudaError_t e;
+    if (n) {
+        const uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
+        if ((e = launch_pdl(pdl, k_cell_rank, dim3(blocks), dim3(256), 0, st, keys, n, cells, s.hist, perm, pos_in,
+                            vfme_in, spos, svfme, offs, (const uint32_t*)s.offs_old, far, bands, N, s.fix_bits)))
+            return e;
+    }
+    const OneBuffer src{pos_in, vfme_in};
+    return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(std::max(collect_grid(n), 1u)),
+                      dim3(kCollectThreads), 0, st, (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s),
+                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells), far);
 }
 
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
@@ -310,14 +448,15 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
     const OneBuffer src{pos_in, vfme_in};
     return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(std::max(collect_grid(n), 1u)),
                       dim3(kCollectThreads), 0, st, (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s),
-                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells));
+                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells),
+                      (const uint32_t*)nullptr);
 }
 
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
                               uint32_t cells, uint32_t* offs, cudaStream_t st) {
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
     k_cell_scan<true><<<chunks, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.fix_ctl, scenes,
-                                                      cell_tile_scene);
+                                                      cell_tile_scene, nullptr, nullptr);
     return cudaGetLastError();
 }
 
@@ -340,7 +479,7 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
     const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
     k_fix_marked<SceneBuffers><<<std::max(collect_grid(n), 1u), kCollectThreads, 0, st>>>(
         s.fix_bits, keys, n, offs, perm, fix_lists(s), s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse,
-        scan_tiles(cells));
+        scan_tiles(cells), nullptr);
     return cudaGetLastError();
 }
 

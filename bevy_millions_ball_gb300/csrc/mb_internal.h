@@ -230,10 +230,13 @@ cudaError_t launch_physics_init(const PhysParams& p, uint32_t n, const uint32_t*
 // table the sort wrote for this order.
 // `pdl`: launched as a programmatic dependent of the kernel before it.  tile:
 // slots per thread block (64, 128 or 256).
+// far (nullable): the far-move list this pass fills for the next frame's rank
+// placement (emptied by this frame's scan).
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                 const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
                                 uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
-                                cudaStream_t st, bool pdl = false, uint32_t tile = kPhysicsTile);
+                                cudaStream_t st, bool pdl = false, uint32_t tile = kPhysicsTile,
+                                uint32_t* far = nullptr);
 // LOOP frames of one world as a single cooperative kernel (all stages of every
 // frame, separated by grid barriers): `frames` frames from state buffer `cur`
 // (the last one lands in cur ^ (frames & 1)), counting sort, sorted copy or
@@ -296,6 +299,18 @@ constexpr uint32_t kFixWarp = 256;
 // of cells above kFixWarp slots is filled.
 enum : int { kFixListSmall = 0, kFixListWarp = 1, kFixListHuge = 2, kFixLists = 3, kFixListDone = 3, kFixCtlWords = 4 };
 
+// Rank placement (MB_SORT_RANK).  Once a frame's input is the previous frame's
+// sorted order, a sphere that moved at most one cell along x and z sits, in that
+// input, inside the old 3 x 3 neighbourhood of its new cell, and so does every
+// other such sphere of that cell: its slot is the cell's offset plus the number
+// of spheres of its new cell that precede it there.  A sphere that moved
+// further (a far move) is listed by the physics pass; up to kFarCap listed far
+// moves are counted in from the list, more send the frame down the claim-and-
+// fixup path.  A far list is a count word followed by kFarCap input slots.
+constexpr uint32_t kFarCap = 256;
+constexpr uint32_t kFarWords = 1u + kFarCap;
+constexpr uint32_t kBloomWords = 128;  // per-block filter of the listed far moves' cells (4096 bits)
+
 struct CountScratch {
     uint32_t max_cells = 0;
     uint32_t* hist = nullptr;     // [max_cells] counts of the keys of the next sort
@@ -305,6 +320,8 @@ struct CountScratch {
     uint32_t fix_cap[kFixLists] = {0u, 0u, 0u};                // their capacities
     uint32_t* fix_tmp = nullptr;  // [max_keys] copy of a large cell's input indices
     uint32_t* fix_bits = nullptr; // [max_keys / 32 + 1] input slots whose run listed its cell
+    uint32_t* offs_old = nullptr; // [max_cells + 1] the previous frame's cell offsets (rank placement)
+    uint32_t* far[2] = {nullptr, nullptr};  // [kFarWords] far-move lists, one per state parity
     uint32_t tiles = 0;
 };
 // Lists are sized from max_keys: a listed cell holds >= 2, > kFixSmall or > kFixWarp keys.
@@ -339,6 +356,20 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
                           float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,
                           bool pdl = false, uint32_t per_thread = 1);
+// Rank placement (MB_SORT_RANK).  count_scan_keep: count_scan that first copies
+// the offsets it replaces to s.offs_old and empties the far list far_reset
+// (the one this frame's physics pass fills).  count_rank: perm, the sorted copy
+// and the band table from the ranks (offs: this frame's offsets, s.offs_old the
+// previous frame's, far: the far moves of the previous physics pass); when far
+// holds more than kFarCap moves it claims slots and fixes cells as
+// count_scatter does.  hist := 0, coarse := 0 either way.
+// Allocates offs_old and the far lists (worlds that may run MB_SORT_RANK).
+cudaError_t count_rank_alloc(CountScratch& s);
+cudaError_t count_scan_keep(CountScratch& s, uint32_t cells, uint32_t* offs, uint32_t* far_reset, cudaStream_t st,
+                            bool pdl = false);
+cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells, const uint32_t* offs,
+                       const uint32_t* far, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
+                       float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st, bool pdl = false);
 // Batched count scan: scene cell ranges are padded to whole scan tiles
 // (cell_tile_scene[t] = scene of tile t); tiles of HOLD scenes are skipped.
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,

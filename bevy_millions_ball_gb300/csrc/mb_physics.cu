@@ -244,6 +244,23 @@ __device__ __forceinline__ void emit_count(uint32_t* hist, uint32_t* coarse, uin
     if ((threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(coarse + t, (uint32_t)__popc(peers));
 }
 
+// Rank placement's far-move list (worlds in MB_SORT_RANK): input slot i of the
+// next frame moved more than one cell along x or z (`f`).  One atomic per warp;
+// once the list has overflowed (the next frame claims and fixes instead) the
+// count is no longer raised.
+__device__ __forceinline__ void note_far(uint32_t* far, uint32_t i, bool f) {
+    const uint32_t am = __activemask();
+    const uint32_t b = __ballot_sync(am, f);
+    if (!b) return;
+    const uint32_t lane = threadIdx.x & 31u, leader = (uint32_t)(__ffs(b) - 1);
+    uint32_t base = 0;
+    if (lane == leader)
+        base = *reinterpret_cast<volatile uint32_t*>(far) > kFarCap ? kFarCap : atomicAdd(far, (uint32_t)__popc(b));
+    base = __shfl_sync(am, base, (int)leader);
+    const uint32_t at = base + (uint32_t)__popc(b & ((1u << lane) - 1u));
+    if (f && at < kFarCap) far[1u + at] = i;
+}
+
 // main, INIT pipeline (physics.wgsl:91-96): gather through perm, re-pack, emit key.
 __global__ void __launch_bounds__(256)
     k_physics_init(PhysParams P, uint32_t n, const uint32_t* __restrict__ perm,
@@ -452,7 +469,8 @@ __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32
                                             const uint4* __restrict__ svfme, const uint32_t* __restrict__ perm,
                                             float4* __restrict__ pos_out,
                                             uint4* __restrict__ vfme_out, uint32_t* __restrict__ keys_out,
-                                            uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse) {
+                                            uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
+                                            uint32_t* far = nullptr, uint32_t ocx = 0, uint32_t ocz = 0) {
     // candidate rows in the reference's order: own row (band 1), below (0), above (2)
     uint32_t c[3], o_s[3], o_g[3];
     bool shared = true;
@@ -515,6 +533,7 @@ __device__ __forceinline__ void step_sphere(const PhysParams& P, Agent a, uint32
     const uint32_t nk = base_c + nz * P.N + nx;
     keys_out[i] = nk;
     emit_count(hist, coarse, nk);
+    if (far) note_far(far, i, nx - ocx + 1u > 2u || nz - ocz + 1u > 2u);  // (ocx, ocz): the cell it was sorted by
 }
 
 // Key of a position (physics.wgsl:115-117).
@@ -580,7 +599,7 @@ __device__ __forceinline__ void physics_tile(
     const uint4* __restrict__ svfme, const uint32_t* __restrict__ perm, float4* __restrict__ pos_out0,
     float4* __restrict__ pos_out1, uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1,
     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
-    uint32_t* __restrict__ err) {
+    uint32_t* __restrict__ err, uint32_t* __restrict__ far = nullptr) {
     static_assert(!(kBatched && kIndirect), "batches stage a sorted copy");
     static_assert(kTile == 64u || kTile == 128u || kTile == 256u, "tiles of 64, 128 or 256 slots");
     constexpr bool kPosOnly = kResp == kSpring;
@@ -778,7 +797,7 @@ __device__ __forceinline__ void physics_tile(
     if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
 
     step_sphere<kIndirect, kCg, kCap, kResp>(P, a, i, n, base_a, base_c, lo, hi, s_pos, s_vfme, s_lo, s_cnt, spos, svfme, perm,
-                                pos_out, vfme_out, keys_out, hist, coarse);
+                                pos_out, vfme_out, keys_out, hist, coarse, kBatched ? nullptr : far, cx, cz);
 }
 
 template <bool kBatched, bool kIndirect, uint32_t kTile = kTileThreads, int kResp = kSpringRuntime>
@@ -789,13 +808,13 @@ __global__ void __launch_bounds__(kTile)
                     const uint4* __restrict__ svfme, const uint32_t* __restrict__ perm, float4* __restrict__ pos_out0,
                     float4* __restrict__ pos_out1, uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1,
                     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
-                    uint32_t* __restrict__ err) {
+                    uint32_t* __restrict__ err, uint32_t* __restrict__ far) {
     __shared__ __align__(16) TileSmemT<kTile, kResp == kSpring> sm;
     __shared__ __align__(8) uint64_t s_bar;
     if (!kIndirect && threadIdx.x == 0) mbar_init(&s_bar, 1u);  // first copy after the tile's CTA barrier
     physics_tile<kBatched, kIndirect, false, kTile, kResp>(blockIdx.x, threadIdx.x, 0u, &sm, &s_bar, P1, scenes, tile_scene, n, offs,
                                       bands, spos, svfme, perm, pos_out0, pos_out1, vfme_out0, vfme_out1, keys_out,
-                                      hist, coarse, err);
+                                      hist, coarse, err, far);
 }
 
 // ---------------------------------------------------------------- fused frame
@@ -1054,16 +1073,16 @@ template <uint32_t kTile, int kResp>
 cudaError_t launch_physics_resp(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                 const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
                                 uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse,
-                                uint32_t* err, cudaStream_t st, bool pdl) {
+                                uint32_t* err, cudaStream_t st, bool pdl, uint32_t* far) {
     const dim3 grid((n + kTile - 1u) / kTile), block(kTile);
     if (perm)
         return launch_pdl(pdl, k_physics_frame<false, true, kTile, kResp>, grid, block, 0, st, p, (const SceneDev*)nullptr,
                           (const uint32_t*)nullptr, n, offs, bands, spos, svfme, perm, pos_out, (float4*)nullptr,
-                          vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err);
+                          vfme_out, (uint4*)nullptr, keys_out, hist, coarse, err, far);
     return launch_pdl(pdl, k_physics_frame<false, false, kTile, kResp>, grid, block, 0, st, p,
                       (const SceneDev*)nullptr, (const uint32_t*)nullptr, n, offs, bands, spos, svfme,
                       (const uint32_t*)nullptr, pos_out, (float4*)nullptr, vfme_out, (uint4*)nullptr, keys_out, hist,
-                      coarse, err);
+                      coarse, err, far);
 }
 
 // One world's response model is known on the host: the kernel is compiled for it.
@@ -1071,27 +1090,27 @@ template <uint32_t kTile>
 cudaError_t launch_physics_tiles(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                  const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
                                  uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse,
-                                 uint32_t* err, cudaStream_t st, bool pdl) {
+                                 uint32_t* err, cudaStream_t st, bool pdl, uint32_t* far) {
     if (p.spring)
         return launch_physics_resp<kTile, kSpring>(p, n, offs, bands, spos, svfme, perm, pos_out, vfme_out,
-                                                   keys_out, hist, coarse, err, st, pdl);
+                                                   keys_out, hist, coarse, err, st, pdl, far);
     return launch_physics_resp<kTile, kRigid>(p, n, offs, bands, spos, svfme, perm, pos_out, vfme_out, keys_out,
-                                              hist, coarse, err, st, pdl);
+                                              hist, coarse, err, st, pdl, far);
 }
 
 cudaError_t launch_physics_loop(const PhysParams& p, uint32_t n, const uint32_t* offs, const uint4* bands,
                                 const float4* spos, const uint4* svfme, const uint32_t* perm, float4* pos_out,
                                 uint4* vfme_out, uint32_t* keys_out, uint32_t* hist, uint32_t* coarse, uint32_t* err,
-                                cudaStream_t st, bool pdl, uint32_t tile) {
+                                cudaStream_t st, bool pdl, uint32_t tile, uint32_t* far) {
     if (!n) return cudaSuccess;
     if (tile == 64u)
         return launch_physics_tiles<64u>(p, n, offs, bands, spos, svfme, perm, pos_out, vfme_out, keys_out, hist,
-                                         coarse, err, st, pdl);
+                                         coarse, err, st, pdl, far);
     if (tile == 256u)
         return launch_physics_tiles<256u>(p, n, offs, bands, spos, svfme, perm, pos_out, vfme_out, keys_out, hist,
-                                          coarse, err, st, pdl);
+                                          coarse, err, st, pdl, far);
     return launch_physics_tiles<128u>(p, n, offs, bands, spos, svfme, perm, pos_out, vfme_out, keys_out, hist,
-                                      coarse, err, st, pdl);
+                                      coarse, err, st, pdl, far);
 }
 
 int fused_blocks_per_sm() {
@@ -1162,7 +1181,7 @@ cudaError_t launch_batch_tiles(const SceneDev* scenes, const uint32_t* tile_scen
     PhysParams unused{};
     k_physics_frame<true, false, kTile><<<(n + kTile - 1u) / kTile, kTile, 0, st>>>(
         unused, scenes, tile_scene, n, offs, bands, spos, svfme, nullptr, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1,
-        keys, hist, coarse, err);
+        keys, hist, coarse, err, nullptr);
     return cudaGetLastError();
 }
 

@@ -262,7 +262,7 @@ typedef struct mb_tuning {
     uint32_t digit_bits_max;   /* widest radix digit of the onesweep sort, 4..11 */
     uint32_t collide_block;    /* sorted slots per thread block of the physics pass: 64, 128
                                   (default) or 256; MB_FRAME_FUSED frames run 128 */
-    uint32_t sort_algorithm;   /* MB_SORT_COUNTING (default) or MB_SORT_ONESWEEP */
+    uint32_t sort_algorithm;   /* MB_SORT_COUNTING (default), MB_SORT_ONESWEEP or MB_SORT_RANK */
     uint32_t frames_per_launch; /* LOOP frames captured per graph launch in multi-frame steps:
                                    1, 2, 4, 8 (default; 0 reads as 8) or 16 */
     uint32_t state_gather;     /* MB_GATHER_COPY or MB_GATHER_INDIRECT (below) */
@@ -295,12 +295,20 @@ typedef struct mb_tuning {
 #define MB_GATHER_COPY 0u
 #define MB_GATHER_INDIRECT 1u
 
-/* Frame sort: both produce the identical stable permutation and cell ranges.
+/* Frame sort: all three produce the identical stable permutation and cell ranges.
  *   MB_SORT_COUNTING: per-cell counts (emitted by the previous physics pass) ->
  *                     scan = cell offsets -> scatter -> in-cell fixup
- *   MB_SORT_ONESWEEP: onesweep LSD radix sort of the keys, then the cell-offset build */
+ *   MB_SORT_ONESWEEP: onesweep LSD radix sort of the keys, then the cell-offset build
+ *   MB_SORT_RANK:     counts -> scan -> each sphere placed at its cell's offset plus
+ *                     its rank among the spheres of its new cell in its old 3 x 3
+ *                     cell neighbourhood (no atomics, no fixup); spheres that moved
+ *                     more than one cell are listed by the physics pass and ranked
+ *                     from the list (up to 256 per frame; beyond that, and in the
+ *                     first LOOP frame after an upload, a grid change or a tuning
+ *                     change, the frame runs the MB_SORT_COUNTING scatter and fixup) */
 #define MB_SORT_COUNTING 0u
 #define MB_SORT_ONESWEEP 1u
+#define MB_SORT_RANK 2u
 mb_status mb_get_tuning(const mb_world* w, mb_tuning* out);
 mb_status mb_set_tuning(mb_world* w, const mb_tuning* t);
 
