@@ -222,6 +222,8 @@ def run_ours(args, rank, world_size, local_rank):
     w = World(p, stream=stream.cuda_stream)
     if args.sort != "default":
         w.set_tuning(sort_algorithm=SORTS[args.sort])
+    if args.tuning:
+        w.set_tuning(**{k: int(v) for k, v in (kv.split("=") for kv in args.tuning.split(","))})
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     flush_read = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB
 
@@ -812,6 +814,8 @@ def main():
     ap.add_argument("--e2e-reps", type=int, default=5)
     ap.add_argument("--sort", choices=["default", *SORTS], default="default",
                     help="frame sort of the world workloads (default: the library's)")
+    ap.add_argument("--tuning", default="",
+                    help="other mb_tuning fields of the world workloads, e.g. scatter_agents=2,collide_block=256")
     args = ap.parse_args()
     rank, world_size, local_rank = env_rank()
     if args.impl == "reference":

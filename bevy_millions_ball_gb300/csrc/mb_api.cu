@@ -157,6 +157,14 @@ cudaError_t mark(mb_world* w, int i, cudaStream_t st, bool capturing) {
 bool counting(const mb_world* w) { return w->tuning.sort_algorithm != MB_SORT_ONESWEEP; }
 // LOOP frames place spheres by rank (falling back to claim-and-fixup by themselves).
 bool rank(const mb_world* w) { return w->tuning.sort_algorithm == MB_SORT_RANK; }
+// Cell offsets a frame reading state buffer `cur` writes.  Rank placement reads
+// the previous frame's offsets while the scan writes new ones, so it alternates
+// two buffers by state parity; the other sorts keep one.
+uint32_t* frame_offs(const mb_world* w, int cur) {
+    return rank(w) && cur ? w->cnt.offs_old : w->scratch.offs;
+}
+// The offsets of the last frame run (the current order's cell ranges).
+uint32_t* cur_offs(const mb_world* w) { return frame_offs(w, w->cur ^ 1); }
 // The physics pass reads the state through the permutation instead of a sorted copy.
 bool indirect(const mb_world* w) { return w->tuning.state_gather == MB_GATHER_INDIRECT; }
 // LOOP frames run as one cooperative kernel per step (profiling needs the
@@ -202,20 +210,22 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
     if ((e = mark(w, 0, st, capturing))) return e;
     if (counting(w) && init) {
         // frame 0 after an upload sorts all-zero keys: identity order, one full cell
-        if ((e = mb::count_init_order(w->cnt, w->n, w->cells, w->scratch.offs, w->perm, st))) return e;
+        if ((e = mb::count_init_order(w->cnt, w->n, w->cells, frame_offs(w, cur), w->perm, st))) return e;
         if ((e = mark(w, 1, st, capturing))) return e;
         hist = w->cnt.hist;
         coarse = w->cnt.coarse;
     } else if (rank(w)) {
-        // cell offsets (keeping the previous frame's), then the order by rank in
-        // the old neighbourhoods; this frame's physics pass lists its far moves
-        // in cnt.far[cur ^ 1] for the next frame
-        if ((e = mb::count_scan_keep(w->cnt, w->cells, w->scratch.offs, w->cnt.far[cur ^ 1], st, pdl && chained)))
+        // cell offsets (into the buffer of this parity: the other holds the
+        // previous frame's), then the order by rank in the old neighbourhoods;
+        // this frame's physics pass lists its far moves in cnt.far[cur ^ 1]
+        if ((e = mb::count_scan(w->cnt, w->scratch.ctl, w->cells, frame_offs(w, cur), st, pdl && chained,
+                                w->cnt.far[cur ^ 1])))
             return e;
         if ((e = mark(w, 1, st, capturing))) return e;
-        if ((e = mb::count_rank(w->cnt, w->keys, w->n, w->cells, w->scratch.offs, w->cnt.far[cur], w->perm,
-                                w->pos[cur], w->vfme[cur], indirect(w) ? nullptr : w->spos,
-                                indirect(w) ? nullptr : w->svfme, w->bands, w->P.N, st, pdl)))
+        if ((e = mb::count_rank(w->cnt, w->keys, w->n, w->cells, frame_offs(w, cur), frame_offs(w, cur ^ 1),
+                                w->cnt.far[cur], w->perm, w->pos[cur], w->vfme[cur], indirect(w) ? nullptr : w->spos,
+                                indirect(w) ? nullptr : w->svfme, w->bands, w->P.N, st, pdl,
+                                w->tuning.scatter_agents)))
             return e;
         hist = w->cnt.hist;
         coarse = w->cnt.coarse;
@@ -245,12 +255,12 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
                                     w->vfme[nxt], w->keys, hist, coarse, st);
         if (!e && hist) e = mb::count_tile_counts(w->cnt, w->cells, st);
     } else if (indirect(w)) {
-        e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->pos[cur], w->vfme[cur], w->perm,
+        e = mb::launch_physics_loop(w->P, w->n, frame_offs(w, cur), w->bands, w->pos[cur], w->vfme[cur], w->perm,
                                     w->pos[nxt], w->vfme[nxt], w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError,
                                     st, pdl && counting(w), w->tuning.collide_block,
                                     rank(w) ? w->cnt.far[nxt] : nullptr);
     } else {
-        e = mb::launch_physics_loop(w->P, w->n, w->scratch.offs, w->bands, w->spos, w->svfme, nullptr, w->pos[nxt],
+        e = mb::launch_physics_loop(w->P, w->n, frame_offs(w, cur), w->bands, w->spos, w->svfme, nullptr, w->pos[nxt],
                                     w->vfme[nxt], w->keys, hist, coarse, w->scratch.ctl + mb::kCtlError, st,
                                     pdl && counting(w), w->tuning.collide_block,
                                     rank(w) ? w->cnt.far[nxt] : nullptr);
@@ -580,11 +590,11 @@ mb_status mb_get_debug(mb_world* w, uint32_t* keys, uint32_t* perm, uint32_t* st
         return cuda_fail(w, "mb_get_debug", e);
     if (start || close) {
         if (where == MB_DEVICE) {
-            if ((e = mb::offsets_to_start_close(w->scratch.offs, w->cells, start, close, w->stream)))
+            if ((e = mb::offsets_to_start_close(cur_offs(w), w->cells, start, close, w->stream)))
                 return cuda_fail(w, "mb_get_debug", e);
         } else {
             std::vector<uint32_t> offs((size_t)w->cells + 1u);
-            if ((e = cudaMemcpyAsync(offs.data(), w->scratch.offs, sizeof(uint32_t) * offs.size(),
+            if ((e = cudaMemcpyAsync(offs.data(), cur_offs(w), sizeof(uint32_t) * offs.size(),
                                      cudaMemcpyDeviceToHost, w->stream)))
                 return cuda_fail(w, "mb_get_debug", e);
             if ((e = cudaStreamSynchronize(w->stream))) return cuda_fail(w, "mb_get_debug", e);
@@ -640,8 +650,14 @@ mb_status mb_set_tuning(mb_world* w, const mb_tuning* t) {
         return fail(w, MB_ERR_INVALID_ARG, "the fused frame kernel cannot be resident on this device");
     drop_graphs(w);
     bool to_counting = t->sort_algorithm != MB_SORT_ONESWEEP && !counting(w);
+    uint32_t* offs_before = cur_offs(w);
     w->tuning = *t;
     w->rank_ready = false;
+    if (cur_offs(w) != offs_before) {  // the current cell ranges move to this sort's buffer
+        cudaError_t e = cudaMemcpyAsync(cur_offs(w), offs_before, sizeof(uint32_t) * ((size_t)w->cells + 1u),
+                                        cudaMemcpyDeviceToDevice, w->stream);
+        if (e) return cuda_fail(w, "mb_set_tuning", e);
+    }
     w->sched = mb::make_schedule(w->n, w->cells, w->tuning.digit_bits_max);
     if (to_counting && w->has_state) {  // counts were not kept while the radix sort ran
         cudaError_t e = recount(w);
@@ -794,7 +810,7 @@ mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* fram
         if ((r = cp(vfme, w->vfme[cur0], sizeof(uint4) * n))) return r;
         if ((r = cp(keys, w->keys, sizeof(uint32_t) * n))) return r;
         if ((r = cp(perm, w->perm, sizeof(uint32_t) * n))) return r;
-        return cp(offs, w->scratch.offs, sizeof(uint32_t) * (C + 1u));
+        return cp(offs, cur_offs(w), sizeof(uint32_t) * (C + 1u));
     };
     if ((e = cudaMalloc(&pos, sizeof(float4) * std::max<size_t>(n, 1))) ||
         (e = cudaMalloc(&vfme, sizeof(uint4) * std::max<size_t>(n, 1))) ||
@@ -809,9 +825,9 @@ mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* fram
     uint32_t best_i = 0;
     mb_status st = MB_OK;
     for (uint32_t c = 0; c < MB_TUNE_CANDIDATES && st == MB_OK; ++c) {
-        if ((e = snap(false))) break;  // every candidate starts from the saved frame
-        w->cur = cur0;
+        w->cur = cur0;  // before the restore: it writes the offsets buffer of this parity
         w->time = time0;
+        if ((e = snap(false))) break;  // every candidate starts from the saved frame
         if ((st = mb_set_tuning(w, &cand[c])) != MB_OK) break;
         if ((e = recount(w))) break;  // counts of the restored keys
         if ((st = mb_step(w, 1)) != MB_OK) break;  // warm-up: graphs built, caches touched
@@ -829,9 +845,9 @@ mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* fram
         }
     }
     // restore the saved frame under the winning tuning
-    cudaError_t e2 = snap(false);
     w->cur = cur0;
     w->time = time0;
+    cudaError_t e2 = snap(false);
     mb_status st2 = mb_set_tuning(w, (e || st != MB_OK) ? &start : &cand[best_i]);
     if (!e2) e2 = recount(w);
     if (!e2) e2 = cudaStreamSynchronize(w->stream);

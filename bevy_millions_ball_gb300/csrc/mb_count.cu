@@ -38,36 +38,37 @@
 namespace mb {
 namespace {
 
-// keep (nullable): the replaced offsets are copied there (rank placement);
-// far_reset (nullable): a far-move list emptied for this frame's physics pass.
+// far_reset (nullable): a far-move list emptied for this frame's physics pass
+// (rank placement).
 template <bool kScenes>
 __global__ void __launch_bounds__(kScanThreads)
     k_cell_scan(const uint32_t* __restrict__ hist, const uint32_t* __restrict__ coarse, uint32_t cells,
                 uint32_t* __restrict__ offs, uint32_t* fix_ctl,
                 const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ cell_tile_scene,
-                uint32_t* __restrict__ keep, uint32_t* __restrict__ far_reset) {
+                uint32_t* __restrict__ far_reset) {
     __shared__ uint32_t s_warp[kScanThreads / 32], s_base[kScanThreads / 32];
     griddep_wait();  // after the previous frame's physics pass, when chained to it
     griddep_launch();
     if (far_reset && blockIdx.x == 0 && threadIdx.x == 0) *far_reset = 0u;
-    scan_chunk<kScenes>(blockIdx.x, hist, coarse, cells, offs, fix_ctl, scenes, cell_tile_scene, s_warp, s_base,
-                        keep);
+    scan_chunk<kScenes>(blockIdx.x, hist, coarse, cells, offs, fix_ctl, scenes, cell_tile_scene, s_warp, s_base);
 }
 
-// Rank placement of one world's spheres (MB_SORT_RANK), one sphere per thread
-// per step.  The input is the previous frame's sorted order, described by
-// offs_old; a sphere of new cell k = (kx, kz) that moved at most one cell sits
-// in the old ranges of cells (kx-1..kx+1, kz-1..kz+1), three slot ranges, one
-// per row.  Its stable slot is offs[k] plus the spheres with key k before it in
-// those ranges, plus the listed far moves with key k before it (a per-block
-// bit filter of their cells spares the others the list).  No atomics, no
-// marks: the order is final, so the band table is written here too.  The first
-// sphere of each cell clears its count for the next frame.  A far list that
-// overflowed (more than kFarCap moves, or forced after an upload or a grid
-// change) sends every block down the claim-and-fixup path instead (the fixup
-// kernel after this one then runs too).
+// Rank placement of one world's spheres (MB_SORT_RANK), kPer spheres per
+// thread (256 kPer per block, their loads issued together).  The input is the
+// previous frame's sorted order, described by offs_old; a sphere of new cell
+// k = (kx, kz) that moved at most one cell sits in the old ranges of cells
+// (kx-1..kx+1, kz-1..kz+1), three slot ranges, one per row.  Its stable slot is
+// offs[k] plus the spheres with key k before it in those ranges, plus the
+// listed far moves with key k before it (a per-block bit filter of their cells
+// spares the others the list).  No atomics, no marks: the order is final, so
+// the band table is written here too.  The first sphere of each cell clears
+// its count for the next frame.  A far list that overflowed (more than kFarCap
+// moves, or forced after an upload, a grid or a tuning change) sends every
+// block down the claim-and-fixup path instead (the fixup kernel after this one
+// then runs too).
 __device__ __forceinline__ uint32_t bloom_bit(uint32_t k) { return (k * 2654435761u) >> 20; }  // 12 bits
 
+template <uint32_t kPer>
 __global__ void __launch_bounds__(256)
     k_cell_rank(const uint32_t* __restrict__ keys, uint32_t n, uint32_t cells, uint32_t* __restrict__ hist,
                 uint32_t* __restrict__ perm, const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in,
@@ -96,52 +97,63 @@ __global__ void __launch_bounds__(256)
         }
         __syncthreads();
     }
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + tid; i < n; i += stride) {
-        const uint32_t k = __ldg(keys + i);
-        if (k >= cells) continue;  // keys the physics pass cannot emit
-        float4 p;
-        uint4 q;
-        if (spos) {
-            p = __ldg(pos_in + i);
-            q = __ldg(vfme_in + i);
+    const uint32_t i0 = blockIdx.x * blockDim.x * kPer + tid;
+    uint32_t k[kPer], lo[kPer][3], hi[kPer][3], base[kPer];
+    float4 p[kPer];
+    uint4 q[kPer];
+#pragma unroll
+    for (uint32_t r = 0; r < kPer; ++r) {
+        const uint32_t i = i0 + r * blockDim.x;
+        k[r] = i < n ? __ldg(keys + i) : cells;
+        if (spos && i < n) {
+            p[r] = __ldg(pos_in + i);
+            q[r] = __ldg(vfme_in + i);
         }
-        const uint32_t base = __ldg(offs + k);
-        const uint32_t kz = k / N, kx = k - kz * N;
+    }
+#pragma unroll
+    for (uint32_t r = 0; r < kPer; ++r) {
+        const uint32_t i = i0 + r * blockDim.x;
+        const bool ok = k[r] < cells;  // keys the physics pass cannot emit are skipped
+        const uint32_t kz = ok ? k[r] / N : 0u, kx = ok ? k[r] - kz * N : 0u;
         const uint32_t c0 = kx > 0u ? kx - 1u : 0u, c1 = (kx + 1u < N ? kx + 1u : kx) + 1u;
-        uint32_t lo[3], hi[3];
+        base[r] = ok ? __ldg(offs + k[r]) : 0u;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const bool row = d == 0 ? kz > 0u : (d == 2 ? kz + 1u < N : true);
-            const uint32_t r = kz + (uint32_t)d - 1u;
-            lo[d] = row ? __ldg(offs_old + r * N + c0) : 0u;
-            hi[d] = row ? min(__ldg(offs_old + r * N + c1), i) : 0u;
+            const bool row = ok && (d == 0 ? kz > 0u : (d == 2 ? kz + 1u < N : true));
+            const uint32_t rw = kz + (uint32_t)d - 1u;
+            lo[r][d] = row ? __ldg(offs_old + rw * N + c0) : 0u;
+            hi[r][d] = row ? min(__ldg(offs_old + rw * N + c1), i) : 0u;
         }
+    }
+#pragma unroll
+    for (uint32_t r = 0; r < kPer; ++r) {
+        const uint32_t i = i0 + r * blockDim.x;
+        if (k[r] >= cells) continue;
         uint32_t cnt = 0;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            for (uint32_t j = lo[d]; j < hi[d]; j += 4u) {
+            for (uint32_t j = lo[r][d]; j < hi[r][d]; j += 4u) {
                 uint32_t kk[4];
 #pragma unroll
-                for (uint32_t u = 0; u < 4u; ++u) kk[u] = __ldg(keys + min(j + u, hi[d] - 1u));
+                for (uint32_t u = 0; u < 4u; ++u) kk[u] = __ldg(keys + min(j + u, hi[r][d] - 1u));
 #pragma unroll
-                for (uint32_t u = 0; u < 4u; ++u) cnt += (j + u < hi[d] && kk[u] == k) ? 1u : 0u;
+                for (uint32_t u = 0; u < 4u; ++u) cnt += (j + u < hi[r][d] && kk[u] == k[r]) ? 1u : 0u;
             }
         }
         if (F) {
-            const uint32_t b = bloom_bit(k);
+            const uint32_t b = bloom_bit(k[r]);
             if (s_bloom[b >> 5] & (1u << (b & 31u)))
-                for (uint32_t t = 0; t < F; ++t) cnt += (s_key[t] == k && s_slot[t] < i) ? 1u : 0u;
+                for (uint32_t t = 0; t < F; ++t) cnt += (s_key[t] == k[r] && s_slot[t] < i) ? 1u : 0u;
         }
-        if (cnt == 0u) hist[k] = 0u;  // the cell's first sphere
-        const uint32_t dst = base + cnt;
+        if (cnt == 0u) hist[k[r]] = 0u;  // the cell's first sphere
+        const uint32_t dst = base[r] + cnt;
         if (dst < n) {
             perm[dst] = i;
             if (spos) {
-                spos[dst] = p;
-                svfme[dst] = q;
+                spos[dst] = p[r];
+                svfme[dst] = q[r];
             }
-            if (bands) write_band_bounds(bands, offs, N, n, dst, k);
+            if (bands) write_band_bounds(bands, offs, N, n, dst, k[r]);
         }
     }
 }
@@ -399,30 +411,25 @@ cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, c
     return cudaGetLastError();
 }
 
-cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st, bool pdl) {
+cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st, bool pdl,
+                       uint32_t* far_reset) {
     (void)ctl;
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
     return launch_pdl(pdl, k_cell_scan<false>, dim3(chunks), dim3(kScanThreads), 0, st, (const uint32_t*)s.hist,
                       (const uint32_t*)s.coarse, cells, offs, s.fix_ctl, (const SceneDev*)nullptr,
-                      (const uint32_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr);
-}
-
-cudaError_t count_scan_keep(CountScratch& s, uint32_t cells, uint32_t* offs, uint32_t* far_reset, cudaStream_t st,
-                            bool pdl) {
-    const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
-    return launch_pdl(pdl, k_cell_scan<false>, dim3(chunks), dim3(kScanThreads), 0, st, (const uint32_t*)s.hist,
-                      (const uint32_t*)s.coarse, cells, offs, s.fix_ctl, (const SceneDev*)nullptr,
-                      (const uint32_t*)nullptr, s.offs_old, far_reset);
+                      (const uint32_t*)nullptr, far_reset);
 }
 
 cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells, const uint32_t* offs,
-                       const uint32_t* far, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
-                       float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st, bool pdl) {
+                       const uint32_t* offs_old, const uint32_t* far, uint32_t* perm, const float4* pos_in,
+                       const uint4* vfme_in, float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,
+                       bool pdl, uint32_t per_thread) {
     cudaError_t e;
     if (n) {
-        const uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, (uint32_t)device_sm_count() * 8u);
-        if ((e = launch_pdl(pdl, k_cell_rank, dim3(blocks), dim3(256), 0, st, keys, n, cells, s.hist, perm, pos_in,
-                            vfme_in, spos, svfme, offs, (const uint32_t*)s.offs_old, far, bands, N, s.fix_bits)))
+        const uint32_t per = per_thread == 4u ? 4u : (per_thread == 2u ? 2u : 1u);
+        auto* kern = per == 4u ? k_cell_rank<4> : (per == 2u ? k_cell_rank<2> : k_cell_rank<1>);
+        if ((e = launch_pdl(pdl, kern, dim3((n + 256u * per - 1u) / (256u * per)), dim3(256), 0, st, keys, n, cells,
+                            s.hist, perm, pos_in, vfme_in, spos, svfme, offs, offs_old, far, bands, N, s.fix_bits)))
             return e;
     }
     const OneBuffer src{pos_in, vfme_in};
@@ -456,7 +463,7 @@ cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uin
                               uint32_t cells, uint32_t* offs, cudaStream_t st) {
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
     k_cell_scan<true><<<chunks, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.fix_ctl, scenes,
-                                                      cell_tile_scene, nullptr, nullptr);
+                                                      cell_tile_scene, nullptr);
     return cudaGetLastError();
 }
 

@@ -22,16 +22,14 @@ namespace {
 // belongs to one scene; its base is that scene's first slot plus the coarse
 // counts of the scene's earlier tiles, and tiles of HOLD scenes are left alone.
 // One chunk (kScanThreads threads); s_warp, s_base: kScanThreads / 32 words each.
-// A block that runs several chunks must synchronise between them.  keep
-// (nullable, worlds only): the offsets being replaced are copied there first
-// (the previous frame's order, which rank placement reads).
+// A block that runs several chunks must synchronise between them.
 template <bool kScenes, bool kCg = false>
 __device__ __forceinline__ void scan_chunk(uint32_t chunk, const uint32_t* __restrict__ hist,
                                            const uint32_t* __restrict__ coarse, uint32_t cells,
                                            uint32_t* __restrict__ offs, uint32_t* fix_ctl,
                                            const SceneDev* __restrict__ scenes,
                                            const uint32_t* __restrict__ cell_tile_scene, uint32_t* s_warp,
-                                           uint32_t* s_base, uint32_t* __restrict__ keep = nullptr) {
+                                           uint32_t* s_base) {
     constexpr int W = kScanThreads / 32;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t c0 = chunk * kScanChunk, tile = c0 / kScanTile;
@@ -91,14 +89,6 @@ __device__ __forceinline__ void scan_chunk(uint32_t chunk, const uint32_t* __res
     }
     if (base + kScanItems <= cells) {
         uint4* o4 = reinterpret_cast<uint4*>(offs + base);
-        if (keep) {
-            uint4 old[kScanItems / 4];
-#pragma unroll
-            for (int q = 0; q < kScanItems / 4; ++q) old[q] = o4[q];
-#pragma unroll
-            for (int q = 0; q < kScanItems / 4; ++q) reinterpret_cast<uint4*>(keep + base)[q] = old[q];
-            if (base + kScanItems == cells) keep[cells] = offs[cells];
-        }
 #pragma unroll
         for (int q = 0; q < kScanItems / 4; ++q) {
             uint4 x;
@@ -114,10 +104,6 @@ __device__ __forceinline__ void scan_chunk(uint32_t chunk, const uint32_t* __res
         for (int q = 0; q < kScanItems; ++q) {
             uint32_t c = base + q;
             if (c < cells) {
-                if (keep) {
-                    keep[c] = offs[c];
-                    if (c + 1u == cells) keep[cells] = offs[cells];
-                }
                 offs[c] = run;
                 run += v[q];
                 if (c + 1u == cells) offs[cells] = run;

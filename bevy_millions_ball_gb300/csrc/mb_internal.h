@@ -320,7 +320,7 @@ struct CountScratch {
     uint32_t fix_cap[kFixLists] = {0u, 0u, 0u};                // their capacities
     uint32_t* fix_tmp = nullptr;  // [max_keys] copy of a large cell's input indices
     uint32_t* fix_bits = nullptr; // [max_keys / 32 + 1] input slots whose run listed its cell
-    uint32_t* offs_old = nullptr; // [max_cells + 1] the previous frame's cell offsets (rank placement)
+    uint32_t* offs_old = nullptr; // [max_cells + 1] second cell-offset buffer (rank placement alternates)
     uint32_t* far[2] = {nullptr, nullptr};  // [kFarWords] far-move lists, one per state parity
     uint32_t tiles = 0;
 };
@@ -337,8 +337,9 @@ cudaError_t count_keys(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
 cudaError_t count_reset_zero_keys(CountScratch& s, uint32_t n, uint32_t cells, cudaStream_t st);
 // offs[0..cells] := exclusive scan of hist (offs[cells] = n); the scatter of
 // count_scatter then counts hist back down to zero.
+// far_reset (nullable): a far-move list emptied for this frame's physics pass.
 cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t* offs, cudaStream_t st,
-                       bool pdl = false);
+                       bool pdl = false, uint32_t* far_reset = nullptr);
 // coarse[t] := sum of hist over scan tile t (after a pass that emitted cell counts
 // only: INIT frames, re-keying); the batched form touches only INIT scenes' tiles.
 cudaError_t count_tile_counts(CountScratch& s, uint32_t cells, cudaStream_t st);
@@ -356,20 +357,19 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
                           float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,
                           bool pdl = false, uint32_t per_thread = 1);
-// Rank placement (MB_SORT_RANK).  count_scan_keep: count_scan that first copies
-// the offsets it replaces to s.offs_old and empties the far list far_reset
-// (the one this frame's physics pass fills).  count_rank: perm, the sorted copy
-// and the band table from the ranks (offs: this frame's offsets, s.offs_old the
-// previous frame's, far: the far moves of the previous physics pass); when far
-// holds more than kFarCap moves it claims slots and fixes cells as
-// count_scatter does.  hist := 0, coarse := 0 either way.
-// Allocates offs_old and the far lists (worlds that may run MB_SORT_RANK).
-cudaError_t count_rank_alloc(CountScratch& s);
-cudaError_t count_scan_keep(CountScratch& s, uint32_t cells, uint32_t* offs, uint32_t* far_reset, cudaStream_t st,
-                            bool pdl = false);
+// Rank placement (MB_SORT_RANK).  count_rank: perm, the sorted copy and the
+// band table from the ranks (offs: this frame's offsets, offs_old: the previous
+// frame's, which describe this frame's input order; far: the far moves of the
+// previous physics pass); when far holds more than kFarCap moves it claims slots
+// and fixes cells as count_scatter does.  hist := 0, coarse := 0 either way.
+// per_thread: spheres each thread places (1, 2 or 4).
 cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells, const uint32_t* offs,
-                       const uint32_t* far, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
-                       float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st, bool pdl = false);
+                       const uint32_t* offs_old, const uint32_t* far, uint32_t* perm, const float4* pos_in,
+                       const uint4* vfme_in, float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,
+                       bool pdl = false, uint32_t per_thread = 1);
+// Allocates offs_old (the second cell-offset buffer that rank placement
+// alternates with the world's own) and the far lists.
+cudaError_t count_rank_alloc(CountScratch& s);
 // Batched count scan: scene cell ranges are padded to whole scan tiles
 // (cell_tile_scene[t] = scene of tile t); tiles of HOLD scenes are skipped.
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,

@@ -111,9 +111,11 @@ def test_rank_far_list_overflows_midrun(built_lib, cuda):
 
 
 @pytest.mark.parametrize("tuning", [{"state_gather": 1}, {"collide_block": 64}, {"collide_block": 256},
-                                    {"frames_per_launch": 1}, {"frames_per_launch": 16}])
+                                    {"frames_per_launch": 1}, {"frames_per_launch": 16}, {"scatter_agents": 2},
+                                    {"scatter_agents": 4}])
 def test_rank_with_other_knobs(built_lib, cuda, tuning):
-    """The gather through the permutation, the other physics tiles and chain lengths."""
+    """The gather through the permutation, the other physics tiles and chain
+    lengths, two and four spheres placed per thread."""
     run_pair(fast_scene(100, 1.6, seed=8), 40, [1, 2, 3, 11, 40], tuning={**RANK, **tuning})
 
 
@@ -124,8 +126,10 @@ def test_rank_switches_and_settings(built_lib, cuda):
         ow = oracle.OracleWorld(sc.plugin.to_c())
         w.set_state(sc.pos_scale, sc.vfme)
         ow.set_state(sc.pos_scale, sc.vfme)
-        for alg, k in [(2, 5), (0, 3), (2, 4), (1, 3), (2, 6)]:
+        for alg, k in [(2, 5), (0, 3), (2, 4), (1, 3), (2, 6), (0, 2)]:
             w.set_tuning(sort_algorithm=alg)
+            if ow.time:
+                compare(w, ow, ow.time)  # the cell ranges follow the sort into its offsets buffer
             w.step(k)
             ow.step(k)
             compare(w, ow, ow.time)
