@@ -146,7 +146,7 @@ def test_rank_switches_and_settings(built_lib, cuda):
         ow.step(7)
         compare(w, ow, 7)
         with pytest.raises(MbError):
-            w.set_tuning(frame_kernel=_abi.MB_FRAME_FUSED)  # the fused kernel runs the claim-and-fixup sort
+            w.set_tuning(sort_algorithm=2, frame_kernel=_abi.MB_FRAME_FUSED)  # fused frames claim and fix
 
 
 def test_rank_full_size_late_frames(built_lib, cuda):
