@@ -63,7 +63,8 @@ struct mb_world {
     uint32_t* sorted_keys = nullptr;
     uint4* bands = nullptr;            // band table of the sorted order (written by the sort)
     uint32_t* perm = nullptr;
-    uint32_t* fused_bar = nullptr;     // grid barrier words of the fused frame kernel (2, zero between launches)
+    uint32_t* fused_bar = nullptr;     // grid barrier words of the fused frame kernel and of rank placement's
+                                       // fallback (2, zero between launches)
     mb::SortScratch scratch;      // onesweep sort scratch + the cell offsets (offs)
     mb::CountScratch cnt;         // counting-sort scratch (per-cell and per-tile counts, fixup lists)
     mb::SortSchedule sched;
@@ -224,8 +225,8 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         if ((e = mark(w, 1, st, capturing))) return e;
         if ((e = mb::count_rank(w->cnt, w->keys, w->n, w->cells, frame_offs(w, cur), frame_offs(w, cur ^ 1),
                                 w->cnt.far[cur], w->perm, w->pos[cur], w->vfme[cur], indirect(w) ? nullptr : w->spos,
-                                indirect(w) ? nullptr : w->svfme, w->bands, w->P.N, st, pdl,
-                                w->tuning.scatter_agents)))
+                                indirect(w) ? nullptr : w->svfme, w->bands, w->P.N, w->fused_bar,
+                                w->scratch.ctl + mb::kCtlError, st, pdl, w->tuning.scatter_agents)))
             return e;
         hist = w->cnt.hist;
         coarse = w->cnt.coarse;
@@ -571,7 +572,8 @@ mb_status mb_sync(mb_world* w) {
         char msg[192];
         std::snprintf(msg, sizeof msg,
                       "a bounded device-side wait gave up (flags 0x%x: 1 sort look-back, 4 band copy, 8 grid "
-                      "barrier of the fused frame); results since the last sync are invalid",
+                      "barrier of the fused frame or of rank placement's fallback); results since the last sync "
+                      "are invalid",
                       flag);
         return fail(w, MB_ERR_TIMEOUT, msg);
     }
