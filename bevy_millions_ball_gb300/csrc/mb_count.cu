@@ -481,6 +481,26 @@ cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
                       s.fix_tmp, nvb, std::max(collect_grid(n), 1u), bar, err);
 }
 
+cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
+                          const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
+                          float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st, bool pdl,
+                          uint32_t per_thread) {
+    cudaError_t e;
+    if (n) {
+        const uint32_t per = per_thread == 4u ? 4u : (per_thread == 2u ? 2u : 1u);
+        const uint32_t blocks = std::min<uint32_t>((n + 256u * per - 1u) / (256u * per),
+                                                   (uint32_t)device_sm_count() * 8u);
+        auto* kern = per == 4u ? k_cell_scatter<4> : (per == 2u ? k_cell_scatter<2> : k_cell_scatter<1>);
+        if ((e = launch_pdl(pdl, kern, dim3(blocks), dim3(256), 0, st, keys, n, s.hist, perm, pos_in, vfme_in, spos,
+                            svfme, offs, bands, N, s.fix_bits)))
+            return e;
+    }
+    const OneBuffer src{pos_in, vfme_in};
+    return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(std::max(collect_grid(n), 1u)),
+                      dim3(kCollectThreads), 0, st, (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s),
+                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells));
+}
+
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
                               uint32_t cells, uint32_t* offs, cudaStream_t st) {
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
