@@ -982,9 +982,10 @@ mb_status mb_last_frame_times(mb_world* w, float* ms) {
 uint32_t mb_kernels_per_frame(const mb_world* w) {
     if (!w) return 0u;
     if (fused(w)) return 1u;  // one launch per step, whatever its frame count
+    // rank placement: scan + rank (its fallback included) + physics;
     // counting: scan + scatter + marked-cell fixup + physics;
     // onesweep: histogram + one kernel per digit pass + cell offsets + gap fill + gather + physics
-    return counting(w) ? 4u : (uint32_t)w->sched.passes + 5u;
+    return rank(w) ? 3u : (counting(w) ? 4u : (uint32_t)w->sched.passes + 5u);
 }
 
 mb_status mb_selftest_divide(uint64_t seed, uint64_t count, uint64_t* mismatches, uint32_t* first_bad) {

@@ -66,10 +66,11 @@ __global__ void __launch_bounds__(kScanThreads)
 // A far list that overflowed (more than kFarCap moves, or forced after an
 // upload, a grid or a tuning change) sends every block down the claim-and-fixup
 // path: the counting scatter, a grid barrier, then the marked-cell fixup (the
-// last block to finish fixes cells over kFixWarp slots).  The grid is never
-// larger than what the device holds at once, so the barrier can complete (the
-// next kernel, a programmatic dependent, is scheduled only once every block of
-// this one has started); its wait is bounded all the same.
+// last block to finish fixes cells over kFixWarp slots), run by the first nfb
+// blocks, no more than the device holds at once; the others leave at once, so
+// all nfb become resident and the barrier can complete (the next kernel, a
+// programmatic dependent, is scheduled only once every block of this one has
+// started or left).  Its wait is bounded all the same.
 __device__ __forceinline__ uint32_t bloom_bit(uint32_t k) { return (k * 2654435761u) >> 20; }  // 12 bits
 
 struct RankSmem {
@@ -152,9 +153,9 @@ __device__ __forceinline__ void rank_block(uint32_t vb, uint32_t F, const RankSm
     }
 }
 
-// nvb: virtual blocks of 256 kPer spheres; nfix: virtual blocks of the fixup.
-// One sphere per thread keeps eight blocks per SM (the fallback path spills a
-// little instead).
+// Block b places spheres [256 kPer b, 256 kPer (b + 1)); nfix: blocks of the
+// fixup, run by the nfb fallback blocks in turn.  One sphere per thread keeps
+// eight blocks per SM (the fallback path spills a little instead).
 template <uint32_t kPer>
 __global__ void __launch_bounds__(256, kPer == 1u ? 8 : 4)
     k_cell_rank(const uint32_t* __restrict__ keys, uint32_t n, uint32_t cells, uint32_t* __restrict__ hist,
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(256, kPer == 1u ? 8 : 4)
                 const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
                 uint4* __restrict__ svfme, const uint32_t* __restrict__ offs, const uint32_t* __restrict__ offs_old,
                 const uint32_t* __restrict__ far, uint4* __restrict__ bands, uint32_t N,
-                uint32_t* __restrict__ fix_bits, FixLists lists, uint32_t* __restrict__ tmp, uint32_t nvb,
+                uint32_t* __restrict__ fix_bits, FixLists lists, uint32_t* __restrict__ tmp, uint32_t nfb,
                 uint32_t nfix, uint32_t* __restrict__ bar, uint32_t* __restrict__ err) {
     __shared__ RankSmem S;
     griddep_wait();  // the scan's offsets, the previous physics pass's keys and far moves
@@ -172,11 +173,12 @@ __global__ void __launch_bounds__(256, kPer == 1u ? 8 : 4)
         for (uint32_t t = tid; t < tiles; t += blockDim.x) coarse[t] = 0u;
     const uint32_t F = __ldcg(far);
     if (F > kFarCap) {
-        scatter_range<false, 1>(blockIdx.x, gridDim.x, keys, n, hist, perm, pos_in, vfme_in, spos, svfme, offs,
-                                bands, N, fix_bits);
-        if (!grid_barrier(bar, err, &S.flag)) return;
+        if (blockIdx.x >= nfb) return;
+        scatter_range<false, 1>(blockIdx.x, nfb, keys, n, hist, perm, pos_in, vfme_in, spos, svfme, offs, bands, N,
+                                fix_bits);
+        if (!grid_barrier(bar, err, &S.flag, nfb)) return;
         const OneBufferT<true> src{pos_in, vfme_in};
-        for (uint32_t vb = blockIdx.x; vb < nfix; vb += gridDim.x) {
+        for (uint32_t vb = blockIdx.x; vb < nfix; vb += nfb) {
             fix_marked_block<OneBufferT<true>, true, true>(vb, nfix, fix_bits, keys, n, offs, perm, lists, tmp, src,
                                                            spos, svfme, S.u.m);
             __syncthreads();  // shared lists free for the next virtual block
@@ -195,9 +197,8 @@ __global__ void __launch_bounds__(256, kPer == 1u ? 8 : 4)
         }
         __syncthreads();
     }
-    for (uint32_t vb = blockIdx.x; vb < nvb; vb += gridDim.x)
-        rank_block<kPer>(vb, F, S, keys, n, cells, hist, perm, pos_in, vfme_in, spos, svfme, offs, offs_old, bands,
-                         N);
+    rank_block<kPer>(blockIdx.x, F, S, keys, n, cells, hist, perm, pos_in, vfme_in, spos, svfme, offs, offs_old,
+                     bands, N);
 }
 
 template <uint32_t kPer>
@@ -466,7 +467,7 @@ cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
     if (!n) return cudaSuccess;
     const uint32_t per = per_thread == 4u ? 4u : (per_thread == 2u ? 2u : 1u);
     auto* kern = per == 4u ? k_cell_rank<4> : (per == 2u ? k_cell_rank<2> : k_cell_rank<1>);
-    // at most the blocks the device holds at once (the fallback's grid barrier)
+    // the fallback runs on at most the blocks the device holds at once (its grid barrier)
     static int resident[3] = {-1, -1, -1};  // per kernel variant; the same on every device of one architecture
     int& per_sm = resident[per == 4u ? 2 : (per == 2u ? 1 : 0)];
     if (per_sm < 0) {
@@ -474,11 +475,11 @@ cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
         per_sm = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 256, 0) ? 0 : b;
     }
     if (per_sm <= 0) return cudaErrorLaunchOutOfResources;
-    const uint32_t nvb = (n + 256u * per - 1u) / (256u * per);
-    const uint32_t grid = std::min<uint32_t>(nvb, (uint32_t)(per_sm * device_sm_count()));
+    const uint32_t grid = (n + 256u * per - 1u) / (256u * per);
+    const uint32_t nfb = std::min<uint32_t>(grid, (uint32_t)(per_sm * device_sm_count()));
     return launch_pdl(pdl, kern, dim3(grid), dim3(256), 0, st, keys, n, cells, s.hist, s.coarse, scan_tiles(cells),
                       perm, pos_in, vfme_in, spos, svfme, offs, offs_old, far, bands, N, s.fix_bits, fix_lists(s),
-                      s.fix_tmp, nvb, std::max(collect_grid(n), 1u), bar, err);
+                      s.fix_tmp, nfb, std::max(collect_grid(n), 1u), bar, err);
 }
 
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,

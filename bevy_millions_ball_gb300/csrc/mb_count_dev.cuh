@@ -29,13 +29,14 @@ __device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
 // resets the count and advances the generation; the others wait for that.  A
 // wait that runs out (or sees that another block's wait ran out) sets bit 8 of
 // the error word and returns false: the caller then leaves the kernel.
-__device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* err, uint32_t* s_flag) {
+// nblocks: the blocks that take part (0: the whole grid).
+__device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* err, uint32_t* s_flag, uint32_t nblocks = 0) {
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t ok = 1u;
         const uint32_t gen = ld_acquire_gpu(bar + 1);
         __threadfence();  // this block's writes before its arrival
-        if (atomicAdd(bar, 1u) == gridDim.x - 1u) {
+        if (atomicAdd(bar, 1u) == (nblocks ? nblocks : gridDim.x) - 1u) {
             __threadfence();  // every other block's writes (their arrivals are read above)
             atomicExch(bar, 0u);
             st_release_gpu(bar + 1, gen + 1u);
