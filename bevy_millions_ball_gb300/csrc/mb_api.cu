@@ -63,8 +63,7 @@ struct mb_world {
     uint32_t* sorted_keys = nullptr;
     uint4* bands = nullptr;            // band table of the sorted order (written by the sort)
     uint32_t* perm = nullptr;
-    uint32_t* fused_bar = nullptr;     // grid barrier words of the fused frame kernel and of rank placement's
-                                       // fallback (2, zero between launches)
+    uint32_t* fused_bar = nullptr;     // grid barrier words of the fused frame kernel (2, zero between launches)
     mb::SortScratch scratch;      // onesweep sort scratch + the cell offsets (offs)
     mb::CountScratch cnt;         // counting-sort scratch (per-cell and per-tile counts, fixup lists)
     mb::SortSchedule sched;
@@ -225,8 +224,8 @@ cudaError_t enqueue_frame(mb_world* w, cudaStream_t st, int cur, bool init, bool
         if ((e = mark(w, 1, st, capturing))) return e;
         if ((e = mb::count_rank(w->cnt, w->keys, w->n, w->cells, frame_offs(w, cur), frame_offs(w, cur ^ 1),
                                 w->cnt.far[cur], w->perm, w->pos[cur], w->vfme[cur], indirect(w) ? nullptr : w->spos,
-                                indirect(w) ? nullptr : w->svfme, w->bands, w->P.N, w->fused_bar,
-                                w->scratch.ctl + mb::kCtlError, st, pdl, w->tuning.scatter_agents)))
+                                indirect(w) ? nullptr : w->svfme, w->bands, w->P.N, st, pdl,
+                                w->tuning.scatter_agents)))
             return e;
         hist = w->cnt.hist;
         coarse = w->cnt.coarse;
@@ -362,7 +361,7 @@ mb_status mb_create(const mb_settings* s, void* cuda_stream, mb_world** out) {
     w->n = s->max_number_of_agents;
     w->tuning.digit_bits_max = 8;
     w->tuning.collide_block = 128;
-    w->tuning.sort_algorithm = MB_SORT_COUNTING;
+    w->tuning.sort_algorithm = MB_SORT_RANK;
     apply_settings(w, *s);
     const size_t n = w->n;
     auto alloc_all = [&]() -> cudaError_t {
@@ -572,8 +571,7 @@ mb_status mb_sync(mb_world* w) {
         char msg[192];
         std::snprintf(msg, sizeof msg,
                       "a bounded device-side wait gave up (flags 0x%x: 1 sort look-back, 4 band copy, 8 grid "
-                      "barrier of the fused frame or of rank placement's fallback); results since the last sync "
-                      "are invalid",
+                      "barrier of the fused frame); results since the last sync are invalid",
                       flag);
         return fail(w, MB_ERR_TIMEOUT, msg);
     }
@@ -763,9 +761,11 @@ mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* fram
     {
         // {sort, digit bits, frames per graph launch, state gather, frame kernel, physics tile,
         //  scatter spheres per thread}
-        const uint32_t C = MB_SORT_COUNTING, O = MB_SORT_ONESWEEP, CP = MB_GATHER_COPY, IN = MB_GATHER_INDIRECT,
-                       G = MB_FRAME_GRAPH, F = MB_FRAME_FUSED;
+        const uint32_t C = MB_SORT_COUNTING, O = MB_SORT_ONESWEEP, R = MB_SORT_RANK, CP = MB_GATHER_COPY,
+                       IN = MB_GATHER_INDIRECT, G = MB_FRAME_GRAPH, F = MB_FRAME_FUSED;
         const uint32_t c6[MB_TUNE_CANDIDATES][7] = {
+            {R, 8u, 8u, CP, G, 128u, 1u},  {R, 8u, 16u, CP, G, 128u, 1u}, {R, 8u, 8u, CP, G, 256u, 1u},
+            {R, 8u, 8u, CP, G, 128u, 2u},  {R, 8u, 8u, IN, G, 128u, 1u},
             {C, 8u, 1u, CP, G, 128u, 1u},  {C, 8u, 8u, CP, G, 128u, 1u},  {C, 8u, 16u, CP, G, 128u, 1u},
             {C, 8u, 8u, CP, G, 64u, 1u},   {C, 8u, 8u, CP, G, 256u, 1u},  {C, 8u, 16u, CP, G, 256u, 1u},
             {C, 8u, 8u, CP, G, 128u, 2u},  {C, 8u, 8u, CP, G, 128u, 4u},  {C, 8u, 16u, CP, G, 256u, 2u},
@@ -982,10 +982,10 @@ mb_status mb_last_frame_times(mb_world* w, float* ms) {
 uint32_t mb_kernels_per_frame(const mb_world* w) {
     if (!w) return 0u;
     if (fused(w)) return 1u;  // one launch per step, whatever its frame count
-    // rank placement: scan + rank (its fallback included) + physics;
-    // counting: scan + scatter + marked-cell fixup + physics;
+    // counting and rank placement: scan + scatter or rank + marked-cell fixup (idle unless the rank
+    // placement fell back) + physics;
     // onesweep: histogram + one kernel per digit pass + cell offsets + gap fill + gather + physics
-    return rank(w) ? 3u : (counting(w) ? 4u : (uint32_t)w->sched.passes + 5u);
+    return counting(w) ? 4u : (uint32_t)w->sched.passes + 5u;
 }
 
 mb_status mb_selftest_divide(uint64_t seed, uint64_t count, uint64_t* mismatches, uint32_t* first_bad) {

@@ -53,46 +53,51 @@ __global__ void __launch_bounds__(kScanThreads)
     scan_chunk<kScenes>(blockIdx.x, hist, coarse, cells, offs, fix_ctl, scenes, cell_tile_scene, s_warp, s_base);
 }
 
-// Rank placement of one world's spheres (MB_SORT_RANK), one kernel per frame.
-// The input is the previous frame's sorted order, described by offs_old; a
-// sphere of new cell k = (kx, kz) that moved at most one cell sits in the old
-// ranges of cells (kx-1..kx+1, kz-1..kz+1), three slot ranges, one per row.  Its
-// stable slot is offs[k] plus the spheres with key k before it in those ranges,
-// plus the listed far moves with key k before it (a per-block bit filter of
-// their cells spares the others the list).  No atomics, no marks: the order is
-// final, so the band table is written here too.  The first sphere of each cell
-// clears its count for the next frame; block 0 clears the tile counts.
-//
-// A far list that overflowed (more than kFarCap moves, or forced after an
-// upload, a grid or a tuning change) sends every block down the claim-and-fixup
-// path: the counting scatter, a grid barrier, then the marked-cell fixup (the
-// last block to finish fixes cells over kFixWarp slots), run by the first nfb
-// blocks, no more than the device holds at once; the others leave at once, so
-// all nfb become resident and the barrier can complete (the next kernel, a
-// programmatic dependent, is scheduled only once every block of this one has
-// started or left).  Its wait is bounded all the same.
+// Rank placement of one world's spheres (MB_SORT_RANK), kPer spheres per
+// thread (256 kPer per block, their loads issued together).  The input is the
+// previous frame's sorted order, described by offs_old; a sphere of new cell
+// k = (kx, kz) that moved at most one cell sits in the old ranges of cells
+// (kx-1..kx+1, kz-1..kz+1), three slot ranges, one per row.  Its stable slot is
+// offs[k] plus the spheres with key k before it in those ranges, plus the
+// listed far moves with key k before it (a per-block bit filter of their cells
+// spares the others the list).  No atomics, no marks: the order is final, so
+// the band table is written here too.  The first sphere of each cell clears
+// its count for the next frame.  A far list that overflowed (more than kFarCap
+// moves, or forced after an upload, a grid or a tuning change) sends every
+// block down the claim-and-fixup path instead (the fixup kernel after this one
+// then runs too).
 __device__ __forceinline__ uint32_t bloom_bit(uint32_t k) { return (k * 2654435761u) >> 20; }  // 12 bits
 
-struct RankSmem {
-    union {
-        struct {
-            uint32_t key[kFarCap], slot[kFarCap], bloom[kBloomWords];
-        } r;
-        MarkedSmem m;
-    } u;
-    uint32_t flag;
-};
-
-// kPer spheres per thread, 256 kPer per (virtual) block vb, loads issued together.
 template <uint32_t kPer>
-__device__ __forceinline__ void rank_block(uint32_t vb, uint32_t F, const RankSmem& S,
-                                           const uint32_t* __restrict__ keys, uint32_t n, uint32_t cells,
-                                           uint32_t* __restrict__ hist, uint32_t* __restrict__ perm,
-                                           const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in,
-                                           float4* __restrict__ spos, uint4* __restrict__ svfme,
-                                           const uint32_t* __restrict__ offs, const uint32_t* __restrict__ offs_old,
-                                           uint4* __restrict__ bands, uint32_t N) {
-    const uint32_t i0 = vb * blockDim.x * kPer + threadIdx.x;
+__global__ void __launch_bounds__(256)
+    k_cell_rank(const uint32_t* __restrict__ keys, uint32_t n, uint32_t cells, uint32_t* __restrict__ hist,
+                uint32_t* __restrict__ perm, const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in,
+                float4* __restrict__ spos, uint4* __restrict__ svfme, const uint32_t* __restrict__ offs,
+                const uint32_t* __restrict__ offs_old, const uint32_t* __restrict__ far, uint4* __restrict__ bands,
+                uint32_t N, uint32_t* __restrict__ fix_bits) {
+    __shared__ uint32_t s_key[kFarCap], s_slot[kFarCap], s_bloom[kBloomWords];
+    griddep_wait();  // the scan's offsets, the previous physics pass's keys and far moves
+    griddep_launch();
+    const uint32_t F = __ldcg(far);
+    if (F > kFarCap) {
+        scatter_range<false, 1>(blockIdx.x, gridDim.x, keys, n, hist, perm, pos_in, vfme_in, spos, svfme, offs,
+                                bands, N, fix_bits);
+        return;
+    }
+    const uint32_t tid = threadIdx.x;
+    if (F) {
+        for (uint32_t t = tid; t < kBloomWords; t += blockDim.x) s_bloom[t] = 0u;
+        __syncthreads();
+        for (uint32_t t = tid; t < F; t += blockDim.x) {
+            const uint32_t sl = min(__ldcg(far + 1u + t), n - 1u), k = __ldg(keys + sl);
+            s_slot[t] = sl;
+            s_key[t] = k;
+            const uint32_t b = bloom_bit(k);
+            atomicOr(&s_bloom[b >> 5], 1u << (b & 31u));
+        }
+        __syncthreads();
+    }
+    const uint32_t i0 = blockIdx.x * blockDim.x * kPer + tid;
     uint32_t k[kPer], lo[kPer][3], hi[kPer][3], base[kPer];
     float4 p[kPer];
     uint4 q[kPer];
@@ -137,8 +142,8 @@ __device__ __forceinline__ void rank_block(uint32_t vb, uint32_t F, const RankSm
         }
         if (F) {
             const uint32_t b = bloom_bit(k[r]);
-            if (S.u.r.bloom[b >> 5] & (1u << (b & 31u)))
-                for (uint32_t t = 0; t < F; ++t) cnt += (S.u.r.key[t] == k[r] && S.u.r.slot[t] < i) ? 1u : 0u;
+            if (s_bloom[b >> 5] & (1u << (b & 31u)))
+                for (uint32_t t = 0; t < F; ++t) cnt += (s_key[t] == k[r] && s_slot[t] < i) ? 1u : 0u;
         }
         if (cnt == 0u) hist[k[r]] = 0u;  // the cell's first sphere
         const uint32_t dst = base[r] + cnt;
@@ -151,54 +156,6 @@ __device__ __forceinline__ void rank_block(uint32_t vb, uint32_t F, const RankSm
             if (bands) write_band_bounds(bands, offs, N, n, dst, k[r]);
         }
     }
-}
-
-// Block b places spheres [256 kPer b, 256 kPer (b + 1)); nfix: blocks of the
-// fixup, run by the nfb fallback blocks in turn.  One sphere per thread keeps
-// eight blocks per SM (the fallback path spills a little instead).
-template <uint32_t kPer>
-__global__ void __launch_bounds__(256, kPer == 1u ? 8 : 4)
-    k_cell_rank(const uint32_t* __restrict__ keys, uint32_t n, uint32_t cells, uint32_t* __restrict__ hist,
-                uint32_t* __restrict__ coarse, uint32_t tiles, uint32_t* __restrict__ perm,
-                const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in, float4* __restrict__ spos,
-                uint4* __restrict__ svfme, const uint32_t* __restrict__ offs, const uint32_t* __restrict__ offs_old,
-                const uint32_t* __restrict__ far, uint4* __restrict__ bands, uint32_t N,
-                uint32_t* __restrict__ fix_bits, FixLists lists, uint32_t* __restrict__ tmp, uint32_t nfb,
-                uint32_t nfix, uint32_t* __restrict__ bar, uint32_t* __restrict__ err) {
-    __shared__ RankSmem S;
-    griddep_wait();  // the scan's offsets, the previous physics pass's keys and far moves
-    griddep_launch();
-    const uint32_t tid = threadIdx.x;
-    if (blockIdx.x == 0)  // read by the scan only, which has completed
-        for (uint32_t t = tid; t < tiles; t += blockDim.x) coarse[t] = 0u;
-    const uint32_t F = __ldcg(far);
-    if (F > kFarCap) {
-        if (blockIdx.x >= nfb) return;
-        scatter_range<false, 1>(blockIdx.x, nfb, keys, n, hist, perm, pos_in, vfme_in, spos, svfme, offs, bands, N,
-                                fix_bits);
-        if (!grid_barrier(bar, err, &S.flag, nfb)) return;
-        const OneBufferT<true> src{pos_in, vfme_in};
-        for (uint32_t vb = blockIdx.x; vb < nfix; vb += nfb) {
-            fix_marked_block<OneBufferT<true>, true, true>(vb, nfix, fix_bits, keys, n, offs, perm, lists, tmp, src,
-                                                           spos, svfme, S.u.m);
-            __syncthreads();  // shared lists free for the next virtual block
-        }
-        return;
-    }
-    if (F) {
-        for (uint32_t t = tid; t < kBloomWords; t += blockDim.x) S.u.r.bloom[t] = 0u;
-        __syncthreads();
-        for (uint32_t t = tid; t < F; t += blockDim.x) {
-            const uint32_t sl = min(__ldcg(far + 1u + t), n - 1u), k = __ldg(keys + sl);
-            S.u.r.slot[t] = sl;
-            S.u.r.key[t] = k;
-            const uint32_t b = bloom_bit(k);
-            atomicOr(&S.u.r.bloom[b >> 5], 1u << (b & 31u));
-        }
-        __syncthreads();
-    }
-    rank_block<kPer>(blockIdx.x, F, S, keys, n, cells, hist, perm, pos_in, vfme_in, spos, svfme, offs, offs_old,
-                     bands, N);
 }
 
 template <uint32_t kPer>
@@ -282,16 +239,19 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// gate (nullable): the far list rank placement read; unless it overflowed the
+// order is final and only the counts are cleared.
 template <class Src>
 __global__ void __launch_bounds__(kCollectThreads)
     k_fix_marked(const uint32_t* __restrict__ fix_bits, const uint32_t* __restrict__ keys, uint32_t n,
                  const uint32_t* __restrict__ offs, uint32_t* perm, FixLists lists, uint32_t* __restrict__ tmp,
                  Src src, float4* __restrict__ spos, uint4* __restrict__ svfme, uint32_t* __restrict__ hist,
-                 uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles) {
+                 uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles, const uint32_t* __restrict__ gate) {
     __shared__ MarkedSmem S;
     griddep_wait();  // the scatter's bitmap and order are complete
     griddep_launch();
     clear_counts(blockIdx.x, gridDim.x, src, hist, cells, coarse, tiles);
+    if (gate && __ldcg(gate) <= kFarCap) return;
     fix_marked_block<Src, false, true>(blockIdx.x, gridDim.x, fix_bits, keys, n, offs, perm, lists, tmp, src, spos,
                                        svfme, S);
 }
@@ -462,24 +422,20 @@ cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t*
 
 cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells, const uint32_t* offs,
                        const uint32_t* offs_old, const uint32_t* far, uint32_t* perm, const float4* pos_in,
-                       const uint4* vfme_in, float4* spos, uint4* svfme, uint4* bands, uint32_t N, uint32_t* bar,
-                       uint32_t* err, cudaStream_t st, bool pdl, uint32_t per_thread) {
-    if (!n) return cudaSuccess;
-    const uint32_t per = per_thread == 4u ? 4u : (per_thread == 2u ? 2u : 1u);
-    auto* kern = per == 4u ? k_cell_rank<4> : (per == 2u ? k_cell_rank<2> : k_cell_rank<1>);
-    // the fallback runs on at most the blocks the device holds at once (its grid barrier)
-    static int resident[3] = {-1, -1, -1};  // per kernel variant; the same on every device of one architecture
-    int& per_sm = resident[per == 4u ? 2 : (per == 2u ? 1 : 0)];
-    if (per_sm < 0) {
-        int b = 0;
-        per_sm = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 256, 0) ? 0 : b;
+                       const uint4* vfme_in, float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,
+                       bool pdl, uint32_t per_thread) {
+    cudaError_t e;
+    if (n) {
+        const uint32_t per = per_thread == 4u ? 4u : (per_thread == 2u ? 2u : 1u);
+        auto* kern = per == 4u ? k_cell_rank<4> : (per == 2u ? k_cell_rank<2> : k_cell_rank<1>);
+        if ((e = launch_pdl(pdl, kern, dim3((n + 256u * per - 1u) / (256u * per)), dim3(256), 0, st, keys, n, cells,
+                            s.hist, perm, pos_in, vfme_in, spos, svfme, offs, offs_old, far, bands, N, s.fix_bits)))
+            return e;
     }
-    if (per_sm <= 0) return cudaErrorLaunchOutOfResources;
-    const uint32_t grid = (n + 256u * per - 1u) / (256u * per);
-    const uint32_t nfb = std::min<uint32_t>(grid, (uint32_t)(per_sm * device_sm_count()));
-    return launch_pdl(pdl, kern, dim3(grid), dim3(256), 0, st, keys, n, cells, s.hist, s.coarse, scan_tiles(cells),
-                      perm, pos_in, vfme_in, spos, svfme, offs, offs_old, far, bands, N, s.fix_bits, fix_lists(s),
-                      s.fix_tmp, nfb, std::max(collect_grid(n), 1u), bar, err);
+    const OneBuffer src{pos_in, vfme_in};
+    return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(std::max(collect_grid(n), 1u)),
+                      dim3(kCollectThreads), 0, st, (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s),
+                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells), far);
 }
 
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
@@ -499,7 +455,8 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
     const OneBuffer src{pos_in, vfme_in};
     return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(std::max(collect_grid(n), 1u)),
                       dim3(kCollectThreads), 0, st, (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s),
-                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells));
+                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells),
+                      (const uint32_t*)nullptr);
 }
 
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
@@ -529,7 +486,7 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
     const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
     k_fix_marked<SceneBuffers><<<std::max(collect_grid(n), 1u), kCollectThreads, 0, st>>>(
         s.fix_bits, keys, n, offs, perm, fix_lists(s), s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse,
-        scan_tiles(cells));
+        scan_tiles(cells), nullptr);
     return cudaGetLastError();
 }
 

@@ -10,55 +10,6 @@
 namespace mb {
 namespace {
 
-// ---------------------------------------------------------------- grid barrier
-// For kernels whose blocks are all resident at once (a cooperative launch, or a
-// grid no larger than what the device holds, launched after its predecessor has
-// let it start): every wait is bounded.
-constexpr uint32_t kBarrierLimit = 1u << 24;  // polls of a grid barrier before it gives up (~2 s)
-
-__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// bar[0] counts arrivals, bar[1] is the generation.  The last block to arrive
-// resets the count and advances the generation; the others wait for that.  A
-// wait that runs out (or sees that another block's wait ran out) sets bit 8 of
-// the error word and returns false: the caller then leaves the kernel.
-// nblocks: the blocks that take part (0: the whole grid).
-__device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* err, uint32_t* s_flag, uint32_t nblocks = 0) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t ok = 1u;
-        const uint32_t gen = ld_acquire_gpu(bar + 1);
-        __threadfence();  // this block's writes before its arrival
-        if (atomicAdd(bar, 1u) == (nblocks ? nblocks : gridDim.x) - 1u) {
-            __threadfence();  // every other block's writes (their arrivals are read above)
-            atomicExch(bar, 0u);
-            st_release_gpu(bar + 1, gen + 1u);
-        } else {
-            uint32_t spins = 0;
-            while (ld_acquire_gpu(bar + 1) == gen) {
-                ++spins;
-                if (spins > kBarrierLimit || ((spins & 1023u) == 0u && (ld_acquire_gpu(err) & 8u))) {
-                    atomicOr(err, 8u);
-                    ok = 0u;
-                    break;
-                }
-                if (spins > 32u) __nanosleep(64);
-            }
-        }
-        __threadfence();
-        *s_flag = ok;
-    }
-    __syncthreads();
-    return *s_flag != 0u;
-}
-
 // ---------------------------------------------------------------- scan
 // Block b of the scan covers the chunk of cells [kScanChunk b, kScanChunk (b + 1))
 // inside tile t = b kScanChunk / 4096 (cells [4096 t, 4096 t + 4096)).  coarse[t] holds the number of

@@ -357,18 +357,16 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
                           const uint32_t* offs, uint32_t* perm, const float4* pos_in, const uint4* vfme_in,
                           float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,
                           bool pdl = false, uint32_t per_thread = 1);
-// Rank placement (MB_SORT_RANK), one kernel.  count_rank: perm, the sorted copy
-// and the band table from the ranks (offs: this frame's offsets, offs_old: the
-// previous frame's, which describe this frame's input order; far: the far moves
-// of the previous physics pass); when far holds more than kFarCap moves it
-// claims slots and fixes cells as count_scatter does, in the same kernel (bar:
-// two grid-barrier words, zero between launches; err: the error word, bit 8 set
-// if the barrier's wait gave up).  hist := 0, coarse := 0 either way.
+// Rank placement (MB_SORT_RANK).  count_rank: perm, the sorted copy and the
+// band table from the ranks (offs: this frame's offsets, offs_old: the previous
+// frame's, which describe this frame's input order; far: the far moves of the
+// previous physics pass); when far holds more than kFarCap moves it claims slots
+// and fixes cells as count_scatter does.  hist := 0, coarse := 0 either way.
 // per_thread: spheres each thread places (1, 2 or 4).
 cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells, const uint32_t* offs,
                        const uint32_t* offs_old, const uint32_t* far, uint32_t* perm, const float4* pos_in,
-                       const uint4* vfme_in, float4* spos, uint4* svfme, uint4* bands, uint32_t N, uint32_t* bar,
-                       uint32_t* err, cudaStream_t st, bool pdl = false, uint32_t per_thread = 1);
+                       const uint4* vfme_in, float4* spos, uint4* svfme, uint4* bands, uint32_t N, cudaStream_t st,
+                       bool pdl = false, uint32_t per_thread = 1);
 // Allocates offs_old (the second cell-offset buffer that rank placement
 // alternates with the world's own) and the far lists.
 cudaError_t count_rank_alloc(CountScratch& s);

@@ -826,6 +826,50 @@ __global__ void __launch_bounds__(kTile)
 // device code as the per-stage kernels, reading data written earlier in the
 // launch from L2 (kCg), so the results are identical.
 constexpr uint32_t kFusedThreads = 256;
+constexpr uint32_t kBarrierLimit = 1u << 24;  // polls of a grid barrier before it gives up (~2 s)
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// bar[0] counts arrivals, bar[1] is the generation.  The last block to arrive
+// resets the count and advances the generation; the others wait for that.  A
+// wait that runs out (or sees that another block's wait ran out) sets bit 8 of
+// the error word and returns false: the caller then leaves the kernel.
+__device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* err, uint32_t* s_flag) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t ok = 1u;
+        const uint32_t gen = ld_acquire_gpu(bar + 1);
+        __threadfence();  // this block's writes before its arrival
+        if (atomicAdd(bar, 1u) == gridDim.x - 1u) {
+            __threadfence();  // every other block's writes (their arrivals are read above)
+            atomicExch(bar, 0u);
+            st_release_gpu(bar + 1, gen + 1u);
+        } else {
+            uint32_t spins = 0;
+            while (ld_acquire_gpu(bar + 1) == gen) {
+                ++spins;
+                if (spins > kBarrierLimit || ((spins & 1023u) == 0u && (ld_acquire_gpu(err) & 8u))) {
+                    atomicOr(err, 8u);
+                    ok = 0u;
+                    break;
+                }
+                if (spins > 32u) __nanosleep(64);
+            }
+        }
+        __threadfence();
+        *s_flag = ok;
+    }
+    __syncthreads();
+    return *s_flag != 0u;
+}
+
 struct FusedArgs {
     PhysParams P;
     uint32_t n, cells, chunks, scan_tiles, phys_tiles, collect_blocks, frames, cur;

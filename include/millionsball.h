@@ -262,24 +262,24 @@ typedef struct mb_tuning {
     uint32_t digit_bits_max;   /* widest radix digit of the onesweep sort, 4..11 */
     uint32_t collide_block;    /* sorted slots per thread block of the physics pass: 64, 128
                                   (default) or 256; MB_FRAME_FUSED frames run 128 */
-    uint32_t sort_algorithm;   /* MB_SORT_COUNTING (default), MB_SORT_ONESWEEP or MB_SORT_RANK */
+    uint32_t sort_algorithm;   /* MB_SORT_RANK (default), MB_SORT_COUNTING or MB_SORT_ONESWEEP */
     uint32_t frames_per_launch; /* LOOP frames captured per graph launch in multi-frame steps:
                                    1, 2, 4, 8 (default; 0 reads as 8) or 16 */
     uint32_t state_gather;     /* MB_GATHER_COPY or MB_GATHER_INDIRECT (below) */
     uint32_t frame_kernel;     /* MB_FRAME_GRAPH or MB_FRAME_FUSED (below) */
-    uint32_t scatter_agents;   /* spheres each thread of the counting sort's scatter takes per
-                                  step: 1 (default; 0 reads as 1), 2 or 4; MB_FRAME_FUSED
-                                  frames run 1 */
+    uint32_t scatter_agents;   /* spheres each thread of the counting sort's scatter (or of the
+                                  rank placement) takes: 1 (default; 0 reads as 1), 2 or 4;
+                                  MB_FRAME_FUSED frames run 1 */
     uint32_t reserved;
 } mb_tuning;
 
 /* How LOOP frames are launched:
- *   MB_FRAME_GRAPH: one kernel per stage (count scan, scatter, marked-cell fixup,
- *                   physics), captured in CUDA graphs (default);
+ *   MB_FRAME_GRAPH: one kernel per stage (count scan, rank placement or scatter,
+ *                   marked-cell fixup, physics), captured in CUDA graphs (default);
  *   MB_FRAME_FUSED: every stage of every frame of an mb_step call in one
  *                   cooperative kernel, the stages separated by grid barriers
  *                   (bounded waits: a barrier that gives up is reported by
- *                   mb_sync as MB_ERR_TIMEOUT).  Counting sort only; with
+ *                   mb_sync as MB_ERR_TIMEOUT).  MB_SORT_COUNTING only; with
  *                   profiling on, frames run as MB_FRAME_GRAPH.
  * Both give identical results. */
 #define MB_FRAME_GRAPH 0u
@@ -351,11 +351,11 @@ mb_status mb_render_view(mb_world* w, uint32_t width, uint32_t height, const flo
  * workgroup shapes, NUMBER_OF_THREADS_PER_WORKGROUP = 256 at src/physics/mod.rs:35).
  * Times every candidate tuning on the world's own scene for `frames` LOOP frames
  * each (CUDA events on the world's stream, one warm-up frame per candidate):
- * nineteen combinations of the sort (counting, or onesweep with 6-, 8- or 11-bit
- * digits), frames per graph launch (1, 8, 16), state gather (sorted copy or
- * through the permutation), frame kernel (per-stage graph or fused), physics
- * tile (64, 128 or 256 slots per thread block) and spheres per scatter thread
- * (1, 2, 4).  The world's
+ * twenty-four combinations of the sort (rank placement, counting, or onesweep
+ * with 6-, 8- or 11-bit digits), frames per graph launch (1, 8, 16), state gather
+ * (sorted copy or through the permutation), frame kernel (per-stage graph or
+ * fused), physics tile (64, 128 or 256 slots per thread block) and spheres per
+ * thread of the scatter or the rank placement (1, 2, 4).  The world's
  * state, keys, permutation, cell ranges and time are saved first and restored
  * afterwards, so the simulation continues exactly as if the tuner had not run.
  * The fastest candidate is applied and written to *best; frame_ms (nullable,
@@ -363,7 +363,7 @@ mb_status mb_render_view(mb_world* w, uint32_t width, uint32_t height, const flo
  * order of tried[] (nullable, same length).  Needs a frame to have run since the
  * last upload (MB_ERR_NOT_READY otherwise).  Allocates temporary device memory.
  */
-#define MB_TUNE_CANDIDATES 19u
+#define MB_TUNE_CANDIDATES 24u
 mb_status mb_autotune(mb_world* w, uint32_t frames, mb_tuning* best, float* frame_ms, mb_tuning* tried);
 
 /*

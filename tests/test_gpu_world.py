@@ -289,7 +289,7 @@ def test_scatter_agents(built_lib, cuda, case, agents):
                 w.set_tuning(scatter_agents=bad)
 
 
-FUSED = {"frame_kernel": 1}
+FUSED = {"frame_kernel": 1, "sort_algorithm": 0}  # fused frames run the claim-and-fixup counting sort
 
 
 @pytest.mark.parametrize("gather", [0, 1])
@@ -332,7 +332,7 @@ def test_fused_switches_and_settings(built_lib, cuda):
         w.set_state(sc.pos_scale, sc.vfme)
         ow.set_state(sc.pos_scale, sc.vfme)
         for kernel, k in [(1, 1), (1, 3), (0, 2), (1, 7), (0, 5), (1, 16)]:
-            w.set_tuning(frame_kernel=kernel)
+            w.set_tuning(frame_kernel=kernel, sort_algorithm=0)
             w.step(k)
             ow.step(k)
             w.sync()
