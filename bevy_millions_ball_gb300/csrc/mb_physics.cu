@@ -364,12 +364,42 @@ __device__ __forceinline__ uint32_t cand_slot(uint32_t t, const uint32_t (&o)[3]
 
 constexpr float kNearScale = 1.0014989f;  // about sqrt(1.003): squared, a 0.3% margin on edge^2
 
+// Packed pairs of floats for the look-ahead bound (sm_100+ f32x2 arithmetic:
+// two IEEE single-precision operations, each rounded to nearest, in one
+// instruction).  A candidate's (x, y) and (z, radius) are adjacent in its
+// float4, so they pair without moves.
+__device__ __forceinline__ unsigned long long f2pack(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2unpack(unsigned long long v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2sub(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2mul(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsigned long long b,
+                                                    unsigned long long c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 template <bool kShared, uint32_t kLook, bool kIndirect, bool kCg, int kResp>
 __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, const float4* __restrict__ bpos,
                                              const uint4* __restrict__ bvfme, const uint32_t (&o)[3],
                                              uint32_t c0, uint32_t c01, uint32_t T, uint32_t tself,
                                              const uint32_t* __restrict__ perm, uint32_t nmax) {
     const float sk = a.scale * kNearScale;
+    const unsigned long long zr_k = f2pack(-1.0f, kNearScale);
     uint32_t t = 0;
     while (t < T) {
         const bool r0 = t < c0, r01 = t < c01;
@@ -386,11 +416,17 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
             }
         }
         uint32_t m = 0;
+        // (dx, dy) = own (x, y) - (x, y); (dz, e) = (z, r) * (-1, kNear) + (own z, sk);
+        // d2 = (dx^2 + dy^2) + dz^2 rounded step by step: within a few ulps of the
+        // exact square, far inside the margin
+        const unsigned long long axy = f2pack(a.position.x, a.position.y), azs = f2pack(a.position.z, sk);
 #pragma unroll
         for (uint32_t q = 0; q < kLook; ++q) {
-            const float e = __fmaf_rn(bp[q].w, kNearScale, sk);
-            const float dx = a.position.x - bp[q].x, dy = a.position.y - bp[q].y, dz = a.position.z - bp[q].z;
-            const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+            const unsigned long long dxy = f2sub(axy, f2pack(bp[q].x, bp[q].y));
+            float dz, e, dx2, dy2;
+            f2unpack(f2fma(f2pack(bp[q].z, bp[q].w), zr_k, azs), dz, e);
+            f2unpack(f2mul(dxy, dxy), dx2, dy2);
+            const float d2 = __fmaf_rn(dz, dz, __fadd_rn(dx2, dy2));
             m |= !(__fmaf_rn(-e, e, d2) > 0.0f) ? 1u << q : 0u;
         }
         if (rem < kLook) m &= (1u << rem) - 1u;
