@@ -476,8 +476,10 @@ class Batch:
         return t
 
     def set_tuning(self, frames_per_launch: int | None = None, collide_block: int | None = None,
-                   scatter_agents: int | None = None) -> None:
+                   scatter_agents: int | None = None, sort_algorithm: int | None = None) -> None:
         t = self.tuning
+        if sort_algorithm is not None:
+            t.sort_algorithm = sort_algorithm
         if scatter_agents is not None:
             t.scatter_agents = scatter_agents
         if frames_per_launch is not None:
@@ -493,8 +495,8 @@ class Batch:
         n = _abi.MB_BATCH_TUNE_CANDIDATES
         best, ms, tried = MbTuning(), (C.c_float * n)(), (MbTuning * n)()
         self._check(self._lib.mb_batch_autotune(self._h, frames, C.byref(best), ms, tried))
-        desc = lambda t: {"frames_per_launch": t.frames_per_launch, "collide_block": t.collide_block,
-                          "scatter_agents": max(t.scatter_agents, 1)}
+        desc = lambda t: {"sort_algorithm": t.sort_algorithm, "frames_per_launch": t.frames_per_launch,
+                          "collide_block": t.collide_block, "scatter_agents": max(t.scatter_agents, 1)}
         return {"best": desc(best), "candidates": [dict(desc(t), ms_per_frame=float(m)) for t, m in zip(tried, ms)]}
 
     def close(self) -> None:

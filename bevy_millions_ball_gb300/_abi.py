@@ -67,7 +67,7 @@ MB_SORT_COUNTING, MB_SORT_ONESWEEP, MB_SORT_RANK = 0, 1, 2
 MB_GATHER_COPY, MB_GATHER_INDIRECT = 0, 1
 MB_FRAME_GRAPH, MB_FRAME_FUSED = 0, 1
 MB_TUNE_CANDIDATES = 24
-MB_BATCH_TUNE_CANDIDATES = 11
+MB_BATCH_TUNE_CANDIDATES = 12
 
 
 class MbServerConfig(C.Structure):

@@ -102,6 +102,13 @@ struct mb_batch {
     bool counts_valid = true;             // hist/coarse match keys
     bool layout_dirty = true;             // scene ranges changed: re-upload tiles, re-capture
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    // rank placement (frames in which every scene is in LOOP): [one frame / a chain]
+    // x [offsets buffer the first frame writes]; ob: the buffer (0: offs, 1:
+    // cnt.offs_old) holding the last frame's offsets; rank_ready: cnt.far[ob ^ 1]
+    // lists the far moves of the last frame, which was ranked too
+    cudaGraphExec_t rgraph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    int ob = 0;
+    bool rank_ready = false;
     std::vector<uint32_t> last_modes;
     mb_tuning tuning{};                   // frames_per_launch (chain length) and collide_block are used
     std::string err;
@@ -124,11 +131,18 @@ void drop_graphs(mb_batch* b) {
         if (g) cudaGraphExecDestroy(g);
         g = nullptr;
     }
+    for (auto& set : b->rgraph)
+        for (auto& g : set) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
 }
 
+uint32_t* offs_buf(const mb_batch* b, int i) { return i ? b->cnt.offs_old : b->offs; }
+
 uint64_t bytes_for(uint64_t agents, uint64_t cells, uint64_t scenes) {
-    // state x2, sorted copy, keys, perm; offs; counts, fixup lists; tile and band tables
-    return agents * (32u * 3u + 8u) + cells * 4u + mb::count_scratch_bytes((uint32_t)cells, (uint32_t)agents) +
+    // state x2, sorted copy, keys, perm; offs x2; counts, fixup lists; tile and band tables
+    return agents * (32u * 3u + 8u) + cells * 8u + mb::count_scratch_bytes((uint32_t)cells, (uint32_t)agents) +
            scenes * sizeof(mb::SceneDev) + (agents / kTile + 1u) * (4u + 32u) + 64u * 1024u;
 }
 
@@ -156,7 +170,8 @@ cudaError_t alloc_pool(mb_batch* b) {
     if ((e = cudaMallocHost(&b->h_tile_scene, sizeof(uint32_t) * (A / kTile + 1u)))) return e;
     if ((e = cudaEventCreateWithFlags(&b->table_ev, cudaEventDisableTiming))) return e;
     if ((e = cudaMemset(b->keys, 0, sizeof(uint32_t) * A))) return e;
-    return mb::count_scratch_alloc(b->cnt, (uint32_t)Cc, (uint32_t)A);
+    if ((e = mb::count_scratch_alloc(b->cnt, (uint32_t)Cc, (uint32_t)A))) return e;
+    return mb::count_rank_alloc(b->cnt);
 }
 
 void free_pool(mb_batch* b) {
@@ -277,17 +292,43 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st, bool may_init) {
     return cudaGetLastError();
 }
 
+// A frame in which every scene is in LOOP, sorted by rank placement: writes the
+// offsets buffer q, reads the previous frame's from q ^ 1, ranks the far moves
+// listed in cnt.far[q] and lists this frame's in cnt.far[q ^ 1] (emptied by the scan).
+cudaError_t enqueue_rank_frame(mb_batch* b, cudaStream_t st, int q) {
+    cudaError_t e;
+    if ((e = mb::count_scan_scenes(b->cnt, b->d_scenes, b->d_cell_tile_scene, b->cells_total, offs_buf(b, q), st,
+                                   b->cnt.far[q ^ 1])))
+        return e;
+    if ((e = mb::count_rank_scenes(b->cnt, b->d_scenes, b->d_tile_scene, b->d_cell_tile_scene, b->keys, b->n_total,
+                                   b->cells_total, offs_buf(b, q), offs_buf(b, q ^ 1), b->cnt.far[q], b->perm,
+                                   b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->spos, b->svfme, b->bands, st)))
+        return e;
+    if ((e = mb::launch_physics_batch(b->d_scenes, b->d_tile_scene, b->n_total, offs_buf(b, q), b->bands, b->spos,
+                                      b->svfme, b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->keys, b->cnt.hist,
+                                      b->cnt.coarse, b->ctl + mb::kCtlError, st, b->tuning.collide_block,
+                                      b->cnt.far[q ^ 1])))
+        return e;
+    const uint32_t S = (uint32_t)b->scenes.size();
+    k_flip_parity<<<(S + 127u) / 128u, 128, 0, st>>>(b->d_scenes, S);
+    return cudaGetLastError();
+}
+
 // graph[0]: one frame; graph[1]: chain_frames(b) frames back to back (used while
 // no scene changes mode; 1, 2, 4, 8 (default) or 16).
 uint32_t chain_frames(const mb_batch* b) {
     return b->tuning.frames_per_launch ? b->tuning.frames_per_launch : 8u;
 }
 
-cudaError_t build_graph(mb_batch* b, int which = 0) {
+// rank >= 0: rank-placement frames, the first writing offsets buffer `rank`
+// (into rgraph[which][rank]).
+cudaError_t build_graph(mb_batch* b, int which = 0, int rank = -1) {
     cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e) return e;
     cudaError_t fe = cudaSuccess;
-    for (uint32_t f = 0; f < (which ? chain_frames(b) : 1u) && !fe; ++f) fe = enqueue_frame(b, b->cap_stream, !which);
+    for (uint32_t f = 0; f < (which ? chain_frames(b) : 1u) && !fe; ++f)
+        fe = rank >= 0 ? enqueue_rank_frame(b, b->cap_stream, rank ^ (int)(f & 1u))
+                       : enqueue_frame(b, b->cap_stream, !which);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(b->cap_stream, &g);
     if (fe) {
@@ -295,7 +336,7 @@ cudaError_t build_graph(mb_batch* b, int which = 0) {
         return fe;
     }
     if (e) return e;
-    e = cudaGraphInstantiate(&b->graph[which], g, 0);
+    e = cudaGraphInstantiate(rank >= 0 ? &b->rgraph[which][rank] : &b->graph[which], g, 0);
     cudaGraphDestroy(g);
     return e;
 }
@@ -312,10 +353,30 @@ cudaError_t recount(mb_batch* b) {
 mb_status run_frame(mb_batch* b, const std::vector<uint32_t>& modes, uint32_t frames = 1) {
     cudaError_t e;
     const int which = frames == 1 ? 0 : 1;  // (a chain of one frame is graph 0)
-    if (!b->counts_valid && (e = recount(b))) return bcuda(b, "batch recount", e);
+    if (!b->counts_valid && (e = recount(b))) {
+        b->rank_ready = false;
+        return bcuda(b, "batch recount", e);
+    }
     if ((e = sync_tables(b, modes))) return bcuda(b, "batch tables", e);
-    if (!b->graph[which] && (e = build_graph(b, which))) return bcuda(b, "batch capture", e);
-    if ((e = cudaGraphLaunch(b->graph[which], b->stream))) return bcuda(b, "batch frame", e);
+    const bool all_loop = std::all_of(modes.begin(), modes.end(), [](uint32_t m) { return m == mb::kModeLoop; });
+    if (b->tuning.sort_algorithm == MB_SORT_RANK && all_loop && b->counts_valid) {
+        const int q = b->ob ^ 1;  // offsets buffer of the first frame
+        if (!b->rank_ready) {
+            // no far list describes this input yet: mark it overflowed, so the first
+            // frame claims slots and fixes cells (its physics pass then lists far moves)
+            if ((e = cudaMemsetAsync(b->cnt.far[q], 0xFF, sizeof(uint32_t), b->stream)))
+                return bcuda(b, "batch frame", e);
+            b->rank_ready = true;
+        }
+        if (!b->rgraph[which][q] && (e = build_graph(b, which, q))) return bcuda(b, "batch capture", e);
+        if ((e = cudaGraphLaunch(b->rgraph[which][q], b->stream))) return bcuda(b, "batch frame", e);
+        b->ob = q ^ (int)((frames - 1u) & 1u);
+    } else {
+        if (!b->graph[which] && (e = build_graph(b, which))) return bcuda(b, "batch capture", e);
+        if ((e = cudaGraphLaunch(b->graph[which], b->stream))) return bcuda(b, "batch frame", e);
+        b->ob = 0;
+        b->rank_ready = false;
+    }
     for (size_t i = 0; i < b->scenes.size(); ++i) {
         SceneHost& h = b->scenes[i];
         if (modes[i] != mb::kModeHold) {
@@ -383,6 +444,7 @@ mb_status mb_batch_create(const mb_settings* scenes, uint32_t num_scenes, uint32
     b->tuning.digit_bits_max = 8;
     b->tuning.collide_block = mb::kPhysicsTile;
     b->tuning.frames_per_launch = 8;
+    b->tuning.sort_algorithm = MB_SORT_RANK;
     cudaError_t e = alloc_pool(b);
     if (e) {
         mb_status st = bcuda(nullptr, "mb_batch_create", e);
@@ -504,7 +566,7 @@ mb_status mb_batch_get_debug(mb_batch* b, uint32_t scene, uint32_t* keys, uint32
         ds = start ? tmp + 2u * h.n : nullptr;
         dc = close ? tmp + 2u * h.n + h.cells : nullptr;
     }
-    k_local_debug<<<(m + 255u) / 256u, 256, 0, b->stream>>>(b->keys, b->perm, b->offs, h.n, h.cells,
+    k_local_debug<<<(m + 255u) / 256u, 256, 0, b->stream>>>(b->keys, b->perm, offs_buf(b, b->ob), h.n, h.cells,
                                                              h.agent_base, h.cell_base, dk, dp, ds, dc);
     e = cudaGetLastError();
     if (!e && where == MB_HOST) {
@@ -534,12 +596,13 @@ mb_status mb_batch_set_tuning(mb_batch* b, const mb_tuning* t) {
         return bfail(b, MB_ERR_INVALID_ARG, "collide_block must be 64, 128 or 256");
     if (t->scatter_agents > 4u || t->scatter_agents == 3u)
         return bfail(b, MB_ERR_INVALID_ARG, "scatter_agents must be 0, 1, 2 or 4");
-    if (t->sort_algorithm != MB_SORT_COUNTING || t->state_gather != MB_GATHER_COPY ||
-        t->frame_kernel != MB_FRAME_GRAPH)
+    if ((t->sort_algorithm != MB_SORT_RANK && t->sort_algorithm != MB_SORT_COUNTING) ||
+        t->state_gather != MB_GATHER_COPY || t->frame_kernel != MB_FRAME_GRAPH)
         return bfail(b, MB_ERR_INVALID_ARG,
-                     "a batch runs the counting sort, the sorted copy and per-stage kernels");
+                     "a batch runs rank placement or the counting sort, the sorted copy and per-stage kernels");
     drop_graphs(b);
     b->tuning = *t;
+    b->rank_ready = false;
     return MB_OK;
 }
 
@@ -559,13 +622,15 @@ mb_status mb_batch_autotune(mb_batch* b, uint32_t frames, mb_tuning* best, float
         for (uint32_t f : fpl)
             for (uint32_t t : tiles) {
                 cand[c] = start;
+                cand[c].sort_algorithm = MB_SORT_RANK;
                 cand[c].frames_per_launch = f;
                 cand[c].collide_block = t;
                 cand[c].scatter_agents = 1u;
                 ++c;
             }
-        for (uint32_t a : {2u, 4u}) {  // spheres per scatter thread
+        for (uint32_t a : {1u, 2u, 4u}) {  // the counting sort, spheres per scatter thread
             cand[c] = start;
+            cand[c].sort_algorithm = MB_SORT_COUNTING;
             cand[c].frames_per_launch = 8u;
             cand[c].collide_block = 128u;
             cand[c].scatter_agents = a;
@@ -591,6 +656,7 @@ mb_status mb_batch_autotune(mb_batch* b, uint32_t frames, mb_tuning* best, float
             if (x) cudaEventDestroy(x);
     };
     const std::vector<SceneHost> saved = b->scenes;
+    const int ob0 = b->ob;  // the offsets buffer holding the saved frame's offsets
     auto snap = [&](bool save) -> cudaError_t {
         cudaError_t r;
         auto cp = [&](void* a, void* d, size_t bytes) {
@@ -602,12 +668,14 @@ mb_status mb_batch_autotune(mb_batch* b, uint32_t frames, mb_tuning* best, float
         }
         if ((r = cp(keys, b->keys, sizeof(uint32_t) * A))) return r;
         if ((r = cp(perm, b->perm, sizeof(uint32_t) * A))) return r;
-        return cp(offs, b->offs, sizeof(uint32_t) * Cc);
+        return cp(offs, offs_buf(b, ob0), sizeof(uint32_t) * Cc);
     };
     auto restore_host = [&]() {
         b->scenes = saved;
         b->last_modes.clear();  // the scene table (parities) is uploaded again before the next frame
         b->counts_valid = false;
+        b->ob = ob0;
+        b->rank_ready = false;
     };
     cudaError_t e = cudaSuccess;
     for (int i = 0; i < 2 && !e; ++i) {

@@ -173,19 +173,17 @@ __global__ void __launch_bounds__(256)
 
 // The same for a batch: slot i's scene (from the tile table) gives the buffer
 // holding its state; spheres of HOLD scenes are left alone.  kPer inputs per
-// thread per step, as in scatter_range.
+// thread per step, as in scatter_range; blocks vb of nvb, grid-strided.
 template <uint32_t kPer>
-__global__ void __launch_bounds__(256)
-    k_cell_scatter_scenes(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
-                          const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
-                          uint32_t* __restrict__ perm, const float4* __restrict__ pos0,
-                          const float4* __restrict__ pos1, const uint4* __restrict__ vfme0,
-                          const uint4* __restrict__ vfme1, float4* __restrict__ spos, uint4* __restrict__ svfme,
-                          const uint32_t* __restrict__ offs, uint32_t* __restrict__ fix_bits,
-                          uint4* __restrict__ bands) {
+__device__ __forceinline__ void scatter_scenes_range(
+    uint32_t vb, uint32_t nvb, const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
+    const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist, uint32_t* __restrict__ perm,
+    const float4* __restrict__ pos0, const float4* __restrict__ pos1, const uint4* __restrict__ vfme0,
+    const uint4* __restrict__ vfme1, float4* __restrict__ spos, uint4* __restrict__ svfme,
+    const uint32_t* __restrict__ offs, uint32_t* __restrict__ fix_bits, uint4* __restrict__ bands) {
     const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
-    const uint32_t stride = gridDim.x * blockDim.x * kPer;
-    for (uint32_t i0 = blockIdx.x * blockDim.x * kPer; i0 < n; i0 += stride) {
+    const uint32_t stride = nvb * blockDim.x * kPer;
+    for (uint32_t i0 = vb * blockDim.x * kPer; i0 < n; i0 += stride) {
         uint32_t k[kPer], sc[kPer];
         bool act[kPer];
         float4 p[kPer];
@@ -239,8 +237,101 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// gate (nullable): the far list rank placement read; unless it overflowed the
-// order is final and only the counts are cleared.
+template <uint32_t kPer>
+__global__ void __launch_bounds__(256)
+    k_cell_scatter_scenes(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
+                          const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
+                          uint32_t* __restrict__ perm, const float4* __restrict__ pos0,
+                          const float4* __restrict__ pos1, const uint4* __restrict__ vfme0,
+                          const uint4* __restrict__ vfme1, float4* __restrict__ spos, uint4* __restrict__ svfme,
+                          const uint32_t* __restrict__ offs, uint32_t* __restrict__ fix_bits,
+                          uint4* __restrict__ bands) {
+    scatter_scenes_range<kPer>(blockIdx.x, gridDim.x, scenes, tile_scene, keys, n, hist, perm, pos0, pos1, vfme0,
+                               vfme1, spos, svfme, offs, fix_bits, bands);
+}
+
+// Rank placement of a batch whose scenes are all in LOOP (k_cell_rank per scene:
+// the neighbourhood in the scene's own cell coordinates, its state from its
+// current buffer); one sphere per thread.  The far list holds pool-wide slots,
+// its keys pool-wide cells.  An overflowed list: the batched scatter instead.
+__global__ void __launch_bounds__(256)
+    k_cell_rank_scenes(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
+                       const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
+                       uint32_t* __restrict__ perm, const float4* __restrict__ pos0, const float4* __restrict__ pos1,
+                       const uint4* __restrict__ vfme0, const uint4* __restrict__ vfme1, float4* __restrict__ spos,
+                       uint4* __restrict__ svfme, const uint32_t* __restrict__ offs,
+                       const uint32_t* __restrict__ offs_old, const uint32_t* __restrict__ far,
+                       uint32_t* __restrict__ fix_bits, uint4* __restrict__ bands) {
+    __shared__ uint32_t s_key[kFarCap], s_slot[kFarCap], s_bloom[kBloomWords];
+    griddep_wait();
+    griddep_launch();
+    const uint32_t F = __ldcg(far);
+    if (F > kFarCap) {
+        scatter_scenes_range<1>(blockIdx.x, gridDim.x, scenes, tile_scene, keys, n, hist, perm, pos0, pos1, vfme0,
+                                vfme1, spos, svfme, offs, fix_bits, bands);
+        return;
+    }
+    const uint32_t tid = threadIdx.x;
+    if (F) {
+        for (uint32_t t = tid; t < kBloomWords; t += blockDim.x) s_bloom[t] = 0u;
+        __syncthreads();
+        for (uint32_t t = tid; t < F; t += blockDim.x) {
+            const uint32_t sl = min(__ldcg(far + 1u + t), n - 1u), k = __ldg(keys + sl);
+            s_slot[t] = sl;
+            s_key[t] = k;
+            const uint32_t b = bloom_bit(k);
+            atomicOr(&s_bloom[b >> 5], 1u << (b & 31u));
+        }
+        __syncthreads();
+    }
+    const uint32_t i = blockIdx.x * blockDim.x + tid;
+    if (i >= n) return;
+    uint32_t sc = __ldg(tile_scene + i / kPhysicsTile);
+    while (i >= __ldg(&scenes[sc].agent_end)) ++sc;
+    const uint32_t k = __ldg(keys + i), cb = __ldg(&scenes[sc].cell_base), N = __ldg(&scenes[sc].P.N);
+    const uint32_t parity = __ldg(&scenes[sc].parity);
+    const float4 p = __ldg((parity ? pos1 : pos0) + i);
+    const uint4 q = __ldg((parity ? vfme1 : vfme0) + i);
+    const uint32_t kl = k - cb;
+    if (kl >= N * N) return;  // keys the physics pass cannot emit
+    const uint32_t base = __ldg(offs + k);
+    const uint32_t kz = kl / N, kx = kl - kz * N;
+    const uint32_t c0 = kx > 0u ? kx - 1u : 0u, c1 = (kx + 1u < N ? kx + 1u : kx) + 1u;
+    const uint32_t* __restrict__ oo = offs_old + cb;
+    uint32_t lo[3], hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const bool row = d == 0 ? kz > 0u : (d == 2 ? kz + 1u < N : true);
+        const uint32_t rw = kz + (uint32_t)d - 1u;
+        lo[d] = row ? __ldg(oo + rw * N + c0) : 0u;
+        hi[d] = row ? min(__ldg(oo + rw * N + c1), i) : 0u;
+    }
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        for (uint32_t j = lo[d]; j < hi[d]; j += 4u) {
+            uint32_t kk[4];
+#pragma unroll
+            for (uint32_t u = 0; u < 4u; ++u) kk[u] = __ldg(keys + min(j + u, hi[d] - 1u));
+#pragma unroll
+            for (uint32_t u = 0; u < 4u; ++u) cnt += (j + u < hi[d] && kk[u] == k) ? 1u : 0u;
+        }
+    }
+    if (F) {
+        const uint32_t b = bloom_bit(k);
+        if (s_bloom[b >> 5] & (1u << (b & 31u)))
+            for (uint32_t t = 0; t < F; ++t) cnt += (s_key[t] == k && s_slot[t] < i) ? 1u : 0u;
+    }
+    if (cnt == 0u) hist[k] = 0u;  // the cell's first sphere
+    const uint32_t dst = base + cnt;
+    if (dst < n) {
+        perm[dst] = i;
+        spos[dst] = p;
+        svfme[dst] = q;
+        if (bands) write_band_bounds(bands, offs + cb, N, n, dst, kl);
+    }
+}
+
 template <class Src>
 __global__ void __launch_bounds__(kCollectThreads)
     k_fix_marked(const uint32_t* __restrict__ fix_bits, const uint32_t* __restrict__ keys, uint32_t n,
@@ -460,10 +551,29 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
 }
 
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
-                              uint32_t cells, uint32_t* offs, cudaStream_t st) {
+                              uint32_t cells, uint32_t* offs, cudaStream_t st, uint32_t* far_reset) {
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
     k_cell_scan<true><<<chunks, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.fix_ctl, scenes,
-                                                      cell_tile_scene, nullptr);
+                                                      cell_tile_scene, far_reset);
+    return cudaGetLastError();
+}
+
+cudaError_t count_rank_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* tile_scene,
+                              const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
+                              const uint32_t* offs, const uint32_t* offs_old, const uint32_t* far, uint32_t* perm,
+                              const float4* pos_buf0, const float4* pos_buf1, const uint4* vfme_buf0,
+                              const uint4* vfme_buf1, float4* spos, uint4* svfme, uint4* bands, cudaStream_t st) {
+    cudaError_t e;
+    if (n) {
+        k_cell_rank_scenes<<<(n + 255u) / 256u, 256, 0, st>>>(scenes, tile_scene, keys, n, s.hist, perm, pos_buf0,
+                                                              pos_buf1, vfme_buf0, vfme_buf1, spos, svfme, offs,
+                                                              offs_old, far, s.fix_bits, bands);
+        if ((e = cudaGetLastError())) return e;
+    }
+    const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
+    k_fix_marked<SceneBuffers><<<std::max(collect_grid(n), 1u), kCollectThreads, 0, st>>>(
+        s.fix_bits, keys, n, offs, perm, fix_lists(s), s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse,
+        scan_tiles(cells), far);
     return cudaGetLastError();
 }
 

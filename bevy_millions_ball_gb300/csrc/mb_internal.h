@@ -274,12 +274,13 @@ cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uin
 // LOOP scene).
 // Batched physics: scene s reads the sorted copy and writes buffer 1 - parity
 // (pos_buf[2] / vfme_buf[2]); a HOLD scene only re-emits the counts of its keys.
+// far (nullable): the far-move list of the next frame's batched rank placement.
 cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n,
                                  const uint32_t* offs, const uint4* bands, const float4* spos, const uint4* svfme,
                                  float4* pos_buf0,
                                  float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1, uint32_t* keys,
                                  uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st,
-                                 uint32_t tile = kPhysicsTile);
+                                 uint32_t tile = kPhysicsTile, uint32_t* far = nullptr);
 
 
 // Counting sort of cell keys (mb_count.cu).
@@ -373,7 +374,16 @@ cudaError_t count_rank_alloc(CountScratch& s);
 // Batched count scan: scene cell ranges are padded to whole scan tiles
 // (cell_tile_scene[t] = scene of tile t); tiles of HOLD scenes are skipped.
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
-                              uint32_t cells, uint32_t* offs, cudaStream_t st);
+                              uint32_t cells, uint32_t* offs, cudaStream_t st, uint32_t* far_reset = nullptr);
+// Batched rank placement, for frames in which every scene is in LOOP: offs /
+// offs_old this frame's and the previous frame's pool-wide offsets, far the
+// far moves of the previous batched physics pass (pool-wide slots); an
+// overflowed list falls back to the batched scatter and fixup.
+cudaError_t count_rank_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* tile_scene,
+                              const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
+                              const uint32_t* offs, const uint32_t* offs_old, const uint32_t* far, uint32_t* perm,
+                              const float4* pos_buf0, const float4* pos_buf1, const uint4* vfme_buf0,
+                              const uint4* vfme_buf1, float4* spos, uint4* svfme, uint4* bands, cudaStream_t st);
 // Batched scatter + fixup: like count_scatter, reading each scene's state from its
 // parity buffer; spheres and cells of HOLD scenes are left alone.
 cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* tile_scene,

@@ -833,7 +833,7 @@ __device__ __forceinline__ void physics_tile(
     if (kBatched && mode == kModeHold) return;  // keeps state, buffer, keys and counts
 
     step_sphere<kIndirect, kCg, kCap, kResp>(P, a, i, n, base_a, base_c, lo, hi, s_pos, s_vfme, s_lo, s_cnt, spos, svfme, perm,
-                                pos_out, vfme_out, keys_out, hist, coarse, kBatched ? nullptr : far, cx, cz);
+                                pos_out, vfme_out, keys_out, hist, coarse, far, cx, cz);
 }
 
 template <bool kBatched, bool kIndirect, uint32_t kTile = kTileThreads, int kResp = kSpringRuntime>
@@ -1213,11 +1213,11 @@ template <uint32_t kTile>
 cudaError_t launch_batch_tiles(const SceneDev* scenes, const uint32_t* tile_scene, uint32_t n, const uint32_t* offs,
                                const uint4* bands, const float4* spos, const uint4* svfme, float4* pos_buf0,
                                float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1, uint32_t* keys, uint32_t* hist,
-                               uint32_t* coarse, uint32_t* err, cudaStream_t st) {
+                               uint32_t* coarse, uint32_t* err, cudaStream_t st, uint32_t* far) {
     PhysParams unused{};
     k_physics_frame<true, false, kTile><<<(n + kTile - 1u) / kTile, kTile, 0, st>>>(
         unused, scenes, tile_scene, n, offs, bands, spos, svfme, nullptr, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1,
-        keys, hist, coarse, err, nullptr);
+        keys, hist, coarse, err, far);
     return cudaGetLastError();
 }
 
@@ -1225,16 +1225,16 @@ cudaError_t launch_physics_batch(const SceneDev* scenes, const uint32_t* tile_sc
                                  const uint32_t* offs, const uint4* bands, const float4* spos, const uint4* svfme,
                                  float4* pos_buf0, float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1,
                                  uint32_t* keys, uint32_t* hist, uint32_t* coarse, uint32_t* err, cudaStream_t st,
-                                 uint32_t tile) {
+                                 uint32_t tile, uint32_t* far) {
     if (!n) return cudaSuccess;
     if (tile == 64u)
         return launch_batch_tiles<64u>(scenes, tile_scene, n, offs, bands, spos, svfme, pos_buf0, pos_buf1, vfme_buf0,
-                                       vfme_buf1, keys, hist, coarse, err, st);
+                                       vfme_buf1, keys, hist, coarse, err, st, far);
     if (tile == 256u)
         return launch_batch_tiles<256u>(scenes, tile_scene, n, offs, bands, spos, svfme, pos_buf0, pos_buf1,
-                                        vfme_buf0, vfme_buf1, keys, hist, coarse, err, st);
+                                        vfme_buf0, vfme_buf1, keys, hist, coarse, err, st, far);
     return launch_batch_tiles<128u>(scenes, tile_scene, n, offs, bands, spos, svfme, pos_buf0, pos_buf1, vfme_buf0,
-                                    vfme_buf1, keys, hist, coarse, err, st);
+                                    vfme_buf1, keys, hist, coarse, err, st, far);
 }
 
 cudaError_t launch_rekey(const PhysParams& p, uint32_t n, const float4* pos, uint32_t* keys,

@@ -419,22 +419,26 @@ mb_status mb_batch_get_debug(mb_batch* b, uint32_t scene, uint32_t* keys, uint32
 
 /*
  * Kernel choices of a batch (the knobs of mb_tuning that apply to a pool):
- * frames_per_launch (frames captured per graph launch while no scene changes
- * mode: 1, 2, 4, 8 (default) or 16), collide_block (physics tile: 64, 128
- * (default) or 256 slots) and scatter_agents (1, 2 or 4).  The other fields
- * must keep their defaults (counting sort, sorted copy, per-stage kernels).
+ * sort_algorithm (MB_SORT_RANK, the default: frames in which every scene is
+ * in LOOP place spheres by rank, other frames claim and fix; or
+ * MB_SORT_COUNTING: every frame claims and fixes), frames_per_launch (frames
+ * captured per graph launch while no scene changes mode: 1, 2, 4, 8 (default)
+ * or 16), collide_block (physics tile: 64, 128 (default) or 256 slots) and
+ * scatter_agents (spheres per thread of the counting scatter: 1, 2 or 4).  The
+ * other fields must keep their defaults (sorted copy, per-stage kernels).
  *
  * mb_batch_autotune: the world autotuner's counterpart for a pool (no
  * counterpart in the reference, whose passes have fixed workgroup shapes,
- * src/physics/mod.rs:35): times frames_per_launch {1, 8, 16} x collide_block
- * {64, 128, 256}, then scatter_agents 2 and 4 at 8 frames per launch and
- * 128-slot tiles, on the pool's own scenes for `frames` frames each (one warm-up
+ * src/physics/mod.rs:35): times rank placement with frames_per_launch
+ * {1, 8, 16} x collide_block {64, 128, 256}, then the counting sort with
+ * scatter_agents 1, 2 and 4 at 8 frames per launch and 128-slot tiles, on the
+ * pool's own scenes for `frames` frames each (one warm-up
  * frame per candidate), restoring every scene's state, keys, order, cell ranges
  * and time before each and at the end, then applies the fastest.  Every scene
  * needs a frame since its upload.  frame_ms / tried (nullable) receive
  * MB_BATCH_TUNE_CANDIDATES entries.  Allocates temporary device memory.
  */
-#define MB_BATCH_TUNE_CANDIDATES 11u
+#define MB_BATCH_TUNE_CANDIDATES 12u
 mb_status mb_batch_get_tuning(const mb_batch* b, mb_tuning* out);
 mb_status mb_batch_set_tuning(mb_batch* b, const mb_tuning* t);
 mb_status mb_batch_autotune(mb_batch* b, uint32_t frames, mb_tuning* best, float* frame_ms, mb_tuning* tried);

@@ -203,10 +203,11 @@ def test_batch_tuning_keeps_results(built_lib, cuda, tile, fpl):
 
 @pytest.mark.parametrize("agents", [2, 4])
 def test_batch_scatter_agents(built_lib, cuda, agents):
-    """2 or 4 spheres per scatter thread in a pool: each scene exactly its lone-world result."""
+    """2 or 4 spheres per scatter thread in a pool (the counting sort, whose scatter
+    they apply to): each scene exactly its lone-world result."""
     scs = mixed_scenes(7, seed=23)
     with Batch([s.plugin for s in scs]) as b:
-        b.set_tuning(scatter_agents=agents)
+        b.set_tuning(scatter_agents=agents, sort_algorithm=_abi.MB_SORT_COUNTING)
         for i, s in enumerate(scs):
             b.set_state(i, s.pos_scale, s.vfme)
         b.step(19)
@@ -228,8 +229,8 @@ def test_batch_autotune_restores_the_pool(built_lib, cuda):
         assert len(res["candidates"]) == _abi.MB_BATCH_TUNE_CANDIDATES
         assert all(c["ms_per_frame"] > 0 for c in res["candidates"])
         t = b.tuning
-        assert {"frames_per_launch": t.frames_per_launch, "collide_block": t.collide_block,
-                "scatter_agents": max(t.scatter_agents, 1)} == res["best"]
+        assert {"sort_algorithm": t.sort_algorithm, "frames_per_launch": t.frames_per_launch,
+                "collide_block": t.collide_block, "scatter_agents": max(t.scatter_agents, 1)} == res["best"]
         assert all(b.time(i) == 5 for i in range(len(scs)))
         b.step(20)
         for i, s in enumerate(scs):

@@ -14,7 +14,9 @@ import numpy as np
 import pytest
 
 import oracle
-from bevy_millions_ball_gb300 import MbError, World, _abi, pack_vfme, scenes, unpack_vfme
+from bevy_millions_ball_gb300 import Batch, MbError, World, _abi, pack_vfme, scenes, unpack_vfme
+from tests.test_gpu_batch import mixed_scenes
+from tests.test_gpu_parity_full import _compare_scene
 from tests.test_gpu_world import compare, run_pair
 
 pytestmark = pytest.mark.gpu
@@ -153,3 +155,49 @@ def test_rank_full_size_late_frames(built_lib, cuda):
     """The 1,048,576-sphere workload ranked for 300 frames (settled floor, several
     contacts per sphere), compared at frames 3, 100 and 300."""
     run_pair(scenes.workload("P-1M"), 300, [3, 100, 300], tuning=RANK)
+
+
+@pytest.mark.parametrize("sort", [_abi.MB_SORT_RANK, _abi.MB_SORT_COUNTING])
+def test_batch_rank_against_the_oracle(built_lib, cuda, sort):
+    """A pool of mixed scenes plus two with fast spheres (far moves listed pool-wide,
+    and more than the list holds in some frames): frames in which every scene is
+    in LOOP are ranked, frames with a held scene claim and fix, and the switch
+    back to ranking starts from a claimed frame; each scene against its own
+    oracle world, at several points of the run."""
+    scs = mixed_scenes(6, seed=41, n_min=500, n_max=20_000) + [fast_scene(90, 1.6, seed=42, n=16_384, grids=128),
+                                                             fast_scene(140, 2.5, seed=43)]
+    ows = [oracle.OracleWorld(s.plugin.to_c()) for s in scs]
+    with Batch([s.plugin for s in scs]) as b:
+        b.set_tuning(sort_algorithm=sort)
+        with pytest.raises(MbError):
+            b.set_tuning(sort_algorithm=_abi.MB_SORT_ONESWEEP)
+        for i, s in enumerate(scs):
+            b.set_state(i, s.pos_scale, s.vfme)
+            ows[i].set_state(s.pos_scale, s.vfme)
+
+        def step(k, skip=()):
+            b.step(k)
+            for i, ow in enumerate(ows):
+                if i not in skip:
+                    ow.step(k)
+
+        def check(what):
+            b.sync()
+            for i, ow in enumerate(ows):
+                _compare_scene(b, i, ow, f"scene {i}, {what}")
+                assert b.time(i) == ow.time
+
+        step(1)  # INIT
+        step(2)
+        check("frame 3")
+        step(9)  # a chain of 8 and a single frame
+        check("frame 12")
+        b.set_active(2, False)
+        step(3, skip={2})
+        b.set_active(2, True)
+        step(1)
+        check("after a hold")
+        step(17)
+        check("late")
+    for ow in ows:
+        ow.close()
