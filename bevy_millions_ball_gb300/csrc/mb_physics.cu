@@ -853,60 +853,6 @@ __global__ void __launch_bounds__(kTile)
                                       hist, coarse, err, far);
 }
 
-// A batch's physics pass: each block runs its tile with the kernel variant of the
-// response model its scenes share (rigid, or spring with position-only bands),
-// or reads the model per scene where the tile spans scenes of both.
-template <uint32_t kTile>
-__global__ void __launch_bounds__(kTile)
-    k_physics_batch(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene, uint32_t n,
-                    const uint32_t* __restrict__ offs, const uint4* __restrict__ bands,
-                    const float4* __restrict__ spos, const uint4* __restrict__ svfme, float4* __restrict__ pos_out0,
-                    float4* __restrict__ pos_out1, uint4* __restrict__ vfme_out0, uint4* __restrict__ vfme_out1,
-                    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ hist, uint32_t* __restrict__ coarse,
-                    uint32_t* __restrict__ err, uint32_t* __restrict__ far) {
-    __shared__ __align__(16) union {
-        TileSmemT<kTile, false> full;
-        TileSmemT<kTile, true> pos;
-    } sm;
-    __shared__ __align__(8) uint64_t s_bar;
-    __shared__ int s_resp;
-    if (threadIdx.x == 0) {
-        mbar_init(&s_bar, 1u);
-        int r = kSpringRuntime;
-        const uint32_t i0 = blockIdx.x * kTile;
-        if (i0 < n) {
-            const uint32_t ilast = min(i0 + kTile, n) - 1u;
-            uint32_t sc = scene_of(scenes, __ldg(tile_scene + i0 / kPhysicsTile), i0);
-            r = __ldg(&scenes[sc].P.spring) ? kSpring : kRigid;
-            while (ilast >= __ldg(&scenes[sc].agent_end)) {  // the tile's other scenes
-                ++sc;
-                if ((__ldg(&scenes[sc].P.spring) ? kSpring : kRigid) != r) {
-                    r = kSpringRuntime;
-                    break;
-                }
-            }
-        }
-        s_resp = r;
-    }
-    __syncthreads();  // the model chosen, the mbarrier initialised
-    const PhysParams unused{};
-    if (s_resp == kRigid)
-        physics_tile<true, false, false, kTile, kRigid>(blockIdx.x, threadIdx.x, 0u, &sm.full, &s_bar, unused, scenes,
-                                                       tile_scene, n, offs, bands, spos, svfme, nullptr, pos_out0,
-                                                       pos_out1, vfme_out0, vfme_out1, keys_out, hist, coarse, err,
-                                                       far);
-    else if (s_resp == kSpring)
-        physics_tile<true, false, false, kTile, kSpring>(blockIdx.x, threadIdx.x, 0u, &sm.pos, &s_bar, unused,
-                                                        scenes, tile_scene, n, offs, bands, spos, svfme, nullptr,
-                                                        pos_out0, pos_out1, vfme_out0, vfme_out1, keys_out, hist,
-                                                        coarse, err, far);
-    else
-        physics_tile<true, false, false, kTile, kSpringRuntime>(blockIdx.x, threadIdx.x, 0u, &sm.full, &s_bar,
-                                                               unused, scenes, tile_scene, n, offs, bands, spos,
-                                                               svfme, nullptr, pos_out0, pos_out1, vfme_out0,
-                                                               vfme_out1, keys_out, hist, coarse, err, far);
-}
-
 // ---------------------------------------------------------------- fused frame
 // LOOP frames as one cooperative kernel: the stages of a frame (count scan,
 // scatter, marked-cell fixup, cells above 256 slots if any, physics) run back to back in one launch,
@@ -1268,9 +1214,10 @@ cudaError_t launch_batch_tiles(const SceneDev* scenes, const uint32_t* tile_scen
                                const uint4* bands, const float4* spos, const uint4* svfme, float4* pos_buf0,
                                float4* pos_buf1, uint4* vfme_buf0, uint4* vfme_buf1, uint32_t* keys, uint32_t* hist,
                                uint32_t* coarse, uint32_t* err, cudaStream_t st, uint32_t* far) {
-    k_physics_batch<kTile><<<(n + kTile - 1u) / kTile, kTile, 0, st>>>(
-        scenes, tile_scene, n, offs, bands, spos, svfme, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, keys, hist, coarse,
-        err, far);
+    PhysParams unused{};
+    k_physics_frame<true, false, kTile><<<(n + kTile - 1u) / kTile, kTile, 0, st>>>(
+        unused, scenes, tile_scene, n, offs, bands, spos, svfme, nullptr, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1,
+        keys, hist, coarse, err, far);
     return cudaGetLastError();
 }
 
