@@ -277,7 +277,8 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st, bool may_init) {
         return e;
     if ((e = mb::count_scatter_scenes(b->cnt, b->d_scenes, b->d_tile_scene, b->d_cell_tile_scene, b->keys, b->n_total,
                                       b->cells_total, b->offs, b->perm, b->pos[0], b->pos[1], b->vfme[0],
-                                      b->vfme[1], b->spos, b->svfme, b->bands, st, b->tuning.scatter_agents)))
+                                      b->vfme[1], b->spos, b->svfme, b->bands, st, b->tuning.scatter_agents,
+                                      may_init)))
         return e;
     if ((e = mb::launch_physics_batch(b->d_scenes, b->d_tile_scene, b->n_total, b->offs, b->bands, b->spos, b->svfme,
                                       b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->keys, b->cnt.hist,

@@ -570,7 +570,7 @@ cudaError_t count_rank_scenes(CountScratch& s, const SceneDev* scenes, const uin
                                                               offs_old, far, s.fix_bits, bands);
         if ((e = cudaGetLastError())) return e;
     }
-    const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
+    const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, false};
     k_fix_marked<SceneBuffers><<<std::max(collect_grid(n), 1u), kCollectThreads, 0, st>>>(
         s.fix_bits, keys, n, offs, perm, fix_lists(s), s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse,
         scan_tiles(cells), far);
@@ -581,7 +581,8 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
                                  const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
                                  const uint32_t* offs, uint32_t* perm, const float4* pos_buf0,
                                  const float4* pos_buf1, const uint4* vfme_buf0, const uint4* vfme_buf1,
-                                 float4* spos, uint4* svfme, uint4* bands, cudaStream_t st, uint32_t per_thread) {
+                                 float4* spos, uint4* svfme, uint4* bands, cudaStream_t st, uint32_t per_thread,
+                                 bool may_init) {
     cudaError_t e;
     if (n) {
         const uint32_t per = per_thread == 4u ? 4u : (per_thread == 2u ? 2u : 1u);
@@ -593,7 +594,7 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
                                      vfme_buf1, spos, svfme, offs, s.fix_bits, bands);
         if ((e = cudaGetLastError())) return e;
     }
-    const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1};
+    const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, may_init};
     k_fix_marked<SceneBuffers><<<std::max(collect_grid(n), 1u), kCollectThreads, 0, st>>>(
         s.fix_bits, keys, n, offs, perm, fix_lists(s), s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse,
         scan_tiles(cells), nullptr);

@@ -270,10 +270,11 @@ struct SceneBuffers {
     const float4* p1;
     const uint4* q0;
     const uint4* q1;
+    bool init;  // a scene may be in its INIT frame (false for chained and ranked frames)
     __device__ __forceinline__ bool tile_active(uint32_t t) const {
         return __ldg(&scenes[__ldg(cell_tile_scene + t)].mode) != kModeHold;
     }
-    __device__ __forceinline__ bool any_init() const { return true; }
+    __device__ __forceinline__ bool any_init() const { return init; }
     __device__ __forceinline__ bool tile_init(uint32_t t) const {
         return __ldg(&scenes[__ldg(cell_tile_scene + t)].mode) == kModeInit;
     }

@@ -385,13 +385,14 @@ cudaError_t count_rank_scenes(CountScratch& s, const SceneDev* scenes, const uin
                               const float4* pos_buf0, const float4* pos_buf1, const uint4* vfme_buf0,
                               const uint4* vfme_buf1, float4* spos, uint4* svfme, uint4* bands, cudaStream_t st);
 // Batched scatter + fixup: like count_scatter, reading each scene's state from its
-// parity buffer; spheres and cells of HOLD scenes are left alone.
+// parity buffer; spheres and cells of HOLD scenes are left alone.  may_init: a
+// scene may be in its INIT frame (its cell counts are then cleared here).
 cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* tile_scene,
                                  const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
                                  const uint32_t* offs, uint32_t* perm, const float4* pos_buf0,
                                  const float4* pos_buf1, const uint4* vfme_buf0, const uint4* vfme_buf1,
                                  float4* spos, uint4* svfme, uint4* bands, cudaStream_t st,
-                                 uint32_t per_thread = 1);
+                                 uint32_t per_thread = 1, bool may_init = true);
 // spos/svfme := pos_in/vfme_in gathered through perm (after the onesweep sort);
 // bands (nullable) := the band table of the sorted keys for an N x N grid.
 cudaError_t gather_state(const uint32_t* perm, uint32_t n, const float4* pos_in, const uint4* vfme_in,
