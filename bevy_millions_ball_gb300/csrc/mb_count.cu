@@ -68,36 +68,8 @@ __global__ void __launch_bounds__(kScanThreads)
 // then runs too).
 __device__ __forceinline__ uint32_t bloom_bit(uint32_t k) { return (k * 2654435761u) >> 20; }  // 12 bits
 
-// Keys equal to k in the slot ranges [lo[d], hi[d]) of the three rows: the
-// first four of every row are loaded together (twelve independent loads, one
-// round trip for the usual neighbourhood), the rest row by row.
-__device__ __forceinline__ uint32_t count_key(const uint32_t* __restrict__ keys, uint32_t k, const uint32_t (&lo)[3],
-                                              const uint32_t (&hi)[3]) {
-    uint32_t kk[3][4];
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-        for (uint32_t u = 0; u < 4u; ++u) kk[d][u] = lo[d] + u < hi[d] ? __ldg(keys + lo[d] + u) : ~k;
-    uint32_t cnt = 0;
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-        for (uint32_t u = 0; u < 4u; ++u) cnt += kk[d][u] == k ? 1u : 0u;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        for (uint32_t j = lo[d] + 4u; j < hi[d]; j += 4u) {
-            uint32_t k4[4];
-#pragma unroll
-            for (uint32_t u = 0; u < 4u; ++u) k4[u] = __ldg(keys + min(j + u, hi[d] - 1u));
-#pragma unroll
-            for (uint32_t u = 0; u < 4u; ++u) cnt += (j + u < hi[d] && k4[u] == k) ? 1u : 0u;
-        }
-    }
-    return cnt;
-}
-
 template <uint32_t kPer>
-__global__ void __launch_bounds__(256, kPer == 1u ? 8 : 1)
+__global__ void __launch_bounds__(256)
     k_cell_rank(const uint32_t* __restrict__ keys, uint32_t n, uint32_t cells, uint32_t* __restrict__ hist,
                 uint32_t* __restrict__ perm, const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in,
                 float4* __restrict__ spos, uint4* __restrict__ svfme, const uint32_t* __restrict__ offs,
@@ -157,7 +129,17 @@ __global__ void __launch_bounds__(256, kPer == 1u ? 8 : 1)
     for (uint32_t r = 0; r < kPer; ++r) {
         const uint32_t i = i0 + r * blockDim.x;
         if (k[r] >= cells) continue;
-        uint32_t cnt = count_key(keys, k[r], lo[r], hi[r]);
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            for (uint32_t j = lo[r][d]; j < hi[r][d]; j += 4u) {
+                uint32_t kk[4];
+#pragma unroll
+                for (uint32_t u = 0; u < 4u; ++u) kk[u] = __ldg(keys + min(j + u, hi[r][d] - 1u));
+#pragma unroll
+                for (uint32_t u = 0; u < 4u; ++u) cnt += (j + u < hi[r][d] && kk[u] == k[r]) ? 1u : 0u;
+            }
+        }
         if (F) {
             const uint32_t b = bloom_bit(k[r]);
             if (s_bloom[b >> 5] & (1u << (b & 31u)))
@@ -272,7 +254,7 @@ __global__ void __launch_bounds__(256)
 // the neighbourhood in the scene's own cell coordinates, its state from its
 // current buffer); one sphere per thread.  The far list holds pool-wide slots,
 // its keys pool-wide cells.  An overflowed list: the batched scatter instead.
-__global__ void __launch_bounds__(256, 8)
+__global__ void __launch_bounds__(256)
     k_cell_rank_scenes(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
                        const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
                        uint32_t* __restrict__ perm, const float4* __restrict__ pos0, const float4* __restrict__ pos1,
@@ -324,7 +306,17 @@ __global__ void __launch_bounds__(256, 8)
         lo[d] = row ? __ldg(oo + rw * N + c0) : 0u;
         hi[d] = row ? min(__ldg(oo + rw * N + c1), i) : 0u;
     }
-    uint32_t cnt = count_key(keys, k, lo, hi);
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        for (uint32_t j = lo[d]; j < hi[d]; j += 4u) {
+            uint32_t kk[4];
+#pragma unroll
+            for (uint32_t u = 0; u < 4u; ++u) kk[u] = __ldg(keys + min(j + u, hi[d] - 1u));
+#pragma unroll
+            for (uint32_t u = 0; u < 4u; ++u) cnt += (j + u < hi[d] && kk[u] == k) ? 1u : 0u;
+        }
+    }
     if (F) {
         const uint32_t b = bloom_bit(k);
         if (s_bloom[b >> 5] & (1u << (b & 31u)))
