@@ -6,7 +6,11 @@ A "step" is one frame of the pipeline over the whole scene.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload P-1M|P-small|P-4M|batch|serving|sort|segments|render]
-                    [--cpu-seconds S]
+                    [--cpu-seconds S] [--sort rank|counting|onesweep]
+                    [--tuning field=value,...]
+
+``--sort`` / ``--tuning`` set the world workloads' mb_tuning (default: the
+library's, rank placement); the JSON line's config names the sort used.
 
 Timing: W untimed frames, then K frames, each bracketed by CUDA events on the
 world's stream; L2 is flushed (a 256 MB write, then a 256 MB read so that no dirty
