@@ -81,7 +81,6 @@ struct SceneHost {
     bool frame_done = false;
     uint32_t parity = 0;   // state buffer holding the current state
     bool prev_loop = false;  // its last frame was LOOP (mirrors SceneDev::prev_loop)
-    int offs_at = 0;         // the offsets buffer holding its cell ranges (written by its last frame)
     int64_t time = -1;
 };
 
@@ -304,16 +303,15 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st, bool may_init) {
     return cudaGetLastError();
 }
 
-// A frame sorted by rank placement: writes the offsets of the scenes that run
-// into buffer q (a held scene's stay in the buffer of its last frame,
-// SceneHost::offs_at), ranks the scenes that ran LOOP the frame before (their
-// previous offsets are in q ^ 1) with the far moves listed in cnt.far[q], claims
+// A frame sorted by rank placement: writes the offsets buffer q (held scenes'
+// offsets copied from q ^ 1, which holds the previous frame's), ranks the scenes
+// that ran LOOP the frame before with the far moves listed in cnt.far[q], claims
 // slots for the others, and lists this frame's far moves in cnt.far[q ^ 1]
 // (emptied by the scan).  may_init: a scene may be in its INIT frame.
 cudaError_t enqueue_rank_frame(mb_batch* b, cudaStream_t st, int q, bool may_init) {
     cudaError_t e;
     if ((e = mb::count_scan_scenes(b->cnt, b->d_scenes, b->d_cell_tile_scene, b->cells_total, offs_buf(b, q), st,
-                                   b->cnt.far[q ^ 1], b->claim_flag)))
+                                   b->cnt.far[q ^ 1], offs_buf(b, q ^ 1), b->claim_flag)))
         return e;
     if ((e = mb::count_rank_scenes(b->cnt, b->d_scenes, b->d_tile_scene, b->d_cell_tile_scene, b->keys, b->n_total,
                                    b->cells_total, offs_buf(b, q), offs_buf(b, q ^ 1), b->cnt.far[q], b->perm,
@@ -405,7 +403,6 @@ mb_status run_frame(mb_batch* b, const std::vector<uint32_t>& modes, uint32_t fr
         }
         if (modes[i] == mb::kModeInit) h.init_pending = false;
         h.prev_loop = modes[i] == mb::kModeLoop;  // mirrors k_flip_parity
-        if (modes[i] != mb::kModeHold) h.offs_at = b->ob;
     }
     return MB_OK;
 }
@@ -587,7 +584,7 @@ mb_status mb_batch_get_debug(mb_batch* b, uint32_t scene, uint32_t* keys, uint32
         ds = start ? tmp + 2u * h.n : nullptr;
         dc = close ? tmp + 2u * h.n + h.cells : nullptr;
     }
-    k_local_debug<<<(m + 255u) / 256u, 256, 0, b->stream>>>(b->keys, b->perm, offs_buf(b, h.offs_at), h.n, h.cells,
+    k_local_debug<<<(m + 255u) / 256u, 256, 0, b->stream>>>(b->keys, b->perm, offs_buf(b, b->ob), h.n, h.cells,
                                                              h.agent_base, h.cell_base, dk, dp, ds, dc);
     e = cudaGetLastError();
     if (!e && where == MB_HOST) {

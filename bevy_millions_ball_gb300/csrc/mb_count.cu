@@ -39,13 +39,16 @@ namespace mb {
 namespace {
 
 // Rank placement: far_reset (nullable) is a far-move list emptied for this
-// frame's physics pass, flag_reset (nullable) this frame's claim flag.
+// frame's physics pass, flag_reset (nullable) this frame's claim flag;
+// offs_prev (nullable, batches): the other offsets buffer, from which held
+// scenes' offsets are copied.
 template <bool kScenes>
 __global__ void __launch_bounds__(kScanThreads)
     k_cell_scan(const uint32_t* __restrict__ hist, const uint32_t* __restrict__ coarse, uint32_t cells,
                 uint32_t* __restrict__ offs, uint32_t* fix_ctl,
                 const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ cell_tile_scene,
-                uint32_t* __restrict__ far_reset, uint32_t* __restrict__ flag_reset) {
+                uint32_t* __restrict__ far_reset, const uint32_t* __restrict__ offs_prev,
+                uint32_t* __restrict__ flag_reset) {
     __shared__ uint32_t s_warp[kScanThreads / 32], s_base[kScanThreads / 32];
     griddep_wait();  // after the previous frame's physics pass, when chained to it
     griddep_launch();
@@ -53,7 +56,8 @@ __global__ void __launch_bounds__(kScanThreads)
         if (far_reset) *far_reset = 0u;
         if (flag_reset) *flag_reset = 0u;
     }
-    scan_chunk<kScenes>(blockIdx.x, hist, coarse, cells, offs, fix_ctl, scenes, cell_tile_scene, s_warp, s_base);
+    scan_chunk<kScenes>(blockIdx.x, hist, coarse, cells, offs, fix_ctl, scenes, cell_tile_scene, s_warp, s_base,
+                        offs_prev);
 }
 
 // Rank placement of one world's spheres (MB_SORT_RANK), kPer spheres per
@@ -261,9 +265,7 @@ __global__ void __launch_bounds__(256)
 // list overflowed claim slots as the batched scatter does (one atomic per run of
 // equal keys in the warp, marks for the fixup, which then runs: *claimed != 0);
 // spheres of held scenes are left alone.  Every lane takes part in the warp's
-// collectives, so no lane leaves before them; a block whose spheres are all
-// ranked (or held) skips the claim's collectives and only clears its words of
-// the fixup bitmap.
+// collectives, so no lane leaves before them.
 __global__ void __launch_bounds__(256)
     k_cell_rank_scenes(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
                        const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
@@ -301,7 +303,6 @@ __global__ void __launch_bounds__(256)
         rank = ranking && mode == kModeLoop && __ldg(&scenes[sc].prev_loop) != 0u;
     }
     const bool act = i < n && mode != kModeHold;
-    const bool all_ranked = __syncthreads_and(rank || !act) != 0;
     float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     uint4 q = make_uint4(0u, 0u, 0u, 0u);
     if (act) {
@@ -314,26 +315,22 @@ __global__ void __launch_bounds__(256)
     // claiming lanes: the batched scatter's claim (other lanes join the collectives)
     const bool claim = act && !rank;
     const bool ident = claim && (k & kInitKeyBit);
-    uint32_t dst = 0xFFFFFFFFu;
-    if (all_ranked) {
-        if (lane == 0u && i < n) fix_bits[i >> 5] = 0u;  // nothing of this warp to fix
-    } else {
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, claim ? (ident ? 0xFFFFFFFEu : k) : 0xFFFFFFFFu);
-        const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
-        uint32_t b = 0;
-        bool mark = false;
-        if (claim && !ident && lane == leader) {
-            const uint32_t g = (uint32_t)__popc(peers);
-            const uint32_t lo = __ldg(offs + k), hi = __ldg(offs + k + 1u);
-            b = hi - atomicSub(hist + k, g);  // the run's first slot
-            mark = listed(lo, hi, b, g);
-        }
-        b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
-        mark_fix(fix_bits, i, n, mark);
-        const bool any_claim = __any_sync(0xFFFFFFFFu, claim);
-        if (lane == 0u && any_claim) atomicOr(claimed, 1u);  // the fixup runs this frame
-        if (claim) dst = ident ? i : b + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, claim ? (ident ? 0xFFFFFFFEu : k) : 0xFFFFFFFFu);
+    const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+    uint32_t b = 0;
+    bool mark = false;
+    if (claim && !ident && lane == leader) {
+        const uint32_t g = (uint32_t)__popc(peers);
+        const uint32_t lo = __ldg(offs + k), hi = __ldg(offs + k + 1u);
+        b = hi - atomicSub(hist + k, g);  // the run's first slot
+        mark = listed(lo, hi, b, g);
     }
+    b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
+    mark_fix(fix_bits, i, n, mark);
+    const bool any_claim = __any_sync(0xFFFFFFFFu, claim);
+    if (lane == 0u && any_claim) atomicOr(claimed, 1u);  // the fixup runs this frame
+    uint32_t dst = 0xFFFFFFFFu;
+    if (claim) dst = ident ? i : b + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 
     // ranked lanes
     if (rank) {
@@ -559,7 +556,7 @@ cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t*
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
     return launch_pdl(pdl, k_cell_scan<false>, dim3(chunks), dim3(kScanThreads), 0, st, (const uint32_t*)s.hist,
                       (const uint32_t*)s.coarse, cells, offs, s.fix_ctl, (const SceneDev*)nullptr,
-                      (const uint32_t*)nullptr, far_reset, (uint32_t*)nullptr);
+                      (const uint32_t*)nullptr, far_reset, (const uint32_t*)nullptr, (uint32_t*)nullptr);
 }
 
 cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells, const uint32_t* offs,
@@ -603,10 +600,10 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
 
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
                               uint32_t cells, uint32_t* offs, cudaStream_t st, uint32_t* far_reset,
-                              uint32_t* flag_reset) {
+                              const uint32_t* offs_prev, uint32_t* flag_reset) {
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
     k_cell_scan<true><<<chunks, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.fix_ctl, scenes,
-                                                      cell_tile_scene, far_reset, flag_reset);
+                                                      cell_tile_scene, far_reset, offs_prev, flag_reset);
     return cudaGetLastError();
 }
 

@@ -374,12 +374,13 @@ cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
 cudaError_t count_rank_alloc(CountScratch& s);
 // Batched count scan: scene cell ranges are padded to whole scan tiles
 // (cell_tile_scene[t] = scene of tile t); tiles of HOLD scenes are skipped.
-// Batched scan (tiles of held scenes skipped); for rank placement block 0 also
-// zeroes far_reset[0] (the far list the physics pass fills) and *flag_reset (the
-// claim flag of this frame).
+// Batched scan for rank placement (offs_prev non-null): the tiles of held scenes
+// copy their offsets from offs_prev, the other buffer, so that both buffers
+// keep every scene's cell ranges; block 0 zeroes far_reset[0] (the far list the
+// physics pass fills) and *flag_reset (the claim flag of this frame).
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
                               uint32_t cells, uint32_t* offs, cudaStream_t st, uint32_t* far_reset = nullptr,
-                              uint32_t* flag_reset = nullptr);
+                              const uint32_t* offs_prev = nullptr, uint32_t* flag_reset = nullptr);
 // Batched rank placement: a scene in LOOP that also ran LOOP the frame before
 // (SceneDev::prev_loop) is ranked (offs / offs_old this frame's and the previous
 // frame's pool-wide offsets, far the far moves of the previous batched physics

@@ -194,7 +194,7 @@ def test_batch_rank_against_the_oracle(built_lib, cuda, sort):
         check("frame 12")
         b.set_active(2, False)
         step(3, skip={2})
-        check("scene 2 held")  # its cell ranges read from the buffer its last frame wrote
+        check("scene 2 held")  # its cell ranges kept in both offsets buffers
         b.set_active(5, False)
         step(2, skip={2, 5})
         b.set_active(2, True)
