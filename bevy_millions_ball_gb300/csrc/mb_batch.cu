@@ -39,14 +39,10 @@ __global__ void k_fill_keys(uint32_t* keys, uint32_t n, uint32_t value) {
     if (i < n) keys[i] = value;
 }
 
-// after a frame: every scene that ran now holds its state in the other buffer,
-// and the next frame may rank the scenes that ran LOOP
+// after a frame: every scene that ran now holds its state in the other buffer
 __global__ void k_flip_parity(mb::SceneDev* scenes, uint32_t count) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < count) {
-        if (scenes[s].mode != mb::kModeHold) scenes[s].parity ^= 1u;
-        scenes[s].prev_loop = scenes[s].mode == mb::kModeLoop ? 1u : 0u;
-    }
+    if (s < count && scenes[s].mode != mb::kModeHold) scenes[s].parity ^= 1u;
 }
 
 // cells of a scene are padded to whole scan tiles, so every tile has one scene
@@ -80,7 +76,6 @@ struct SceneHost {
     bool active = true;
     bool frame_done = false;
     uint32_t parity = 0;   // state buffer holding the current state
-    bool prev_loop = false;  // its last frame was LOOP (mirrors SceneDev::prev_loop)
     int64_t time = -1;
 };
 
@@ -107,15 +102,13 @@ struct mb_batch {
     bool counts_valid = true;             // hist/coarse match keys
     bool layout_dirty = true;             // scene ranges changed: re-upload tiles, re-capture
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    // rank placement: [one frame / a chain] x [offsets buffer the first frame
-    // writes]; ob: the buffer (0: offs, 1: cnt.offs_old) holding the last frame's
-    // offsets; rank_ready: cnt.far[ob ^ 1] lists the far moves of the last frame,
-    // which was a rank-placement frame too; claim_flag: some sphere of the frame
-    // claimed its slot (the fixup runs)
+    // rank placement (frames in which every scene is in LOOP): [one frame / a chain]
+    // x [offsets buffer the first frame writes]; ob: the buffer (0: offs, 1:
+    // cnt.offs_old) holding the last frame's offsets; rank_ready: cnt.far[ob ^ 1]
+    // lists the far moves of the last frame, which was ranked too
     cudaGraphExec_t rgraph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     int ob = 0;
     bool rank_ready = false;
-    uint32_t* claim_flag = nullptr;
     std::vector<uint32_t> last_modes;
     mb_tuning tuning{};                   // frames_per_launch (chain length) and collide_block are used
     std::string err;
@@ -168,7 +161,6 @@ cudaError_t alloc_pool(mb_batch* b) {
     if ((e = cudaMalloc(&b->perm, sizeof(uint32_t) * A))) return e;
     if ((e = cudaMalloc(&b->offs, sizeof(uint32_t) * (Cc + 1u)))) return e;
     if ((e = cudaMalloc(&b->ctl, sizeof(uint32_t) * mb::kCtlWords))) return e;
-    if ((e = cudaMalloc(&b->claim_flag, sizeof(uint32_t)))) return e;
     if ((e = cudaMemset(b->ctl, 0, sizeof(uint32_t) * mb::kCtlWords))) return e;
     if ((e = cudaMalloc(&b->d_tile_scene, sizeof(uint32_t) * (A / kTile + 1u)))) return e;
     if ((e = cudaMalloc(&b->d_cell_tile_scene, sizeof(uint32_t) * (Cc / mb::kScanTile + 1u)))) return e;
@@ -195,7 +187,6 @@ void free_pool(mb_batch* b) {
     cudaFree(b->perm);
     cudaFree(b->offs);
     cudaFree(b->ctl);
-    cudaFree(b->claim_flag);
     cudaFree(b->d_tile_scene);
     cudaFree(b->d_cell_tile_scene);
     if (b->h_cell_tile_scene) cudaFreeHost(b->h_cell_tile_scene);
@@ -247,7 +238,6 @@ cudaError_t sync_tables(mb_batch* b, const std::vector<uint32_t>& modes) {
         d.cell_base = h.cell_base;
         d.mode = modes[i];
         d.parity = h.parity;
-        d.prev_loop = h.prev_loop ? 1u : 0u;
     }
     if ((e = cudaMemcpyAsync(b->d_scenes, b->h_scenes, sizeof(mb::SceneDev) * S, cudaMemcpyHostToDevice,
                              b->stream)))
@@ -303,29 +293,22 @@ cudaError_t enqueue_frame(mb_batch* b, cudaStream_t st, bool may_init) {
     return cudaGetLastError();
 }
 
-// A frame sorted by rank placement: writes the offsets buffer q (held scenes'
-// offsets copied from q ^ 1, which holds the previous frame's), ranks the scenes
-// that ran LOOP the frame before with the far moves listed in cnt.far[q], claims
-// slots for the others, and lists this frame's far moves in cnt.far[q ^ 1]
-// (emptied by the scan).  may_init: a scene may be in its INIT frame.
-cudaError_t enqueue_rank_frame(mb_batch* b, cudaStream_t st, int q, bool may_init) {
+// A frame in which every scene is in LOOP, sorted by rank placement: writes the
+// offsets buffer q, reads the previous frame's from q ^ 1, ranks the far moves
+// listed in cnt.far[q] and lists this frame's in cnt.far[q ^ 1] (emptied by the scan).
+cudaError_t enqueue_rank_frame(mb_batch* b, cudaStream_t st, int q) {
     cudaError_t e;
     if ((e = mb::count_scan_scenes(b->cnt, b->d_scenes, b->d_cell_tile_scene, b->cells_total, offs_buf(b, q), st,
-                                   b->cnt.far[q ^ 1], offs_buf(b, q ^ 1), b->claim_flag)))
+                                   b->cnt.far[q ^ 1])))
         return e;
     if ((e = mb::count_rank_scenes(b->cnt, b->d_scenes, b->d_tile_scene, b->d_cell_tile_scene, b->keys, b->n_total,
                                    b->cells_total, offs_buf(b, q), offs_buf(b, q ^ 1), b->cnt.far[q], b->perm,
-                                   b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->spos, b->svfme, b->bands,
-                                   b->claim_flag, may_init, st)))
+                                   b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->spos, b->svfme, b->bands, st)))
         return e;
     if ((e = mb::launch_physics_batch(b->d_scenes, b->d_tile_scene, b->n_total, offs_buf(b, q), b->bands, b->spos,
                                       b->svfme, b->pos[0], b->pos[1], b->vfme[0], b->vfme[1], b->keys, b->cnt.hist,
                                       b->cnt.coarse, b->ctl + mb::kCtlError, st, b->tuning.collide_block,
                                       b->cnt.far[q ^ 1])))
-        return e;
-    // INIT scenes emitted cell counts only: their tile counts from the cell counts
-    if (may_init &&
-        (e = mb::count_tile_counts_scenes(b->cnt, b->d_scenes, b->d_cell_tile_scene, b->cells_total, st)))
         return e;
     const uint32_t S = (uint32_t)b->scenes.size();
     k_flip_parity<<<(S + 127u) / 128u, 128, 0, st>>>(b->d_scenes, S);
@@ -345,7 +328,7 @@ cudaError_t build_graph(mb_batch* b, int which = 0, int rank = -1) {
     if (e) return e;
     cudaError_t fe = cudaSuccess;
     for (uint32_t f = 0; f < (which ? chain_frames(b) : 1u) && !fe; ++f)
-        fe = rank >= 0 ? enqueue_rank_frame(b, b->cap_stream, rank ^ (int)(f & 1u), !which)
+        fe = rank >= 0 ? enqueue_rank_frame(b, b->cap_stream, rank ^ (int)(f & 1u))
                        : enqueue_frame(b, b->cap_stream, !which);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(b->cap_stream, &g);
@@ -376,7 +359,8 @@ mb_status run_frame(mb_batch* b, const std::vector<uint32_t>& modes, uint32_t fr
         return bcuda(b, "batch recount", e);
     }
     if ((e = sync_tables(b, modes))) return bcuda(b, "batch tables", e);
-    if (b->tuning.sort_algorithm == MB_SORT_RANK) {
+    const bool all_loop = std::all_of(modes.begin(), modes.end(), [](uint32_t m) { return m == mb::kModeLoop; });
+    if (b->tuning.sort_algorithm == MB_SORT_RANK && all_loop && b->counts_valid) {
         const int q = b->ob ^ 1;  // offsets buffer of the first frame
         if (!b->rank_ready) {
             // no far list describes this input yet: mark it overflowed, so the first
@@ -402,7 +386,6 @@ mb_status run_frame(mb_batch* b, const std::vector<uint32_t>& modes, uint32_t fr
             h.parity ^= frames & 1u;  // mirrors k_flip_parity
         }
         if (modes[i] == mb::kModeInit) h.init_pending = false;
-        h.prev_loop = modes[i] == mb::kModeLoop;  // mirrors k_flip_parity
     }
     return MB_OK;
 }

@@ -38,26 +38,19 @@
 namespace mb {
 namespace {
 
-// Rank placement: far_reset (nullable) is a far-move list emptied for this
-// frame's physics pass, flag_reset (nullable) this frame's claim flag;
-// offs_prev (nullable, batches): the other offsets buffer, from which held
-// scenes' offsets are copied.
+// far_reset (nullable): a far-move list emptied for this frame's physics pass
+// (rank placement).
 template <bool kScenes>
 __global__ void __launch_bounds__(kScanThreads)
     k_cell_scan(const uint32_t* __restrict__ hist, const uint32_t* __restrict__ coarse, uint32_t cells,
                 uint32_t* __restrict__ offs, uint32_t* fix_ctl,
                 const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ cell_tile_scene,
-                uint32_t* __restrict__ far_reset, const uint32_t* __restrict__ offs_prev,
-                uint32_t* __restrict__ flag_reset) {
+                uint32_t* __restrict__ far_reset) {
     __shared__ uint32_t s_warp[kScanThreads / 32], s_base[kScanThreads / 32];
     griddep_wait();  // after the previous frame's physics pass, when chained to it
     griddep_launch();
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (far_reset) *far_reset = 0u;
-        if (flag_reset) *flag_reset = 0u;
-    }
-    scan_chunk<kScenes>(blockIdx.x, hist, coarse, cells, offs, fix_ctl, scenes, cell_tile_scene, s_warp, s_base,
-                        offs_prev);
+    if (far_reset && blockIdx.x == 0 && threadIdx.x == 0) *far_reset = 0u;
+    scan_chunk<kScenes>(blockIdx.x, hist, coarse, cells, offs, fix_ctl, scenes, cell_tile_scene, s_warp, s_base);
 }
 
 // Rank placement of one world's spheres (MB_SORT_RANK), kPer spheres per
@@ -257,15 +250,10 @@ __global__ void __launch_bounds__(256)
                                vfme1, spos, svfme, offs, fix_bits, bands);
 }
 
-// Rank placement of a batch (one sphere per thread).  A sphere of a scene that
-// is in LOOP and ran LOOP the frame before is ranked as k_cell_rank does, in its
-// scene's own cell coordinates, its state read from its scene's current buffer;
-// the far list holds pool-wide slots, its keys pool-wide cells.  Spheres of
-// scenes in INIT, of scenes back from a hold, and every sphere when the far
-// list overflowed claim slots as the batched scatter does (one atomic per run of
-// equal keys in the warp, marks for the fixup, which then runs: *claimed != 0);
-// spheres of held scenes are left alone.  Every lane takes part in the warp's
-// collectives, so no lane leaves before them.
+// Rank placement of a batch whose scenes are all in LOOP (k_cell_rank per scene:
+// the neighbourhood in the scene's own cell coordinates, its state from its
+// current buffer); one sphere per thread.  The far list holds pool-wide slots,
+// its keys pool-wide cells.  An overflowed list: the batched scatter instead.
 __global__ void __launch_bounds__(256)
     k_cell_rank_scenes(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
                        const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
@@ -273,14 +261,18 @@ __global__ void __launch_bounds__(256)
                        const uint4* __restrict__ vfme0, const uint4* __restrict__ vfme1, float4* __restrict__ spos,
                        uint4* __restrict__ svfme, const uint32_t* __restrict__ offs,
                        const uint32_t* __restrict__ offs_old, const uint32_t* __restrict__ far,
-                       uint32_t* __restrict__ fix_bits, uint4* __restrict__ bands, uint32_t* __restrict__ claimed) {
+                       uint32_t* __restrict__ fix_bits, uint4* __restrict__ bands) {
     __shared__ uint32_t s_key[kFarCap], s_slot[kFarCap], s_bloom[kBloomWords];
     griddep_wait();
     griddep_launch();
     const uint32_t F = __ldcg(far);
-    const bool ranking = F <= kFarCap;
-    const uint32_t tid = threadIdx.x, lane = tid & 31u;
-    if (ranking && F) {
+    if (F > kFarCap) {
+        scatter_scenes_range<1>(blockIdx.x, gridDim.x, scenes, tile_scene, keys, n, hist, perm, pos0, pos1, vfme0,
+                                vfme1, spos, svfme, offs, fix_bits, bands);
+        return;
+    }
+    const uint32_t tid = threadIdx.x;
+    if (F) {
         for (uint32_t t = tid; t < kBloomWords; t += blockDim.x) s_bloom[t] = 0u;
         __syncthreads();
         for (uint32_t t = tid; t < F; t += blockDim.x) {
@@ -293,104 +285,64 @@ __global__ void __launch_bounds__(256)
         __syncthreads();
     }
     const uint32_t i = blockIdx.x * blockDim.x + tid;
-    uint32_t sc = 0, mode = kModeHold, parity = 0, k = 0xFFFFFFFFu;
-    bool rank = false;
-    if (i < n) {
-        sc = __ldg(tile_scene + i / kPhysicsTile);
-        while (i >= __ldg(&scenes[sc].agent_end)) ++sc;
-        mode = __ldg(&scenes[sc].mode);
-        parity = __ldg(&scenes[sc].parity);
-        rank = ranking && mode == kModeLoop && __ldg(&scenes[sc].prev_loop) != 0u;
+    if (i >= n) return;
+    uint32_t sc = __ldg(tile_scene + i / kPhysicsTile);
+    while (i >= __ldg(&scenes[sc].agent_end)) ++sc;
+    const uint32_t k = __ldg(keys + i), cb = __ldg(&scenes[sc].cell_base), N = __ldg(&scenes[sc].P.N);
+    const uint32_t parity = __ldg(&scenes[sc].parity);
+    const float4 p = __ldg((parity ? pos1 : pos0) + i);
+    const uint4 q = __ldg((parity ? vfme1 : vfme0) + i);
+    const uint32_t kl = k - cb;
+    if (kl >= N * N) return;  // keys the physics pass cannot emit
+    const uint32_t base = __ldg(offs + k);
+    const uint32_t kz = kl / N, kx = kl - kz * N;
+    const uint32_t c0 = kx > 0u ? kx - 1u : 0u, c1 = (kx + 1u < N ? kx + 1u : kx) + 1u;
+    const uint32_t* __restrict__ oo = offs_old + cb;
+    uint32_t lo[3], hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const bool row = d == 0 ? kz > 0u : (d == 2 ? kz + 1u < N : true);
+        const uint32_t rw = kz + (uint32_t)d - 1u;
+        lo[d] = row ? __ldg(oo + rw * N + c0) : 0u;
+        hi[d] = row ? min(__ldg(oo + rw * N + c1), i) : 0u;
     }
-    const bool act = i < n && mode != kModeHold;
-    float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    uint4 q = make_uint4(0u, 0u, 0u, 0u);
-    if (act) {
-        k = __ldg(keys + i);
-        p = __ldg((parity ? pos1 : pos0) + i);
-        q = __ldg((parity ? vfme1 : vfme0) + i);
-    }
-    const uint32_t cb = act ? __ldg(&scenes[sc].cell_base) : 0u, N = act ? __ldg(&scenes[sc].P.N) : 1u;
-
-    // claiming lanes: the batched scatter's claim (other lanes join the collectives)
-    const bool claim = act && !rank;
-    const bool ident = claim && (k & kInitKeyBit);
-    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, claim ? (ident ? 0xFFFFFFFEu : k) : 0xFFFFFFFFu);
-    const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
-    uint32_t b = 0;
-    bool mark = false;
-    if (claim && !ident && lane == leader) {
-        const uint32_t g = (uint32_t)__popc(peers);
-        const uint32_t lo = __ldg(offs + k), hi = __ldg(offs + k + 1u);
-        b = hi - atomicSub(hist + k, g);  // the run's first slot
-        mark = listed(lo, hi, b, g);
-    }
-    b = __shfl_sync(0xFFFFFFFFu, b, (int)leader);
-    mark_fix(fix_bits, i, n, mark);
-    const bool any_claim = __any_sync(0xFFFFFFFFu, claim);
-    if (lane == 0u && any_claim) atomicOr(claimed, 1u);  // the fixup runs this frame
-    uint32_t dst = 0xFFFFFFFFu;
-    if (claim) dst = ident ? i : b + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-
-    // ranked lanes
-    if (rank) {
-        const uint32_t kl = k - cb;
-        if (kl < N * N) {  // keys the physics pass cannot emit are left
-            const uint32_t base = __ldg(offs + k);
-            const uint32_t kz = kl / N, kx = kl - kz * N;
-            const uint32_t c0 = kx > 0u ? kx - 1u : 0u, c1 = (kx + 1u < N ? kx + 1u : kx) + 1u;
-            const uint32_t* __restrict__ oo = offs_old + cb;
-            uint32_t lo[3], hi[3];
+    uint32_t cnt = 0;
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const bool row = d == 0 ? kz > 0u : (d == 2 ? kz + 1u < N : true);
-                const uint32_t rw = kz + (uint32_t)d - 1u;
-                lo[d] = row ? __ldg(oo + rw * N + c0) : 0u;
-                hi[d] = row ? min(__ldg(oo + rw * N + c1), i) : 0u;
-            }
-            uint32_t cnt = 0;
+    for (int d = 0; d < 3; ++d) {
+        for (uint32_t j = lo[d]; j < hi[d]; j += 4u) {
+            uint32_t kk[4];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                for (uint32_t j = lo[d]; j < hi[d]; j += 4u) {
-                    uint32_t kk[4];
+            for (uint32_t u = 0; u < 4u; ++u) kk[u] = __ldg(keys + min(j + u, hi[d] - 1u));
 #pragma unroll
-                    for (uint32_t u = 0; u < 4u; ++u) kk[u] = __ldg(keys + min(j + u, hi[d] - 1u));
-#pragma unroll
-                    for (uint32_t u = 0; u < 4u; ++u) cnt += (j + u < hi[d] && kk[u] == k) ? 1u : 0u;
-                }
-            }
-            if (F) {
-                const uint32_t bb = bloom_bit(k);
-                if (s_bloom[bb >> 5] & (1u << (bb & 31u)))
-                    for (uint32_t t = 0; t < F; ++t) cnt += (s_key[t] == k && s_slot[t] < i) ? 1u : 0u;
-            }
-            if (cnt == 0u) hist[k] = 0u;  // the cell's first sphere
-            dst = base + cnt;
+            for (uint32_t u = 0; u < 4u; ++u) cnt += (j + u < hi[d] && kk[u] == k) ? 1u : 0u;
         }
     }
-    if (act && dst < n) {  // only counts that disagree with the keys fail dst < n
+    if (F) {
+        const uint32_t b = bloom_bit(k);
+        if (s_bloom[b >> 5] & (1u << (b & 31u)))
+            for (uint32_t t = 0; t < F; ++t) cnt += (s_key[t] == k && s_slot[t] < i) ? 1u : 0u;
+    }
+    if (cnt == 0u) hist[k] = 0u;  // the cell's first sphere
+    const uint32_t dst = base + cnt;
+    if (dst < n) {
         perm[dst] = i;
         spos[dst] = p;
         svfme[dst] = q;
-        if (bands && !ident) write_band_bounds(bands, offs + cb, N, n, dst, k - cb);
+        if (bands) write_band_bounds(bands, offs + cb, N, n, dst, kl);
     }
 }
 
-// gate (nullable): the fixup only clears the counts unless *gate > gate_max (a
-// world's far-move count above kFarCap, or a batch frame's claim flag set):
-// when no sphere claimed a slot, the order is final.
 template <class Src>
 __global__ void __launch_bounds__(kCollectThreads)
     k_fix_marked(const uint32_t* __restrict__ fix_bits, const uint32_t* __restrict__ keys, uint32_t n,
                  const uint32_t* __restrict__ offs, uint32_t* perm, FixLists lists, uint32_t* __restrict__ tmp,
                  Src src, float4* __restrict__ spos, uint4* __restrict__ svfme, uint32_t* __restrict__ hist,
-                 uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles, const uint32_t* __restrict__ gate,
-                 uint32_t gate_max) {
+                 uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles, const uint32_t* __restrict__ gate) {
     __shared__ MarkedSmem S;
     griddep_wait();  // the scatter's bitmap and order are complete
     griddep_launch();
     clear_counts(blockIdx.x, gridDim.x, src, hist, cells, coarse, tiles);
-    if (gate && __ldcg(gate) <= gate_max) return;
+    if (gate && __ldcg(gate) <= kFarCap) return;
     fix_marked_block<Src, false, true>(blockIdx.x, gridDim.x, fix_bits, keys, n, offs, perm, lists, tmp, src, spos,
                                        svfme, S);
 }
@@ -556,7 +508,7 @@ cudaError_t count_scan(CountScratch& s, uint32_t* ctl, uint32_t cells, uint32_t*
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
     return launch_pdl(pdl, k_cell_scan<false>, dim3(chunks), dim3(kScanThreads), 0, st, (const uint32_t*)s.hist,
                       (const uint32_t*)s.coarse, cells, offs, s.fix_ctl, (const SceneDev*)nullptr,
-                      (const uint32_t*)nullptr, far_reset, (const uint32_t*)nullptr, (uint32_t*)nullptr);
+                      (const uint32_t*)nullptr, far_reset);
 }
 
 cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells, const uint32_t* offs,
@@ -574,7 +526,7 @@ cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
     const OneBuffer src{pos_in, vfme_in};
     return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(std::max(collect_grid(n), 1u)),
                       dim3(kCollectThreads), 0, st, (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s),
-                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells), far, kFarCap);
+                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells), far);
 }
 
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
@@ -595,15 +547,14 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
     return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(std::max(collect_grid(n), 1u)),
                       dim3(kCollectThreads), 0, st, (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s),
                       s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells),
-                      (const uint32_t*)nullptr, 0u);
+                      (const uint32_t*)nullptr);
 }
 
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
-                              uint32_t cells, uint32_t* offs, cudaStream_t st, uint32_t* far_reset,
-                              const uint32_t* offs_prev, uint32_t* flag_reset) {
+                              uint32_t cells, uint32_t* offs, cudaStream_t st, uint32_t* far_reset) {
     const uint32_t chunks = (cells + kScanChunk - 1u) / kScanChunk;
     k_cell_scan<true><<<chunks, kScanThreads, 0, st>>>(s.hist, s.coarse, cells, offs, s.fix_ctl, scenes,
-                                                      cell_tile_scene, far_reset, offs_prev, flag_reset);
+                                                      cell_tile_scene, far_reset);
     return cudaGetLastError();
 }
 
@@ -611,19 +562,18 @@ cudaError_t count_rank_scenes(CountScratch& s, const SceneDev* scenes, const uin
                               const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
                               const uint32_t* offs, const uint32_t* offs_old, const uint32_t* far, uint32_t* perm,
                               const float4* pos_buf0, const float4* pos_buf1, const uint4* vfme_buf0,
-                              const uint4* vfme_buf1, float4* spos, uint4* svfme, uint4* bands, uint32_t* claimed,
-                              bool may_init, cudaStream_t st) {
+                              const uint4* vfme_buf1, float4* spos, uint4* svfme, uint4* bands, cudaStream_t st) {
     cudaError_t e;
     if (n) {
         k_cell_rank_scenes<<<(n + 255u) / 256u, 256, 0, st>>>(scenes, tile_scene, keys, n, s.hist, perm, pos_buf0,
                                                               pos_buf1, vfme_buf0, vfme_buf1, spos, svfme, offs,
-                                                              offs_old, far, s.fix_bits, bands, claimed);
+                                                              offs_old, far, s.fix_bits, bands);
         if ((e = cudaGetLastError())) return e;
     }
-    const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, may_init};
+    const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, false};
     k_fix_marked<SceneBuffers><<<std::max(collect_grid(n), 1u), kCollectThreads, 0, st>>>(
         s.fix_bits, keys, n, offs, perm, fix_lists(s), s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse,
-        scan_tiles(cells), claimed, 0u);
+        scan_tiles(cells), far);
     return cudaGetLastError();
 }
 
@@ -647,7 +597,7 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
     const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, may_init};
     k_fix_marked<SceneBuffers><<<std::max(collect_grid(n), 1u), kCollectThreads, 0, st>>>(
         s.fix_bits, keys, n, offs, perm, fix_lists(s), s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse,
-        scan_tiles(cells), nullptr, 0u);
+        scan_tiles(cells), nullptr);
     return cudaGetLastError();
 }
 

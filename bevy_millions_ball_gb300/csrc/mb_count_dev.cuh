@@ -22,15 +22,14 @@ namespace {
 // belongs to one scene; its base is that scene's first slot plus the coarse
 // counts of the scene's earlier tiles, and tiles of HOLD scenes are left alone.
 // One chunk (kScanThreads threads); s_warp, s_base: kScanThreads / 32 words each.
-// A block that runs several chunks must synchronise between them.  offs_prev
-// (nullable, batches): a held scene's chunk copies its offsets from there.
+// A block that runs several chunks must synchronise between them.
 template <bool kScenes, bool kCg = false>
 __device__ __forceinline__ void scan_chunk(uint32_t chunk, const uint32_t* __restrict__ hist,
                                            const uint32_t* __restrict__ coarse, uint32_t cells,
                                            uint32_t* __restrict__ offs, uint32_t* fix_ctl,
                                            const SceneDev* __restrict__ scenes,
                                            const uint32_t* __restrict__ cell_tile_scene, uint32_t* s_warp,
-                                           uint32_t* s_base, const uint32_t* __restrict__ offs_prev = nullptr) {
+                                           uint32_t* s_base) {
     constexpr int W = kScanThreads / 32;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t c0 = chunk * kScanChunk, tile = c0 / kScanTile;
@@ -40,12 +39,7 @@ __device__ __forceinline__ void scan_chunk(uint32_t chunk, const uint32_t* __res
     uint32_t first_tile = 0, base_slot = 0;
     if (kScenes) {
         const uint32_t sc = __ldg(cell_tile_scene + tile);
-        if (__ldg(&scenes[sc].mode) == kModeHold) {
-            if (offs_prev)  // (the entry after the chunk is the next scene's first: the same in both buffers)
-                for (uint32_t c = c0 + tid; c <= c0 + kScanChunk && c <= cells; c += kScanThreads)
-                    offs[c] = __ldg(offs_prev + c);
-            return;
-        }
+        if (__ldg(&scenes[sc].mode) == kModeHold) return;
         first_tile = __ldg(&scenes[sc].cell_base) / kScanTile;
         base_slot = __ldg(&scenes[sc].agent_base);
     }

@@ -132,8 +132,7 @@ struct SceneDev {
     uint32_t cell_base;              // cells [cell_base, cell_base + N*N)
     uint32_t mode;                   // kModeHold / kModeInit / kModeLoop
     uint32_t parity;                 // which state buffer holds the scene's current state
-    uint32_t prev_loop;              // the scene ran a LOOP frame last (rank placement may rank it)
-    uint32_t pad[2];
+    uint32_t pad[3];
 };
 constexpr uint32_t kPhysicsTile = 128;  // slots per block of the physics pass
 
@@ -374,26 +373,17 @@ cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
 cudaError_t count_rank_alloc(CountScratch& s);
 // Batched count scan: scene cell ranges are padded to whole scan tiles
 // (cell_tile_scene[t] = scene of tile t); tiles of HOLD scenes are skipped.
-// Batched scan for rank placement (offs_prev non-null): the tiles of held scenes
-// copy their offsets from offs_prev, the other buffer, so that both buffers
-// keep every scene's cell ranges; block 0 zeroes far_reset[0] (the far list the
-// physics pass fills) and *flag_reset (the claim flag of this frame).
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
-                              uint32_t cells, uint32_t* offs, cudaStream_t st, uint32_t* far_reset = nullptr,
-                              const uint32_t* offs_prev = nullptr, uint32_t* flag_reset = nullptr);
-// Batched rank placement: a scene in LOOP that also ran LOOP the frame before
-// (SceneDev::prev_loop) is ranked (offs / offs_old this frame's and the previous
-// frame's pool-wide offsets, far the far moves of the previous batched physics
-// pass, pool-wide slots); scenes in INIT, scenes back from a hold and every
-// scene when the far list overflowed claim slots and are fixed as
-// count_scatter_scenes does (*claimed is set, the fixup then runs).  may_init:
-// a scene may be in its INIT frame.
+                              uint32_t cells, uint32_t* offs, cudaStream_t st, uint32_t* far_reset = nullptr);
+// Batched rank placement, for frames in which every scene is in LOOP: offs /
+// offs_old this frame's and the previous frame's pool-wide offsets, far the
+// far moves of the previous batched physics pass (pool-wide slots); an
+// overflowed list falls back to the batched scatter and fixup.
 cudaError_t count_rank_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* tile_scene,
                               const uint32_t* cell_tile_scene, const uint32_t* keys, uint32_t n, uint32_t cells,
                               const uint32_t* offs, const uint32_t* offs_old, const uint32_t* far, uint32_t* perm,
                               const float4* pos_buf0, const float4* pos_buf1, const uint4* vfme_buf0,
-                              const uint4* vfme_buf1, float4* spos, uint4* svfme, uint4* bands, uint32_t* claimed,
-                              bool may_init, cudaStream_t st);
+                              const uint4* vfme_buf1, float4* spos, uint4* svfme, uint4* bands, cudaStream_t st);
 // Batched scatter + fixup: like count_scatter, reading each scene's state from its
 // parity buffer; spheres and cells of HOLD scenes are left alone.  may_init: a
 // scene may be in its INIT frame (its cell counts are then cleared here).

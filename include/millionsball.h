@@ -419,10 +419,9 @@ mb_status mb_batch_get_debug(mb_batch* b, uint32_t scene, uint32_t* keys, uint32
 
 /*
  * Kernel choices of a batch (the knobs of mb_tuning that apply to a pool):
- * sort_algorithm (MB_SORT_RANK, the default: the spheres of every scene that
- * ran LOOP the frame before are placed by rank, those of scenes in INIT or back
- * from a hold claim slots and are fixed in the same frame; or MB_SORT_COUNTING:
- * every frame claims and fixes), frames_per_launch (frames
+ * sort_algorithm (MB_SORT_RANK, the default: frames in which every scene is
+ * in LOOP place spheres by rank, other frames claim and fix; or
+ * MB_SORT_COUNTING: every frame claims and fixes), frames_per_launch (frames
  * captured per graph launch while no scene changes mode: 1, 2, 4, 8 (default)
  * or 16), collide_block (physics tile: 64, 128 (default) or 256 slots) and
  * scatter_agents (spheres per thread of the counting scatter: 1, 2 or 4).  The
