@@ -154,15 +154,12 @@ __device__ __forceinline__ bool spring_of(const PhysParams& P) {
     return kResp == kSpringRuntime ? P.spring != 0u : kResp == kSpring;
 }
 
-// solve_sphere_constraint (physics.wgsl:300-331).  Returns false when the
-// sphere's position is left as it was (no contact, or a spring contact too
-// shallow to push it: only its force changes).
+// solve_sphere_constraint (physics.wgsl:300-331)
 template <int kResp>
-__device__ __forceinline__ bool sphere(const PhysParams& P, Agent& a, const Agent& b) {
+__device__ __forceinline__ void sphere(const PhysParams& P, Agent& a, const Agent& b) {
     float edge = b.scale + a.scale;
     V3 tpos = a.position - b.position;
     float dist = len3(tpos);
-    bool moved = false;
     if (dist <= edge) {
         V3 norm = normalize3(tpos);
         if (!spring_of<kResp>(P)) {
@@ -179,7 +176,6 @@ __device__ __forceinline__ bool sphere(const PhysParams& P, Agent& a, const Agen
             }
             float h = 0.5f * (edge - dist);
             a.position = a.position + h * norm;
-            moved = true;
         } else {
             float makeup = edge - dist;
             V3 kforce = (P.k_agent * makeup) * norm;
@@ -188,11 +184,9 @@ __device__ __forceinline__ bool sphere(const PhysParams& P, Agent& a, const Agen
             float limit = makeup - P.r_agent * a.scale;
             if (limit > 0.0f) {
                 a.position = a.position + limit * norm;
-                moved = true;
             }
         }
     }
-    return moved;
 }
 
 // solve_cube_constraint (physics.wgsl:269-298)
@@ -438,31 +432,22 @@ __device__ __forceinline__ void contact_walk(const PhysParams& P, Agent& a, cons
         if (rem < kLook) m &= (1u << rem) - 1u;
         if (tself - t < kLook) m &= ~(1u << (tself - t));
         if (m) {
-            // solve the window's may-touch candidates in order; while a solve leaves
-            // the position as it was, the window's tests (made at that position)
-            // still decide the rest of it, so the next one is solved without a reload
-            uint32_t q = (uint32_t)(__ffs(m) - 1);
-            bool moved;
-            for (;;) {
-                const uint32_t j = j0 + q;
-                if constexpr (kResp == kSpring) {  // the neighbour's packed state is not read
-                    if (kShared) {
-                        moved = sphere<kResp>(P, a, unpack_pos(bpos[j]));
-                    } else {
-                        const uint32_t sj = kIndirect ? min(ld_in<kCg>(perm + j), nmax) : j;
-                        moved = sphere<kResp>(P, a, unpack_pos(ld_in<kCg>(bpos + sj)));
-                    }
-                } else if (kShared) {
-                    moved = sphere<kResp>(P, a, unpack(bpos[j], bvfme[j]));
+            const uint32_t q = (uint32_t)(__ffs(m) - 1);
+            t += q + 1u;
+            const uint32_t j = j0 + q;
+            if constexpr (kResp == kSpring) {  // the neighbour's packed state is not read
+                if (kShared) {
+                    sphere<kResp>(P, a, unpack_pos(bpos[j]));
                 } else {
                     const uint32_t sj = kIndirect ? min(ld_in<kCg>(perm + j), nmax) : j;
-                    moved = sphere<kResp>(P, a, unpack(ld_in<kCg>(bpos + sj), ld_in<kCg>(bvfme + sj)));
+                    sphere<kResp>(P, a, unpack_pos(ld_in<kCg>(bpos + sj)));
                 }
-                m &= m - 1u;
-                if (moved || !m) break;
-                q = (uint32_t)(__ffs(m) - 1);
+            } else if (kShared) {
+                sphere<kResp>(P, a, unpack(bpos[j], bvfme[j]));
+            } else {
+                const uint32_t sj = kIndirect ? min(ld_in<kCg>(perm + j), nmax) : j;
+                sphere<kResp>(P, a, unpack(ld_in<kCg>(bpos + sj), ld_in<kCg>(bvfme + sj)));
             }
-            t += moved ? q + 1u : min(rem, kLook);  // resume after the push, or after the window
         } else {
             t += min(rem, kLook);
         }
