@@ -398,15 +398,15 @@ __device__ __forceinline__ void fix_warp_cell(uint32_t lo, uint32_t m, uint32_t 
 
 // ---------------------------------------------------------------- marked cells
 // The sort of this frame is past its scan: clear the tile counts for the next
-// frame's physics pass (block 0) and the cell counts of scenes in their INIT
-// frame, which the scatter does not count down (they keep identity order).
+// frame's physics pass and the cell counts of scenes in their INIT frame, which
+// the scatter does not count down (they keep identity order); both spread over
+// the blocks (a batch has thousands of tiles, each checked against its scene).
 template <class Src>
 __device__ __forceinline__ void clear_counts(uint32_t vb, uint32_t nvb, const Src& src, uint32_t* __restrict__ hist,
                                              uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles) {
     const uint32_t tid = threadIdx.x;
-    if (vb == 0)
-        for (uint32_t t = tid; t < tiles; t += blockDim.x)
-            if (src.tile_active(t)) coarse[t] = 0u;
+    for (uint32_t t = vb * blockDim.x + tid; t < tiles; t += nvb * blockDim.x)
+        if (src.tile_active(t)) coarse[t] = 0u;
     if (src.any_init())
         for (uint32_t c = (vb * blockDim.x + tid) * 4u; c < cells; c += nvb * blockDim.x * 4u)
             if (src.tile_init(c / kScanTile)) *reinterpret_cast<uint4*>(hist + c) = make_uint4(0u, 0u, 0u, 0u);
