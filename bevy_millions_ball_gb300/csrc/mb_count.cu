@@ -337,14 +337,18 @@ __global__ void __launch_bounds__(kCollectThreads)
     k_fix_marked(const uint32_t* __restrict__ fix_bits, const uint32_t* __restrict__ keys, uint32_t n,
                  const uint32_t* __restrict__ offs, uint32_t* perm, FixLists lists, uint32_t* __restrict__ tmp,
                  Src src, float4* __restrict__ spos, uint4* __restrict__ svfme, uint32_t* __restrict__ hist,
-                 uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles, const uint32_t* __restrict__ gate) {
+                 uint32_t cells, uint32_t* __restrict__ coarse, uint32_t tiles, const uint32_t* __restrict__ gate,
+                 uint32_t nvb) {
     __shared__ MarkedSmem S;
     griddep_wait();  // the scatter's bitmap and order are complete
     griddep_launch();
     clear_counts(blockIdx.x, gridDim.x, src, hist, cells, coarse, tiles);
     if (gate && __ldcg(gate) <= kFarCap) return;
-    fix_marked_block<Src, false, true>(blockIdx.x, gridDim.x, fix_bits, keys, n, offs, perm, lists, tmp, src, spos,
-                                       svfme, S);
+    // nvb blocks' worth of the bitmap, taken in turn by the launched blocks
+    for (uint32_t vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+        fix_marked_block<Src, false, true>(vb, nvb, fix_bits, keys, n, offs, perm, lists, tmp, src, spos, svfme, S);
+        __syncthreads();  // shared lists free for the next one
+    }
 }
 
 // INIT frame after an upload: every key is 0, so the stable order is the
@@ -422,6 +426,12 @@ FixLists fix_lists(const CountScratch& s) {
 }
 uint32_t fix_words(uint32_t max_keys) { return max_keys / 32u + 1u; }
 uint32_t collect_grid(uint32_t n) { return ((n + 31u) / 32u + kCollectWords - 1u) / kCollectWords; }
+// Blocks the fixup launches: at most eight per SM, each taking collect_grid's
+// blocks of the bitmap in turn (an idle fixup, the usual case under rank
+// placement, then costs little to launch).
+uint32_t fix_grid(uint32_t n) {
+    return std::max(std::min<uint32_t>(collect_grid(n), (uint32_t)device_sm_count() * 8u), 1u);
+}
 uint32_t scan_tiles(uint32_t cells) { return (cells + kScanTile - 1u) / kScanTile; }
 uint32_t fix_capacity(int cls, uint32_t max_cells, uint32_t max_keys) {
     if (cls != kFixListHuge) return 1u;  // only cells above kFixWarp slots are listed
@@ -524,9 +534,10 @@ cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
             return e;
     }
     const OneBuffer src{pos_in, vfme_in};
-    return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(std::max(collect_grid(n), 1u)),
+    return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(fix_grid(n)),
                       dim3(kCollectThreads), 0, st, (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s),
-                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells), far);
+                      s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells), far,
+                      std::max(collect_grid(n), 1u));
 }
 
 cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uint32_t cells,
@@ -544,10 +555,10 @@ cudaError_t count_scatter(CountScratch& s, const uint32_t* keys, uint32_t n, uin
             return e;
     }
     const OneBuffer src{pos_in, vfme_in};
-    return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(std::max(collect_grid(n), 1u)),
+    return launch_pdl(pdl && n, k_fix_marked<OneBuffer>, dim3(fix_grid(n)),
                       dim3(kCollectThreads), 0, st, (const uint32_t*)s.fix_bits, keys, n, offs, perm, fix_lists(s),
                       s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse, scan_tiles(cells),
-                      (const uint32_t*)nullptr);
+                      (const uint32_t*)nullptr, std::max(collect_grid(n), 1u));
 }
 
 cudaError_t count_scan_scenes(CountScratch& s, const SceneDev* scenes, const uint32_t* cell_tile_scene,
@@ -571,9 +582,9 @@ cudaError_t count_rank_scenes(CountScratch& s, const SceneDev* scenes, const uin
         if ((e = cudaGetLastError())) return e;
     }
     const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, false};
-    k_fix_marked<SceneBuffers><<<std::max(collect_grid(n), 1u), kCollectThreads, 0, st>>>(
+    k_fix_marked<SceneBuffers><<<fix_grid(n), kCollectThreads, 0, st>>>(
         s.fix_bits, keys, n, offs, perm, fix_lists(s), s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse,
-        scan_tiles(cells), far);
+        scan_tiles(cells), far, std::max(collect_grid(n), 1u));
     return cudaGetLastError();
 }
 
@@ -595,9 +606,9 @@ cudaError_t count_scatter_scenes(CountScratch& s, const SceneDev* scenes, const 
         if ((e = cudaGetLastError())) return e;
     }
     const SceneBuffers src{scenes, tile_scene, cell_tile_scene, pos_buf0, pos_buf1, vfme_buf0, vfme_buf1, may_init};
-    k_fix_marked<SceneBuffers><<<std::max(collect_grid(n), 1u), kCollectThreads, 0, st>>>(
+    k_fix_marked<SceneBuffers><<<fix_grid(n), kCollectThreads, 0, st>>>(
         s.fix_bits, keys, n, offs, perm, fix_lists(s), s.fix_tmp, src, spos, svfme, s.hist, cells, s.coarse,
-        scan_tiles(cells), nullptr);
+        scan_tiles(cells), nullptr, std::max(collect_grid(n), 1u));
     return cudaGetLastError();
 }
 
