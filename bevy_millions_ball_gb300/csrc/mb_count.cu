@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(kScanThreads)
 }
 
 // Rank placement of one world's spheres (MB_SORT_RANK), kPer spheres per
-// thread (256 kPer per block, their loads issued together).  The input is the
+// thread (kRankThreads kPer per block, their loads issued together).  The input is the
 // previous frame's sorted order, described by offs_old; a sphere of new cell
 // k = (kx, kz) that moved at most one cell sits in the old ranges of cells
 // (kx-1..kx+1, kz-1..kz+1), three slot ranges, one per row.  Its stable slot is
@@ -68,8 +68,10 @@ __global__ void __launch_bounds__(kScanThreads)
 // then runs too).
 __device__ __forceinline__ uint32_t bloom_bit(uint32_t k) { return (k * 2654435761u) >> 20; }  // 12 bits
 
+constexpr uint32_t kRankThreads = 128;  // (256-thread blocks: P-1M frame +1.8 us)
+
 template <uint32_t kPer>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kRankThreads)
     k_cell_rank(const uint32_t* __restrict__ keys, uint32_t n, uint32_t cells, uint32_t* __restrict__ hist,
                 uint32_t* __restrict__ perm, const float4* __restrict__ pos_in, const uint4* __restrict__ vfme_in,
                 float4* __restrict__ spos, uint4* __restrict__ svfme, const uint32_t* __restrict__ offs,
@@ -529,7 +531,8 @@ cudaError_t count_rank(CountScratch& s, const uint32_t* keys, uint32_t n, uint32
     if (n) {
         const uint32_t per = per_thread == 4u ? 4u : (per_thread == 2u ? 2u : 1u);
         auto* kern = per == 4u ? k_cell_rank<4> : (per == 2u ? k_cell_rank<2> : k_cell_rank<1>);
-        if ((e = launch_pdl(pdl, kern, dim3((n + 256u * per - 1u) / (256u * per)), dim3(256), 0, st, keys, n, cells,
+        if ((e = launch_pdl(pdl, kern, dim3((n + kRankThreads * per - 1u) / (kRankThreads * per)), dim3(kRankThreads),
+                            0, st, keys, n, cells,
                             s.hist, perm, pos_in, vfme_in, spos, svfme, offs, offs_old, far, bands, N, s.fix_bits)))
             return e;
     }
