@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(256)
 // the neighbourhood in the scene's own cell coordinates, its state from its
 // current buffer); one sphere per thread.  The far list holds pool-wide slots,
 // its keys pool-wide cells.  An overflowed list: the batched scatter instead.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kRankThreads)
     k_cell_rank_scenes(const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ tile_scene,
                        const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
                        uint32_t* __restrict__ perm, const float4* __restrict__ pos0, const float4* __restrict__ pos1,
@@ -579,7 +579,8 @@ cudaError_t count_rank_scenes(CountScratch& s, const SceneDev* scenes, const uin
                               const uint4* vfme_buf1, float4* spos, uint4* svfme, uint4* bands, cudaStream_t st) {
     cudaError_t e;
     if (n) {
-        k_cell_rank_scenes<<<(n + 255u) / 256u, 256, 0, st>>>(scenes, tile_scene, keys, n, s.hist, perm, pos_buf0,
+        k_cell_rank_scenes<<<(n + kRankThreads - 1u) / kRankThreads, kRankThreads, 0, st>>>(
+            scenes, tile_scene, keys, n, s.hist, perm, pos_buf0,
                                                               pos_buf1, vfme_buf0, vfme_buf1, spos, svfme, offs,
                                                               offs_old, far, s.fix_bits, bands);
         if ((e = cudaGetLastError())) return e;
